@@ -1,0 +1,723 @@
+/* CPU restatement of AMDAT's hot path: TEST INFRASTRUCTURE ONLY (see header).
+ * Compile with -ffp-contract=off: the reference is built by g++ on x86-64
+ * without FMA contraction, and REF32 mode must reproduce its roundings on any
+ * host (aarch64 gcc contracts a*b+c by default). */
+#include "amdat_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define TWO_PI 6.283185307179586476925286766559
+
+/* ------------------------------------------------------------------------- */
+/* time scheme: system.cpp:83-140 (parse), :218 (n_timegaps),                 */
+/* :3542-3566 (create_timelist), :3763-3787 (displacement_times)              */
+/* ------------------------------------------------------------------------- */
+
+void orc_scheme_init(orc_scheme* s, int32_t kind, int32_t a, int32_t b, float base, int32_t frt,
+                     int32_t first_exponent, float unit) {
+  memset(s, 0, sizeof(*s));
+  s->kind = kind;
+  if (kind == ORC_LINEAR) { /* 'linear n_timesteps unit' */
+    s->n_exponentials = a - 1;
+    s->n_exponential_steps = 1;
+    s->exp_base = 1.0f;
+    s->frt = 0;
+    s->first_exponent = 0;
+    s->time_unit = unit;
+  } else if (kind == ORC_EXPONENTIAL) {
+    s->n_exponentials = a;
+    s->n_exponential_steps = b;
+    s->exp_base = base;
+    s->frt = frt;
+    s->first_exponent = first_exponent;
+    s->time_unit = unit;
+  } else { /* snapshot */
+    s->n_exponentials = 1;
+    s->n_exponential_steps = 0;
+    s->exp_base = 1.0f;
+    s->time_unit = 1.0f;
+  }
+}
+
+int32_t orc_n_timesteps(const orc_scheme* s) {
+  if (s->kind == ORC_EXPONENTIAL) return s->n_exponential_steps * s->n_exponentials + 1;
+  if (s->kind == ORC_LINEAR) return s->n_exponentials + 1;
+  return 1;
+}
+
+int32_t orc_n_timegaps(const orc_scheme* s) {
+  return s->n_exponential_steps + s->n_exponentials - 1 + (s->frt ? 0 : 1);
+}
+
+void orc_timelist(const orc_scheme* s, float* t) {
+  int ii = 0;
+  float block_start = 0.0f;
+  t[0] = 0.0f;
+  for (int b = 0; b < s->n_exponentials; ++b) {
+    for (int e = 1; e <= s->n_exponential_steps; ++e) {
+      ++ii;
+      double p = pow((double)s->exp_base, (double)(e - 1 + s->first_exponent));
+      if (p <= e)
+        t[ii] = block_start + (float)e * s->time_unit;
+      else
+        t[ii] = block_start + (float)floor(p) * s->time_unit;
+    }
+    block_start = t[ii];
+  }
+}
+
+void orc_displacement_times(const orc_scheme* s, float* gap) {
+  int T = orc_n_timesteps(s), G = orc_n_timegaps(s), K = s->n_exponential_steps;
+  float* t = (float*)malloc(sizeof(float) * T);
+  orc_timelist(s, t);
+  int frt = s->frt ? 1 : 0;
+  for (int g = 0; g < K; ++g) gap[g] = t[g + frt] - t[frt];
+  for (int b = 1; b < s->n_exponentials; ++b) gap[b + K - 1] = t[K * b + frt] - t[frt];
+  if (!frt) gap[G - 1] = t[T - 1] - t[0];
+  free(t);
+}
+
+/* System::timegap_weighting(bool) (system.cpp:4599-4628), including its '+1'
+ * on cross-block gaps (it cancels in the ISF normalisation). */
+void orc_timegap_weighting(const orc_scheme* s, int32_t fullblock, int32_t* w) {
+  int K = s->n_exponential_steps, I = s->n_exponentials, G = orc_n_timegaps(s);
+  int lim = s->limit, frt = s->frt ? 1 : 0;
+  for (int g = 0; g < K; ++g) {
+    w[g] = I;
+    if (w[g] > lim && lim != 0) w[g] = lim;
+  }
+  for (int g = K; g < G - 1 + frt; ++g) {
+    int bg = g - K + 1;
+    w[g] = (I - bg) + (fullblock ? 1 : 0) * (I - bg) * (K - 1) + 1;
+    if (w[g] > lim && lim != 0) w[g] = lim;
+  }
+  if (!frt) w[G - 1] = 1;
+}
+
+static void put_pair(int64_t n, int32_t* gap, int32_t* t0, int32_t* t1, int g, int a, int b) {
+  if (gap) { gap[n] = g; t0[n] = a; t1[n] = b; }
+}
+
+/* System::displacement_list(Analysis*, bool) (system.cpp:4090-4179) */
+int64_t orc_pairs_list(const orc_scheme* s, int32_t fullblock, int32_t* gap, int32_t* t0,
+                       int32_t* t1) {
+  int K = s->n_exponential_steps, I = s->n_exponentials, G = orc_n_timegaps(s);
+  int T = orc_n_timesteps(s), frt = s->frt ? 1 : 0, lim = s->limit;
+  int64_t n = 0;
+  for (int g = 0; g < K; ++g) {
+    int count = 0, abort_ = 0;
+    for (int b = 0; b < I; ++b) {
+      if (abort_) continue;
+      int a = K * b + frt;
+      put_pair(n++, gap, t0, t1, g, a, a + g);
+      ++count;
+      abort_ = (count == lim && lim != 0);
+    }
+  }
+  for (int g = K; g < G - 1 + frt; ++g) {
+    int count = 0, abort_ = 0, bg = g - K + 1;
+    for (int e = 0; e < (fullblock ? 1 : 0) * (K - 1) + 1; ++e) {
+      if (abort_) continue;
+      for (int b = 0; b < I - bg; ++b) {
+        if (abort_) continue;
+        int a = K * b + e + frt;
+        put_pair(n++, gap, t0, t1, g, a, a + K * bg);
+        ++count;
+        abort_ = (count == lim && lim != 0);
+      }
+    }
+  }
+  if (!frt) put_pair(n++, gap, t0, t1, G - 1, 0, T - 1);
+  return n;
+}
+
+/* System::displacement_loop(Analysis*, Trajectory*, bool) (system.cpp:3918-3964) */
+int64_t orc_pairs_loop(const orc_scheme* s, int32_t fullblock, int32_t* gap, int32_t* t0,
+                       int32_t* t1) {
+  int K = s->n_exponential_steps, I = s->n_exponentials, G = orc_n_timegaps(s);
+  int T = orc_n_timesteps(s), frt = s->frt ? 1 : 0, lim = s->limit;
+  int64_t n = 0;
+  for (int g = 0; g < K; ++g) {
+    int count = 0;
+    for (int b = 0; b < I; ++b) {
+      int a = K * b + frt;
+      put_pair(n++, gap, t0, t1, g, a, a + g);
+      ++count;
+      if (count == lim) break;
+    }
+  }
+  for (int g = K; g < G - 1 + frt; ++g) {
+    int count = 0, bg = g - K + 1;
+    for (int e = 0; e < (fullblock ? 1 : 0) * (K - 1) + 1; ++e) {
+      for (int b = 0; b < I - bg; ++b) {
+        int a = K * b + e + frt;
+        put_pair(n++, gap, t0, t1, g, a, a + K * bg);
+        ++count;
+        if (count == lim) break;
+      }
+      if (count == lim) break;
+    }
+  }
+  if (!frt) put_pair(n++, gap, t0, t1, G - 1, 0, T - 1);
+  return n;
+}
+
+typedef struct {
+  int64_t n;
+  int32_t *gap, *t0, *t1;
+} pairs_t;
+
+static pairs_t make_pairs(const orc_scheme* s, int fullblock, int loop_order) {
+  pairs_t p;
+  p.n = loop_order ? orc_pairs_loop(s, fullblock, 0, 0, 0) : orc_pairs_list(s, fullblock, 0, 0, 0);
+  size_t bytes = sizeof(int32_t) * (size_t)(p.n > 0 ? p.n : 1);
+  p.gap = (int32_t*)malloc(bytes);
+  p.t0 = (int32_t*)malloc(bytes);
+  p.t1 = (int32_t*)malloc(bytes);
+  if (loop_order) orc_pairs_loop(s, fullblock, p.gap, p.t0, p.t1);
+  else orc_pairs_list(s, fullblock, p.gap, p.t0, p.t1);
+  return p;
+}
+
+static void free_pairs(pairs_t* p) { free(p->gap); free(p->t0); free(p->t1); }
+
+/* ------------------------------------------------------------------------- */
+/* coordinates                                                               */
+/* ------------------------------------------------------------------------- */
+
+#define POS(arr, t, a, c) ((arr)[((size_t)(t) * (size_t)n_atoms + (size_t)(a)) * 3 + (c)])
+
+/* Trajectory::distance (trajectory.cpp:326): |u(t1)-u(t0)| in FP32,
+ * Coordinate::length = sqrt(x*x+y*y+z*z) (coordinate.h:55) */
+static float dist32(const float* u, int n_atoms, int a, int ta, int tb) {
+  float dx = POS(u, tb, a, 0) - POS(u, ta, a, 0);
+  float dy = POS(u, tb, a, 1) - POS(u, ta, a, 1);
+  float dz = POS(u, tb, a, 2) - POS(u, ta, a, 2);
+  return sqrtf(dx * dx + dy * dy + dz * dz);
+}
+
+static double dist2_64(const float* u, int n_atoms, int a, int ta, int tb) {
+  double dx = (double)POS(u, tb, a, 0) - (double)POS(u, ta, a, 0);
+  double dy = (double)POS(u, tb, a, 1) - (double)POS(u, ta, a, 1);
+  double dz = (double)POS(u, tb, a, 2) - (double)POS(u, ta, a, 2);
+  return dx * dx + dy * dy + dz * dz;
+}
+
+/* ------------------------------------------------------------------------- */
+/* displacement family                                                       */
+/* ------------------------------------------------------------------------- */
+
+void orc_msd(const orc_scheme* s, const float* u, int32_t n_atoms, const int32_t* list,
+             int32_t n_list, int32_t mode, double* msd, double* weighting) {
+  int G = orc_n_timegaps(s);
+  pairs_t p = make_pairs(s, 0, 0); /* analyze(): displacement_list(this,false) */
+  if (mode == ORC_REF32) {
+    float* m = (float*)calloc(G, sizeof(float));
+    float* w = (float*)calloc(G, sizeof(float));
+    for (int64_t i = 0; i < p.n; ++i) {
+      int g = p.gap[i];
+      w[g] += (float)n_list;
+      for (int j = 0; j < n_list; ++j) {
+        float d = dist32(u, n_atoms, list[j], p.t0[i], p.t1[i]);
+        m[g] += d * d;
+      }
+    }
+    for (int g = 0; g < G; ++g) {
+      m[g] /= (float)w[g];
+      msd[g] = m[g];
+      if (weighting) weighting[g] = w[g];
+    }
+    free(m); free(w);
+  } else {
+    double* m = (double*)calloc(G, sizeof(double));
+    double* w = (double*)calloc(G, sizeof(double));
+    for (int64_t i = 0; i < p.n; ++i) {
+      int g = p.gap[i];
+      w[g] += n_list;
+      for (int j = 0; j < n_list; ++j) m[g] += dist2_64(u, n_atoms, list[j], p.t0[i], p.t1[i]);
+    }
+    for (int g = 0; g < G; ++g) {
+      msd[g] = m[g] / w[g];
+      if (weighting) weighting[g] = w[g];
+    }
+    free(m); free(w);
+  }
+  free_pairs(&p);
+}
+
+void orc_ngp(const orc_scheme* s, const float* u, int32_t n_atoms, const int32_t* list,
+             int32_t n_list, int32_t mode, double* ngp) {
+  int G = orc_n_timegaps(s);
+  double* msd = (double*)malloc(sizeof(double) * G);
+  orc_msd(s, u, n_atoms, list, n_list, mode, msd, 0); /* Control::ngp runs MSD first */
+  pairs_t p = make_pairs(s, 0, 0);
+  if (mode == ORC_REF32) {
+    float* q = (float*)calloc(G, sizeof(float));
+    long* w = (long*)calloc(G, sizeof(long));
+    for (int64_t i = 0; i < p.n; ++i) {
+      int g = p.gap[i];
+      w[g] += n_list;
+      for (int j = 0; j < n_list; ++j) {
+        float d = dist32(u, n_atoms, list[j], p.t0[i], p.t1[i]);
+        q[g] = (float)((double)q[g] + pow((double)d, 4.0)); /* float += double pow */
+      }
+    }
+    for (int g = 0; g < G; ++g) {
+      float m = (float)msd[g];
+      double f = (3.0 / (double)(float)w[g]) / (5 * pow((double)m, 2.0));
+      q[g] = (float)((double)q[g] * f);
+      q[g] = (float)((double)q[g] - 1.0);
+      ngp[g] = q[g];
+    }
+    free(q); free(w);
+  } else {
+    double* q = (double*)calloc(G, sizeof(double));
+    double* w = (double*)calloc(G, sizeof(double));
+    for (int64_t i = 0; i < p.n; ++i) {
+      int g = p.gap[i];
+      w[g] += n_list;
+      for (int j = 0; j < n_list; ++j) {
+        double d2 = dist2_64(u, n_atoms, list[j], p.t0[i], p.t1[i]);
+        q[g] += d2 * d2;
+      }
+    }
+    for (int g = 0; g < G; ++g) ngp[g] = q[g] * (3.0 / w[g]) / (5.0 * msd[g] * msd[g]) - 1.0;
+    free(q); free(w);
+  }
+  free(msd);
+  free_pairs(&p);
+}
+
+void orc_disp_moments(const orc_scheme* s, int32_t fullblock, const float* u, int32_t n_atoms,
+                      const int32_t* list, int32_t n_list, double* sum_d2, double* sum_d4,
+                      int64_t* count) {
+  int G = orc_n_timegaps(s);
+  pairs_t p = make_pairs(s, fullblock, 0);
+  for (int g = 0; g < G; ++g) { sum_d2[g] = 0; sum_d4[g] = 0; count[g] = 0; }
+  for (int64_t i = 0; i < p.n; ++i) {
+    int g = p.gap[i];
+    count[g] += n_list;
+    for (int j = 0; j < n_list; ++j) {
+      double d2 = dist2_64(u, n_atoms, list ? list[j] : j, p.t0[i], p.t1[i]);
+      sum_d2[g] += d2;
+      sum_d4[g] += d2 * d2;
+    }
+  }
+  free_pairs(&p);
+}
+
+void orc_isfs(const orc_scheme* s, int32_t fullblock, const float* u, int32_t n_atoms,
+              const int32_t* list, int32_t n_list, const int32_t* kvec_n, const int32_t* off,
+              int32_t n_shells, float spacing, double box_len, int32_t mode, double* corr) {
+  int G = orc_n_timegaps(s);
+  pairs_t p = make_pairs(s, fullblock, 0);
+  int nk = off[n_shells];
+  if (mode == ORC_REF32) {
+    /* wave vectors as Wave_Vectors::read_vectors stores them: n * spacing in FP32 */
+    float* k = (float*)malloc(sizeof(float) * 3 * (nk > 0 ? nk : 1));
+    for (int i = 0; i < 3 * nk; ++i) k[i] = (float)kvec_n[i] * spacing;
+    float* c = (float*)calloc((size_t)G * n_shells, sizeof(float));
+    float* na = (float*)calloc(G, sizeof(float));
+    for (int64_t i = 0; i < p.n; ++i) {
+      int g = p.gap[i], ta = p.t0[i], tb = p.t1[i];
+      for (int j = 0; j < n_list; ++j) {
+        int a = list[j];
+        na[g] += 1.0f;
+        float dx = POS(u, tb, a, 0) - POS(u, ta, a, 0);
+        float dy = POS(u, tb, a, 1) - POS(u, ta, a, 1);
+        float dz = POS(u, tb, a, 2) - POS(u, ta, a, 2);
+        for (int m = 0; m < n_shells; ++m) {
+          double tmp = 0;
+          int cnt = off[m + 1] - off[m];
+          for (int v = off[m]; v < off[m + 1]; ++v) {
+            float kr = k[3 * v] * dx + k[3 * v + 1] * dy + k[3 * v + 2] * dz;
+            tmp += (double)cosf(kr) / (double)cnt;
+          }
+          c[(size_t)g * n_shells + m] += (float)tmp;
+        }
+      }
+    }
+    for (int g = 0; g < G; ++g)
+      for (int m = 0; m < n_shells; ++m) {
+        c[(size_t)g * n_shells + m] /= (float)na[g];
+        corr[(size_t)g * n_shells + m] = c[(size_t)g * n_shells + m];
+      }
+    free(k); free(c); free(na);
+  } else {
+    double* c = (double*)calloc((size_t)G * n_shells, sizeof(double));
+    double* na = (double*)calloc(G, sizeof(double));
+    double tpl = TWO_PI / box_len;
+    for (int64_t i = 0; i < p.n; ++i) {
+      int g = p.gap[i], ta = p.t0[i], tb = p.t1[i];
+      for (int j = 0; j < n_list; ++j) {
+        int a = list[j];
+        na[g] += 1.0;
+        double dx = (double)POS(u, tb, a, 0) - (double)POS(u, ta, a, 0);
+        double dy = (double)POS(u, tb, a, 1) - (double)POS(u, ta, a, 1);
+        double dz = (double)POS(u, tb, a, 2) - (double)POS(u, ta, a, 2);
+        for (int m = 0; m < n_shells; ++m) {
+          double tmp = 0;
+          int cnt = off[m + 1] - off[m];
+          for (int v = off[m]; v < off[m + 1]; ++v)
+            tmp += cos(tpl * (kvec_n[3 * v] * dx + kvec_n[3 * v + 1] * dy + kvec_n[3 * v + 2] * dz));
+          c[(size_t)g * n_shells + m] += tmp / cnt;
+        }
+      }
+    }
+    for (int g = 0; g < G; ++g)
+      for (int m = 0; m < n_shells; ++m)
+        corr[(size_t)g * n_shells + m] = c[(size_t)g * n_shells + m] / na[g];
+    free(c); free(na);
+  }
+  free_pairs(&p);
+}
+
+/* Space_Time_Correlation_Function PI (space_time_correlation_function.cpp:20) */
+#define STCF_PI 3.141592653589793238462643383280
+
+void orc_vhs(const orc_scheme* s, const float* u, int32_t n_atoms, const int32_t* list,
+             int32_t n_list, float max_value, int32_t n_bins, int64_t* counts, int64_t* weighting,
+             double* corr) {
+  int G = orc_n_timegaps(s);
+  pairs_t p = make_pairs(s, 0, 0); /* analyze(): displacement_list(this) */
+  float bin_size = max_value / (float)n_bins;
+  float* c = (float*)calloc((size_t)G * n_bins, sizeof(float));
+  int* w = (int*)calloc(G, sizeof(int));
+  for (size_t i = 0; i < (size_t)G * n_bins; ++i) counts[i] = 0;
+  for (int64_t i = 0; i < p.n; ++i) {
+    int g = p.gap[i];
+    for (int j = 0; j < n_list; ++j) {
+      float d = dist32(u, n_atoms, list[j], p.t0[i], p.t1[i]);
+      int b = (int)(d / bin_size);
+      if (b >= 0 && b < n_bins) {
+        c[(size_t)g * n_bins + b] += 1.0f;
+        counts[(size_t)g * n_bins + b]++;
+      }
+      w[g]++;
+    }
+  }
+  for (int b = 0; b < n_bins; ++b) {
+    float rshell = b * bin_size;
+    float shellvolume = (float)((4.0 / 3.0) * STCF_PI *
+                                (pow(rshell + bin_size, 3.0) - pow(rshell, 3.0)));
+    for (int g = 0; g < G; ++g) {
+      c[(size_t)g * n_bins + b] /= ((float)w[g] * shellvolume);
+      corr[(size_t)g * n_bins + b] = c[(size_t)g * n_bins + b];
+    }
+  }
+  for (int g = 0; g < G; ++g) weighting[g] = w[g];
+  free(c); free(w);
+  free_pairs(&p);
+}
+
+/* ------------------------------------------------------------------------- */
+/* Fourier densities                                                         */
+/* ------------------------------------------------------------------------- */
+
+void orc_rhok(const float* r, int32_t n_atoms, const int32_t* list, int32_t n_list,
+              const int32_t* frames, int32_t n_frames, const int32_t* kvec_n, int32_t n_k,
+              float spacing, double box_len, int32_t mode, double* rho) {
+  float* k = (float*)malloc(sizeof(float) * 3 * (n_k > 0 ? n_k : 1));
+  for (int i = 0; i < 3 * n_k; ++i) k[i] = (float)kvec_n[i] * spacing;
+  double tpl = TWO_PI / box_len;
+  for (int f = 0; f < n_frames; ++f) {
+    int t = frames[f];
+    double* out = rho + (size_t)f * n_k * 2;
+    for (int v = 0; v < 2 * n_k; ++v) out[v] = 0;
+    for (int j = 0; j < n_list; ++j) {
+      int a = list[j];
+      float x = POS(r, t, a, 0), y = POS(r, t, a, 1), z = POS(r, t, a, 2);
+      for (int v = 0; v < n_k; ++v) {
+        if (mode == ORC_REF32) {
+          float kr = k[3 * v] * x + k[3 * v + 1] * y + k[3 * v + 2] * z;
+          out[2 * v] += (double)cosf(kr);
+          out[2 * v + 1] += (double)sinf(kr);
+        } else {
+          double ph = tpl * ((double)kvec_n[3 * v] * x + (double)kvec_n[3 * v + 1] * y +
+                             (double)kvec_n[3 * v + 2] * z);
+          out[2 * v] += cos(ph);
+          out[2 * v + 1] += sin(ph);
+        }
+      }
+    }
+  }
+  free(k);
+}
+
+void orc_isf(const orc_scheme* s, int32_t fullblock, const double* rho1, const double* rho2,
+             int32_t n_k, const int32_t* off, int32_t n_shells, int32_t n_list, int32_t mode,
+             double* corr) {
+  int G = orc_n_timegaps(s);
+  pairs_t p = make_pairs(s, fullblock, 1); /* displacement_loop order */
+  int32_t* w = (int32_t*)malloc(sizeof(int32_t) * G);
+  orc_timegap_weighting(s, fullblock, w);
+  if (mode == ORC_REF32) {
+    float* c = (float*)calloc((size_t)G * n_shells, sizeof(float));
+    float* na = (float*)calloc(G, sizeof(float));
+    for (int64_t i = 0; i < p.n; ++i) {
+      int g = p.gap[i];
+      const double* a = rho1 + (size_t)p.t0[i] * n_k * 2;
+      const double* b = rho2 + (size_t)p.t1[i] * n_k * 2;
+      for (int m = 0; m < n_shells; ++m) {
+        int cnt = off[m + 1] - off[m];
+        for (int v = off[m]; v < off[m + 1]; ++v) {
+          double val = (a[2 * v] * b[2 * v] + a[2 * v + 1] * b[2 * v + 1]) / (double)(float)cnt;
+          c[(size_t)g * n_shells + m] = (float)((double)c[(size_t)g * n_shells + m] + val);
+        }
+      }
+      na[g] += (float)n_list / (float)w[g];
+    }
+    for (int g = 0; g < G; ++g)
+      for (int m = 0; m < n_shells; ++m) {
+        c[(size_t)g * n_shells + m] /= (float)(na[g] * (float)w[g]);
+        corr[(size_t)g * n_shells + m] = c[(size_t)g * n_shells + m];
+      }
+    free(c); free(na);
+  } else {
+    double* c = (double*)calloc((size_t)G * n_shells, sizeof(double));
+    double* na = (double*)calloc(G, sizeof(double));
+    for (int64_t i = 0; i < p.n; ++i) {
+      int g = p.gap[i];
+      const double* a = rho1 + (size_t)p.t0[i] * n_k * 2;
+      const double* b = rho2 + (size_t)p.t1[i] * n_k * 2;
+      for (int m = 0; m < n_shells; ++m) {
+        int cnt = off[m + 1] - off[m];
+        double acc = 0;
+        for (int v = off[m]; v < off[m + 1]; ++v) acc += a[2 * v] * b[2 * v] + a[2 * v + 1] * b[2 * v + 1];
+        c[(size_t)g * n_shells + m] += acc / cnt;
+      }
+      na[g] += n_list; /* the reference's n/w * w cancels to the atom-pair count */
+    }
+    for (int g = 0; g < G; ++g)
+      for (int m = 0; m < n_shells; ++m) corr[(size_t)g * n_shells + m] = c[(size_t)g * n_shells + m] / na[g];
+    free(c); free(na);
+  }
+  free(w);
+  free_pairs(&p);
+}
+
+/* frames visited by Analysis_Onetime::analyze (analysis_onetime.cpp:22-50) */
+static int onetime_frames(const orc_scheme* s, int ts, int* out) {
+  int n = 0;
+  if (ts == -1) {
+    for (int t = 0; t < orc_n_timesteps(s); ++t) out[n++] = t;
+  } else if (ts < -1) {
+    out[n++] = -ts - 2;
+  } else {
+    for (int t = ts; t < s->n_exponentials; t += s->n_exponential_steps) out[n++] = t;
+  }
+  return n;
+}
+
+void orc_structure_factor(const orc_scheme* s, int32_t ts, const float* r, int32_t n_atoms,
+                          const int32_t* list, int32_t n_list, const int32_t* kvec_n,
+                          const int32_t* off, int32_t n_shells, float spacing, double box_len,
+                          int32_t mode, double* sq) {
+  int T = orc_n_timesteps(s);
+  int* fr = (int*)malloc(sizeof(int) * (T + 1));
+  int nf = onetime_frames(s, ts, fr);
+  int nk = off[n_shells];
+  if (mode == ORC_REF32) {
+    float* k = (float*)malloc(sizeof(float) * 3 * (nk > 0 ? nk : 1));
+    for (int i = 0; i < 3 * nk; ++i) k[i] = (float)kvec_n[i] * spacing;
+    float* re = (float*)malloc(sizeof(float) * (nk > 0 ? nk : 1));
+    float* im = (float*)malloc(sizeof(float) * (nk > 0 ? nk : 1));
+    float* S = (float*)calloc(n_shells, sizeof(float));
+    int na = 0;
+    for (int f = 0; f < nf; ++f) {
+      int t = fr[f];
+      for (int v = 0; v < nk; ++v) { re[v] = 0; im[v] = 0; }
+      for (int j = 0; j < n_list; ++j) {
+        int a = list[j];
+        float x = POS(r, t, a, 0), y = POS(r, t, a, 1), z = POS(r, t, a, 2);
+        for (int v = 0; v < nk; ++v) {
+          float kr = k[3 * v] * x + k[3 * v + 1] * y + k[3 * v + 2] * z;
+          re[v] += cosf(kr);
+          im[v] += sinf(kr);
+        }
+      }
+      for (int m = 0; m < n_shells; ++m) {
+        int cnt = off[m + 1] - off[m];
+        for (int v = off[m]; v < off[m + 1]; ++v) S[m] += (re[v] * re[v] + im[v] * im[v]) / (float)cnt;
+      }
+      na += n_list;
+    }
+    for (int m = 0; m < n_shells; ++m) {
+      if ((float)na != 0) S[m] /= (float)na;
+      else S[m] = 0;
+      sq[m] = S[m];
+    }
+    free(k); free(re); free(im); free(S);
+  } else {
+    double* rho = (double*)malloc(sizeof(double) * 2 * (nk > 0 ? nk : 1));
+    double* S = (double*)calloc(n_shells, sizeof(double));
+    double na = 0;
+    for (int f = 0; f < nf; ++f) {
+      orc_rhok(r, n_atoms, list, n_list, &fr[f], 1, kvec_n, nk, spacing, box_len, ORC_F64, rho);
+      for (int m = 0; m < n_shells; ++m) {
+        int cnt = off[m + 1] - off[m];
+        double acc = 0;
+        for (int v = off[m]; v < off[m + 1]; ++v) acc += rho[2 * v] * rho[2 * v] + rho[2 * v + 1] * rho[2 * v + 1];
+        S[m] += cnt ? acc / cnt : 0;
+      }
+      na += n_list;
+    }
+    for (int m = 0; m < n_shells; ++m) sq[m] = na != 0 ? S[m] / na : 0;
+    free(rho); free(S);
+  }
+  free(fr);
+}
+
+/* ------------------------------------------------------------------------- */
+/* pair histograms                                                           */
+/* ------------------------------------------------------------------------- */
+
+/* Coordinate::length_unwrapped (coordinate.cpp:126-137) */
+static float min_image_len(float dx, float dy, float dz, const float* box) {
+  float ax = fabsf(dx), ay = fabsf(dy), az = fabsf(dz);
+  float bx = box[0] - ax, by = box[1] - ay, bz = box[2] - az;
+  float mx = ax < bx ? ax : bx, my = ay < by ? ay : by, mz = az < bz ? az : bz;
+  return sqrtf(mx * mx + my * my + mz * mz);
+}
+
+#define RDF_PI 3.1459265 /* radial_distribution_function.cpp:11, as written */
+
+void orc_rdf(const orc_scheme* s, int32_t ts, const float* r, int32_t n_atoms, const float* box,
+             const int32_t* list, int32_t n_list, int32_t n_bins, float max_distance,
+             int64_t* counts, double* mean_rdf) {
+  int T = orc_n_timesteps(s);
+  int* fr = (int*)malloc(sizeof(int) * (T + 1));
+  int nf = onetime_frames(s, ts, fr);
+  float bin_size = max_distance / (float)n_bins;
+  float* trdf = (float*)calloc((size_t)nf * n_bins, sizeof(float));
+  float* mean = (float*)calloc(n_bins, sizeof(float));
+  for (size_t i = 0; i < (size_t)nf * n_bins; ++i) counts[i] = 0;
+  for (int f = 0; f < nf; ++f) {
+    int t = fr[f];
+    for (int i = 0; i < n_list; ++i) {
+      int a = list[i];
+      for (int j = 0; j < n_list; ++j) {
+        int b = list[j];
+        if (a == b) continue;
+        float dx = POS(r, t, b, 0) - POS(r, t, a, 0);
+        float dy = POS(r, t, b, 1) - POS(r, t, a, 1);
+        float dz = POS(r, t, b, 2) - POS(r, t, a, 2);
+        float d = min_image_len(dx, dy, dz, box);
+        int bi = (int)(d / bin_size);
+        if (bi >= 0 && bi < n_bins) {
+          trdf[(size_t)f * n_bins + bi] += 1.0f;
+          counts[(size_t)f * n_bins + bi]++;
+        }
+      }
+    }
+  }
+  int ni_total = 0;
+  for (int f = 0; f < nf; ++f) {
+    float vol = box[0] * box[1] * box[2];
+    float rhoj = (float)n_list / vol;
+    ni_total += n_list;
+    for (int b = 0; b < n_bins; ++b) {
+      float rshell = (float)b * bin_size;
+      float shellvolume = (float)((4.0 / 3.0) * RDF_PI * (pow(rshell + bin_size, 3.0) - pow(rshell, 3.0)));
+      trdf[(size_t)f * n_bins + b] /= ((float)n_list * rhoj * shellvolume);
+      mean[b] += trdf[(size_t)f * n_bins + b] * (float)n_list;
+    }
+  }
+  for (int b = 0; b < n_bins; ++b) {
+    mean[b] /= (float)ni_total;
+    mean_rdf[b] = mean[b];
+  }
+  free(fr); free(trdf); free(mean);
+}
+
+void orc_vhd(const orc_scheme* s, int32_t fullblock, const float* r, int32_t n_atoms,
+             const float* box, const int32_t* list, int32_t n_list, float max_value,
+             int32_t n_bins, int64_t* counts, int64_t* weighting) {
+  int G = orc_n_timegaps(s);
+  pairs_t p = make_pairs(s, fullblock, 0);
+  float bin_size = max_value / (float)n_bins;
+  for (size_t i = 0; i < (size_t)G * n_bins; ++i) counts[i] = 0;
+  for (int g = 0; g < G; ++g) weighting[g] = 0;
+  for (int64_t q = 0; q < p.n; ++q) {
+    int g = p.gap[q], ta = p.t0[q], tb = p.t1[q];
+    weighting[g] += (int64_t)n_list * (n_list - 1);
+    for (int i = 0; i < n_list; ++i) {
+      int a = list[i];
+      for (int j = 0; j < n_list; ++j) {
+        int b = list[j];
+        if (a == b) continue;
+        float dx = POS(r, tb, b, 0) - POS(r, ta, a, 0);
+        float dy = POS(r, tb, b, 1) - POS(r, ta, a, 1);
+        float dz = POS(r, tb, b, 2) - POS(r, ta, a, 2);
+        float d = min_image_len(dx, dy, dz, box);
+        int bi = (int)(d / bin_size);
+        if (bi >= 0 && bi < n_bins) counts[(size_t)g * n_bins + bi]++;
+      }
+    }
+  }
+  free_pairs(&p);
+}
+
+/* ------------------------------------------------------------------------- */
+/* timed CPU baselines (FP64, OpenMP)                                        */
+/* ------------------------------------------------------------------------- */
+
+void orc_disp_fs_parallel(const orc_scheme* s, int32_t fullblock, const float* u,
+                          int32_t n_atoms, const int32_t* kvec_n, int32_t n_k, double box_len,
+                          int32_t n_threads, double* sum_d2, double* fs_sum) {
+  int G = orc_n_timegaps(s);
+  double tpl = TWO_PI / box_len;
+  pairs_t p = make_pairs(s, fullblock, 0);
+  for (int g = 0; g < G; ++g) { sum_d2[g] = 0; fs_sum[g] = 0; }
+#ifdef _OPENMP
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+#endif
+  for (int64_t i = 0; i < p.n; ++i) {
+    int g = p.gap[i], ta = p.t0[i], tb = p.t1[i];
+    double d2acc = 0, fsacc = 0;
+#pragma omp parallel for reduction(+ : d2acc, fsacc) schedule(static)
+    for (int a = 0; a < n_atoms; ++a) {
+      double dx = (double)POS(u, tb, a, 0) - (double)POS(u, ta, a, 0);
+      double dy = (double)POS(u, tb, a, 1) - (double)POS(u, ta, a, 1);
+      double dz = (double)POS(u, tb, a, 2) - (double)POS(u, ta, a, 2);
+      d2acc += dx * dx + dy * dy + dz * dz;
+      double f = 0;
+      for (int v = 0; v < n_k; ++v)
+        f += cos(tpl * (kvec_n[3 * v] * dx + kvec_n[3 * v + 1] * dy + kvec_n[3 * v + 2] * dz));
+      fsacc += f;
+    }
+    sum_d2[g] += d2acc;
+    fs_sum[g] += fsacc;
+  }
+  free_pairs(&p);
+}
+
+void orc_rhok_parallel(const float* r, int32_t n_atoms, const int32_t* frames, int32_t n_frames,
+                       const int32_t* kvec_n, int32_t n_k, double box_len, int32_t n_threads,
+                       double* rho) {
+  double tpl = TWO_PI / box_len;
+#ifdef _OPENMP
+  if (n_threads > 0) omp_set_num_threads(n_threads);
+#endif
+  for (int f = 0; f < n_frames; ++f) {
+    int t = frames[f];
+    double* out = rho + (size_t)f * n_k * 2;
+#pragma omp parallel for schedule(static)
+    for (int v = 0; v < n_k; ++v) {
+      double re = 0, im = 0;
+      double kx = tpl * kvec_n[3 * v], ky = tpl * kvec_n[3 * v + 1], kz = tpl * kvec_n[3 * v + 2];
+      for (int a = 0; a < n_atoms; ++a) {
+        double ph = kx * POS(r, t, a, 0) + ky * POS(r, t, a, 1) + kz * POS(r, t, a, 2);
+        re += cos(ph);
+        im += sin(ph);
+      }
+      out[2 * v] = re;
+      out[2 * v + 1] = im;
+    }
+  }
+}

@@ -1,0 +1,165 @@
+"""Generates the golden parity fixtures under tests/golden/<case>/.
+
+For each case: a seeded synthetic trajectory (amdat_gb300.synth) is written as
+a LAMMPS custom dump, the reference AMDAT binary (built from its own sources by
+oracle/ref.mk) runs an input script of the hot-path commands on it, and the
+fixture keeps
+  traj.npz    FP32 unwrapped positions, box, types, time scheme
+  script.in   the command part of the input script (after the system block)
+  *.dat       the reference's output files, verbatim.
+The reference tree itself is not needed to use the fixtures.
+Run: python tests/golden/make_golden.py [case ...]
+"""
+from __future__ import annotations
+
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+
+from amdat_gb300 import synth  # noqa: E402
+from oracle import build_oracle  # noqa: E402
+
+CASES = {
+    # single species, blocked-exponential scheme, all seven hot commands
+    "exp_small": dict(
+        n=216, box=8.0, sigma=0.5, seed=11, fractions=(1.0,),
+        scheme=synth.TimeScheme.exponential(4, 8, 1.3, 0, 0, 0.005),
+        commands="""create_list all
+all
+msd ./msd.dat
+list all
+ngp ./ngp.dat
+list all
+isfs ./isfs.dat 10 12 xyz 0
+list all
+isfs ./isfs_fb.dat 14 15 xyz 0 1
+list all
+vhs ./vhs.dat 0.5 50
+list all
+structure_factor ./sk.dat symmetric xyz 0 -1
+list all
+isf ./isf.dat auto symmetric xyz 0 0 20
+list all
+isf ./isf_fb.dat auto symmetric xyz 1 3 6
+list all
+rdf ./rdf.dat symmetric 100 -1 0
+list all
+limit 3
+msd ./msd_lim.dat
+list all
+isfs ./isfs_lim.dat 12 12 xyz 0 1
+list all
+"""),
+    # binary 80:20 mixture, linear scheme (its dropped-last-start quirk), type lists
+    "lin_binary": dict(
+        n=250, box=7.0, sigma=0.08, seed=22, fractions=(0.8, 0.2), time_scaled=False,
+        scheme=synth.TimeScheme.linear(20, 1.0),
+        commands="""create_list all
+all
+create_list a
+type_system 1
+create_list b
+type_system 2
+msd ./msd_a.dat
+list a
+ngp ./ngp_b.dat
+list b
+isfs ./isfs_a.dat 6 9 xyz 0
+list a
+vhs ./vhs.dat 1.0 40
+list all
+structure_factor ./sk_b.dat symmetric xyz 0 -1
+list b
+isf ./isf.dat auto symmetric xyz 0 0 15
+list all
+rdf ./rdf.dat symmetric 60 -1 0
+list all
+rdf ./rdf_a.dat symmetric 30 -1 2.5
+list a
+"""),
+    # frt = 1, first_exponent = 2, base 1.5 (other branches of create_timelist)
+    "exp_frt": dict(
+        n=64, box=5.0, sigma=0.3, seed=33, fractions=(1.0,),
+        scheme=synth.TimeScheme.exponential(5, 6, 1.5, 1, 2, 0.01),
+        commands="""create_list all
+all
+msd ./msd.dat
+list all
+ngp ./ngp.dat
+list all
+isfs ./isfs.dat 3 5 xyz 0 1
+list all
+vhs ./vhs.dat 0.8 20
+list all
+isf ./isf.dat auto symmetric xyz 1 0 8
+list all
+"""),
+}
+
+
+def make(case: str) -> None:
+    cfg = CASES[case]
+    ref = build_oracle.build_reference()
+    if ref is None:
+        raise SystemExit("reference source tree not found; set AMDAT_REFERENCE")
+    traj = synth.random_walk(cfg["n"], cfg["box"], cfg["scheme"], cfg["sigma"], cfg["seed"],
+                             type_fractions=cfg["fractions"],
+                             time_scaled=cfg.get("time_scaled", True))
+    out_dir = os.path.join(HERE, case)
+    os.makedirs(out_dir, exist_ok=True)
+    s = cfg["scheme"]
+    np.savez_compressed(os.path.join(out_dir, "traj.npz"), unwrapped=traj.unwrapped,
+                        box=traj.box, box_lo=traj.box_lo, types=traj.types,
+                        scheme=np.asarray([s.n_exponentials, s.n_exponential_steps, s.frt,
+                                           s.first_exponent]),
+                        scheme_f=np.asarray([s.exp_base, s.time_unit]),
+                        scheme_kind=np.asarray(s.kind))
+    with open(os.path.join(out_dir, "script.in"), "w") as f:
+        f.write(cfg["commands"])
+    with tempfile.TemporaryDirectory() as tmp:
+        dump = os.path.join(tmp, "traj.dump")
+        synth.write_custom_dump(traj, dump)
+        with open(os.path.join(tmp, "in.amdat"), "w") as f:
+            f.write(synth.system_header(traj, dump) + cfg["commands"])
+        r = subprocess.run([ref, "-i", "in.amdat"], cwd=tmp, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise SystemExit(f"reference failed on {case}:\n{r.stdout[-2000:]}\n{r.stderr[-2000:]}")
+        for fn in sorted(os.listdir(tmp)):
+            if fn.endswith(".dat"):
+                shutil.copy(os.path.join(tmp, fn), os.path.join(out_dir, fn))
+    print(case, "->", out_dir)
+
+
+def load(case: str):
+    """Fixture loader: (Trajectory, script text, {name: text})."""
+    d = os.path.join(HERE, case)
+    z = np.load(os.path.join(d, "traj.npz"))
+    kind = str(z["scheme_kind"])
+    a, b, frt, fe = (int(v) for v in z["scheme"])
+    base, unit = (float(v) for v in z["scheme_f"])
+    if kind == "linear":
+        s = synth.TimeScheme.linear(a + 1, unit)
+    else:
+        s = synth.TimeScheme.exponential(a, b, base, frt, fe, unit)
+    ntypes = int(z["types"].max()) + 1
+    traj = synth.Trajectory(unwrapped=z["unwrapped"], box=z["box"], box_lo=z["box_lo"],
+                            types=z["types"], scheme=s,
+                            type_names=tuple(str(i + 1) for i in range(ntypes)))
+    with open(os.path.join(d, "script.in")) as f:
+        script = f.read()
+    outs = {fn: open(os.path.join(d, fn)).read() for fn in sorted(os.listdir(d))
+            if fn.endswith(".dat")}
+    return traj, script, outs
+
+
+if __name__ == "__main__":
+    for c in (sys.argv[1:] or list(CASES)):
+        make(c)

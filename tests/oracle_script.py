@@ -1,0 +1,173 @@
+"""Runs an AMDAT command script through the C oracle and renders the output
+files the reference writes (test-side checker).
+
+Formats follow the reference writers: Mean_Square_Displacement::write
+(mean_square_displacement.cpp:186), Non_Gaussian_Parameter::write,
+Correlation_2D::write (correlation_2d.cpp:475-504),
+Space_Time_Correlation_Function::write (space_time_correlation_function.cpp:240),
+Structure_Factor::write (structure_factor.cpp:323-344) and
+Radial_Distribution_Function::write (radial_distribution_function.cpp:326).
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from amdat_files import fmt
+from oracle import oracle as orc
+from oracle import wavevectors as wv
+
+VERSION = "1.0.1"
+f32 = np.float32
+
+
+class OracleRun:
+    def __init__(self, traj, qvec, mode=orc.REF32):
+        self.traj = traj
+        self.mode = mode
+        self.qn, self.qoff = qvec
+        self.unwrapped = np.ascontiguousarray(traj.unwrapped, np.float32)
+        self.wrapped = traj.wrapped()
+        self.limit = 0
+        self.lists = {}
+        self.files = {}
+
+    def scheme(self):
+        return orc.scheme(self.traj.scheme, self.limit)
+
+    def shells(self, m0, m1):
+        kv = self.qn[self.qoff[m0]:self.qoff[m1 + 1]]
+        off = self.qoff[m0:m1 + 2] - self.qoff[m0]
+        return kv, off
+
+    def min_box(self):
+        return float(f32(self.traj.box.min()))
+
+    def run(self, script: str):
+        lines = [ln.strip() for ln in script.splitlines() if ln.strip()]
+        i = 0
+        while i < len(lines):
+            a = lines[i].split()
+            i += 1
+            cmd = a[0]
+            if cmd == "create_list":
+                sel = lines[i].split()
+                i += 1
+                self.lists[a[1]] = self.select(sel)
+                continue
+            if cmd == "limit":
+                self.limit = int(a[1])
+                continue
+            target = lines[i].split()
+            i += 1
+            lst = self.lists[target[1]]
+            getattr(self, "cmd_" + cmd)(a, lst)
+        return self.files
+
+    def select(self, sel):
+        if sel[0] == "all":
+            return np.arange(self.traj.n_atoms, dtype=np.int32)
+        if sel[0] == "type_system":
+            t = list(self.traj.type_names).index(sel[1])
+            return np.nonzero(self.traj.types == t)[0].astype(np.int32)
+        raise ValueError(sel)
+
+    def name(self, p):
+        return p.split("/")[-1]
+
+    def times(self, s):
+        return orc.displacement_times(s)
+
+    def cmd_msd(self, a, lst):
+        s = self.scheme()
+        m = orc.msd(s, self.unwrapped, lst, self.mode)
+        t = self.times(s)
+        txt = f"Mean square displacement data created by AMDAT v.{VERSION}\n"
+        txt += "".join(f"{fmt(t[g])}\t{fmt(f32(m[g]))}\n" for g in range(len(t)))
+        self.files[self.name(a[1])] = txt
+
+    def cmd_ngp(self, a, lst):
+        s = self.scheme()
+        q = orc.ngp(s, self.unwrapped, lst, self.mode)
+        t = self.times(s)
+        txt = f"Non-Gaussian parameter data created by AMDAT v.{VERSION}\n"
+        txt += "".join(f"{fmt(t[g])}\t{fmt(f32(q[g]))}\n" for g in range(len(t)))
+        self.files[self.name(a[1])] = txt
+
+    def correlation_2d(self, sp, m0, m1, corr, s):
+        approx = wv.approx_wavenumbers(sp)
+        t = self.times(s)
+        txt = f"Correlation data created by AMDAT v.{VERSION}\n\t"
+        txt += "".join(fmt(approx[m]) + "\t" for m in range(m0, m1 + 1)) + "\n"
+        for g in range(len(t)):
+            txt += fmt(t[g]) + "\t" + "".join(fmt(f32(v)) + "\t" for v in corr[g]) + "\n"
+        return txt
+
+    def cmd_isfs(self, a, lst):
+        m0, m1 = int(a[2]), int(a[3])
+        maxlen = float(a[5])
+        fb = int(a[6]) if len(a) > 6 else 0
+        L = maxlen if maxlen > 0 else self.min_box()
+        sp = wv.spacing(L)
+        kv, off = self.shells(m0, m1)
+        s = self.scheme()
+        corr = orc.isfs(s, self.unwrapped, lst, kv, off, float(sp), L, fb, self.mode)
+        self.files[self.name(a[1])] = self.correlation_2d(sp, m0, m1, corr, s)
+
+    def cmd_isf(self, a, lst):
+        fb = int(a[5])
+        m0, m1 = int(a[6]), int(a[7])
+        L = self.min_box()
+        sp = wv.spacing(L)
+        kv, off = self.shells(m0, m1)
+        s = self.scheme()
+        frames = np.arange(orc.n_timesteps(s), dtype=np.int32)
+        rho = orc.rhok(self.wrapped, lst, frames, kv, float(sp), L, self.mode)
+        corr = orc.isf(s, rho, rho, off, len(lst), fb, self.mode)
+        self.files[self.name(a[1])] = self.correlation_2d(sp, m0, m1, corr, s)
+
+    def cmd_vhs(self, a, lst):
+        rmax, nb = float(a[2]), int(a[3])
+        vmax = f32(rmax) if f32(rmax) != 0 else f32(f32(self.traj.box.min()) / f32(2))
+        s = self.scheme()
+        counts, w, corr = orc.vhs(s, self.unwrapped, lst, float(vmax), nb)
+        bs = f32(vmax / f32(nb))
+        t = self.times(s)
+        txt = f"Correlation data created by AMDAT v.{VERSION}\n{nb} bins\n{len(t)} times\n\n\t"
+        txt += "".join(fmt(f32(f32(bs / f32(2)) + f32(f32(b) * bs))) + "\t" for b in range(nb)) + "\n"
+        for g in range(len(t)):
+            vals = [fmt(f32(v)) for v in corr[g]]
+            txt += fmt(t[g]) + "\t" + "".join(v + "\t" for v in vals[:-1]) + vals[-1] + "\n"
+        self.files[self.name(a[1])] = txt
+
+    def cmd_structure_factor(self, a, lst):
+        maxlen = float(a[4])
+        ts = int(a[5])
+        L = maxlen if maxlen > 0 else self.min_box()
+        sp = wv.spacing(L)
+        kv, off = self.shells(0, 98)
+        s = self.scheme()
+        S = orc.structure_factor(s, ts, self.wrapped, lst, kv, off, float(sp), L, self.mode)
+        approx = wv.approx_wavenumbers(sp)
+        txt = (f"Structure factor data created by AMDAT v.{VERSION}\n"
+               "Nominal_q\tMean_q\tStddev_q\tMean_qx\tMean_qy\tMean_qz\tS(q)\n")
+        for m in range(99):
+            vecs = wv.shell_vectors(kv[off[m]:off[m + 1]], sp)
+            mv = wv.mean_wavevector(vecs)
+            txt += "\t".join([fmt(approx[m]), fmt(wv.mean_wavenumber(vecs)),
+                              fmt(wv.stdev_wavenumber(vecs)), fmt(mv[0]), fmt(mv[1]), fmt(mv[2]),
+                              fmt(f32(S[m]))]) + "\n"
+        txt += "\n"
+        self.files[self.name(a[1])] = txt
+
+    def cmd_rdf(self, a, lst):
+        nb, ts, maxlen = int(a[3]), int(a[4]), float(a[5])
+        minbox = f32(self.traj.box.min())
+        maxd = f32(maxlen) if (f32(maxlen) > 0 and f32(maxlen) < f32(minbox / f32(2))) \
+            else f32(minbox / f32(2))
+        s = self.scheme()
+        counts, mean = orc.rdf(s, ts, self.wrapped, self.traj.box, lst, nb, float(maxd))
+        bs = f32(maxd / f32(nb))
+        txt = f"Radial distribution function data created by AMDAT v.{VERSION}\n"
+        txt += "".join(fmt(f32(f32(f32(b) * bs) + f32(bs / f32(2)))) + "\t" for b in range(nb)) + "\n"
+        txt += "".join(fmt(f32(v)) + "\t" for v in mean) + "\n"
+        self.files[self.name(a[1])] = txt
