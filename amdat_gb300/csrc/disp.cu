@@ -1,0 +1,699 @@
+// Displacement family on the GPU: the per-atom kernels of
+//   Mean_Square_Displacement::listkernel   (src/mean_square_displacement.cpp:164)
+//   Non_Gaussian_Parameter::listkernel     (src/non_gaussian_parameter.cpp:125)
+//   Incoherent_Scattering_Function::listkernel (src/incoherent_scattering_function.cpp:272)
+//   Van_Hove_Self::listkernel + bin        (src/van_hove_self.cpp:98,
+//                                           src/space_time_correlation_function.cpp:216)
+// fused into one pass over every (list, time pair, atom) of the time-pair
+// scheduler (System::displacement_list, src/system.cpp:4090).
+//
+// Work is cut into items (list, time pair, range of <= CHUNK list members).
+// A persistent grid (a few blocks per SM) pulls items from an atomic counter.
+// Per item a block streams u(t0), u(t1) for its atoms from the FP32 planes,
+// accumulates |dr|^2, |dr|^4 and the F_s shell means with Kahan-compensated
+// FP32 per thread, reduces them with compensated warp shuffles, and writes
+// one FP64 partial per output; G_s counts go to a shared-memory histogram and
+// are flushed with integer atomics (order-independent, exact).  A finalize
+// kernel adds the partials of each (list, gap) in a fixed order in FP64, so
+// results are deterministic run to run.
+//
+// F_s phases: the displacement is turned into a fixed-point fraction of the
+// box per axis (units of 2^-31 turns, int32), so the phase of n.dr/L for any
+// integer lattice vector n is an exact integer combination (wrapping int32
+// arithmetic is arithmetic modulo whole turns) and only the final conversion
+// rounds; cos is then cospif of that phase.  Two shell modes:
+//   list mode    - any vector set (e.g. the reference's q-vector files):
+//                  one cospif per vector;
+//   octant mode  - shells closed under sign flips of each component (whole
+//                  lattice shells): sum_k cos(k.dr) = sum over octant
+//                  representatives of w * cos(2pi nx tx) cos(2pi ny ty)
+//                  cos(2pi nz tz), with per-axis cosine tables in shared memory,
+//                  so a vector costs ~0.6 FMA instead of a cosine.
+#include <algorithm>
+#include <array>
+#include <map>
+#include <cmath>
+#include <cstring>
+
+#include "engine.h"
+
+namespace amdat {
+
+constexpr int DISP_CHUNK = 4096;  // list members per item
+constexpr int MAX_FS = 8;         // shells per pass
+constexpr int DISP_THREADS = 256;
+constexpr int FS_THREADS = 128;
+
+struct DispItem {
+  int32_t list;  // slot in the launch's list table
+  int32_t pair;
+  int32_t a0, a1;  // member range [a0, a1) of the list
+};
+
+struct ListDev {
+  int32_t n;
+  int32_t first;
+  const int32_t* idx;  // nullptr: members are atoms first..first+n-1
+};
+
+struct DispParams {
+  const float* u;
+  int64_t n_pad;
+  const int32_t* t0;
+  const int32_t* t1;
+  const int32_t* gap;
+  const DispItem* items;
+  int32_t n_items;
+  const ListDev* lists;
+  int32_t* counter;
+  double* part;  // [n_items][n_out]
+  int32_t n_out;
+  int32_t want_moments;
+  // G_s
+  unsigned long long* gs;  // [list][gap][bin]
+  int32_t n_gaps;
+  int32_t n_bins;
+  float bin_size;
+  // F_s
+  int32_t n_fs;              // shells in this pass (<= MAX_FS)
+  int32_t fs_mode;           // 0 none, 1 list, 2 octant
+  const int4* kv;            // list mode: (nx, ny, nz, _) per vector
+  const int32_t* kv_off;     // [n_fs + 1]
+  const float* inv_count;    // [n_fs] 1 / vectors in shell
+  int32_t nmax;              // octant mode table size - 1
+  float period;              // L of k = 2 pi n / L
+};
+
+// --- compensated FP32 helpers ------------------------------------------------
+struct KSum {
+  float s, c;
+};
+__device__ __forceinline__ void kadd(KSum& k, float v) {
+  float y = __fsub_rn(v, k.c);
+  float t = __fadd_rn(k.s, y);
+  k.c = __fsub_rn(__fsub_rn(t, k.s), y);
+  k.s = t;
+}
+// error-free sum of two compensated values (TwoSum of the leading parts)
+__device__ __forceinline__ KSum kmerge(KSum a, KSum b) {
+  float s = __fadd_rn(a.s, b.s);
+  float bb = __fsub_rn(s, a.s);
+  float err = __fadd_rn(__fsub_rn(a.s, __fsub_rn(s, bb)), __fsub_rn(b.s, bb));
+  // a KSum holds the value s - c: (a.s - a.c) + (b.s - b.c) = s + err - a.c - b.c
+  KSum r;
+  r.s = s;
+  r.c = __fsub_rn(__fadd_rn(a.c, b.c), err);
+  return r;
+}
+__device__ __forceinline__ KSum kshfl(KSum v, int off) {
+  KSum o;
+  o.s = __shfl_down_sync(0xffffffffu, v.s, off);
+  o.c = __shfl_down_sync(0xffffffffu, v.c, off);
+  return o;
+}
+
+// fraction of a turn dr/L, as int32 in units of 2^-31 turns (exact wrap)
+__device__ __forceinline__ int32_t turns_fixed(float d, float period) {
+  float t = __fdiv_rn(d, period);
+  t = __fsub_rn(t, rintf(t));  // [-0.5, 0.5]
+  return __float2int_rn(__fmul_rn(t, 2147483648.0f));
+}
+// cos(2 pi * phase * 2^-31)
+__device__ __forceinline__ float cos_fixed(int32_t phase) {
+  return cospif(__fmul_rn((float)phase, 9.313225746154785e-10f));  // 2^-30
+}
+
+template <int MODE, bool GS>
+__global__ void __launch_bounds__(MODE == 0 ? DISP_THREADS : FS_THREADS)
+    disp_mixed_kernel(DispParams p) {
+  extern __shared__ float smem[];
+  __shared__ int s_item;
+  __shared__ KSum s_red[(MODE == 0 ? DISP_THREADS : FS_THREADS) / 32][2 + MAX_FS];
+  unsigned int* hist = reinterpret_cast<unsigned int*>(smem);  // [n_bins] when GS
+  float* tab = smem + (GS ? ((p.n_bins + 3) & ~3) : 0);         // octant tables
+  const int tid = threadIdx.x, nthr = blockDim.x;
+  const int lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
+  const int n_fs = MODE ? p.n_fs : 0;
+
+  for (;;) {
+    if (tid == 0) s_item = atomicAdd(p.counter, 1);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= p.n_items) break;
+    const DispItem it = p.items[item];
+    const ListDev L = p.lists[it.list];
+    const int t0 = p.t0[it.pair], t1 = p.t1[it.pair], g = p.gap[it.pair];
+    const float* X0 = p.u + (int64_t)t0 * 3 * p.n_pad;
+    const float* X1 = p.u + (int64_t)t1 * 3 * p.n_pad;
+    if (GS)
+      for (int b = tid; b < p.n_bins; b += nthr) hist[b] = 0u;
+    if (GS) __syncthreads();
+
+    KSum m2 = {0.f, 0.f}, m4 = {0.f, 0.f};
+    KSum fs[MAX_FS];
+#pragma unroll
+    for (int s = 0; s < MAX_FS; ++s) fs[s] = KSum{0.f, 0.f};
+
+    for (int a = it.a0 + tid; a < it.a1; a += nthr) {
+      const int atom = L.idx ? __ldg(L.idx + a) : L.first + a;
+      const float dx = __fsub_rn(__ldg(X1 + atom), __ldg(X0 + atom));
+      const float dy = __fsub_rn(__ldg(X1 + p.n_pad + atom), __ldg(X0 + p.n_pad + atom));
+      const float dz = __fsub_rn(__ldg(X1 + 2 * p.n_pad + atom), __ldg(X0 + 2 * p.n_pad + atom));
+      if (p.want_moments) {
+        const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        kadd(m2, d2);
+        kadd(m4, d2 * d2);
+      }
+      if (GS) {
+        // the reference's FP32 chain: sqrt((dx*dx + dy*dy) + dz*dz) / bin_size
+        const float s2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+        const int b = (int)__fdiv_rn(__fsqrt_rn(s2), p.bin_size);
+        if (b >= 0 && b < p.n_bins) atomicAdd(hist + b, 1u);
+      }
+      if (MODE == 1) {
+        const int32_t fx = turns_fixed(dx, p.period);
+        const int32_t fy = turns_fixed(dy, p.period);
+        const int32_t fz = turns_fixed(dz, p.period);
+        for (int s = 0; s < n_fs; ++s) {
+          KSum acc = {0.f, 0.f};
+          float blk = 0.f;
+          int cnt = 0;
+          for (int v = p.kv_off[s]; v < p.kv_off[s + 1]; ++v) {
+            const int4 n = __ldg(p.kv + v);
+            const int32_t ph = (int32_t)((uint32_t)n.x * (uint32_t)fx + (uint32_t)n.y * (uint32_t)fy +
+                                         (uint32_t)n.z * (uint32_t)fz);
+            blk += cos_fixed(ph);
+            if (++cnt == 32) {
+              kadd(acc, blk);
+              blk = 0.f;
+              cnt = 0;
+            }
+          }
+          kadd(acc, blk);
+          kadd(fs[s], __fmul_rn(__fsub_rn(acc.s, acc.c), p.inv_count[s]));
+        }
+      }
+      if (MODE == 2) {
+        // per-thread cosine tables cos(2 pi n t_axis), n = 0..nmax, layout
+        // [axis][n][thread] (conflict-free: each thread owns a column)
+        const int32_t f[3] = {turns_fixed(dx, p.period), turns_fixed(dy, p.period),
+                              turns_fixed(dz, p.period)};
+        const int stride = (p.nmax + 1) * nthr;
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax)
+          for (int n = 0; n <= p.nmax; ++n)
+            tab[ax * stride + n * nthr + tid] = cos_fixed((int32_t)((uint32_t)n * (uint32_t)f[ax]));
+        const float* cx = tab + tid;
+        const float* cy = tab + stride + tid;
+        const float* cz = tab + 2 * stride + tid;
+        for (int s = 0; s < n_fs; ++s) {
+          KSum acc = {0.f, 0.f};
+          float blk = 0.f;
+          int cnt = 0;
+          for (int v = p.kv_off[s]; v < p.kv_off[s + 1]; ++v) {
+            const int4 r = __ldg(p.kv + v);  // octant representative, .w = multiplicity
+            blk = fmaf((float)r.w * cx[r.x * nthr] * cy[r.y * nthr], cz[r.z * nthr], blk);
+            if (++cnt == 32) {
+              kadd(acc, blk);
+              blk = 0.f;
+              cnt = 0;
+            }
+          }
+          kadd(acc, blk);
+          kadd(fs[s], __fmul_rn(__fsub_rn(acc.s, acc.c), p.inv_count[s]));
+        }
+      }
+    }
+
+    // block reduction of the compensated sums
+    const int n_red = 2 + n_fs;
+    for (int k = 0; k < n_red; ++k) {
+      KSum v = k == 0 ? m2 : (k == 1 ? m4 : fs[0]);
+      if (MODE) {
+#pragma unroll
+        for (int s = 0; s < MAX_FS; ++s)
+          if (k == 2 + s) v = fs[s];
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) v = kmerge(v, kshfl(v, off));
+      if (lane == 0) s_red[warp][k] = v;
+    }
+    __syncthreads();
+    if (tid < n_red) {
+      double acc = 0.0;
+      for (int w = 0; w < nwarp; ++w) acc += (double)s_red[w][tid].s - (double)s_red[w][tid].c;
+      p.part[(int64_t)item * p.n_out + tid] = acc;
+    }
+    if (GS) {
+      __syncthreads();
+      unsigned long long* dst = p.gs + ((int64_t)it.list * p.n_gaps + g) * p.n_bins;
+      for (int b = tid; b < p.n_bins; b += nthr)
+        if (hist[b]) atomicAdd(dst + b, (unsigned long long)hist[b]);
+    }
+    __syncthreads();
+  }
+}
+
+// Sums the partials of each (list, gap) in a fixed order (FP64).
+__global__ void disp_finalize_kernel(const double* __restrict__ part, int32_t n_out,
+                                     const int32_t* __restrict__ item_first,  // [n_lists*G + 1]
+                                     int32_t k_begin, double* __restrict__ out_d2,
+                                     double* __restrict__ out_d4, double* __restrict__ out_fs,
+                                     int32_t fs_stride, int32_t fs_offset, int32_t n_fs,
+                                     int32_t want_moments) {
+  const int lg = blockIdx.x;
+  const int i0 = item_first[lg], i1 = item_first[lg + 1];
+  __shared__ double red[8][32];
+  const int n_red = 2 + n_fs;
+  for (int k = 0; k < n_red; ++k) {
+    double acc = 0.0;
+    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) acc += part[(int64_t)i * n_out + k];
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][k & 31] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w][k & 31];
+      if (k == 0 && want_moments && out_d2) out_d2[lg] = t;
+      if (k == 1 && want_moments && out_d4) out_d4[lg] = t;
+      if (k >= 2 && out_fs) out_fs[(int64_t)lg * fs_stride + fs_offset + (k - 2)] = t;
+    }
+    __syncthreads();
+  }
+  (void)k_begin;
+}
+
+// ---------------------------------------------------------------------------
+// plain FP64 path: one thread per (pair, atom), FP64 arithmetic, direct cos,
+// block reduction then one FP64 atomic per block and output
+// ---------------------------------------------------------------------------
+struct PlainParams {
+  const double* u;
+  int64_t n_pad;
+  const int32_t* t0;
+  const int32_t* t1;
+  const int32_t* gap;
+  int64_t n_pairs;
+  ListDev list;
+  int32_t blocks_per_pair;
+  double* d2;  // [G]
+  double* d4;
+  double* fs;  // [G][S]
+  int32_t n_shells;
+  const int4* kv;
+  const int32_t* kv_off;
+  double two_pi_over_l;
+  unsigned long long* gs;
+  int32_t n_bins;
+  double bin_size;
+};
+
+__global__ void disp_plain_kernel(PlainParams p) {
+  const int64_t pair = blockIdx.x / p.blocks_per_pair;
+  const int a = (int)(blockIdx.x % p.blocks_per_pair) * blockDim.x + threadIdx.x;
+  __shared__ double red[32];
+  double v2 = 0, v4 = 0;
+  double dx = 0, dy = 0, dz = 0;
+  bool live = a < p.list.n;
+  const int g = p.gap[pair];
+  if (live) {
+    const int atom = p.list.idx ? p.list.idx[a] : p.list.first + a;
+    const double* X0 = p.u + (int64_t)p.t0[pair] * 3 * p.n_pad;
+    const double* X1 = p.u + (int64_t)p.t1[pair] * 3 * p.n_pad;
+    dx = X1[atom] - X0[atom];
+    dy = X1[p.n_pad + atom] - X0[p.n_pad + atom];
+    dz = X1[2 * p.n_pad + atom] - X0[2 * p.n_pad + atom];
+    v2 = dx * dx + dy * dy + dz * dz;
+    v4 = v2 * v2;
+    if (p.n_bins > 0) {
+      const int b = (int)(sqrt(v2) / p.bin_size);
+      if (b >= 0 && b < p.n_bins) atomicAdd(p.gs + (int64_t)g * p.n_bins + b, 1ull);
+    }
+  }
+  auto block_sum = [&](double v) -> double {
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    __syncthreads();
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double t = 0;
+    if (threadIdx.x == 0)
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+    return t;
+  };
+  double s2 = block_sum(v2);
+  double s4 = block_sum(v4);
+  if (threadIdx.x == 0) {
+    atomicAdd(p.d2 + g, s2);
+    atomicAdd(p.d4 + g, s4);
+  }
+  for (int s = 0; s < p.n_shells; ++s) {
+    double f = 0;
+    if (live) {
+      const int cnt = p.kv_off[s + 1] - p.kv_off[s];
+      for (int v = p.kv_off[s]; v < p.kv_off[s + 1]; ++v) {
+        const int4 n = p.kv[v];
+        f += cos(p.two_pi_over_l * (n.x * dx + n.y * dy + n.z * dz));
+      }
+      f /= cnt;
+    }
+    double sf = block_sum(f);
+    if (threadIdx.x == 0) atomicAdd(p.fs + (int64_t)g * p.n_shells + s, sf);
+  }
+}
+
+void ensure_fp64(amdat_ctx* ctx);
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+struct ShellSet {
+  int mode = 0;             // 1 list, 2 octant
+  std::vector<int4> kv;     // vectors or octant representatives
+  std::vector<int32_t> off; // [n + 1]
+  std::vector<float> inv_count;
+  int nmax = 0;
+};
+
+// Octant reduction of shells that are closed under sign flips of each
+// component; returns false when some shell is not (then list mode is used).
+static bool octant_shells(const int32_t* off, const int32_t* kvec, int n_shells, ShellSet& out) {
+  out.kv.clear();
+  out.off.assign(1, 0);
+  out.inv_count.clear();
+  out.nmax = 0;
+  for (int s = 0; s < n_shells; ++s) {
+    std::map<std::array<int, 3>, int> seen;
+    for (int v = off[s]; v < off[s + 1]; ++v) seen[{kvec[3 * v], kvec[3 * v + 1], kvec[3 * v + 2]}]++;
+    for (auto& kvp : seen) {
+      if (kvp.second != 1) return false;
+      const auto& n = kvp.first;
+      for (int m = 1; m < 8; ++m) {
+        std::array<int, 3> q = {(m & 1) ? -n[0] : n[0], (m & 2) ? -n[1] : n[1], (m & 4) ? -n[2] : n[2]};
+        if (!seen.count(q)) return false;
+      }
+    }
+    for (auto& kvp : seen) {
+      const auto& n = kvp.first;
+      if (n[0] < 0 || n[1] < 0 || n[2] < 0) continue;
+      const int w = (n[0] ? 2 : 1) * (n[1] ? 2 : 1) * (n[2] ? 2 : 1);
+      out.kv.push_back(make_int4(n[0], n[1], n[2], w));
+      out.nmax = std::max(out.nmax, std::max(n[0], std::max(n[1], n[2])));
+    }
+    out.off.push_back((int32_t)out.kv.size());
+    const int cnt = off[s + 1] - off[s];
+    out.inv_count.push_back(cnt ? 1.0f / (float)cnt : 0.0f);
+  }
+  out.mode = 2;
+  return true;
+}
+
+static void list_shells(const int32_t* off, const int32_t* kvec, int n_shells, ShellSet& out) {
+  out.kv.clear();
+  out.off.assign(1, 0);
+  out.inv_count.clear();
+  for (int s = 0; s < n_shells; ++s) {
+    for (int v = off[s]; v < off[s + 1]; ++v)
+      out.kv.push_back(make_int4(kvec[3 * v], kvec[3 * v + 1], kvec[3 * v + 2], 0));
+    out.off.push_back((int32_t)out.kv.size());
+    const int cnt = off[s + 1] - off[s];
+    out.inv_count.push_back(cnt ? 1.0f / (float)cnt : 0.0f);
+  }
+  out.mode = 1;
+}
+
+static void check_request(amdat_ctx* ctx, const amdat_disp_request* r) {
+  AMDAT_REQUIRE(r != nullptr, "null request");
+  if (!ctx->have_traj) throw Error(AMDAT_ERR_STATE, "no trajectory uploaded");
+  AMDAT_REQUIRE(r->precision == AMDAT_MIXED || r->precision == AMDAT_PLAIN_FP64, "bad precision");
+  AMDAT_REQUIRE(r->n_shells >= 0 && r->n_bins >= 0, "negative shell or bin count");
+  if (r->n_shells > 0) {
+    AMDAT_REQUIRE(r->shell_offsets && r->kvec_n, "F_s requested without vectors");
+    AMDAT_REQUIRE(r->kvec_period > 0.0f, "kvec_period must be positive");
+    AMDAT_REQUIRE(r->shell_offsets[0] == 0, "shell_offsets[0] must be 0");
+    for (int s = 0; s < r->n_shells; ++s)
+      AMDAT_REQUIRE(r->shell_offsets[s + 1] >= r->shell_offsets[s], "shell_offsets must ascend");
+    const int nk = r->shell_offsets[r->n_shells];
+    for (int i = 0; i < 3 * nk; ++i)
+      AMDAT_REQUIRE(std::abs(r->kvec_n[i]) < (1 << 20), "lattice index too large");
+  }
+  if (r->n_bins > 0) {
+    AMDAT_REQUIRE(r->bin_max > 0.0f, "bin_max must be positive");
+    AMDAT_REQUIRE(r->n_bins <= 16384, "at most 16384 G_s bins");
+  }
+}
+
+template <class T>
+static void to_out(amdat_ctx* ctx, T* dst, const T* dev_src, size_t n, int32_t flags) {
+  if (!dst || n == 0) return;
+  AMDAT_CUDA(cudaMemcpyAsync(dst, dev_src, n * sizeof(T),
+                             flags == AMDAT_OUT_DEVICE ? cudaMemcpyDeviceToDevice
+                                                       : cudaMemcpyDeviceToHost,
+                             ctx->stream));
+}
+
+static void disp_run_impl(amdat_ctx* ctx, const amdat_disp_request* req, const int32_t* lists,
+                          int32_t n_lists, int32_t out_flags, double* sum_d2, double* sum_d4,
+                          int64_t* atom_pairs, double* fs_sum, int64_t* gs_counts) {
+  check_request(ctx, req);
+  AMDAT_REQUIRE(n_lists >= 1, "need >= 1 list");
+  AMDAT_REQUIRE(out_flags == AMDAT_OUT_HOST || out_flags == AMDAT_OUT_DEVICE, "bad out_flags");
+  const PairTable& P = pair_table(ctx, req->fullblock != 0, false);
+  const int G = P.n_gaps;
+  const int S = req->n_shells;
+  const int NB = req->n_bins;
+
+  // list table and item table (list-major, pair-major, chunk)
+  std::vector<ListDev> ldev(n_lists);
+  std::vector<int32_t> lsize(n_lists);
+  for (int l = 0; l < n_lists; ++l) {
+    const ListEntry& e = list_entry(ctx, lists[l]);
+    ldev[l] = ListDev{e.n, e.first, e.contiguous ? nullptr : e.idx.ptr};
+    lsize[l] = e.n;
+  }
+  // atom_pairs: list size (membership is static) per pair of the gap
+  std::vector<int64_t> counts((size_t)n_lists * G, 0);
+  for (int l = 0; l < n_lists; ++l)
+    for (int g = 0; g < G; ++g)
+      counts[(size_t)l * G + g] = (int64_t)lsize[l] * (P.gap_first[g + 1] - P.gap_first[g]);
+
+  // scratch layout
+  const double h_unused = 0;
+  (void)h_unused;
+  double* d_out_d2 = nullptr;
+  double* d_out_d4 = nullptr;
+  double* d_out_fs = nullptr;
+  unsigned long long* d_out_gs = nullptr;
+  const size_t n_lg = (size_t)n_lists * G;
+
+  if (req->precision == AMDAT_PLAIN_FP64) {
+    AMDAT_REQUIRE(n_lists == 1, "the plain FP64 path runs one list per call");
+    ensure_fp64(ctx);
+    const size_t bytes = n_lg * (2 + S) * sizeof(double) + n_lg * NB * sizeof(unsigned long long) +
+                         (S ? (size_t)(req->shell_offsets[S]) * sizeof(int4) + (S + 1) * 4 : 0) + 256;
+    unsigned char* base = ctx->scratch.reserve(bytes);
+    AMDAT_CUDA(cudaMemsetAsync(base, 0, bytes, ctx->stream));
+    d_out_d2 = (double*)base;
+    d_out_d4 = d_out_d2 + n_lg;
+    d_out_fs = d_out_d4 + n_lg;
+    d_out_gs = (unsigned long long*)(d_out_fs + n_lg * S);
+    int4* d_kv = (int4*)(((uintptr_t)(d_out_gs + n_lg * NB) + 15) & ~(uintptr_t)15);
+    int32_t* d_off = nullptr;
+    if (S) {
+      ShellSet sh;
+      list_shells(req->shell_offsets, req->kvec_n, S, sh);
+      d_off = (int32_t*)(d_kv + sh.kv.size());
+      AMDAT_CUDA(cudaMemcpyAsync(d_kv, sh.kv.data(), sh.kv.size() * sizeof(int4), cudaMemcpyHostToDevice, ctx->stream));
+      AMDAT_CUDA(cudaMemcpyAsync(d_off, sh.off.data(), sh.off.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    PlainParams pp{};
+    pp.u = ctx->u64.ptr;
+    pp.n_pad = ctx->n_pad;
+    pp.t0 = P.t0.ptr;
+    pp.t1 = P.t1.ptr;
+    pp.gap = P.gap.ptr;
+    pp.n_pairs = P.n_pairs;
+    pp.list = ldev[0];
+    pp.blocks_per_pair = (int32_t)std::max<int64_t>(1, ceil_div(lsize[0], 256));
+    pp.d2 = d_out_d2;
+    pp.d4 = d_out_d4;
+    pp.fs = d_out_fs;
+    pp.n_shells = S;
+    pp.kv = d_kv;
+    pp.kv_off = d_off;
+    pp.two_pi_over_l = S ? 6.283185307179586476925286766559 / (double)req->kvec_period : 0.0;
+    pp.gs = d_out_gs;
+    pp.n_bins = NB;
+    pp.bin_size = NB ? (double)(req->bin_max / (float)NB) : 1.0;
+    const int64_t blocks = P.n_pairs * pp.blocks_per_pair;
+    if (blocks > 0 && lsize[0] > 0) {
+      disp_plain_kernel<<<(unsigned)blocks, 256, 0, ctx->stream>>>(pp);
+      check_launch("disp_plain_kernel");
+      count_launch(ctx);
+    }
+  } else {
+    // ---- mixed path
+    ShellSet sh;
+    if (S) {
+      if (!octant_shells(req->shell_offsets, req->kvec_n, S, sh) || sh.nmax > 48)
+        list_shells(req->shell_offsets, req->kvec_n, S, sh);
+    }
+    std::vector<DispItem> items;
+    std::vector<int32_t> item_first(n_lg + 1, 0);
+    for (int l = 0; l < n_lists; ++l) {
+      const int nch = (int)std::max<int64_t>(1, ceil_div(lsize[l], DISP_CHUNK));
+      for (int g = 0; g < G; ++g) {
+        item_first[(size_t)l * G + g] = (int32_t)items.size();
+        if (lsize[l] == 0) continue;
+        for (int pr = P.gap_first[g]; pr < P.gap_first[g + 1]; ++pr)
+          for (int c = 0; c < nch; ++c) {
+            const int a0 = (int)((int64_t)lsize[l] * c / nch);
+            const int a1 = (int)((int64_t)lsize[l] * (c + 1) / nch);
+            items.push_back(DispItem{l, pr, a0, a1});
+          }
+      }
+    }
+    item_first[n_lg] = (int32_t)items.size();
+    const int n_items = (int)items.size();
+    const int n_passes = S ? (int)ceil_div(S, MAX_FS) : 1;
+    const int max_fs_pass = S ? std::min(S, MAX_FS) : 0;
+    const int n_out = 2 + max_fs_pass;
+
+    // scratch: [items | item_first | lists | counter | part | outputs | gs | kv | off | invc]
+    auto align = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    size_t o = 0;
+    const size_t o_items = o; o = align(o + items.size() * sizeof(DispItem));
+    const size_t o_first = o; o = align(o + item_first.size() * 4);
+    const size_t o_lists = o; o = align(o + ldev.size() * sizeof(ListDev));
+    const size_t o_counter = o; o = align(o + 4 * (size_t)n_passes);
+    const size_t o_part = o; o = align(o + (size_t)std::max(n_items, 1) * n_out * sizeof(double));
+    const size_t o_d2 = o; o = align(o + n_lg * sizeof(double));
+    const size_t o_d4 = o; o = align(o + n_lg * sizeof(double));
+    const size_t o_fs = o; o = align(o + n_lg * std::max(S, 1) * sizeof(double));
+    const size_t o_gs = o; o = align(o + n_lg * std::max(NB, 1) * sizeof(unsigned long long));
+    const size_t o_kv = o; o = align(o + std::max<size_t>(sh.kv.size(), 1) * sizeof(int4));
+    const size_t o_off = o; o = align(o + std::max<size_t>(sh.off.size(), 1) * 4);
+    const size_t o_inv = o; o = align(o + std::max<size_t>(sh.inv_count.size(), 1) * 4);
+    unsigned char* base = ctx->scratch.reserve(o);
+    // host staging of the small tables in one buffer, one copy
+    std::vector<unsigned char> host(o_part, 0);
+    std::memcpy(host.data() + o_items, items.data(), items.size() * sizeof(DispItem));
+    std::memcpy(host.data() + o_first, item_first.data(), item_first.size() * 4);
+    std::memcpy(host.data() + o_lists, ldev.data(), ldev.size() * sizeof(ListDev));
+    AMDAT_CUDA(cudaMemcpyAsync(base, host.data(), o_part, cudaMemcpyHostToDevice, ctx->stream));
+    if (S) {
+      AMDAT_CUDA(cudaMemcpyAsync(base + o_kv, sh.kv.data(), sh.kv.size() * sizeof(int4), cudaMemcpyHostToDevice, ctx->stream));
+      AMDAT_CUDA(cudaMemcpyAsync(base + o_off, sh.off.data(), sh.off.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+      AMDAT_CUDA(cudaMemcpyAsync(base + o_inv, sh.inv_count.data(), sh.inv_count.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    if (NB) AMDAT_CUDA(cudaMemsetAsync(base + o_gs, 0, n_lg * NB * sizeof(unsigned long long), ctx->stream));
+    d_out_d2 = (double*)(base + o_d2);
+    d_out_d4 = (double*)(base + o_d4);
+    d_out_fs = (double*)(base + o_fs);
+    d_out_gs = (unsigned long long*)(base + o_gs);
+    if (n_items == 0) {
+      AMDAT_CUDA(cudaMemsetAsync(base + o_d2, 0, o_gs - o_d2, ctx->stream));
+    }
+
+    for (int pass = 0; pass < n_passes && n_items > 0; ++pass) {
+      const int s0 = pass * MAX_FS;
+      const int nfs = S ? std::min(MAX_FS, S - s0) : 0;
+      DispParams p{};
+      p.u = ctx->u.ptr;
+      p.n_pad = ctx->n_pad;
+      p.t0 = P.t0.ptr;
+      p.t1 = P.t1.ptr;
+      p.gap = P.gap.ptr;
+      p.items = (const DispItem*)(base + o_items);
+      p.n_items = n_items;
+      p.lists = (const ListDev*)(base + o_lists);
+      p.counter = (int32_t*)(base + o_counter) + pass;
+      p.part = (double*)(base + o_part);
+      p.n_out = n_out;
+      p.want_moments = pass == 0;
+      p.gs = d_out_gs;
+      p.n_gaps = G;
+      p.n_bins = pass == 0 ? NB : 0;
+      p.bin_size = NB ? req->bin_max / (float)NB : 1.0f;
+      p.n_fs = nfs;
+      p.fs_mode = S ? sh.mode : 0;
+      p.kv = (const int4*)(base + o_kv);
+      p.kv_off = (const int32_t*)(base + o_off) + s0;
+      p.inv_count = (const float*)(base + o_inv) + s0;
+      p.nmax = sh.nmax;
+      p.period = S ? req->kvec_period : 1.0f;
+      AMDAT_CUDA(cudaMemsetAsync(p.counter, 0, 4, ctx->stream));
+      const bool gs = p.n_bins > 0;
+      const int mode = nfs ? sh.mode : 0;
+      const int threads = mode ? FS_THREADS : DISP_THREADS;
+      size_t shm = gs ? (size_t)((NB + 3) & ~3) * 4 : 0;
+      if (mode == 2) shm += (size_t)3 * (sh.nmax + 1) * threads * 4;
+      int blocks_per_sm = mode ? 4 : 8;
+      auto launch = [&](auto kernel) {
+        if (shm > 48 * 1024) AMDAT_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+        int occ = 0;
+        AMDAT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, threads, shm));
+        const int grid = (int)std::min<int64_t>((int64_t)std::max(1, std::min(occ, blocks_per_sm)) * ctx->n_sm, n_items);
+        kernel<<<grid, threads, shm, ctx->stream>>>(p);
+        check_launch("disp_mixed_kernel");
+        count_launch(ctx);
+      };
+      if (mode == 0) { if (gs) launch(disp_mixed_kernel<0, true>); else launch(disp_mixed_kernel<0, false>); }
+      else if (mode == 1) { if (gs) launch(disp_mixed_kernel<1, true>); else launch(disp_mixed_kernel<1, false>); }
+      else { if (gs) launch(disp_mixed_kernel<2, true>); else launch(disp_mixed_kernel<2, false>); }
+      disp_finalize_kernel<<<(unsigned)n_lg, 256, 0, ctx->stream>>>(
+          p.part, n_out, (const int32_t*)(base + o_first), 0, pass == 0 ? d_out_d2 : nullptr,
+          pass == 0 ? d_out_d4 : nullptr, S ? d_out_fs : nullptr, std::max(S, 1), s0, nfs,
+          pass == 0 ? 1 : 0);
+      check_launch("disp_finalize_kernel");
+      count_launch(ctx);
+    }
+    // lists with no members: zero outputs
+    for (int l = 0; l < n_lists; ++l)
+      if (lsize[l] == 0) {
+        AMDAT_CUDA(cudaMemsetAsync(d_out_d2 + (size_t)l * G, 0, G * sizeof(double), ctx->stream));
+        AMDAT_CUDA(cudaMemsetAsync(d_out_d4 + (size_t)l * G, 0, G * sizeof(double), ctx->stream));
+        if (S) AMDAT_CUDA(cudaMemsetAsync(d_out_fs + (size_t)l * G * S, 0, (size_t)G * S * sizeof(double), ctx->stream));
+      }
+  }
+  to_out(ctx, sum_d2, d_out_d2, n_lg, out_flags);
+  to_out(ctx, sum_d4, d_out_d4, n_lg, out_flags);
+  if (S) to_out(ctx, fs_sum, d_out_fs, n_lg * S, out_flags);
+  if (NB) to_out(ctx, (unsigned long long*)gs_counts, d_out_gs, n_lg * NB, out_flags);
+  if (atom_pairs) {
+    if (out_flags == AMDAT_OUT_DEVICE)
+      AMDAT_CUDA(cudaMemcpyAsync(atom_pairs, counts.data(), counts.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+    else
+      std::memcpy(atom_pairs, counts.data(), counts.size() * 8);
+  }
+  AMDAT_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+}  // namespace amdat
+
+using namespace amdat;
+
+extern "C" {
+
+amdat_status amdat_disp_run(amdat_ctx* ctx, const amdat_disp_request* req, int32_t out_flags,
+                            double* sum_d2, double* sum_d4, int64_t* atom_pairs, double* fs_sum,
+                            int64_t* gs_counts) {
+  return guarded([&] {
+    check_ctx(ctx);
+    AMDAT_REQUIRE(req != nullptr, "null request");
+    const int32_t l = req->list;
+    disp_run_impl(ctx, req, &l, 1, out_flags, sum_d2, sum_d4, atom_pairs, fs_sum, gs_counts);
+  });
+}
+
+amdat_status amdat_disp_run_lists(amdat_ctx* ctx, const amdat_disp_request* req,
+                                  const int32_t* lists, int32_t n_lists, int32_t out_flags,
+                                  double* sum_d2, double* sum_d4, int64_t* atom_pairs,
+                                  double* fs_sum, int64_t* gs_counts) {
+  return guarded([&] {
+    check_ctx(ctx);
+    AMDAT_REQUIRE(lists != nullptr && n_lists >= 1, "need >= 1 list");
+    disp_run_impl(ctx, req, lists, n_lists, out_flags, sum_d2, sum_d4, atom_pairs, fs_sum, gs_counts);
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,225 @@
+// Pair histograms: the radial distribution function's per-frame pair loop
+// (Radial_Distribution_Function::listkernel2 + bin,
+// src/radial_distribution_function.cpp:233-253) and the distinct van Hove
+// pair loop over time pairs (Van_Hove_Distinct::listkernel2,
+// src/van_hove_distinct.cpp:200-213, with the distance the reference meant to
+// bin: the minimum-image |r_j(t1) - r_i(t0)|).
+//
+// Every distance follows the reference's FP32 chain exactly -
+// Coordinate::length_unwrapped (src/coordinate.cpp:126-137): per axis
+// d = r_j - r_i, m = min(|d|, L - |d|); length = sqrtf((mx*mx + my*my) + mz*mz);
+// bin = int(length / bin_size) - with correctly rounded, uncontracted
+// operations, so the integer counts equal the reference's bit for bit.
+// Pairs whose squared length is safely beyond the last bin skip the square
+// root and the division.
+//
+// A block owns 256 members i of list 1 (positions in registers) and streams
+// list 2 through shared memory in tiles of 1024.  Counts go to per-warp
+// shared-memory histograms, then once per block to the global int64
+// histogram with integer atomics (exact, order-independent).  For the RDF
+// with list1 == list2 the unordered pairs j > i are visited once and counted
+// twice (|d| is symmetric to the bit under exchange of i and j).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "engine.h"
+
+namespace amdat {
+
+constexpr int PH_THREADS = 256;
+constexpr int PH_JT = 1024;
+
+struct PHList {
+  int32_t n;
+  int32_t first;
+  const int32_t* idx;
+};
+
+static PHList phview(const ListEntry& e) {
+  return PHList{e.n, e.first, e.contiguous ? nullptr : e.idx.ptr};
+}
+
+__device__ __forceinline__ int member(const PHList& l, int a) {
+  return l.idx ? l.idx[a] : l.first + a;
+}
+
+__device__ __forceinline__ float min_image(float d, float L) {
+  const float a = fabsf(d);
+  const float b = __fsub_rn(L, a);
+  return a < b ? a : b;
+}
+
+struct PHParams {
+  const float* w;
+  int64_t n_pad;
+  PHList l1, l2;
+  const int32_t* frame_a;  // [n_rows] frame of list-1 positions
+  const int32_t* frame_b;  // [n_rows] frame of list-2 positions
+  const int32_t* row_of;   // [n_rows] output row (frame index or gap)
+  int32_t symmetric;       // l1 == l2 and frame_a == frame_b: visit j > i, count 2
+  float3 box;
+  float bin_size;
+  float s2_cut;
+  int32_t n_bins;
+  unsigned long long* counts;  // [rows][n_bins]
+};
+
+__global__ void __launch_bounds__(PH_THREADS)
+    pair_hist_kernel(PHParams p) {
+  extern __shared__ unsigned int sh_hist[];  // [8 warps][n_bins]
+  __shared__ float sx[PH_JT], sy[PH_JT], sz[PH_JT];
+  __shared__ int sid[PH_JT];
+  const int q = blockIdx.y;
+  const float* A = p.w + (int64_t)p.frame_a[q] * 3 * p.n_pad;
+  const float* B = p.w + (int64_t)p.frame_b[q] * 3 * p.n_pad;
+  const int warp = threadIdx.x >> 5;
+  unsigned int* hist = sh_hist + warp * p.n_bins;
+  for (int b = threadIdx.x; b < 8 * p.n_bins; b += blockDim.x) sh_hist[b] = 0u;
+  const int i0 = blockIdx.x * PH_THREADS;
+  const int i = i0 + threadIdx.x;
+  const bool live = i < p.l1.n;
+  int ai = -1;
+  float xi = 0.f, yi = 0.f, zi = 0.f;
+  if (live) {
+    ai = member(p.l1, i);
+    xi = A[ai];
+    yi = A[p.n_pad + ai];
+    zi = A[2 * p.n_pad + ai];
+  }
+  const unsigned int inc = p.symmetric ? 2u : 1u;
+  const int j_begin = p.symmetric ? i0 : 0;
+  __syncthreads();
+  for (int j0 = j_begin; j0 < p.l2.n; j0 += PH_JT) {
+    const int nj = min(PH_JT, p.l2.n - j0);
+    __syncthreads();
+    for (int t = threadIdx.x; t < nj; t += blockDim.x) {
+      const int aj = member(p.l2, j0 + t);
+      sid[t] = aj;
+      sx[t] = B[aj];
+      sy[t] = B[p.n_pad + aj];
+      sz[t] = B[2 * p.n_pad + aj];
+    }
+    __syncthreads();
+    if (!live) continue;
+    int t_begin = 0;
+    if (p.symmetric) t_begin = max(0, i + 1 - j0);  // j > i
+    for (int t = t_begin; t < nj; ++t) {
+      if (sid[t] == ai) continue;  // i != j (same atom in both lists)
+      const float mx = min_image(__fsub_rn(sx[t], xi), p.box.x);
+      const float my = min_image(__fsub_rn(sy[t], yi), p.box.y);
+      const float mz = min_image(__fsub_rn(sz[t], zi), p.box.z);
+      const float s2 = __fadd_rn(__fadd_rn(__fmul_rn(mx, mx), __fmul_rn(my, my)), __fmul_rn(mz, mz));
+      if (s2 < p.s2_cut) {
+        const int b = (int)__fdiv_rn(__fsqrt_rn(s2), p.bin_size);
+        if (b >= 0 && b < p.n_bins) atomicAdd(hist + b, inc);
+      }
+    }
+  }
+  __syncthreads();
+  unsigned long long* dst = p.counts + (int64_t)p.row_of[q] * p.n_bins;
+  for (int b = threadIdx.x; b < p.n_bins; b += blockDim.x) {
+    unsigned long long s = 0;
+    for (int w = 0; w < 8; ++w) s += sh_hist[w * p.n_bins + b];
+    if (s) atomicAdd(dst + b, s);
+  }
+}
+
+static void run_pair_hist(amdat_ctx* ctx, const ListEntry& l1, const ListEntry& l2, bool symmetric,
+                          const std::vector<int32_t>& fa, const std::vector<int32_t>& fb,
+                          const std::vector<int32_t>& row, int32_t n_rows_out, float max_distance,
+                          int32_t n_bins, int32_t out_flags, int64_t* counts) {
+  AMDAT_REQUIRE(n_bins >= 1 && n_bins <= 4096, "n_bins must be in [1, 4096]");
+  AMDAT_REQUIRE(max_distance > 0.0f, "max_distance must be positive");
+  AMDAT_REQUIRE(counts != nullptr, "null output");
+  const size_t n_q = fa.size();
+  const size_t n_out = (size_t)n_rows_out * n_bins;
+  auto align = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  size_t o = 0;
+  const size_t o_fa = o; o = align(o + std::max<size_t>(n_q, 1) * 4);
+  const size_t o_fb = o; o = align(o + std::max<size_t>(n_q, 1) * 4);
+  const size_t o_row = o; o = align(o + std::max<size_t>(n_q, 1) * 4);
+  const size_t o_cnt = o; o = align(o + n_out * 8);
+  unsigned char* base = ctx->scratch.reserve(o);
+  std::vector<unsigned char> host(o_cnt, 0);
+  if (n_q) {
+    std::memcpy(host.data() + o_fa, fa.data(), n_q * 4);
+    std::memcpy(host.data() + o_fb, fb.data(), n_q * 4);
+    std::memcpy(host.data() + o_row, row.data(), n_q * 4);
+  }
+  AMDAT_CUDA(cudaMemcpyAsync(base, host.data(), o_cnt, cudaMemcpyHostToDevice, ctx->stream));
+  AMDAT_CUDA(cudaMemsetAsync(base + o_cnt, 0, n_out * 8, ctx->stream));
+  PHParams p{};
+  p.w = ctx->w.ptr;
+  p.n_pad = ctx->n_pad;
+  p.l1 = phview(l1);
+  p.l2 = phview(l2);
+  p.frame_a = (const int32_t*)(base + o_fa);
+  p.frame_b = (const int32_t*)(base + o_fb);
+  p.row_of = (const int32_t*)(base + o_row);
+  p.symmetric = symmetric ? 1 : 0;
+  p.box = make_float3(ctx->box[0], ctx->box[1], ctx->box[2]);
+  p.bin_size = max_distance / (float)n_bins;
+  // squared lengths at or above this are past the last bin for sure
+  const double cut = (double)max_distance * (1.0 + 1e-5);
+  p.s2_cut = (float)(cut * cut);
+  p.n_bins = n_bins;
+  p.counts = (unsigned long long*)(base + o_cnt);
+  if (n_q && l1.n > 0 && l2.n > 0) {
+    const size_t shm = (size_t)8 * n_bins * 4;
+    if (shm > 48 * 1024)
+      AMDAT_CUDA(cudaFuncSetAttribute(pair_hist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+    AMDAT_REQUIRE(n_q <= 65535, "at most 65535 frames or time pairs per call");
+    dim3 grid((unsigned)ceil_div(l1.n, PH_THREADS), (unsigned)n_q);
+    pair_hist_kernel<<<grid, PH_THREADS, shm, ctx->stream>>>(p);
+    check_launch("pair_hist_kernel");
+    count_launch(ctx);
+  }
+  AMDAT_CUDA(cudaMemcpyAsync(counts, base + o_cnt, n_out * 8,
+                             out_flags == AMDAT_OUT_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                             ctx->stream));
+  AMDAT_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+}  // namespace amdat
+
+using namespace amdat;
+
+extern "C" {
+
+amdat_status amdat_rdf_run(amdat_ctx* ctx, int32_t list1, int32_t list2, const int32_t* frames,
+                           int32_t n_frames, float max_distance, int32_t n_bins, int32_t out_flags,
+                           int64_t* counts) {
+  return guarded([&] {
+    check_ctx(ctx);
+    if (!ctx->have_traj) throw Error(AMDAT_ERR_STATE, "no trajectory uploaded");
+    AMDAT_REQUIRE(frames != nullptr && n_frames >= 1, "need >= 1 frame");
+    for (int f = 0; f < n_frames; ++f)
+      AMDAT_REQUIRE(frames[f] >= 0 && frames[f] < ctx->n_frames, "frame index out of range");
+    const ListEntry& a = list_entry(ctx, list1);
+    const ListEntry& b = list_entry(ctx, list2);
+    std::vector<int32_t> fa(frames, frames + n_frames), row(n_frames);
+    for (int f = 0; f < n_frames; ++f) row[f] = f;
+    run_pair_hist(ctx, a, b, list1 == list2, fa, fa, row, n_frames, max_distance, n_bins,
+                  out_flags, counts);
+  });
+}
+
+amdat_status amdat_vhd_run(amdat_ctx* ctx, int32_t list1, int32_t list2, int32_t fullblock,
+                           float max_distance, int32_t n_bins, int32_t out_flags, int64_t* counts) {
+  return guarded([&] {
+    check_ctx(ctx);
+    if (!ctx->have_traj) throw Error(AMDAT_ERR_STATE, "no trajectory uploaded");
+    const ListEntry& a = list_entry(ctx, list1);
+    const ListEntry& b = list_entry(ctx, list2);
+    const PairTable& P = pair_table(ctx, fullblock != 0, false);
+    Pairs hp = scheme_pairs(ctx->scheme, fullblock != 0, false);
+    // time pairs with t0 == t1 (gap 0) are the same-time pair loop: symmetric counting
+    // applies only when t0 == t1; keep the general ordered loop for every pair.
+    run_pair_hist(ctx, a, b, false, hp.t0, hp.t1, hp.gap, P.n_gaps, max_distance, n_bins,
+                  out_flags, counts);
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,230 @@
+/* amdat_gb300 - GB300 engine for AMDAT's time-resolved trajectory statistics.
+ *
+ * C ABI of the engine's hot path.  Plain pointers and sizes, no C++ or CUDA
+ * types; every call returns an amdat_status (0 = success) and never exits the
+ * process; amdat_last_error() gives the message of the calling thread's last
+ * failure.  One context drives one GPU from one host thread; calls issue work
+ * on the context's stream and return when their host-visible results are
+ * ready (results written to device pointers, AMDAT_OUT_DEVICE, are ready when
+ * the stream is).  Caller-owned arrays are never retained.
+ *
+ * Reference interfaces replaced (paths in the AMDAT source tree):
+ *   time scheme + time-pair scheduler  System::System time line (src/system.cpp:83-140),
+ *       create_timelist (:3542), displacement_times (:3763), timegap_weighting (:4599),
+ *       displacement_list (:4090-4179), displacement_loop (:3918-3964), 'limit' (src/control.cpp:1860)
+ *   trajectory store                   Trajectory::unwrapped / coordinates (src/trajectory.h:37-38)
+ *   lists                              Static_Trajectory_List / Trajectory_List::listloop
+ *                                      (src/trajectory_list.cpp:191-222)
+ *   displacement family                Mean_Square_Displacement::listkernel (src/mean_square_displacement.cpp:164),
+ *                                      Non_Gaussian_Parameter::listkernel (src/non_gaussian_parameter.cpp:125),
+ *                                      Incoherent_Scattering_Function::listkernel (src/incoherent_scattering_function.cpp:272),
+ *                                      Van_Hove_Self::listkernel (src/van_hove_self.cpp:98)
+ *   Fourier densities                  Wave_Density::analyze / listkernel (src/wave_density.cpp:313-365),
+ *                                      Structure_Factor::listkernel (src/structure_factor.cpp:293)
+ *   coherent correlator                Intermediate_Scattering_Function::displacementkernel
+ *                                      (src/intermediate_scattering_function.cpp:551-566)
+ *   static structure factor            Structure_Factor::timekernel (src/structure_factor.cpp:201-230)
+ *   pair histograms                    Radial_Distribution_Function::listkernel2 + bin
+ *                                      (src/radial_distribution_function.cpp:233-253),
+ *                                      Van_Hove_Distinct::listkernel2 (src/van_hove_distinct.cpp:200-213)
+ */
+#ifndef AMDAT_GB300_H
+#define AMDAT_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  AMDAT_OK = 0,
+  AMDAT_ERR_ARGUMENT = 1, /* null pointer, size or index out of range */
+  AMDAT_ERR_STATE = 2,    /* call out of order (e.g. no trajectory uploaded) */
+  AMDAT_ERR_CUDA = 3,     /* CUDA runtime failure (message has the CUDA error) */
+  AMDAT_ERR_NO_DEVICE = 4,
+  AMDAT_ERR_MEMORY = 5,   /* device allocation failed */
+  AMDAT_ERR_TIMEOUT = 6   /* a bounded device-side wait gave up */
+} amdat_status;
+
+/* output placement flag for run calls */
+#define AMDAT_OUT_HOST 0
+#define AMDAT_OUT_DEVICE 1
+
+/* arithmetic of a run: mixed = FP32 compensated with FP64 final reduction;
+ * plain_fp64 = straightforward FP64 kernels (throughput denominator) */
+#define AMDAT_MIXED 0
+#define AMDAT_PLAIN_FP64 1
+
+typedef struct amdat_ctx amdat_ctx;
+
+const char* amdat_version(void);
+const char* amdat_last_error(void);
+
+/* ---------------------------------------------------------------------------
+ * Time scheme and time-pair scheduler (host only, no GPU needed)
+ * ------------------------------------------------------------------------- */
+#define AMDAT_LINEAR 0
+#define AMDAT_EXPONENTIAL 1
+#define AMDAT_SNAPSHOT 2
+
+typedef struct {
+  int32_t kind;                /* AMDAT_LINEAR / AMDAT_EXPONENTIAL / AMDAT_SNAPSHOT */
+  int32_t n_exponentials;      /* blocks (linear: n_timesteps - 1) */
+  int32_t n_exponential_steps; /* frames per block (linear: 1) */
+  float exp_base;
+  int32_t frt;
+  int32_t first_exponent;
+  float time_unit;
+  int32_t limit;               /* time pairs per gap cap ('limit'); 0 = none */
+} amdat_scheme;
+
+/* Fill a scheme from the arguments of the system block's time line:
+ * linear:      a = n_timesteps, unit
+ * exponential: a = blocks, b = steps per block, base, frt, first_exponent, unit
+ * snapshot:    no arguments.  Replaces System::System (src/system.cpp:83-140). */
+amdat_status amdat_scheme_init(amdat_scheme* s, int32_t kind, int32_t a, int32_t b, float base,
+                               int32_t frt, int32_t first_exponent, float unit);
+/* n_timesteps, n_timegaps (src/system.cpp:218) and the number of time pairs that
+ * displacement_list (loop_order = 0) or displacement_loop (loop_order = 1) visits. */
+amdat_status amdat_scheme_counts(const amdat_scheme* s, int32_t fullblock, int32_t loop_order,
+                                 int32_t* n_timesteps, int32_t* n_timegaps, int64_t* n_pairs);
+/* frame times (create_timelist, src/system.cpp:3542) and gap times
+ * (displacement_times, src/system.cpp:3763); either pointer may be NULL. */
+amdat_status amdat_scheme_times(const amdat_scheme* s, float* timelist, float* gap_times);
+/* System::timegap_weighting(bool) (src/system.cpp:4599-4628) */
+amdat_status amdat_scheme_weighting(const amdat_scheme* s, int32_t fullblock, int32_t* weighting);
+/* the (gap, t0, t1) triples in scheduler order (displacement_list or displacement_loop) */
+amdat_status amdat_scheme_pairs(const amdat_scheme* s, int32_t fullblock, int32_t loop_order,
+                                int32_t* gap, int32_t* t0, int32_t* t1);
+
+/* ---------------------------------------------------------------------------
+ * Context, trajectory store and lists
+ * ------------------------------------------------------------------------- */
+amdat_status amdat_create(int32_t device, amdat_ctx** out);
+amdat_status amdat_destroy(amdat_ctx* ctx);
+/* Issue work on an existing cudaStream_t (passed as void*); NULL restores the
+ * context's own stream. */
+amdat_status amdat_set_stream(amdat_ctx* ctx, void* cuda_stream);
+amdat_status amdat_synchronize(amdat_ctx* ctx);
+/* number of kernels this context has launched (for launch accounting) */
+amdat_status amdat_launch_count(amdat_ctx* ctx, int64_t* count);
+
+/* Upload a trajectory: host arrays [n_frames][n_atoms][3] of unwrapped
+ * coordinates and (optionally) wrapped ones.  With wrapped == NULL the wrapped
+ * coordinates are derived as the custom reader does (c = u - L*floor((u-lo)/L),
+ * FP32, src/system.cpp read_custom).  box / box_lo: [3] constant box.  The
+ * engine keeps unwrapped coordinates re-referenced to frame 0 (FP32) and
+ * wrapped ones as FP32 structure-of-arrays planes.  Replaces the per-atom
+ * Coordinate arrays of Trajectory (src/trajectory.h:37-38). */
+amdat_status amdat_traj_upload(amdat_ctx* ctx, int32_t n_frames, int32_t n_atoms,
+                               const float* unwrapped, const float* wrapped, const float* box,
+                               const float* box_lo);
+/* Same from FP64 host coordinates (re-referencing is then done in FP64). */
+amdat_status amdat_traj_upload_f64(amdat_ctx* ctx, int32_t n_frames, int32_t n_atoms,
+                                   const double* unwrapped, const double* wrapped,
+                                   const float* box, const float* box_lo);
+/* Upload from device memory (pointers on this context's GPU) */
+amdat_status amdat_traj_upload_device(amdat_ctx* ctx, int32_t n_frames, int32_t n_atoms,
+                                      const float* d_unwrapped, const float* box,
+                                      const float* box_lo);
+/* Register a static list (Static_Trajectory_List): ascending atom indices.
+ * Handle 0 is always the list of all atoms. */
+amdat_status amdat_list_create(amdat_ctx* ctx, const int32_t* atoms, int32_t n_atoms,
+                               int32_t* handle);
+amdat_status amdat_list_size(amdat_ctx* ctx, int32_t handle, int32_t* n_atoms);
+
+/* ---------------------------------------------------------------------------
+ * Displacement family: MSD, NGP moments, F_s(q,t), G_s(r,t) in one pass
+ * ------------------------------------------------------------------------- */
+typedef struct {
+  int32_t list;           /* list handle */
+  int32_t fullblock;      /* cross-block pairs use every in-block offset */
+  int32_t precision;      /* AMDAT_MIXED or AMDAT_PLAIN_FP64 */
+  /* self intermediate scattering function: shells of integer lattice vectors,
+   * wave vector k = 2*pi*n/kvec_period.  n_shells = 0 disables it. */
+  int32_t n_shells;
+  const int32_t* shell_offsets; /* [n_shells + 1] */
+  const int32_t* kvec_n;        /* [3 * shell_offsets[n_shells]] */
+  float kvec_period;
+  /* self van Hove histogram: n_bins bins of |dr| in [0, bin_max); 0 disables */
+  int32_t n_bins;
+  float bin_max;
+} amdat_disp_request;
+
+/* Runs every time pair of the context's scheme (amdat_set_scheme) over the
+ * list.  Outputs, per gap g (n_timegaps rows), any of which may be NULL:
+ *   sum_d2[g]      sum over pairs and atoms of |dr|^2
+ *   sum_d4[g]      sum of |dr|^4
+ *   atom_pairs[g]  number of (atom, time pair) terms
+ *   fs_sum[g][s]   sum of the shell mean of cos(k.dr)
+ *   gs_counts[g][b] histogram counts (bin = int(|dr| / (bin_max/n_bins)))
+ * out_flags = AMDAT_OUT_DEVICE: the five pointers are device pointers. */
+amdat_status amdat_disp_run(amdat_ctx* ctx, const amdat_disp_request* req, int32_t out_flags,
+                            double* sum_d2, double* sum_d4, int64_t* atom_pairs, double* fs_sum,
+                            int64_t* gs_counts);
+/* Many lists in one persistent launch: outputs are [n_lists][...] stacks of
+ * the single-list outputs (req->list is ignored). */
+amdat_status amdat_disp_run_lists(amdat_ctx* ctx, const amdat_disp_request* req,
+                                  const int32_t* lists, int32_t n_lists, int32_t out_flags,
+                                  double* sum_d2, double* sum_d4, int64_t* atom_pairs,
+                                  double* fs_sum, int64_t* gs_counts);
+amdat_status amdat_set_scheme(amdat_ctx* ctx, const amdat_scheme* scheme);
+
+/* ---------------------------------------------------------------------------
+ * Fourier densities rho(k,t) = sum_j exp(i 2 pi n.r_j(t) / period)
+ * ------------------------------------------------------------------------- */
+/* Explicit vector list (e.g. the reference's q-vector shells), frames given.
+ * The table stays on the device; returns a handle. */
+amdat_status amdat_wave_density(amdat_ctx* ctx, int32_t list, const int32_t* kvec_n, int32_t n_k,
+                                float period, const int32_t* frames, int32_t n_frames,
+                                int32_t precision, int32_t* handle);
+/* Every half-space lattice vector with |k| <= kmax (k = 2 pi n / period), sorted
+ * into shells of width dk (shell s: s*dk <= |k| < (s+1)*dk).  Returns the handle,
+ * the vector count and the number of shells. */
+amdat_status amdat_wave_density_lattice(amdat_ctx* ctx, int32_t list, float kmax, float dk,
+                                        float period, const int32_t* frames, int32_t n_frames,
+                                        int32_t precision, int32_t* handle, int32_t* n_k,
+                                        int32_t* n_shells);
+/* Vectors and shell offsets of a lattice density (host arrays sized from the
+ * counts above; either may be NULL). */
+amdat_status amdat_wave_density_vectors(amdat_ctx* ctx, int32_t handle, int32_t* kvec_n,
+                                        int32_t* shell_offsets);
+/* Copy rho [n_frames][n_k][2] (FP32 re, im) to host or device memory. */
+amdat_status amdat_wave_density_read(amdat_ctx* ctx, int32_t handle, int32_t out_flags,
+                                     float* rho);
+amdat_status amdat_wave_density_free(amdat_ctx* ctx, int32_t handle);
+
+/* Coherent intermediate scattering function: for every time pair (t0,t1) of
+ * the scheme in displacement_loop order, corr_sum[g][s] += sum_{k in shell s}
+ * Re(rho1(k,t0) conj(rho2(k,t1))) / H_s.  Both densities must cover every
+ * frame 0..n_timesteps-1.  pair_count[g] = number of time pairs of gap g. */
+amdat_status amdat_isf_run(amdat_ctx* ctx, int32_t density1, int32_t density2, int32_t fullblock,
+                           const int32_t* shell_offsets, int32_t n_shells, int32_t out_flags,
+                           double* corr_sum, int64_t* pair_count);
+/* Static structure factor: s_sum[s] = sum over the density's frames and the
+ * shell's vectors of Re(rho1 conj(rho2)) / H_s. */
+amdat_status amdat_structure_factor_run(amdat_ctx* ctx, int32_t density1, int32_t density2,
+                                        const int32_t* shell_offsets, int32_t n_shells,
+                                        int32_t out_flags, double* s_sum);
+
+/* ---------------------------------------------------------------------------
+ * Pair histograms (FP32 arithmetic identical to the reference's, so counts
+ * are bit-exact): bin = int(minimage(|r_j - r_i|) / (max_distance/n_bins)).
+ * ------------------------------------------------------------------------- */
+/* RDF: ordered pairs i in list1, j in list2, i != j, per frame:
+ * counts[f][b] for the given frames. */
+amdat_status amdat_rdf_run(amdat_ctx* ctx, int32_t list1, int32_t list2, const int32_t* frames,
+                           int32_t n_frames, float max_distance, int32_t n_bins, int32_t out_flags,
+                           int64_t* counts);
+/* Distinct van Hove: for every time pair of the scheme (displacement_list
+ * order), ordered pairs i in list1 at t0, j in list2 at t1, i != j:
+ * counts[g][b]. */
+amdat_status amdat_vhd_run(amdat_ctx* ctx, int32_t list1, int32_t list2, int32_t fullblock,
+                           float max_distance, int32_t n_bins, int32_t out_flags, int64_t* counts);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* AMDAT_GB300_H */

@@ -20,3 +20,19 @@ def qvectors():
     import numpy as np
     z = np.load(os.path.join(TESTS, "golden", "qvectors3d.npz"))
     return z["n"].astype(np.int32), z["offsets"].astype(np.int32)
+
+
+@pytest.fixture(scope="session")
+def engine_mod():
+    """The engine binding; builds the native library if needed (GPU tests only)."""
+    from amdat_gb300 import build
+    build.build()
+    from amdat_gb300 import engine
+    return engine
+
+
+@pytest.fixture()
+def eng(engine_mod):
+    e = engine_mod.Engine(0)
+    yield e
+    e.close()

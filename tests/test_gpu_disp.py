@@ -1,0 +1,204 @@
+"""GPU parity of the displacement family (MSD/NGP moments, F_s, G_s) against
+the oracle, through the C ABI.  Tolerances: MSD and |dr|^4 sums <= 1e-6
+relative to the FP64 oracle; F_s (normalised, F_s(q,0) = 1) <= 1e-6 absolute;
+G_s counts equal to the reference's FP32 binning except counted bin-edge ties
+(the engine forms dr from frame-0-referenced coordinates)."""
+import numpy as np
+import pytest
+
+from amdat_gb300 import synth
+from golden.make_golden import CASES, load
+from oracle import oracle as orc
+from oracle import wavevectors as wv
+
+pytestmark = pytest.mark.gpu
+
+
+def _ref_shells(qvec, m0, m1):
+    n, off = qvec
+    return n[off[m0]:off[m1 + 1]], off[m0:m1 + 2] - off[m0]
+
+
+def lattice_shell(period, kmin, kmax):
+    """All integer lattice vectors with kmin <= |2 pi n / period| < kmax."""
+    nmax = int(np.ceil(kmax * period / (2 * np.pi))) + 1
+    r = np.arange(-nmax, nmax + 1)
+    g = np.stack(np.meshgrid(r, r, r, indexing="ij"), -1).reshape(-1, 3)
+    k = 2 * np.pi * np.linalg.norm(g, axis=1) / period
+    return g[(k >= kmin) & (k < kmax)].astype(np.int32)
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_moments_match_oracle(case, eng):
+    traj, _, _ = load(case)
+    eng.upload(traj.unwrapped, traj.box, traj.box_lo)
+    for fb in (0, 1):
+        eng.set_scheme(traj.scheme)
+        out = eng.disp(0, fullblock=fb)
+        s = orc.scheme(traj.scheme)
+        d2, d4, cnt = orc.disp_moments(s, traj.unwrapped, None, fb)
+        np.testing.assert_array_equal(out["atom_pairs"], cnt)
+        m = cnt > 0
+        np.testing.assert_allclose(out["sum_d2"][m], d2[m], rtol=1e-6, atol=1e-12)
+        np.testing.assert_allclose(out["sum_d4"][m], d4[m], rtol=1e-6, atol=1e-14)
+
+
+def test_msd_ngp_normalised_vs_oracle(eng):
+    traj, _, _ = load("exp_small")
+    eng.upload(traj.unwrapped, traj.box)
+    eng.set_scheme(traj.scheme)
+    out = eng.disp(0)
+    s = orc.scheme(traj.scheme)
+    lst = np.arange(traj.n_atoms, dtype=np.int32)
+    msd = orc.msd(s, traj.unwrapped, lst, orc.F64)
+    ngp = orc.ngp(s, traj.unwrapped, lst, orc.F64)
+    w = out["atom_pairs"].astype(float)
+    gm = out["sum_d2"] / w
+    np.testing.assert_allclose(gm[1:], msd[1:], rtol=1e-6)
+    gn = out["sum_d4"] * 3.0 / w / (5.0 * gm * gm) - 1.0
+    np.testing.assert_allclose(gn[1:], ngp[1:], rtol=1e-6, atol=1e-9)
+
+
+@pytest.mark.parametrize("limit", [0, 3])
+def test_limit_and_lists(eng, limit):
+    traj, _, _ = load("lin_binary")
+    eng.upload(traj.unwrapped, traj.box)
+    eng.set_scheme(traj.scheme, limit=limit)
+    s = orc.scheme(traj.scheme, limit)
+    a = np.nonzero(traj.types == 0)[0].astype(np.int32)
+    b = np.nonzero(traj.types == 1)[0].astype(np.int32)
+    odd = np.arange(1, traj.n_atoms, 2, dtype=np.int32)   # gathered (non-contiguous) list
+    for lst in (a, b, odd):
+        h = eng.list(lst)
+        out = eng.disp(h)
+        d2, d4, cnt = orc.disp_moments(s, traj.unwrapped, lst, 0)
+        np.testing.assert_array_equal(out["atom_pairs"], cnt)
+        np.testing.assert_allclose(out["sum_d2"], d2, rtol=1e-6, atol=1e-12)
+
+
+def test_empty_and_single_atom_lists(eng):
+    traj, _, _ = load("exp_frt")
+    eng.upload(traj.unwrapped, traj.box)
+    eng.set_scheme(traj.scheme)
+    h0 = eng.list(np.zeros(0, np.int32))
+    out = eng.disp(h0)
+    assert (out["atom_pairs"] == 0).all() and (out["sum_d2"] == 0).all()
+    h1 = eng.list([5])
+    out = eng.disp(h1)
+    s = orc.scheme(traj.scheme)
+    d2, d4, cnt = orc.disp_moments(s, traj.unwrapped, np.array([5], np.int32), 0)
+    np.testing.assert_allclose(out["sum_d2"], d2, rtol=1e-6, atol=1e-14)
+    # NGP of a single atom at gap 0 is 0/0, as in the reference
+    with np.errstate(invalid="ignore", divide="ignore"):
+        ngp0 = out["sum_d4"][0] * 3 / out["atom_pairs"][0] / (5 * (out["sum_d2"][0] / out["atom_pairs"][0]) ** 2) - 1
+    assert np.isnan(ngp0)
+
+
+@pytest.mark.parametrize("case,m0,m1,fb", [("exp_small", 10, 12, 0), ("exp_small", 14, 15, 1),
+                                          ("lin_binary", 6, 9, 0), ("exp_frt", 3, 5, 1)])
+def test_fs_reference_shells(case, m0, m1, fb, eng, qvectors):
+    traj, _, _ = load(case)
+    eng.upload(traj.unwrapped, traj.box)
+    eng.set_scheme(traj.scheme)
+    L = float(np.float32(traj.box.min()))
+    kv, off = _ref_shells(qvectors, m0, m1)
+    out = eng.disp(0, fullblock=fb, shells=(kv, off), period=L)
+    s = orc.scheme(traj.scheme)
+    lst = np.arange(traj.n_atoms, dtype=np.int32)
+    ref = orc.isfs(s, traj.unwrapped, lst, kv, off, float(wv.spacing(L)), L, fb, orc.F64)
+    got = out["fs_sum"] / out["atom_pairs"][:, None]
+    assert np.abs(got - ref).max() <= 1e-6
+
+
+def test_fs_lattice_shell_octant_mode(eng):
+    """Whole lattice shell |k| in [7.0, 7.2] (sign-symmetric: octant tables)."""
+    box = 16.8
+    scheme = synth.TimeScheme.exponential(3, 6, 1.3, 0, 0, 0.005)
+    traj = synth.random_walk(300, box, scheme, 0.5, seed=5)
+    shell = lattice_shell(box, 7.0, 7.2)
+    eng.upload(traj.unwrapped, traj.box)
+    eng.set_scheme(scheme)
+    off = np.array([0, len(shell)], np.int32)
+    out = eng.disp(0, shells=(shell, off), period=box)
+    s = orc.scheme(scheme)
+    lst = np.arange(traj.n_atoms, dtype=np.int32)
+    ref = orc.isfs(s, traj.unwrapped, lst, shell, off, float(wv.spacing(box)), box, 0, orc.F64)
+    got = out["fs_sum"] / out["atom_pairs"][:, None]
+    assert np.abs(got - ref).max() <= 1e-6
+    # many shells in one request (> 8 per pass)
+    shells = [lattice_shell(box, 1.0 + 0.5 * i, 1.5 + 0.5 * i) for i in range(11)]
+    kv = np.concatenate(shells)
+    off = np.concatenate([[0], np.cumsum([len(x) for x in shells])]).astype(np.int32)
+    out = eng.disp(0, shells=(kv, off), period=box)
+    ref = orc.isfs(s, traj.unwrapped, lst, kv, off, float(wv.spacing(box)), box, 0, orc.F64)
+    got = out["fs_sum"] / out["atom_pairs"][:, None]
+    assert np.abs(got - ref).max() <= 1e-6
+
+
+@pytest.mark.parametrize("case,rmax,nb", [("exp_small", 0.5, 50), ("lin_binary", 1.0, 40),
+                                          ("exp_frt", 0.8, 20)])
+def test_gs_counts(case, rmax, nb, eng):
+    traj, _, _ = load(case)
+    eng.upload(traj.unwrapped, traj.box)
+    eng.set_scheme(traj.scheme)
+    out = eng.disp(0, n_bins=nb, bin_max=rmax)
+    s = orc.scheme(traj.scheme)
+    lst = np.arange(traj.n_atoms, dtype=np.int32)
+    counts, w, _ = orc.vhs(s, traj.unwrapped, lst, rmax, nb)
+    diff = np.abs(out["gs_counts"] - counts).sum()
+    # every atom-pair lands in exactly one bin or beyond the last one in both
+    assert diff <= 2 * max(1, counts.sum() // 100000), diff
+    np.testing.assert_array_equal(out["atom_pairs"], w)
+
+
+def test_plain_fp64_path(eng, qvectors):
+    traj, _, _ = load("exp_small")
+    eng.upload(traj.unwrapped, traj.box)
+    eng.set_scheme(traj.scheme)
+    L = float(np.float32(traj.box.min()))
+    kv, off = _ref_shells(qvectors, 10, 12)
+    a = eng.disp(0, shells=(kv, off), period=L, n_bins=50, bin_max=0.5)
+    b = eng.disp(0, shells=(kv, off), period=L, n_bins=50, bin_max=0.5, precision=1)
+    np.testing.assert_allclose(a["sum_d2"], b["sum_d2"], rtol=1e-6, atol=1e-12)
+    np.testing.assert_allclose(a["fs_sum"] / a["atom_pairs"][:, None],
+                               b["fs_sum"] / b["atom_pairs"][:, None], atol=1e-6)
+    assert np.abs(a["gs_counts"] - b["gs_counts"]).sum() <= 4
+
+
+def test_many_lists_one_launch(eng):
+    traj, _, _ = load("lin_binary")
+    eng.upload(traj.unwrapped, traj.box)
+    eng.set_scheme(traj.scheme)
+    rng = np.random.default_rng(3)
+    perm = rng.permutation(traj.n_atoms)
+    sizes = [1, 7, 50, 120, 250]
+    handles = [eng.list(np.sort(perm[:n]).astype(np.int32)) for n in sizes]
+    shell = lattice_shell(7.0, 3.0, 3.4)
+    off = np.array([0, len(shell)], np.int32)
+    batch = eng.disp_lists(handles, shells=(shell, off), period=7.0, n_bins=30, bin_max=1.0)
+    for i, h in enumerate(handles):
+        one = eng.disp(h, shells=(shell, off), period=7.0, n_bins=30, bin_max=1.0)
+        np.testing.assert_allclose(batch["sum_d2"][i], one["sum_d2"], rtol=1e-12)
+        np.testing.assert_allclose(batch["fs_sum"][i], one["fs_sum"], rtol=1e-12, atol=1e-12)
+        np.testing.assert_array_equal(batch["gs_counts"][i], one["gs_counts"])
+
+
+def test_errors_are_status_codes(eng, engine_mod):
+    with pytest.raises(engine_mod.AmdatError) as e:
+        eng.disp(0)
+    assert e.value.status == 2  # no trajectory yet
+    traj, _, _ = load("exp_frt")
+    eng.upload(traj.unwrapped, traj.box)
+    with pytest.raises(engine_mod.AmdatError):
+        eng.disp(0)  # no scheme
+    eng.set_scheme(traj.scheme)
+    with pytest.raises(engine_mod.AmdatError) as e:
+        eng.disp(99)
+    assert e.value.status == 1
+    with pytest.raises(engine_mod.AmdatError):
+        eng.list([3, 2])  # not ascending
+    # a scheme needing more frames than uploaded
+    eng.set_scheme(synth.TimeScheme.linear(500, 1.0))
+    with pytest.raises(engine_mod.AmdatError) as e:
+        eng.disp(0)
+    assert e.value.status == 2

@@ -1,0 +1,114 @@
+"""GPU parity of the Fourier densities rho(k,t), the coherent ISF correlator
+and S(k) against the FP64 oracle.  Tolerances: |rho_gpu - rho_oracle| <=
+2e-6 * sqrt(N) per element (N unit phasors); coherent F(k,t) and S(k) <= 1e-5
+relative to their values scaled by S(k) (F(k,0) = S(k))."""
+import numpy as np
+import pytest
+
+from amdat_gb300 import synth
+from golden.make_golden import load
+from oracle import oracle as orc
+from oracle import wavevectors as wv
+
+pytestmark = pytest.mark.gpu
+
+
+def _shells(qvec, m0, m1):
+    n, off = qvec
+    return n[off[m0]:off[m1 + 1]], off[m0:m1 + 2] - off[m0]
+
+
+@pytest.mark.parametrize("case", ["exp_small", "lin_binary"])
+def test_rhok_reference_shells(case, eng, qvectors):
+    traj, _, _ = load(case)
+    eng.upload(traj.unwrapped, traj.box)
+    eng.set_scheme(traj.scheme)
+    L = float(np.float32(traj.box.min()))
+    kv, off = _shells(qvectors, 0, 98)
+    frames = np.arange(traj.n_frames, dtype=np.int32)
+    h = eng.wave_density(0, kv, L, frames)
+    rho = eng.wave_density_read(h, len(frames), len(kv)).astype(np.float64)
+    lst = np.arange(traj.n_atoms, dtype=np.int32)
+    ref = orc.rhok(traj.wrapped(), lst, frames, kv, float(wv.spacing(L)), L, orc.F64)
+    err = np.abs(rho - ref).max() / np.sqrt(traj.n_atoms)
+    assert err <= 2e-6, err
+    eng.wave_density_free(h)
+
+
+@pytest.mark.parametrize("fb", [0, 1])
+def test_isf_and_sk_reference_shells(fb, eng, qvectors):
+    traj, _, _ = load("exp_small")
+    eng.upload(traj.unwrapped, traj.box)
+    eng.set_scheme(traj.scheme)
+    L = float(np.float32(traj.box.min()))
+    kv, off = _shells(qvectors, 0, 20)
+    frames = np.arange(traj.n_frames, dtype=np.int32)
+    h = eng.wave_density(0, kv, L, frames)
+    corr, pc = eng.isf(h, h, off, fullblock=fb)
+    N = traj.n_atoms
+    got = corr / (pc[:, None] * N)
+    lst = np.arange(N, dtype=np.int32)
+    s = orc.scheme(traj.scheme)
+    rho = orc.rhok(traj.wrapped(), lst, frames, kv, float(wv.spacing(L)), L, orc.F64)
+    ref = orc.isf(s, rho, rho, off, N, fb, orc.F64)
+    scale = np.maximum(np.abs(ref[0]), 1e-3)
+    assert (np.abs(got - ref) / scale).max() <= 1e-5
+    sk = eng.structure_factor(h, h, off) / (N * traj.n_frames)
+    ref_sk = orc.structure_factor(s, -1, traj.wrapped(), lst, kv, off, float(wv.spacing(L)), L,
+                                  orc.F64)
+    np.testing.assert_allclose(sk, ref_sk, rtol=1e-5, atol=1e-7)
+
+
+def test_rhok_lattice_mode(eng):
+    """All half-space lattice vectors |k| <= kmax, shell-sorted: every element
+    against the FP64 oracle on the returned vector list."""
+    box = 9.0
+    scheme = synth.TimeScheme.linear(4, 1.0)
+    traj = synth.random_walk(700, box, scheme, 0.1, seed=9, time_scaled=False)
+    eng.upload(traj.unwrapped, traj.box)
+    eng.set_scheme(scheme)
+    frames = np.arange(4, dtype=np.int32)
+    h, nk, ns = eng.wave_density_lattice(0, 9.0, 0.1, box, frames)
+    kv, off = eng.wave_density_vectors(h, nk, ns)
+    # half-space, |k| <= kmax, no duplicates, sorted into 0.1-wide shells
+    k = 2 * np.pi * np.linalg.norm(kv, axis=1) / box
+    assert (k <= 9.0 + 1e-9).all() and len(np.unique(kv, axis=0)) == nk
+    assert ((kv[:, 2] > 0) | ((kv[:, 2] == 0) & ((kv[:, 1] > 0) | ((kv[:, 1] == 0) & (kv[:, 0] > 0))))).all()
+    R = 9.0 * box / (2 * np.pi)
+    full = sum(1 for x in range(-20, 21) for y in range(-20, 21) for z in range(-20, 21)
+               if 0 < x * x + y * y + z * z <= R * R)
+    assert nk == full // 2
+    sh = np.repeat(np.arange(ns), np.diff(off))
+    assert (np.floor(k / 0.1).astype(int).clip(max=ns - 1) == sh).all()
+    rho = eng.wave_density_read(h, 4, nk).astype(np.float64)
+    lst = np.arange(traj.n_atoms, dtype=np.int32)
+    ref = orc.rhok(traj.wrapped(), lst, frames, kv, float(wv.spacing(box)), box, orc.F64)
+    err = np.abs(rho - ref).max() / np.sqrt(traj.n_atoms)
+    assert err <= 2e-6, err
+    # the same vectors through list mode agree
+    h2 = eng.wave_density(0, kv, box, frames)
+    rho2 = eng.wave_density_read(h2, 4, nk).astype(np.float64)
+    assert np.abs(rho2 - ref).max() / np.sqrt(traj.n_atoms) <= 2e-6
+
+
+def test_rhok_plain_fp64(eng, qvectors):
+    traj, _, _ = load("exp_frt")
+    eng.upload(traj.unwrapped, traj.box)
+    L = float(np.float32(traj.box.min()))
+    kv, off = _shells(qvectors, 0, 30)
+    frames = np.array([0, 5, 30], np.int32)
+    a = eng.wave_density_read(eng.wave_density(0, kv, L, frames), 3, len(kv))
+    b = eng.wave_density_read(eng.wave_density(0, kv, L, frames, precision=1), 3, len(kv))
+    assert np.abs(a - b).max() <= 2e-6 * np.sqrt(traj.n_atoms)
+
+
+def test_rhok_sublist(eng, qvectors):
+    traj, _, _ = load("lin_binary")
+    eng.upload(traj.unwrapped, traj.box)
+    L = float(np.float32(traj.box.min()))
+    kv, off = _shells(qvectors, 0, 10)
+    b = np.nonzero(traj.types == 1)[0].astype(np.int32)
+    h = eng.wave_density(eng.list(b), kv, L, np.array([3], np.int32))
+    rho = eng.wave_density_read(h, 1, len(kv)).astype(np.float64)
+    ref = orc.rhok(traj.wrapped(), b, np.array([3], np.int32), kv, float(wv.spacing(L)), L, orc.F64)
+    assert np.abs(rho - ref).max() <= 2e-6 * np.sqrt(len(b))
