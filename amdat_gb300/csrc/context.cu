@@ -79,8 +79,7 @@ __device__ __forceinline__ float wrap_coord(float u, float lo, float L) {
 template <class Real>
 __global__ void stage_kernel(const Real* __restrict__ raw, const Real* __restrict__ raw_w,
                              int32_t T, int32_t N, int32_t n_pad, float3 box, float3 lo,
-                             float* __restrict__ u, float* __restrict__ w,
-                             double* __restrict__ u64, double* __restrict__ w64) {
+                             float* __restrict__ u, float* __restrict__ w) {
   const int64_t total = (int64_t)T * N;
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < total;
        i += (int64_t)gridDim.x * blockDim.x) {
@@ -100,8 +99,6 @@ __global__ void stage_kernel(const Real* __restrict__ raw, const Real* __restric
         wc = wrap_coord((float)r[c], los[c], Ls[c]);
       }
       w[o] = wc;
-      if (u64) u64[o] = (double)r[c];
-      if (w64) w64[o] = raw_w ? (double)raw_w[i * 3 + c] : (double)wc;
     }
   }
 }
@@ -142,7 +139,7 @@ static void upload_impl(amdat_ctx* ctx, int32_t T, int32_t N, const Real* unwrap
   const int threads = 256;
   const int64_t blocks = std::min<int64_t>(ceil_div((int64_t)T * N, threads), (int64_t)ctx->n_sm * 16);
   stage_kernel<Real><<<(unsigned)blocks, threads, 0, ctx->stream>>>(
-      d_raw, d_raw_w, T, N, n_pad, b, l, ctx->u.ptr, ctx->w.ptr, nullptr, nullptr);
+      d_raw, d_raw_w, T, N, n_pad, b, l, ctx->u.ptr, ctx->w.ptr);
   check_launch("stage_kernel");
   count_launch(ctx);
   ctx->n_frames = T;
@@ -153,12 +150,15 @@ static void upload_impl(amdat_ctx* ctx, int32_t T, int32_t N, const Real* unwrap
   else std::memset(ctx->box_lo, 0, sizeof(ctx->box_lo));
   for (auto& kv : ctx->pair_cache) delete kv.second;
   ctx->pair_cache.clear();
-  // the FP64 copies for the plain path are built lazily from the same input,
-  // so keep the raw input on the device when it is small enough to matter
   AMDAT_CUDA(cudaStreamSynchronize(ctx->stream));
   ctx->have_traj = true;
-  // list 0 = all atoms (contiguous)
+  // list 0 = all atoms (contiguous); lists of a trajectory with another atom
+  // count no longer apply and are dropped
   if (ctx->lists.empty()) ctx->lists.push_back(new ListEntry());
+  if (ctx->lists[0]->n != N) {
+    for (size_t i = 1; i < ctx->lists.size(); ++i) delete ctx->lists[i];
+    ctx->lists.resize(1);
+  }
   ctx->lists[0]->n = N;
   ctx->lists[0]->first = 0;
   ctx->lists[0]->contiguous = true;
@@ -171,13 +171,97 @@ using namespace amdat;
 amdat_ctx::~amdat_ctx() {
   for (auto* l : lists) delete l;
   for (auto& kv : pair_cache) delete kv.second;
-  for (auto& kv : densities) delete kv.second;
+  for (auto& kv : densities) {
+    delete kv.second->rho;
+    delete kv.second;
+  }
+  for (auto* b : rho_pool) delete b;
+  amdat::lattice_plans_free(this);
+  for (auto& r : prof_pending) {
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  for (auto e : event_pool) cudaEventDestroy(e);
   if (own_stream) cudaStreamDestroy(own_stream);
 }
 
-// FP64 planes for the plain path, derived from the FP32 store: raw coordinates
-// are u + r(0) where r(0) is kept implicitly as frame 0's wrapped/unwrapped
-// input; the plain path instead keeps its own exact copy built at first use.
+namespace amdat {
+
+DevBuf<float2>* rho_acquire(amdat_ctx* ctx, size_t count) {
+  // smallest pooled buffer that fits, else a new one
+  int best = -1;
+  for (int i = 0; i < (int)ctx->rho_pool.size(); ++i)
+    if (ctx->rho_pool[i]->n >= count && (best < 0 || ctx->rho_pool[i]->n < ctx->rho_pool[best]->n))
+      best = i;
+  if (best >= 0) {
+    DevBuf<float2>* b = ctx->rho_pool[best];
+    ctx->rho_pool.erase(ctx->rho_pool.begin() + best);
+    return b;
+  }
+  auto* b = new DevBuf<float2>();
+  try {
+    b->reserve(count);
+  } catch (...) {
+    // free the pool and retry once before giving up
+    for (auto* q : ctx->rho_pool) delete q;
+    ctx->rho_pool.clear();
+    try {
+      b->reserve(count);
+    } catch (...) {
+      delete b;
+      throw;
+    }
+  }
+  return b;
+}
+
+void rho_release(amdat_ctx* ctx, DevBuf<float2>* b) {
+  if (b) ctx->rho_pool.push_back(b);
+}
+
+static cudaEvent_t take_event(amdat_ctx* ctx) {
+  if (!ctx->event_pool.empty()) {
+    cudaEvent_t e = ctx->event_pool.back();
+    ctx->event_pool.pop_back();
+    return e;
+  }
+  cudaEvent_t e;
+  AMDAT_CUDA(cudaEventCreate(&e));
+  return e;
+}
+
+KernelTimer::KernelTimer(amdat_ctx* c, const char* n) : ctx(c), name(n) {
+  if (!ctx->profiling) return;
+  a = take_event(ctx);
+  b = take_event(ctx);
+  cudaEventRecord(a, ctx->stream);
+}
+
+KernelTimer::~KernelTimer() {
+  if (!a) return;
+  cudaEventRecord(b, ctx->stream);
+  ctx->prof_pending.push_back(ProfRec{name, a, b});
+}
+
+static void prof_collect(amdat_ctx* ctx) {
+  for (auto& r : ctx->prof_pending) {
+    float ms = 0.f;
+    AMDAT_CUDA(cudaEventSynchronize(r.b));
+    AMDAT_CUDA(cudaEventElapsedTime(&ms, r.a, r.b));
+    auto& st = ctx->prof_stats[r.name];
+    st.first += 1;
+    st.second += ms;
+    ctx->event_pool.push_back(r.a);
+    ctx->event_pool.push_back(r.b);
+  }
+  ctx->prof_pending.clear();
+}
+
+}  // namespace amdat
+
+// FP64 planes for the plain path: the stored FP32 planes promoted to FP64 at
+// first use (displacements u(t1) - u(t0) and wrapped positions are then
+// formed in FP64 from the same values the mixed path reads).
 namespace amdat {
 __global__ void promote_kernel(const float* __restrict__ src, double* __restrict__ dst, int64_t n) {
   for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
@@ -309,6 +393,27 @@ amdat_status amdat_list_size(amdat_ctx* ctx, int32_t handle, int32_t* n) {
     check_ctx(ctx);
     AMDAT_REQUIRE(n != nullptr, "null output");
     *n = list_entry(ctx, handle).n;
+  });
+}
+
+amdat_status amdat_profile_reset(amdat_ctx* ctx, int32_t enable) {
+  return guarded([&] {
+    check_ctx(ctx);
+    prof_collect(ctx);
+    ctx->prof_stats.clear();
+    ctx->profiling = enable != 0;
+  });
+}
+
+amdat_status amdat_profile_kernel(amdat_ctx* ctx, const char* kernel, int64_t* launches,
+                                  double* total_ms) {
+  return guarded([&] {
+    check_ctx(ctx);
+    AMDAT_REQUIRE(kernel != nullptr, "null kernel name");
+    prof_collect(ctx);
+    auto it = ctx->prof_stats.find(kernel);
+    if (launches) *launches = it == ctx->prof_stats.end() ? 0 : it->second.first;
+    if (total_ms) *total_ms = it == ctx->prof_stats.end() ? 0.0 : it->second.second;
   });
 }
 

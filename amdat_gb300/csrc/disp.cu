@@ -526,6 +526,7 @@ static void disp_run_impl(amdat_ctx* ctx, const amdat_disp_request* req, const i
     pp.bin_size = NB ? (double)(req->bin_max / (float)NB) : 1.0;
     const int64_t blocks = P.n_pairs * pp.blocks_per_pair;
     if (blocks > 0 && lsize[0] > 0) {
+      KernelTimer kt(ctx, "disp_plain_kernel");
       disp_plain_kernel<<<(unsigned)blocks, 256, 0, ctx->stream>>>(pp);
       check_launch("disp_plain_kernel");
       count_launch(ctx);
@@ -633,6 +634,7 @@ static void disp_run_impl(amdat_ctx* ctx, const amdat_disp_request* req, const i
         int occ = 0;
         AMDAT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, threads, shm));
         const int grid = (int)std::min<int64_t>((int64_t)std::max(1, std::min(occ, blocks_per_sm)) * ctx->n_sm, n_items);
+        KernelTimer kt(ctx, "disp_mixed_kernel");
         kernel<<<grid, threads, shm, ctx->stream>>>(p);
         check_launch("disp_mixed_kernel");
         count_launch(ctx);

@@ -106,6 +106,8 @@ struct PairTable {
   DevBuf<int32_t> t0, t1, gap;
 };
 
+struct LatticePlanDev;
+
 struct Density {
   int32_t list = 0;
   int32_t n_k = 0;
@@ -114,7 +116,13 @@ struct Density {
   std::vector<int32_t> frames;     // system frame of each row
   std::vector<int32_t> kvec;       // [3*n_k] (lattice mode: shell-sorted)
   std::vector<int32_t> shell_off;  // lattice mode
-  DevBuf<float2> rho;              // [n_frames][n_k]
+  DevBuf<float2>* rho = nullptr;   // [n_frames][n_k], from the context's pool
+};
+
+// per-kernel CUDA-event timing (amdat_profile_*)
+struct ProfRec {
+  const char* name;
+  cudaEvent_t a, b;
 };
 
 }  // namespace amdat
@@ -146,6 +154,13 @@ struct amdat_ctx {
   amdat::DevBuf<unsigned char> scratch;
   amdat::DevBuf<unsigned char> scratch2;
   amdat::DevBuf<unsigned char> staging;
+  std::vector<amdat::DevBuf<float2>*> rho_pool;        // released density tables
+  std::map<std::string, amdat::LatticePlanDev*> lattice_plans;
+
+  bool profiling = false;
+  std::vector<amdat::ProfRec> prof_pending;
+  std::vector<cudaEvent_t> event_pool;
+  std::map<std::string, std::pair<int64_t, double>> prof_stats;  // launches, total ms
 
   ~amdat_ctx();
 };
@@ -158,5 +173,17 @@ Density& density(amdat_ctx* ctx, int32_t handle);
 void ensure_fp64(amdat_ctx* ctx);
 void count_launch(amdat_ctx* ctx, int n = 1);
 void check_launch(const char* what);
+DevBuf<float2>* rho_acquire(amdat_ctx* ctx, size_t count);
+void rho_release(amdat_ctx* ctx, DevBuf<float2>* b);
+void lattice_plans_free(amdat_ctx* ctx);
+
+// RAII event pair around one kernel launch when profiling is enabled
+struct KernelTimer {
+  amdat_ctx* ctx;
+  const char* name;
+  cudaEvent_t a = nullptr, b = nullptr;
+  KernelTimer(amdat_ctx* c, const char* n);
+  ~KernelTimer();
+};
 inline int64_t ceil_div(int64_t a, int64_t b) { return (a + b - 1) / b; }
 }  // namespace amdat

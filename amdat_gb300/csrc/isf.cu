@@ -192,8 +192,9 @@ amdat_status amdat_isf_run(amdat_ctx* ctx, int32_t h1, int32_t h2, int32_t fullb
       const size_t shm = (size_t)(same ? 1 : 2) * T * KT * sizeof(float2);
       auto launch = [&](auto kernel) {
         AMDAT_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+        KernelTimer kt(ctx, "isf_pairs_kernel");
         kernel<<<(unsigned)tiles.size(), 256, shm, ctx->stream>>>(
-            d1.rho.ptr, d2.rho.ptr, T, d1.n_k, (const KTile*)(base + o_t), P.t0.ptr, P.t1.ptr,
+            d1.rho->ptr, d2.rho->ptr, T, d1.n_k, (const KTile*)(base + o_t), P.t0.ptr, P.t1.ptr,
             (const int32_t*)(base + o_gf), G, part);
       };
       switch (KT) {
@@ -255,8 +256,9 @@ amdat_status amdat_structure_factor_run(amdat_ctx* ctx, int32_t h1, int32_t h2,
     double* part = (double*)(base + o_part);
     double* out = (double*)(base + o_out);
     if (!tiles.empty()) {
+      KernelTimer kt(ctx, "sk_frames_kernel");
       sk_frames_kernel<<<(unsigned)tiles.size(), 256, 0, ctx->stream>>>(
-          d1.rho.ptr, d2.rho.ptr, d1.n_frames, d1.n_k, (const KTile*)(base + o_t), part);
+          d1.rho->ptr, d2.rho->ptr, d1.n_frames, d1.n_k, (const KTile*)(base + o_t), part);
       check_launch("sk_frames_kernel");
       count_launch(ctx);
     }

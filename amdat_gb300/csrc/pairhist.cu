@@ -172,6 +172,7 @@ static void run_pair_hist(amdat_ctx* ctx, const ListEntry& l1, const ListEntry& 
       AMDAT_CUDA(cudaFuncSetAttribute(pair_hist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
     AMDAT_REQUIRE(n_q <= 65535, "at most 65535 frames or time pairs per call");
     dim3 grid((unsigned)ceil_div(l1.n, PH_THREADS), (unsigned)n_q);
+    KernelTimer kt(ctx, "pair_hist_kernel");
     pair_hist_kernel<<<grid, PH_THREADS, shm, ctx->stream>>>(p);
     check_launch("pair_hist_kernel");
     count_launch(ctx);

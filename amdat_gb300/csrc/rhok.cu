@@ -29,6 +29,7 @@
 // FP32 accumulators are folded into Kahan-compensated sums every 128 atoms.
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <numeric>
 
@@ -319,7 +320,7 @@ Density& density(amdat_ctx* ctx, int32_t h) {
 
 static void run_list_density(amdat_ctx* ctx, Density& d, float period, int32_t precision) {
   const ListEntry& e = list_entry(ctx, d.list);
-  d.rho.reserve((size_t)d.n_frames * std::max(d.n_k, 1));
+  if (!d.rho) d.rho = rho_acquire(ctx, (size_t)d.n_frames * std::max(d.n_k, 1));
   DevBuf<int4> kv;
   kv.reserve(std::max(d.n_k, 1));
   std::vector<int4> hk(d.n_k);
@@ -328,7 +329,7 @@ static void run_list_density(amdat_ctx* ctx, Density& d, float period, int32_t p
   if (d.n_k) AMDAT_CUDA(cudaMemcpyAsync(kv.ptr, hk.data(), d.n_k * sizeof(int4), cudaMemcpyHostToDevice, ctx->stream));
   DevBuf<int32_t> d_frames;
   if (e.n == 0 || d.n_k == 0) {
-    AMDAT_CUDA(cudaMemsetAsync(d.rho.ptr, 0, (size_t)d.n_frames * std::max(d.n_k, 1) * sizeof(float2), ctx->stream));
+    AMDAT_CUDA(cudaMemsetAsync(d.rho->ptr, 0, (size_t)d.n_frames * std::max(d.n_k, 1) * sizeof(float2), ctx->stream));
     AMDAT_CUDA(cudaStreamSynchronize(ctx->stream));
     return;
   }
@@ -337,15 +338,17 @@ static void run_list_density(amdat_ctx* ctx, Density& d, float period, int32_t p
     d_frames.reserve(d.n_frames);
     AMDAT_CUDA(cudaMemcpyAsync(d_frames.ptr, d.frames.data(), d.n_frames * 4, cudaMemcpyHostToDevice, ctx->stream));
     dim3 grid((unsigned)ceil_div(d.n_k, 128), (unsigned)d.n_frames);
+    KernelTimer kt(ctx, "rhok_plain_kernel");
     rhok_plain_kernel<<<grid, 128, 0, ctx->stream>>>(ctx->w64.ptr, ctx->n_pad, d_frames.ptr, view(e),
                                                       kv.ptr, d.n_k, 6.283185307179586476925286766559 / (double)period,
-                                                      d.rho.ptr);
+                                                      d.rho->ptr);
     check_launch("rhok_plain_kernel");
     count_launch(ctx);
   } else {
     int4* fx = fixed_turns(ctx, d, e, period, d_frames);
     dim3 grid((unsigned)ceil_div(d.n_k, RL_TILE), (unsigned)d.n_frames);
-    rhok_list_kernel<<<grid, RL_THREADS, 0, ctx->stream>>>(fx, e.n, kv.ptr, d.n_k, d.rho.ptr);
+    KernelTimer kt(ctx, "rhok_list_kernel");
+    rhok_list_kernel<<<grid, RL_THREADS, 0, ctx->stream>>>(fx, e.n, kv.ptr, d.n_k, d.rho->ptr);
     check_launch("rhok_list_kernel");
     count_launch(ctx);
   }
@@ -363,6 +366,20 @@ struct LatticePlan {
   std::vector<LatticeTile> tiles;
   std::vector<int32_t> entry_k;    // tile-major map to shell-sorted k, -1 = unused
 };
+
+}  // namespace amdat
+namespace amdat {
+struct LatticePlanDev {
+  std::vector<int32_t> kvec, shell_off;
+  DevBuf<LatticeTile> tiles;
+  DevBuf<int32_t> entry_k;
+  int32_t n_tiles = 0;
+};
+
+void lattice_plans_free(amdat_ctx* ctx) {
+  for (auto& kv : ctx->lattice_plans) delete kv.second;
+  ctx->lattice_plans.clear();
+}
 
 static LatticePlan plan_lattice(float kmax, float dk, float period) {
   const double two_pi = 6.283185307179586476925286766559;
@@ -446,6 +463,7 @@ amdat_status amdat_wave_density(amdat_ctx* ctx, int32_t list, const int32_t* kve
     try {
       run_list_density(ctx, *d, period, precision);
     } catch (...) {
+      rho_release(ctx, d->rho);
       delete d;
       throw;
     }
@@ -465,7 +483,23 @@ amdat_status amdat_wave_density_lattice(amdat_ctx* ctx, int32_t list, float kmax
     AMDAT_REQUIRE(precision == AMDAT_MIXED || precision == AMDAT_PLAIN_FP64, "bad precision");
     check_frames(ctx, frames, n_frames);
     const ListEntry& e = list_entry(ctx, list);
-    LatticePlan P = plan_lattice(kmax, dk, period);
+    // plans depend only on (kmax, dk, period): build once, keep on the device
+    char key[96];
+    std::snprintf(key, sizeof(key), "%a/%a/%a", (double)kmax, (double)dk, (double)period);
+    auto it = ctx->lattice_plans.find(key);
+    if (it == ctx->lattice_plans.end()) {
+      LatticePlan P = plan_lattice(kmax, dk, period);
+      auto* pd = new LatticePlanDev();
+      pd->kvec = std::move(P.kvec);
+      pd->shell_off = std::move(P.shell_off);
+      pd->n_tiles = (int32_t)P.tiles.size();
+      pd->tiles.reserve(P.tiles.size());
+      pd->entry_k.reserve(P.entry_k.size());
+      AMDAT_CUDA(cudaMemcpy(pd->tiles.ptr, P.tiles.data(), P.tiles.size() * sizeof(LatticeTile), cudaMemcpyHostToDevice));
+      AMDAT_CUDA(cudaMemcpy(pd->entry_k.ptr, P.entry_k.data(), P.entry_k.size() * 4, cudaMemcpyHostToDevice));
+      it = ctx->lattice_plans.emplace(key, pd).first;
+    }
+    const LatticePlanDev& P = *it->second;
     auto* d = new Density();
     d->list = list;
     d->n_k = (int32_t)(P.kvec.size() / 3);
@@ -478,22 +512,19 @@ amdat_status amdat_wave_density_lattice(amdat_ctx* ctx, int32_t list, float kmax
       if (precision == AMDAT_PLAIN_FP64 || e.n == 0) {
         run_list_density(ctx, *d, period, precision);
       } else {
-        d->rho.reserve((size_t)n_frames * std::max(d->n_k, 1));
-        DevBuf<LatticeTile> dt;
-        DevBuf<int32_t> de, d_frames;
-        dt.reserve(P.tiles.size());
-        de.reserve(P.entry_k.size());
-        AMDAT_CUDA(cudaMemcpyAsync(dt.ptr, P.tiles.data(), P.tiles.size() * sizeof(LatticeTile), cudaMemcpyHostToDevice, ctx->stream));
-        AMDAT_CUDA(cudaMemcpyAsync(de.ptr, P.entry_k.data(), P.entry_k.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+        d->rho = rho_acquire(ctx, (size_t)n_frames * std::max(d->n_k, 1));
+        DevBuf<int32_t> d_frames;
         int4* fx = fixed_turns(ctx, *d, e, period, d_frames);
-        dim3 grid((unsigned)P.tiles.size(), (unsigned)n_frames);
-        rhok_lattice_kernel<<<grid, LT_THREADS, 0, ctx->stream>>>(fx, e.n, dt.ptr, de.ptr, d->n_k,
-                                                                 d->rho.ptr);
+        dim3 grid((unsigned)P.n_tiles, (unsigned)n_frames);
+        KernelTimer kt(ctx, "rhok_lattice_kernel");
+        rhok_lattice_kernel<<<grid, LT_THREADS, 0, ctx->stream>>>(fx, e.n, P.tiles.ptr, P.entry_k.ptr,
+                                                                 d->n_k, d->rho->ptr);
         check_launch("rhok_lattice_kernel");
         count_launch(ctx);
         AMDAT_CUDA(cudaStreamSynchronize(ctx->stream));
       }
     } catch (...) {
+      rho_release(ctx, d->rho);
       delete d;
       throw;
     }
@@ -520,7 +551,7 @@ amdat_status amdat_wave_density_read(amdat_ctx* ctx, int32_t handle, int32_t out
     check_ctx(ctx);
     AMDAT_REQUIRE(rho != nullptr, "null output");
     Density& d = density(ctx, handle);
-    AMDAT_CUDA(cudaMemcpyAsync(rho, d.rho.ptr, (size_t)d.n_frames * d.n_k * sizeof(float2),
+    AMDAT_CUDA(cudaMemcpyAsync(rho, d.rho->ptr, (size_t)d.n_frames * d.n_k * sizeof(float2),
                                out_flags == AMDAT_OUT_DEVICE ? cudaMemcpyDeviceToDevice
                                                              : cudaMemcpyDeviceToHost,
                                ctx->stream));
@@ -534,6 +565,7 @@ amdat_status amdat_wave_density_free(amdat_ctx* ctx, int32_t handle) {
     auto it = ctx->densities.find(handle);
     if (it == ctx->densities.end()) throw Error(AMDAT_ERR_ARGUMENT, "unknown density handle");
     AMDAT_CUDA(cudaStreamSynchronize(ctx->stream));
+    rho_release(ctx, it->second->rho);
     delete it->second;
     ctx->densities.erase(it);
   });

@@ -50,6 +50,7 @@ EXPORTED = [
     "amdat_set_scheme", "amdat_wave_density", "amdat_wave_density_lattice",
     "amdat_wave_density_vectors", "amdat_wave_density_read", "amdat_wave_density_free",
     "amdat_isf_run", "amdat_structure_factor_run", "amdat_rdf_run", "amdat_vhd_run",
+    "amdat_profile_reset", "amdat_profile_kernel",
 ]
 
 _lib = None
@@ -165,6 +166,23 @@ class Engine:
         n = C.c_int64()
         _check(lib().amdat_launch_count(self._ctx, C.byref(n)))
         return n.value
+
+    def profile_reset(self, enable: bool = True):
+        _check(lib().amdat_profile_reset(self._ctx, int(enable)))
+
+    def profile_kernel(self, name: str):
+        """(launches, total device ms) of a kernel since the last profile_reset."""
+        n, ms = C.c_int64(), C.c_double()
+        _check(lib().amdat_profile_kernel(self._ctx, name.encode(), C.byref(n), C.byref(ms)))
+        return n.value, ms.value
+
+    def upload_ptr(self, host_ptr: int, n_frames: int, n_atoms: int, box, box_lo=None):
+        """Upload FP32 [T][N][3] coordinates from a raw host pointer (e.g. pinned memory)."""
+        box = np.ascontiguousarray(box, np.float32)
+        lo = None if box_lo is None else np.ascontiguousarray(box_lo, np.float32)
+        _check(lib().amdat_traj_upload(self._ctx, n_frames, n_atoms, C.c_void_p(host_ptr), None,
+                                       _p(box), _p(lo)))
+        self.n_frames, self.n_atoms = n_frames, n_atoms
 
     def upload(self, unwrapped, box, box_lo=None, wrapped=None):
         u = np.ascontiguousarray(unwrapped)

@@ -1,0 +1,474 @@
+"""Benchmark of the amdat_gb300 hot path on GB300.
+
+Headline workload (the reference's coherent-ISF + static S(k) configuration):
+binary 80:20 mixture, N = 32000 atoms, cubic box L = 33.6, 400 linear frames,
+Gaussian random-walk steps sigma = 0.03 per frame (seeded, synthetic).  One
+step = the whole coherent-ISF command: rho(k,t) for every half-space
+integer-lattice vector with |k| <= 20 (2,562,052 vectors; the other half
+space is the complex conjugate) over all 400 frames, the coherent F(k,t)
+correlator over all 79,801 time pairs of the linear scheme in 0.1-wide shells,
+and S(k).  Metric: atom*k/s = N * frames * vectors / step time.
+
+Secondary workload (the MSD + self-ISF configuration): N = 4000, L = 16.8,
+blocked-exponential 10 x 27 frames (base 1.3, unit 0.005), steps
+0.05*sqrt(dt); one step = MSD, NGP moments and F_s at all lattice vectors with
+|k| in [7.0, 7.2]; metric atom*time-pairs/s.
+
+Both report the mixed-precision engine against its plain FP64 GPU path.
+`--impl reference` times the CPU restatement of the reference algorithm on
+the host cores instead (the reference binary itself is x86-only here).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "atom·time-pairs/s (MSD+Fs) & atom·k/s (rho_k): mixed vs FP64 plain, 1 GB300"
+PEAKS_FILE = os.path.join(HERE, "MEASURED_PEAKS.json")
+FP32_LANES_PER_SM = 128
+
+
+# ---------------------------------------------------------------------------
+# workloads
+# ---------------------------------------------------------------------------
+def isf_workload(frames: int = 400, n_atoms: int = 32000):
+    from amdat_gb300 import synth
+    scheme = synth.TimeScheme.linear(frames, 1.0)
+    traj = synth.random_walk(n_atoms, 33.6, scheme, 0.03, seed=2, type_fractions=(0.8, 0.2),
+                             time_scaled=False)
+    return traj, scheme, dict(kmax=20.0, dk=0.1, period=33.6)
+
+
+def msd_workload():
+    from amdat_gb300 import synth
+    scheme = synth.TimeScheme.exponential(10, 27, 1.3, 0, 0, 0.005)
+    traj = synth.random_walk(4000, 16.8, scheme, 0.05, seed=1)
+    return traj, scheme
+
+
+def lattice_shell(period, kmin, kmax):
+    nmax = int(np.ceil(kmax * period / (2 * np.pi))) + 1
+    r = np.arange(-nmax, nmax + 1)
+    g = np.stack(np.meshgrid(r, r, r, indexing="ij"), -1).reshape(-1, 3)
+    k = 2 * np.pi * np.linalg.norm(g, axis=1) / period
+    return g[(k >= kmin) & (k <= kmax)].astype(np.int32)
+
+
+def lattice_halfspace(period, kmax):
+    nmax = int(np.floor(kmax * period / (2 * np.pi)))
+    r = np.arange(-nmax, nmax + 1)
+    g = np.stack(np.meshgrid(r, r, r, indexing="ij"), -1).reshape(-1, 3)
+    n2 = (g.astype(np.float64) ** 2).sum(1)
+    R = kmax * period / (2 * np.pi)
+    x, y, z = g[:, 0], g[:, 1], g[:, 2]
+    half = (z > 0) | ((z == 0) & ((y > 0) | ((y == 0) & (x > 0))))
+    return g[(n2 <= R * R) & half].astype(np.int32)
+
+
+# ---------------------------------------------------------------------------
+# environment: ranks, clocks, peaks
+# ---------------------------------------------------------------------------
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo")
+        pg = dist
+    return world, rank, local, pg
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.samples = []
+        self.proc = None
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) == 7:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=5)
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no nvidia-smi samples"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4)
+                          if s[3 + i].lower().startswith("active")})
+        pw = [float(s[2]) for s in self.samples if s[2].replace(".", "").isdigit()]
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "power_w_max": max(pw) if pw else None, "samples": len(self.samples)}
+
+
+def measured_peaks():
+    try:
+        with open(PEAKS_FILE) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline (restatement of the reference algorithm, all host threads)
+# ---------------------------------------------------------------------------
+def cpu_rhok_sample(traj, vectors, threads, target_s=12.0):
+    """rho(k) of one frame over a vector sample, FP64, OpenMP over vectors;
+    grows the sample until it takes about target_s."""
+    from oracle import oracle as orc
+    wrapped = traj.wrapped()
+    rng = np.random.default_rng(0)
+    nk = 2000
+    frames = np.array([traj.n_frames // 2], np.int32)
+    while True:
+        sel = vectors[rng.choice(len(vectors), size=min(nk, len(vectors)), replace=False)]
+        t0 = time.perf_counter()
+        orc.rhok_parallel(wrapped, frames, sel, float(traj.box[0]), threads)
+        dt = time.perf_counter() - t0
+        units = traj.n_atoms * len(sel)
+        if dt >= target_s / 4 or nk >= len(vectors):
+            return units / dt, f"1 frame x {len(sel)} random vectors x {traj.n_atoms} atoms", dt
+        nk = int(min(len(vectors), nk * max(2.0, (target_s / 4) / max(dt, 1e-3))))
+
+
+def cpu_disp_sample(traj, scheme, shell, threads):
+    from oracle import oracle as orc
+    s = orc.scheme(scheme)
+    t0 = time.perf_counter()
+    orc.disp_fs_parallel(s, traj.unwrapped, shell, float(traj.box[0]), threads)
+    dt = time.perf_counter() - t0
+    npairs = len(orc.pairs(s, 0)[0])
+    return npairs * traj.n_atoms / dt, f"all {npairs} time pairs x {traj.n_atoms} atoms, {len(shell)} vectors", dt
+
+
+def run_reference(args):
+    world, rank, local, pg = dist_setup()
+    if rank != 0:
+        return
+    from oracle import build_oracle
+    build_oracle.build_lib()
+    threads = os.cpu_count() or 1
+    traj, scheme, lat = isf_workload()
+    vectors = lattice_halfspace(lat["period"], lat["kmax"])
+    # size one step to a few seconds of host work
+    rate, sample, dt = cpu_rhok_sample(traj, vectors, threads, target_s=4.0 * max(1, 12 // max(args.steps, 1)))
+    vals = []
+    for _ in range(args.warmup):
+        cpu_rhok_sample(traj, vectors, threads, target_s=dt * 4)
+    for _ in range(args.steps):
+        r, sample, _ = cpu_rhok_sample(traj, vectors, threads, target_s=dt * 4)
+        vals.append(r)
+    value = statistics.median(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "atom·k/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * dt, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "coherent ISF + S(k): rho_k(t), N=32000, L=33.6, 400 linear "
+                                   "frames, all half-space lattice k with |k|<=20",
+                       "sample_per_step": sample},
+            "cpu_baseline": {"value": value, "unit": "atom·k/s", "cores": threads,
+                             "kind": "port", "sample": sample},
+            "e2e": {"value": value, "unit": "atom·k/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "note": "CPU restatement of the reference's Wave_Density loop (FP64, OpenMP over "
+                    "vectors); the reference binary builds only on the x86 host"}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# GPU arm
+# ---------------------------------------------------------------------------
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--frames", type=int, default=400, help="frames of the headline workload")
+    ap.add_argument("--only", default="", choices=["", "isf", "msd"],
+                    help="run one workload only (profiling)")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import torch
+    from amdat_gb300 import build
+    from amdat_gb300 import engine as E
+
+    world, rank, local, pg = dist_setup()
+    torch.cuda.set_device(local)
+    build.build()
+    peaks = measured_peaks()
+    sm_count = torch.cuda.get_device_properties(local).multi_processor_count
+    stream = torch.cuda.current_stream()
+    eng = E.Engine(local)
+    eng.set_stream(stream.cuda_stream)
+
+    def barrier():
+        if pg is not None:
+            pg.barrier()
+
+    def max_over_ranks(x):
+        if pg is None:
+            return x
+        t = torch.tensor([x], dtype=torch.float64)
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        return float(t.item())
+
+    result = {}
+    clocks = ClockSampler(local)
+    if args.only in ("", "isf"):
+        traj, scheme, lat = isf_workload(args.frames)
+        T, N = traj.n_frames, traj.n_atoms
+        eng.upload(traj.unwrapped, traj.box)
+        eng.set_scheme(scheme)
+        frames = np.arange(T, dtype=np.int32)
+        h, nk, ns = eng.wave_density_lattice(0, lat["kmax"], lat["dk"], lat["period"], frames)
+        kv, off = eng.wave_density_vectors(h, nk, ns)
+        eng.wave_density_free(h)
+        G = eng.n_timegaps
+        d_corr = torch.empty((G, ns), dtype=torch.float64, device="cuda")
+        d_pc = torch.empty(G, dtype=torch.int64, device="cuda")
+        d_sk = torch.empty(ns, dtype=torch.float64, device="cuda")
+
+        def step():
+            hh, _, _ = eng.wave_density_lattice(0, lat["kmax"], lat["dk"], lat["period"], frames)
+            eng.isf(hh, hh, off, out_device=(d_corr.data_ptr(), d_pc.data_ptr()))
+            eng.structure_factor(hh, hh, off, out_device=d_sk.data_ptr())
+            eng.wave_density_free(hh)
+
+        for _ in range(args.warmup):
+            step()
+        torch.cuda.synchronize()
+        barrier()
+        eng.profile_reset(True)
+        l0 = eng.launch_count()
+        clocks.start()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            step()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        clocks.stop()
+        barrier()
+        ms = e0.elapsed_time(e1) / args.steps
+        ms = max_over_ranks(ms)
+        launches = eng.launch_count() - l0
+        n_lat, ms_lat = eng.profile_kernel("rhok_lattice_kernel")
+        n_isf, ms_isf = eng.profile_kernel("isf_pairs_kernel")
+        eng.profile_reset(False)
+        units = float(N) * T * nk
+        value = units * world / (ms / 1e3)
+        # roofline of the dominant kernel: FP32 pipe, 8 flops (4 FMA: one complex
+        # multiply-accumulate) per atom*vector
+        lat_ms = ms_lat / max(n_lat, 1)
+        flops = 8.0 * N * T * nk
+        achieved = flops / (lat_ms / 1e3) / 1e12
+        clk = clocks.summary()
+        fp32_peak_max = 2 * FP32_LANES_PER_SM * sm_count * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
+        # plain FP64 path on one frame of the same workload
+        fr1 = np.array([T // 2], np.int32)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        hp, _, _ = eng.wave_density_lattice(0, lat["kmax"], lat["dk"], lat["period"], fr1, precision=1)
+        eng.synchronize()
+        plain_s = time.perf_counter() - t0
+        eng.wave_density_free(hp)
+        plain_rate = float(N) * nk / plain_s
+        # end to end through the C ABI: pinned host trajectory in, results out
+        pinned = torch.empty((T, N, 3), dtype=torch.float32, pin_memory=True)
+        pinned.numpy()[...] = traj.unwrapped
+        corr_h = np.zeros((G, ns))
+        sk_h = np.zeros(ns)
+
+        def e2e_step():
+            eng.upload_ptr(pinned.data_ptr(), T, N, traj.box)
+            eng.set_scheme(scheme)
+            hh, _, _ = eng.wave_density_lattice(0, lat["kmax"], lat["dk"], lat["period"], frames)
+            c, pc = eng.isf(hh, hh, off)
+            corr_h[...] = c
+            sk_h[...] = eng.structure_factor(hh, hh, off)
+            eng.wave_density_free(hh)
+
+        e2e_step()
+        torch.cuda.synchronize()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(max(1, min(args.steps, 2))):
+            e2e_step()
+        torch.cuda.synchronize()
+        e2e_ms = max_over_ranks(1e3 * (time.perf_counter() - t0) / max(1, min(args.steps, 2)))
+        result["isf"] = dict(
+            value=value, ms=ms, launches=launches, nk=nk, ns=ns, T=T, N=N,
+            lat_ms=lat_ms, n_lat=n_lat, isf_ms=ms_isf / max(n_isf, 1), achieved=achieved,
+            fp32_peak_max=fp32_peak_max, clocks=clk, plain_rate=plain_rate,
+            e2e=units * world / (e2e_ms / 1e3), e2e_ms=e2e_ms,
+            h2d=int(T * N * 3 * 4), d2h=int(G * ns * 8 + G * 8 + ns * 8))
+        del pinned
+
+    if args.only in ("", "msd"):
+        mtraj, mscheme = msd_workload()
+        shell = lattice_shell(16.8, 7.0, 7.2)
+        off = np.array([0, len(shell)], np.int32)
+        eng.upload(mtraj.unwrapped, mtraj.box)
+        eng.set_scheme(mscheme)
+        G = eng.n_timegaps
+        d_out = [torch.zeros(G, dtype=torch.float64, device="cuda") for _ in range(2)]
+        d_cnt = torch.zeros(G, dtype=torch.int64, device="cuda")
+        d_fs = torch.zeros(G, dtype=torch.float64, device="cuda")
+
+        def mstep(precision=0):
+            eng.disp_device((d_out[0].data_ptr(), d_out[1].data_ptr(), d_cnt.data_ptr(),
+                             d_fs.data_ptr(), 0), 0, shells=(shell, off), period=16.8,
+                            precision=precision)
+
+        for _ in range(max(3, args.warmup)):
+            mstep()
+        torch.cuda.synchronize()
+        msteps = 50
+        eng.profile_reset(True)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(msteps):
+            mstep()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        mms = max_over_ranks(e0.elapsed_time(e1) / msteps)
+        n_d, ms_d = eng.profile_kernel("disp_mixed_kernel")
+        eng.profile_reset(False)
+        npairs = int(d_cnt.sum().item()) // mtraj.n_atoms
+        munits = float(npairs) * mtraj.n_atoms
+        t0 = time.perf_counter()
+        mstep(precision=1)
+        eng.synchronize()
+        mplain = munits / (time.perf_counter() - t0)
+        result["msd"] = dict(value=munits * world / (mms / 1e3), ms=mms, kernel_ms=ms_d / max(n_d, 1),
+                             plain=mplain, npairs=npairs, nvec=len(shell))
+
+    # CPU baseline on rank 0 (bounded samples of both workloads)
+    cpu = None
+    if rank == 0 and not args.no_cpu and args.only in ("", "isf"):
+        from oracle import build_oracle
+        build_oracle.build_lib()
+        threads = os.cpu_count() or 1
+        traj, _, lat = isf_workload(args.frames)
+        vectors = lattice_halfspace(lat["period"], lat["kmax"])
+        rate, sample, dt = cpu_rhok_sample(traj, vectors, threads)
+        cpu = {"value": rate, "unit": "atom·k/s", "cores": threads, "kind": "port",
+               "sample": sample + f" ({dt:.1f} s)"}
+        if "msd" in result:
+            mtraj, mscheme = msd_workload()
+            r2, s2, dt2 = cpu_disp_sample(mtraj, mscheme, lattice_shell(16.8, 7.0, 7.2), threads)
+            result["msd"]["cpu"] = {"value": r2, "unit": "atom·time-pairs/s", "cores": threads,
+                                    "kind": "port", "sample": s2 + f" ({dt2:.1f} s)"}
+
+    if rank != 0:
+        eng.close()
+        return
+    line = {"metric": METRIC, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Gaussian random walk)"}
+    if "isf" in result:
+        r = result["isf"]
+        hbm = peaks.get("hbm_gbs")
+        line.update({
+            "value": r["value"], "unit": "atom·k/s", "ms_per_step": r["ms"],
+            "config": {"workload": f"coherent ISF + S(k): rho_k(t) over all half-space lattice k "
+                                   f"with |k|<=20 ({r['nk']} vectors, {r['ns']} shells of 0.1), "
+                                   f"N={r['N']} (80:20), L=33.6, {r['T']} linear frames, "
+                                   f"F(k,t) over all time pairs, S(k)",
+                       "global_batch": r["N"], "frames": r["T"], "vectors": r["nk"],
+                       "parallelism": f"replicas x{world}",
+                       "l2": "inputs larger than L2 (trajectory 154 MB, rho table "
+                             f"{r['T'] * r['nk'] * 8 / 1e9:.1f} GB); no flush"},
+            "roofline": {"bound": "fp32", "achieved": r["achieved"],
+                         "peak": r["fp32_peak_max"], "unit": "TFLOP/s",
+                         "frac": r["achieved"] / r["fp32_peak_max"], "traffic": None,
+                         "kernel": "rhok_lattice_kernel",
+                         "kernel_ms": r["lat_ms"], "kernel_launches": r["n_lat"],
+                         "flops_per_launch": 8.0 * r["N"] * r["T"] * r["nk"],
+                         "peak_source": "FP32 FMA peak = 2 x 128 lanes x SMs x sm_max_mhz of "
+                                        "MEASURED_PEAKS.json (the file has no FP32 figure; "
+                                        "HBM/bf16 peaks do not bound this kernel)",
+                         "hbm_peak_gbs": hbm},
+            "e2e": {"value": r["e2e"], "unit": "atom·k/s", "h2d_bytes_per_step": r["h2d"],
+                    "d2h_bytes_per_step": r["d2h"], "ms_per_step": r["e2e_ms"]},
+            "gpu_launches": r["launches"],
+            "clocks": r["clocks"],
+            "fp64_plain": {"value": r["plain_rate"], "unit": "atom·k/s",
+                           "sample": "1 frame, all vectors",
+                           "mixed_over_plain": r["value"] / world / r["plain_rate"]},
+            "isf_correlator_ms": r["isf_ms"],
+        })
+    if cpu:
+        line["cpu_baseline"] = cpu
+    if "msd" in result:
+        m = result["msd"]
+        sec = {"workload": f"MSD+NGP+F_s: N=4000, L=16.8, exponential 10x27 base 1.3, "
+                           f"{m['npairs']} time pairs, F_s over {m['nvec']} lattice vectors "
+                           f"|k| in [7.0,7.2]",
+               "value": m["value"], "unit": "atom·time-pairs/s", "ms_per_step": m["ms"],
+               "kernel_ms": m["kernel_ms"],
+               "fp64_plain": {"value": m["plain"], "mixed_over_plain": m["value"] / world / m["plain"]}}
+        if "cpu" in m:
+            sec["cpu_baseline"] = m["cpu"]
+        if "value" not in line:
+            line.update({"value": m["value"], "unit": "atom·time-pairs/s",
+                         "ms_per_step": m["ms"], "config": {"workload": sec["workload"]}})
+        else:
+            line["secondary"] = sec
+    print(json.dumps(line), flush=True)
+    eng.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -110,6 +110,16 @@ amdat_status amdat_set_stream(amdat_ctx* ctx, void* cuda_stream);
 amdat_status amdat_synchronize(amdat_ctx* ctx);
 /* number of kernels this context has launched (for launch accounting) */
 amdat_status amdat_launch_count(amdat_ctx* ctx, int64_t* count);
+/* Per-kernel timing: with enable != 0 every hot kernel launch is bracketed by
+ * CUDA events on the context's stream; amdat_profile_kernel returns the number
+ * of launches and their total device time (ms) since the last reset.  Kernel
+ * names: disp_mixed_kernel, disp_plain_kernel, rhok_list_kernel,
+ * rhok_lattice_kernel, rhok_plain_kernel, isf_pairs_kernel, sk_frames_kernel,
+ * pair_hist_kernel.  (No counterpart in the reference, which times commands
+ * with time(NULL), e.g. src/control.cpp:2190-2196.) */
+amdat_status amdat_profile_reset(amdat_ctx* ctx, int32_t enable);
+amdat_status amdat_profile_kernel(amdat_ctx* ctx, const char* kernel, int64_t* launches,
+                                  double* total_ms);
 
 /* Upload a trajectory: host arrays [n_frames][n_atoms][3] of unwrapped
  * coordinates and (optionally) wrapped ones.  With wrapped == NULL the wrapped
