@@ -533,15 +533,35 @@ static void disp_run_impl(amdat_ctx* ctx, const amdat_disp_request* req, const i
     }
   } else {
     // ---- mixed path
+    static thread_local std::string sh_key;
+    static thread_local ShellSet sh_cached;
     ShellSet sh;
     if (S) {
-      if (!octant_shells(req->shell_offsets, req->kvec_n, S, sh) || sh.nmax > 48)
-        list_shells(req->shell_offsets, req->kvec_n, S, sh);
+      std::string key((const char*)req->shell_offsets, sizeof(int32_t) * (S + 1));
+      key.append((const char*)req->kvec_n, sizeof(int32_t) * 3 * (size_t)req->shell_offsets[S]);
+      if (key == sh_key) {
+        sh = sh_cached;
+      } else {
+        if (!octant_shells(req->shell_offsets, req->kvec_n, S, sh) || sh.nmax > 48)
+          list_shells(req->shell_offsets, req->kvec_n, S, sh);
+        sh_key = std::move(key);
+        sh_cached = sh;
+      }
     }
     std::vector<DispItem> items;
     std::vector<int32_t> item_first(n_lg + 1, 0);
+    // chunk size: full chunks stream memory efficiently; with F_s (compute
+    // bound) or few pairs, smaller chunks keep every SM busy
+    int64_t total_atoms = 0;
+    for (int l = 0; l < n_lists; ++l) total_atoms += lsize[l];
+    const int64_t want_items = (int64_t)ctx->n_sm * 16;
+    int64_t chunk = DISP_CHUNK;
+    if (P.n_pairs > 0 && total_atoms > 0) {
+      const int64_t by_fill = ceil_div(total_atoms * P.n_pairs, want_items);
+      chunk = std::max<int64_t>(S ? 128 : 1024, std::min<int64_t>(DISP_CHUNK, by_fill));
+    }
     for (int l = 0; l < n_lists; ++l) {
-      const int nch = (int)std::max<int64_t>(1, ceil_div(lsize[l], DISP_CHUNK));
+      const int nch = (int)std::max<int64_t>(1, ceil_div(lsize[l], chunk));
       for (int g = 0; g < G; ++g) {
         item_first[(size_t)l * G + g] = (int32_t)items.size();
         if (lsize[l] == 0) continue;
@@ -631,8 +651,17 @@ static void disp_run_impl(amdat_ctx* ctx, const amdat_disp_request* req, const i
       int blocks_per_sm = mode ? 4 : 8;
       auto launch = [&](auto kernel) {
         if (shm > 48 * 1024) AMDAT_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+        // occupancy per (kernel, shared memory size), computed once
+        static thread_local std::map<std::pair<const void*, size_t>, int> occ_cache;
+        const auto okey = std::make_pair((const void*)kernel, shm);
         int occ = 0;
-        AMDAT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, threads, shm));
+        auto oit = occ_cache.find(okey);
+        if (oit != occ_cache.end()) {
+          occ = oit->second;
+        } else {
+          AMDAT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, threads, shm));
+          occ_cache[okey] = occ;
+        }
         const int grid = (int)std::min<int64_t>((int64_t)std::max(1, std::min(occ, blocks_per_sm)) * ctx->n_sm, n_items);
         KernelTimer kt(ctx, "disp_mixed_kernel");
         kernel<<<grid, threads, shm, ctx->stream>>>(p);

@@ -50,7 +50,7 @@ EXPORTED = [
     "amdat_set_scheme", "amdat_wave_density", "amdat_wave_density_lattice",
     "amdat_wave_density_vectors", "amdat_wave_density_read", "amdat_wave_density_free",
     "amdat_isf_run", "amdat_structure_factor_run", "amdat_rdf_run", "amdat_vhd_run",
-    "amdat_profile_reset", "amdat_profile_kernel",
+    "amdat_profile_reset", "amdat_profile_kernel", "amdat_run_script", "amdat_script_error",
 ]
 
 _lib = None
@@ -65,9 +65,10 @@ def lib():
         L = C.CDLL(LIB_PATH)
         L.amdat_version.restype = C.c_char_p
         L.amdat_last_error.restype = C.c_char_p
+        L.amdat_script_error.restype = C.c_char_p
         for name in EXPORTED:
             fn = getattr(L, name)
-            if name not in ("amdat_version", "amdat_last_error"):
+            if name not in ("amdat_version", "amdat_last_error", "amdat_script_error"):
                 fn.restype = C.c_int
         _lib = L
     return _lib
@@ -101,6 +102,13 @@ def make_scheme(ts, limit: int = 0) -> Scheme:
                                        C.c_float(1.0)))
     s.limit = limit
     return s
+
+
+def run_script(path: str, device: int = 0):
+    """Run an AMDAT input script (hot-path commands) through amdat_run_script."""
+    st = lib().amdat_run_script(path.encode(), int(device))
+    if st != 0:
+        raise AmdatError(st, lib().amdat_script_error().decode())
 
 
 def scheme_counts(s: Scheme, fullblock=0, loop_order=0):

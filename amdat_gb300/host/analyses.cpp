@@ -1,0 +1,406 @@
+// Analysis classes of the host mirror: each analyze() issues one engine call
+// for the whole time-pair scheduler and list, then normalises and writes the
+// reference's output file format (see amdat_host.h for the reference files).
+#include <algorithm>
+#include <cmath>
+#include <fstream>
+#include <iostream>
+
+#include "amdat_host.h"
+
+namespace amdat_host {
+
+namespace {
+
+// glibc on x86-64 prints the default quiet NaN of 0*inf as "-nan"; write that
+// on every host so output files match the reference's
+struct Num {
+  float v;
+};
+std::ostream& operator<<(std::ostream& o, Num n) {
+  if (std::isnan(n.v)) return o << "-nan";
+  return o << n.v;
+}
+
+std::ofstream open_out(const std::string& file) {
+  std::ofstream out(file.c_str());
+  if (!out) throw Error(AMDAT_ERR_ARGUMENT, "Cannot write to filename.");
+  return out;
+}
+
+struct DispOut {
+  std::vector<double> d2, d4, fs;
+  std::vector<int64_t> pairs, gs;
+};
+
+DispOut disp(System* sys, int list, bool fullblock, const std::vector<int32_t>* kvec,
+             const std::vector<int32_t>* off, float period, int n_bins, float bin_max) {
+  const int G = sys->n_timegaps();
+  amdat_disp_request r{};
+  r.list = list;
+  r.fullblock = fullblock ? 1 : 0;
+  r.precision = AMDAT_MIXED;
+  if (kvec && off) {
+    r.n_shells = (int32_t)off->size() - 1;
+    r.shell_offsets = off->data();
+    r.kvec_n = kvec->data();
+    r.kvec_period = period;
+  }
+  r.n_bins = n_bins;
+  r.bin_max = bin_max;
+  DispOut o;
+  o.d2.assign(G, 0);
+  o.d4.assign(G, 0);
+  o.pairs.assign(G, 0);
+  o.fs.assign((size_t)G * std::max(r.n_shells, 1), 0);
+  o.gs.assign((size_t)G * std::max(n_bins, 1), 0);
+  check(amdat_disp_run(sys->ctx(), &r, AMDAT_OUT_HOST, o.d2.data(), o.d4.data(), o.pairs.data(),
+                       r.n_shells ? o.fs.data() : nullptr, n_bins ? o.gs.data() : nullptr),
+        "displacement run");
+  return o;
+}
+
+const double PI_STCF = 3.141592653589793238462643383280;  // space_time_correlation_function.cpp:20
+const double PI_RDF = 3.1459265;                          // radial_distribution_function.cpp:11
+
+}  // namespace
+
+void Analysis::analyze(Trajectory_List*, Trajectory_List*) {
+  throw Error(AMDAT_ERR_ARGUMENT,
+              "Trajectory list targets with two lists not implemented for this analysis method.");
+}
+
+// --- MSD -------------------------------------------------------------------
+Mean_Square_Displacement::Mean_Square_Displacement(System* sys) { system = sys; }
+
+void Mean_Square_Displacement::analyze(Trajectory_List* list) {
+  // analyze(): displacement_list(this, false); msd /= weighting
+  DispOut o = disp(system, list->handle(), false, nullptr, nullptr, 1.f, 0, 0.f);
+  const int G = system->n_timegaps();
+  msd_.assign(G, 0.f);
+  weighting_.assign(G, 0.0);
+  sum_d4 = o.d4;
+  for (int g = 0; g < G; ++g) {
+    weighting_[g] = (double)o.pairs[g];
+    msd_[g] = (float)(o.d2[g] / (double)o.pairs[g]);
+  }
+}
+
+void Mean_Square_Displacement::write(const std::string& file) const {
+  std::ofstream out = open_out(file);
+  out << "Mean square displacement data created by AMDAT v." << SEMVER << "\n";
+  for (int g = 0; g < system->n_timegaps(); ++g)
+    out << system->timegaps()[g] << "\t" << Num{msd_[g]} << "\n";
+}
+
+// --- NGP -------------------------------------------------------------------
+Non_Gaussian_Parameter::Non_Gaussian_Parameter(System* sys) { system = sys; }
+
+void Non_Gaussian_Parameter::analyze(Trajectory_List* list) {
+  DispOut o = disp(system, list->handle(), false, nullptr, nullptr, 1.f, 0, 0.f);
+  const int G = system->n_timegaps();
+  ngp_.assign(G, 0.f);
+  for (int g = 0; g < G; ++g) {
+    // alpha2 = 3 <d^4> / (5 <d^2>^2) - 1 (non_gaussian_parameter.cpp:138);
+    // 0/0 at gap 0 gives NaN as in the reference
+    const double w = (double)o.pairs[g];
+    const double msd = o.d2[g] / w;
+    ngp_[g] = (float)(o.d4[g] * (3.0 / w) / (5.0 * msd * msd) - 1.0);
+  }
+}
+
+int Non_Gaussian_Parameter::max() const {
+  int best = -1;
+  float bv = 0;
+  for (int g = 1; g < (int)ngp_.size(); ++g)
+    if (ngp_[g] > bv) {
+      bv = ngp_[g];
+      best = g;
+    }
+  return best;
+}
+
+void Non_Gaussian_Parameter::write(const std::string& file) const {
+  std::ofstream out = open_out(file);
+  out << "Non-Gaussian parameter data created by AMDAT v." << SEMVER << "\n";
+  for (int g = 0; g < system->n_timegaps(); ++g)
+    out << system->timegaps()[g] << "\t" << Num{ngp_[g]} << "\n";
+}
+
+// --- F_s -------------------------------------------------------------------
+Incoherent_Scattering_Function::Incoherent_Scattering_Function(System* sys, const Wave_Vectors* wv,
+                                                               int inner, int outer, bool fb)
+    : wv_(wv), first_(inner), last_(outer), fullblock_(fb) {
+  system = sys;
+  if (inner < 0 || outer >= wv->n_shells() || outer < inner)
+    throw Error(AMDAT_ERR_ARGUMENT, "wavenumber index out of range");
+}
+
+void Incoherent_Scattering_Function::analyze(Trajectory_List* list) {
+  std::vector<int32_t> kv, off;
+  wv_->shells(first_, last_, kv, off);
+  DispOut o = disp(system, list->handle(), fullblock_, &kv, &off, wv_->period(), 0, 0.f);
+  const int G = system->n_timegaps(), S = last_ - first_ + 1;
+  corr_.assign((size_t)G * S, 0.f);
+  for (int g = 0; g < G; ++g)
+    for (int s = 0; s < S; ++s)
+      corr_[(size_t)g * S + s] = (float)(o.fs[(size_t)g * S + s] / (double)o.pairs[g]);
+}
+
+static void write_corr2d(const std::string& file, const System* sys, const Wave_Vectors* wv, int first,
+                         int last, const std::vector<float>& corr) {
+  // Correlation_2D::write (correlation_2d.cpp:475-504)
+  std::ofstream out = open_out(file);
+  out << "Correlation data created by AMDAT v." << SEMVER << "\n";
+  out << "\t";
+  for (int m = first; m <= last; ++m) out << wv->approx_wavenumber(m) << "\t";
+  out << "\n";
+  const int S = last - first + 1;
+  for (int g = 0; g < sys->n_timegaps(); ++g) {
+    out << sys->timegaps()[g] << "\t";
+    for (int s = 0; s < S; ++s) out << Num{corr[(size_t)g * S + s]} << "\t";
+    out << "\n";
+  }
+}
+
+void Incoherent_Scattering_Function::write(const std::string& file) const {
+  write_corr2d(file, system, wv_, first_, last_, corr_);
+}
+
+// --- van Hove self / distinct ------------------------------------------------
+Van_Hove_Self::Van_Hove_Self(System* sys, int n_bins, float max_value) : n_bins_(n_bins) {
+  system = sys;
+  if (n_bins < 1) throw Error(AMDAT_ERR_ARGUMENT, "need >= 1 bin");
+  // initialize(): max_value 0 means half the smallest box length (van_hove_self.cpp:53)
+  const Coord s = sys->size();
+  max_value_ = max_value == 0 ? std::min(s.x, std::min(s.y, s.z)) / 2 : max_value;
+  bin_size_ = max_value_ / (float)n_bins_;
+}
+
+static void normalise_stcf(const std::vector<int64_t>& counts, const std::vector<int64_t>& w,
+                           int G, int nb, float bin_size, std::vector<float>& corr) {
+  // Space_Time_Correlation_Function::postprocess_list (space_time_correlation_function.cpp:345-360)
+  corr.assign((size_t)G * nb, 0.f);
+  for (int b = 0; b < nb; ++b) {
+    const float rshell = b * bin_size;
+    const float shellvolume =
+        (float)((4.0 / 3.0) * PI_STCF * (std::pow(rshell + bin_size, 3.0) - std::pow(rshell, 3.0)));
+    for (int g = 0; g < G; ++g) {
+      float c = (float)counts[(size_t)g * nb + b];
+      c /= ((float)w[g] * shellvolume);
+      corr[(size_t)g * nb + b] = c;
+    }
+  }
+}
+
+void Van_Hove_Self::analyze(Trajectory_List* list) {
+  DispOut o = disp(system, list->handle(), false, nullptr, nullptr, 1.f, n_bins_, max_value_);
+  normalise_stcf(o.gs, o.pairs, system->n_timegaps(), n_bins_, bin_size_, corr_);
+}
+
+void Van_Hove_Self::write(const std::string& file) const {
+  // Space_Time_Correlation_Function::write (space_time_correlation_function.cpp:240-271)
+  std::ofstream out = open_out(file);
+  const int G = system->n_timegaps();
+  out << "Correlation data created by AMDAT v." << SEMVER << "\n";
+  out << n_bins_ << " bins\n";
+  out << G << " times\n\n";
+  out << "\t";
+  for (int b = 0; b < n_bins_; ++b) out << bin_size_ / 2 + float(b) * bin_size_ << "\t";
+  out << "\n";
+  for (int g = 0; g < G; ++g) {
+    out << system->timegaps()[g] << "\t";
+    for (int b = 0; b < n_bins_ - 1; ++b) out << Num{corr_[(size_t)g * n_bins_ + b]} << "\t";
+    out << Num{corr_[(size_t)g * n_bins_ + n_bins_ - 1]} << "\n";
+  }
+}
+
+Van_Hove_Distinct::Van_Hove_Distinct(System* sys, int n_bins, float max_value)
+    : Van_Hove_Self(sys, n_bins, max_value) {}
+
+void Van_Hove_Distinct::analyze(Trajectory_List* list) { analyze(list, list); }
+
+void Van_Hove_Distinct::analyze(Trajectory_List* a, Trajectory_List* b) {
+  const int G = system->n_timegaps();
+  std::vector<int64_t> counts((size_t)G * n_bins_);
+  check(amdat_vhd_run(system->ctx(), a->handle(), b->handle(), 0, max_value_, n_bins_,
+                      AMDAT_OUT_HOST, counts.data()),
+        "distinct van Hove run");
+  // weighting: sum over time pairs of n1(t0) * n2 less the i == j pairs
+  int64_t overlap = 0;
+  {
+    const auto& x = a->atoms();
+    const auto& y = b->atoms();
+    size_t i = 0, j = 0;
+    while (i < x.size() && j < y.size()) {
+      if (x[i] == y[j]) { ++overlap; ++i; ++j; }
+      else if (x[i] < y[j]) ++i;
+      else ++j;
+    }
+  }
+  int64_t np = 0;
+  int32_t T = 0, GG = 0;
+  check(amdat_scheme_counts(&system->scheme(), 0, 0, &T, &GG, &np), "scheme");
+  std::vector<int32_t> gap(np), t0(np), t1(np);
+  check(amdat_scheme_pairs(&system->scheme(), 0, 0, gap.data(), t0.data(), t1.data()), "pairs");
+  std::vector<int64_t> w(G, 0);
+  for (int64_t p = 0; p < np; ++p)
+    w[gap[p]] += (int64_t)a->show_n_trajectories() * b->show_n_trajectories() - overlap;
+  normalise_stcf(counts, w, G, n_bins_, bin_size_, corr_);
+}
+
+// --- Fourier densities -------------------------------------------------------
+Wave_Density::Wave_Density(System* sys, const Wave_Vectors* wv, int inner, int outer)
+    : system_(sys), wv_(wv), first_(inner), last_(outer) {
+  if (inner < 0 || outer >= wv->n_shells() || outer < inner)
+    throw Error(AMDAT_ERR_ARGUMENT, "wavenumber index out of range");
+}
+
+Wave_Density::~Wave_Density() {
+  if (handle_ >= 0) amdat_wave_density_free(system_->ctx(), handle_);
+}
+
+void Wave_Density::analyze(Trajectory_List* list) {
+  std::vector<int32_t> kv, off;
+  wv_->shells(first_, last_, kv, off);
+  std::vector<int32_t> frames(system_->n_timesteps());
+  for (int t = 0; t < (int)frames.size(); ++t) frames[t] = t;
+  if (handle_ >= 0) amdat_wave_density_free(system_->ctx(), handle_);
+  check(amdat_wave_density(system_->ctx(), list->handle(), kv.data(), (int32_t)kv.size() / 3,
+                           wv_->period(), frames.data(), (int32_t)frames.size(), AMDAT_MIXED,
+                           &handle_),
+        "wave density");
+  n_list_ = list->show_n_trajectories();
+}
+
+Intermediate_Scattering_Function::Intermediate_Scattering_Function(System* sys, Wave_Density* wd1,
+                                                                   Wave_Density* wd2, int inner,
+                                                                   int outer, bool fb)
+    : system_(sys), wv_(wd1->wavevectors()), first_(inner), last_(outer) {
+  if (wd1->wavevectors() != wd2->wavevectors())
+    throw Error(AMDAT_ERR_ARGUMENT, "Wave vectors for density distributions do not match!");
+  if (inner < wd1->first() || inner < wd2->first() || outer > wd1->last() || outer > wd2->last())
+    throw Error(AMDAT_ERR_ARGUMENT, "requested wavenumber outside the Fourier density's range");
+  const int G = sys->n_timegaps(), S = outer - inner + 1;
+  // shells inner..outer inside the densities' vector list
+  std::vector<int32_t> kv, off_all, off;
+  wv_->shells(wd1->first(), wd1->last(), kv, off_all);
+  for (int m = inner; m <= outer + 1; ++m) off.push_back(off_all[m - wd1->first()]);
+  std::vector<double> corr((size_t)G * S);
+  std::vector<int64_t> pc(G);
+  check(amdat_isf_run(sys->ctx(), wd1->handle(), wd2->handle(), fb ? 1 : 0, off.data(), S,
+                      AMDAT_OUT_HOST, corr.data(), pc.data()),
+        "coherent ISF");
+  // corr / (n_atoms * weighting) = corr / (pairs * N(t0)) (intermediate_scattering_function.cpp:312)
+  corr_.assign((size_t)G * S, 0.f);
+  for (int g = 0; g < G; ++g)
+    for (int s = 0; s < S; ++s)
+      corr_[(size_t)g * S + s] = (float)(corr[(size_t)g * S + s] / ((double)pc[g] * wd1->n_list()));
+}
+
+void Intermediate_Scattering_Function::write(const std::string& file) const {
+  write_corr2d(file, system_, wv_, first_, last_, corr_);
+}
+
+// --- S(k) ------------------------------------------------------------------
+Structure_Factor::Structure_Factor(System* sys, const Wave_Vectors* wv, int timescheme)
+    : wv_(wv), timescheme_(timescheme) {
+  system = sys;
+}
+
+void Structure_Factor::analyze(Trajectory_List* list) { analyze(list, list); }
+
+void Structure_Factor::analyze(Trajectory_List* a, Trajectory_List* b) {
+  std::vector<int32_t> kv, off;
+  const int S = wv_->n_shells();
+  wv_->shells(0, S - 1, kv, off);
+  const std::vector<int32_t> frames = onetime_frames(*system, timescheme_);
+  int32_t h1 = -1, h2 = -1;
+  check(amdat_wave_density(system->ctx(), a->handle(), kv.data(), (int32_t)kv.size() / 3,
+                           wv_->period(), frames.data(), (int32_t)frames.size(), AMDAT_MIXED, &h1),
+        "wave density");
+  if (b != a)
+    check(amdat_wave_density(system->ctx(), b->handle(), kv.data(), (int32_t)kv.size() / 3,
+                             wv_->period(), frames.data(), (int32_t)frames.size(), AMDAT_MIXED, &h2),
+          "wave density");
+  std::vector<double> s(S);
+  const amdat_status st = amdat_structure_factor_run(system->ctx(), h1, b != a ? h2 : h1, off.data(),
+                                                     S, AMDAT_OUT_HOST, s.data());
+  amdat_wave_density_free(system->ctx(), h1);
+  if (h2 >= 0) amdat_wave_density_free(system->ctx(), h2);
+  check(st, "structure factor");
+  // postprocess_list: S /= sum over frames of n(t) (structure_factor.cpp:272-285)
+  const double n_total = (double)a->show_n_trajectories() * frames.size();
+  sq_.assign(S, 0.f);
+  for (int m = 0; m < S; ++m) sq_[m] = n_total != 0 ? (float)(s[m] / n_total) : 0.f;
+}
+
+void Structure_Factor::write(const std::string& file) const {
+  std::ofstream out = open_out(file);
+  out << "Structure factor data created by AMDAT v." << SEMVER << "\n";
+  out << "Nominal_q\tMean_q\tStddev_q\tMean_qx\tMean_qy\tMean_qz\tS(q)\n";
+  for (int m = 0; m < wv_->n_shells(); ++m) {
+    const Coord mv = wv_->mean_wavevector(m);
+    out << wv_->approx_wavenumber(m) << "\t" << wv_->mean_wavenumber(m) << "\t"
+        << wv_->stdev_wavenumber(m) << "\t" << mv.x << "\t" << mv.y << "\t" << mv.z << "\t"
+        << Num{sq_[m]} << std::endl;
+  }
+  out << "\n";
+}
+
+// --- RDF -------------------------------------------------------------------
+Radial_Distribution_Function::Radial_Distribution_Function(System* sys, int n_bins, int timescheme,
+                                                           float maxdistance)
+    : n_bins_(n_bins), timescheme_(timescheme) {
+  system = sys;
+  if (n_bins < 1) throw Error(AMDAT_ERR_ARGUMENT, "need >= 1 bin");
+  // constructor (radial_distribution_function.cpp:32-79)
+  float minbox = sys->min_box();
+  if (std::fabs(minbox - 1.0f) <= 1e-7f) {
+    const Coord s = sys->size();
+    minbox = std::min(s.x, s.y);
+  }
+  max_distance_ = (maxdistance > 0 && maxdistance < minbox / 2) ? maxdistance : minbox / 2;
+  bin_size_ = max_distance_ / float(n_bins_);
+}
+
+void Radial_Distribution_Function::analyze(Trajectory_List* list) { analyze(list, list); }
+
+void Radial_Distribution_Function::analyze(Trajectory_List* a, Trajectory_List* b) {
+  const std::vector<int32_t> frames = onetime_frames(*system, timescheme_);
+  const int F = (int)frames.size();
+  std::vector<int64_t> counts((size_t)F * n_bins_);
+  check(amdat_rdf_run(system->ctx(), a->handle(), b->handle(), frames.data(), F, max_distance_,
+                      n_bins_, AMDAT_OUT_HOST, counts.data()),
+        "rdf run");
+  // postprocess_list (radial_distribution_function.cpp:256-285), FP32
+  const Coord box = system->size();
+  const float boxvolume = box.x * box.y * box.z;
+  const int ni = a->show_n_trajectories(), nj = b->show_n_trajectories();
+  mean_rdf_.assign(n_bins_, 0.f);
+  int n_i_total = 0;
+  for (int f = 0; f < F; ++f) {
+    const float rhoj = float(nj) / boxvolume;
+    n_i_total += ni;
+    for (int bi = 0; bi < n_bins_; ++bi) {
+      const float rshell = float(bi) * bin_size_;
+      const float shellvolume =
+          (float)((4.0 / 3.0) * PI_RDF * (std::pow(rshell + bin_size_, 3.0) - std::pow(rshell, 3.0)));
+      float t = (float)counts[(size_t)f * n_bins_ + bi];
+      t /= (float(ni) * rhoj * shellvolume);
+      mean_rdf_[bi] += t * float(ni);
+    }
+  }
+  for (int bi = 0; bi < n_bins_; ++bi) mean_rdf_[bi] /= float(n_i_total);
+}
+
+void Radial_Distribution_Function::write(const std::string& file) const {
+  std::ofstream out = open_out(file);
+  out << "Radial distribution function data created by AMDAT v." << SEMVER << "\n";
+  for (int b = 0; b < n_bins_; ++b) out << float(b) * bin_size_ + bin_size_ / 2 << "\t";
+  out << "\n";
+  for (int b = 0; b < n_bins_; ++b) out << Num{mean_rdf_[b]} << "\t";
+  out << "\n";
+}
+
+}  // namespace amdat_host

@@ -1,0 +1,239 @@
+// Input-script interpreter for the hot-path commands of AMDAT's Control
+// (src/control.cpp: system :191-240, create_list :1873, limit :1860, msd :2163,
+// ngp :3345, isfs :3198, isf :3107, structure_factor :2655, rdf :2836,
+// vhs :2517, vhd :2559, pathcheck :1136).  Command lines, their arguments and
+// the "list <name>" target lines are read exactly as the reference reads
+// them; output files are written by the analysis classes.  Failures are
+// reported as an amdat_status with a message instead of exit().
+#include <filesystem>
+#include <fstream>
+#include <iostream>
+#include <map>
+
+#include "amdat_host.h"
+
+namespace amdat_host {
+
+namespace {
+
+class Control {
+ public:
+  explicit Control(int device) : device_(device) {}
+
+  void run(const std::string& path) {
+    std::ifstream in(path);
+    if (!in) throw Error(AMDAT_ERR_ARGUMENT, "input file " + path + " not found");
+    std::string line;
+    while (std::getline(in, line)) {
+      const auto t = tokenize(line);
+      if (t.empty() || t[0].find('#') != std::string::npos) continue;
+      lines_.push_back(line);
+    }
+    while (pos_ < lines_.size()) execute(tokenize(lines_[pos_++]));
+  }
+
+ private:
+  std::string read_line() {
+    if (pos_ >= lines_.size()) throw Error(AMDAT_ERR_ARGUMENT, "input script ended early");
+    return lines_[pos_++];
+  }
+
+  static void pathcheck(const std::string& f) {
+    const std::filesystem::path p(f);
+    if (!std::filesystem::is_directory(p.parent_path()))
+      throw Error(AMDAT_ERR_ARGUMENT, "Cannot write to filename.");
+  }
+
+  static void argcheck(const std::vector<std::string>& a, size_t lo, size_t hi) {
+    if (a.size() < lo || a.size() > hi)
+      throw Error(AMDAT_ERR_ARGUMENT, "Incorrect number of arguments for " + a[0] + ".");
+  }
+
+  System& sys() {
+    if (!sys_) throw Error(AMDAT_ERR_STATE, "no system defined before " + lines_[pos_ - 1]);
+    return *sys_;
+  }
+
+  Trajectory_List* list(const std::string& name) {
+    auto it = lists_.find(name);
+    if (it == lists_.end()) throw Error(AMDAT_ERR_ARGUMENT, "Trajectory list '" + name + "' not found.");
+    return it->second.get();
+  }
+
+  // target line "list <name> [<name2>]"
+  std::vector<Trajectory_List*> targets() {
+    const auto a = tokenize(read_line());
+    if (a.size() < 2 || a[0] != "list")
+      throw Error(AMDAT_ERR_ARGUMENT, "only 'list <name>' targets are supported by this engine");
+    std::vector<Trajectory_List*> out;
+    for (size_t i = 1; i < a.size(); ++i) out.push_back(list(a[i]));
+    return out;
+  }
+
+  void analyze_write(Analysis& an, const std::string& file) {
+    auto t = targets();
+    if (t.size() == 1) an.analyze(t[0]);
+    else an.analyze(t[0], t[1]);
+    an.write(file);
+  }
+
+  // selection commands of Analysis::analyze(string) (src/analysis.cpp:130-209)
+  std::vector<int32_t> select(const std::vector<std::string>& a) {
+    std::vector<int32_t> out;
+    const auto& ty = sys().atom_types();
+    const auto& sp = sys().atom_species();
+    size_t i = 0;
+    while (i < a.size()) {
+      const std::string& c = a[i++];
+      if (c == "all") {
+        for (int k = 0; k < sys().n_atoms(); ++k) out.push_back(k);
+      } else if (c == "type_system") {
+        if (i >= a.size()) throw Error(AMDAT_ERR_ARGUMENT, "Insufficient arguments for type_system.");
+        const int t = sys().atomtype_index(a[i++]);
+        if (t < 0) throw Error(AMDAT_ERR_ARGUMENT, "atom type not found.");
+        for (int k = 0; k < sys().n_atoms(); ++k)
+          if (ty[k] == t) out.push_back(k);
+      } else if (c == "species") {
+        if (i >= a.size()) throw Error(AMDAT_ERR_ARGUMENT, "Insufficient arguments for species.");
+        const int s = sys().species_index(a[i++]);
+        if (s < 0) throw Error(AMDAT_ERR_ARGUMENT, "species not found.");
+        for (int k = 0; k < sys().n_atoms(); ++k)
+          if (sp[k] == s) out.push_back(k);
+      } else if (c == "type_species") {
+        if (i + 1 >= a.size()) throw Error(AMDAT_ERR_ARGUMENT, "Insufficient arguments for type_species.");
+        const int s = sys().species_index(a[i++]);
+        const int t = sys().atomtype_index(a[i++]);
+        if (s < 0 || t < 0) throw Error(AMDAT_ERR_ARGUMENT, "species or atom type not found.");
+        for (int k = 0; k < sys().n_atoms(); ++k)
+          if (sp[k] == s && ty[k] == t) out.push_back(k);
+      } else {
+        throw Error(AMDAT_ERR_ARGUMENT, "Atom set command " + c + " for analysis not understood.");
+      }
+    }
+    return out;
+  }
+
+  void execute(const std::vector<std::string>& a) {
+    const std::string& cmd = a[0];
+    if (cmd == "system" || cmd == "system_nv") {
+      std::vector<std::string> block;
+      for (int k = 0; k < 4; ++k) block.push_back(read_line());
+      const size_t n_species = tokenize(block[3]).size() / 2;
+      block.push_back(read_line());  // atom types
+      for (size_t s = 0; s < n_species; ++s) block.push_back(read_line());
+      lists_.clear();
+      sys_.reset();
+      sys_ = std::make_unique<System>(block, device_);
+    } else if (cmd == "limit") {
+      argcheck(a, 2, 2);
+      sys().set_limit(std::atoi(a[1].c_str()));
+    } else if (cmd == "create_list") {
+      argcheck(a, 2, 2);
+      auto sel = select(tokenize(read_line()));
+      lists_[a[1]] = std::make_unique<Trajectory_List>(&sys(), std::move(sel));
+    } else if (cmd == "msd") {
+      argcheck(a, 2, 2);
+      pathcheck(a[1]);
+      Mean_Square_Displacement m(&sys());
+      analyze_write(m, a[1]);
+    } else if (cmd == "ngp") {
+      argcheck(a, 2, 2);
+      pathcheck(a[1]);
+      Non_Gaussian_Parameter n(&sys());
+      analyze_write(n, a[1]);
+    } else if (cmd == "isfs") {
+      argcheck(a, 6, 7);
+      pathcheck(a[1]);
+      Wave_Vectors wv(&sys(), a[4], (float)std::atof(a[5].c_str()));
+      Incoherent_Scattering_Function f(&sys(), &wv, std::atoi(a[2].c_str()), std::atoi(a[3].c_str()),
+                                       a.size() == 7 && std::atoi(a[6].c_str()) != 0);
+      analyze_write(f, a[1]);
+    } else if (cmd == "vhs") {
+      argcheck(a, 4, 4);
+      pathcheck(a[1]);
+      Van_Hove_Self v(&sys(), std::atoi(a[3].c_str()), (float)std::atof(a[2].c_str()));
+      analyze_write(v, a[1]);
+    } else if (cmd == "vhd") {
+      argcheck(a, 5, 5);
+      pathcheck(a[1]);
+      Van_Hove_Distinct v(&sys(), std::atoi(a[4].c_str()), (float)std::atof(a[3].c_str()));
+      analyze_write(v, a[1]);
+    } else if (cmd == "structure_factor") {
+      argcheck(a, 6, 6);
+      pathcheck(a[1]);
+      Wave_Vectors wv(&sys(), a[3], (float)std::atof(a[4].c_str()));
+      Structure_Factor s(&sys(), &wv, std::atoi(a[5].c_str()));
+      auto t1 = targets();
+      if (a[2] == "symmetric") s.analyze(t1[0]);
+      else if (a[2] == "asymmetric") s.analyze(t1[0], targets()[0]);
+      else throw Error(AMDAT_ERR_ARGUMENT, "structure factor symmetry must be symmetric or asymmetric");
+      s.write(a[1]);
+    } else if (cmd == "isf") {
+      argcheck(a, 8, 8);
+      if (a[2] != "auto") throw Error(AMDAT_ERR_ARGUMENT, "only the 'auto' isf method is supported");
+      pathcheck(a[1]);
+      Wave_Vectors wv(&sys(), a[4]);
+      const int inner = std::atoi(a[6].c_str()), outer = std::atoi(a[7].c_str());
+      Wave_Density wd1(&sys(), &wv, inner, outer);
+      wd1.analyze(targets()[0]);
+      if (a[3] == "symmetric") {
+        Intermediate_Scattering_Function f(&sys(), &wd1, &wd1, inner, outer, std::atoi(a[5].c_str()) != 0);
+        f.write(a[1]);
+      } else if (a[3] == "asymmetric") {
+        Wave_Density wd2(&sys(), &wv, inner, outer);
+        wd2.analyze(targets()[0]);
+        Intermediate_Scattering_Function f(&sys(), &wd1, &wd2, inner, outer, std::atoi(a[5].c_str()) != 0);
+        f.write(a[1]);
+      } else {
+        throw Error(AMDAT_ERR_ARGUMENT, "isf symmetry must be symmetric or asymmetric");
+      }
+    } else if (cmd == "rdf") {
+      argcheck(a, 6, 6);
+      pathcheck(a[1]);
+      Radial_Distribution_Function r(&sys(), std::atoi(a[3].c_str()), std::atoi(a[4].c_str()),
+                                     (float)std::atof(a[5].c_str()));
+      auto t1 = targets();
+      if (a[2] == "symmetric") r.analyze(t1[0]);
+      else if (a[2] == "asymmetric") r.analyze(t1[0], targets()[0]);
+      else throw Error(AMDAT_ERR_ARGUMENT, "rdf symmetry must be symmetric or asymmetric");
+      r.write(a[1]);
+    } else {
+      throw Error(AMDAT_ERR_ARGUMENT, "command '" + cmd + "' is not part of this engine's hot path");
+    }
+  }
+
+  int device_;
+  std::vector<std::string> lines_;
+  size_t pos_ = 0;
+  std::unique_ptr<System> sys_;
+  std::map<std::string, std::unique_ptr<Trajectory_List>> lists_;
+};
+
+}  // namespace
+
+int run_script(const std::string& path, int device, std::string* error) {
+  try {
+    Control c(device);
+    c.run(path);
+    return AMDAT_OK;
+  } catch (const Error& e) {
+    if (error) *error = e.what();
+    return e.status;
+  } catch (const std::exception& e) {
+    if (error) *error = e.what();
+    return AMDAT_ERR_ARGUMENT;
+  }
+}
+
+}  // namespace amdat_host
+
+static thread_local std::string g_script_error;
+
+extern "C" amdat_status amdat_run_script(const char* input_path, int32_t device) {
+  g_script_error.clear();
+  if (!input_path) return AMDAT_ERR_ARGUMENT;
+  const int s = amdat_host::run_script(input_path, device, &g_script_error);
+  return (amdat_status)s;
+}
+
+extern "C" const char* amdat_script_error(void) { return g_script_error.c_str(); }

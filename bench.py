@@ -247,7 +247,10 @@ def main():
     build.build()
     peaks = measured_peaks()
     sm_count = torch.cuda.get_device_properties(local).multi_processor_count
-    stream = torch.cuda.current_stream()
+    # a dedicated stream: the engine launches on it and the CUDA events below
+    # are recorded on it (torch's default stream is the legacy NULL stream)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     eng = E.Engine(local)
     eng.set_stream(stream.cuda_stream)
 

@@ -234,6 +234,18 @@ amdat_status amdat_rdf_run(amdat_ctx* ctx, int32_t list1, int32_t list2, const i
 amdat_status amdat_vhd_run(amdat_ctx* ctx, int32_t list1, int32_t list2, int32_t fullblock,
                            float max_distance, int32_t n_bins, int32_t out_flags, int64_t* counts);
 
+/* ---------------------------------------------------------------------------
+ * Input scripts: run an AMDAT input file's hot-path commands (system with a
+ * custom dump, create_list, limit, msd, ngp, isfs, isf, structure_factor, rdf,
+ * vhs, vhd) on one GPU and write the reference's output files.  Replaces
+ * Control::Control / execute_commands (src/control.cpp:108, :191) for those
+ * commands; q-vector files are read from the prefix in AMDAT_QVECTORS
+ * (the reference's compiled-in WV3D).  Errors return a status; the message
+ * is in amdat_script_error().
+ * ------------------------------------------------------------------------- */
+amdat_status amdat_run_script(const char* input_path, int32_t device);
+const char* amdat_script_error(void);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,70 @@
+"""Drop-in check: the engine's command-line driver runs the golden input
+scripts unchanged and writes the reference's output files.  Integer-count
+outputs (vhs, rdf) must match the reference binary's files token for token;
+floating-point outputs must agree with the FP64 oracle to the 6 printed
+digits (+-2 in the last) and with the reference's own FP32 results to its
+accuracy (2e-3 relative)."""
+import math
+import os
+
+import pytest
+
+from amdat_files import tokens, ulp_close
+from cli_util import run_cli
+from golden.make_golden import CASES, load
+from oracle import oracle as orc
+from oracle_script import OracleRun
+
+pytestmark = pytest.mark.gpu
+
+EXACT = ("vhs", "rdf")
+
+
+def _num(t):
+    try:
+        return float(t)
+    except ValueError:
+        return None
+
+
+@pytest.mark.parametrize("case", sorted(CASES))
+def test_cli_matches_reference_files(case, tmp_path, engine_mod, qvectors):
+    traj, script, golden = load(case)
+    r = run_cli(traj, script, str(tmp_path), qvectors)
+    assert r.returncode == 0, r.stdout[-2000:] + r.stderr[-2000:]
+    f64 = OracleRun(traj, qvectors, orc.F64).run(script)
+    for name, ref_text in golden.items():
+        got_text = open(os.path.join(tmp_path, name)).read()
+        got_lines, ref_lines = got_text.splitlines(), ref_text.splitlines()
+        assert len(got_lines) == len(ref_lines), name
+        # header names the producing program; everything after it is data
+        got, ref, o64 = (tokens("\n".join(x.splitlines()[1:])) for x in (got_text, ref_text, f64[name]))
+        assert len(got) == len(ref) == len(o64), name
+        mism = 0
+        for g, w, o in zip(got, ref, o64):
+            fg, fw = _num(g), _num(w)
+            if fg is None or fw is None:
+                assert g == w, (name, g, w)
+                continue
+            if name.startswith(EXACT):
+                mism += g != w
+                continue
+            if math.isnan(fw):
+                assert math.isnan(fg), (name, g, w)
+                continue
+            assert abs(fg - fw) <= 2e-3 * max(abs(fw), 1e-2), (name, g, w)
+            assert ulp_close(g, o, 2), (name, g, o)
+        assert mism <= 2, f"{case}/{name}: {mism} count-derived tokens differ"
+
+
+def test_cli_errors(tmp_path, engine_mod, qvectors):
+    traj, script, _ = load("exp_frt")
+    r = run_cli(traj, "create_list all\nall\nmsd ./no_such_dir/msd.dat\nlist all\n", str(tmp_path))
+    assert r.returncode == 1 and "Cannot write to filename" in r.stderr
+    r = run_cli(traj, "create_list all\nall\nmsd ./m.dat\nlist nothere\n", str(tmp_path))
+    assert r.returncode == 1 and "not found" in r.stderr
+    r = run_cli(traj, "create_list all\nall\nisfs ./f.dat 3 200 xyz 0\nlist all\n", str(tmp_path), qvectors)
+    assert r.returncode == 1 and "out of range" in r.stderr
+    r = run_cli(traj, "create_list all\nall\nisfs ./f.dat 3 4 xyz 0\nlist all\n", str(tmp_path),
+                extra_env={"AMDAT_QVECTORS": str(tmp_path / "missing" / "qvector")})
+    assert r.returncode == 1 and "vector file" in r.stderr
