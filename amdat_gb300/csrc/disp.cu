@@ -31,7 +31,10 @@
 //                  so a vector costs ~0.6 FMA instead of a cosine.
 #include <algorithm>
 #include <array>
+#include <cstdio>
+#include <cstdlib>
 #include <map>
+#include <memory>
 #include <cmath>
 #include <cstring>
 
@@ -66,6 +69,7 @@ struct DispParams {
   int32_t n_items;
   const ListDev* lists;
   int32_t* counter;
+  const int32_t* schedule;  // processing order of items (locality), nullptr = table order
   double* part;  // [n_items][n_out]
   int32_t n_out;
   int32_t want_moments;
@@ -138,8 +142,9 @@ __global__ void __launch_bounds__(MODE == 0 ? DISP_THREADS : FS_THREADS)
   for (;;) {
     if (tid == 0) s_item = atomicAdd(p.counter, 1);
     __syncthreads();
-    const int item = s_item;
-    if (item >= p.n_items) break;
+    const int slot = s_item;
+    if (slot >= p.n_items) break;
+    const int item = p.schedule ? __ldg(p.schedule + slot) : slot;
     const DispItem it = p.items[item];
     const ListDev L = p.lists[it.list];
     const int t0 = p.t0[it.pair], t1 = p.t1[it.pair], g = p.gap[it.pair];
@@ -451,251 +456,431 @@ static void to_out(amdat_ctx* ctx, T* dst, const T* dev_src, size_t n, int32_t f
                              ctx->stream));
 }
 
+// ---------------------------------------------------------------------------
+// plain FP64 path (one list, direct kernels)
+// ---------------------------------------------------------------------------
+static void disp_plain(amdat_ctx* ctx, const amdat_disp_request* req, int32_t out_flags,
+                       double* sum_d2, double* sum_d4, int64_t* atom_pairs, double* fs_sum,
+                       int64_t* gs_counts) {
+  const PairTable& P = pair_table(ctx, req->fullblock != 0, false);
+  const int G = P.n_gaps, S = req->n_shells, NB = req->n_bins;
+  const ListEntry& e = list_entry(ctx, req->list);
+  ensure_fp64(ctx);
+  const size_t n_lg = (size_t)G;
+  ShellSet sh;
+  if (S) list_shells(req->shell_offsets, req->kvec_n, S, sh);
+  auto align = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  size_t o = 0;
+  const size_t o_d2 = o; o = align(o + n_lg * 8);
+  const size_t o_d4 = o; o = align(o + n_lg * 8);
+  const size_t o_fs = o; o = align(o + n_lg * std::max(S, 1) * 8);
+  const size_t o_gs = o; o = align(o + n_lg * std::max(NB, 1) * 8);
+  const size_t o_kv = o; o = align(o + std::max<size_t>(sh.kv.size(), 1) * sizeof(int4));
+  const size_t o_off = o; o = align(o + std::max<size_t>(sh.off.size(), 1) * 4);
+  unsigned char* base = ctx->scratch.reserve(o);
+  AMDAT_CUDA(cudaMemsetAsync(base, 0, o_kv, ctx->stream));
+  if (S) {
+    AMDAT_CUDA(cudaMemcpyAsync(base + o_kv, sh.kv.data(), sh.kv.size() * sizeof(int4), cudaMemcpyHostToDevice, ctx->stream));
+    AMDAT_CUDA(cudaMemcpyAsync(base + o_off, sh.off.data(), sh.off.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+  }
+  PlainParams pp{};
+  pp.u = ctx->u64.ptr;
+  pp.n_pad = ctx->n_pad;
+  pp.t0 = P.t0.ptr;
+  pp.t1 = P.t1.ptr;
+  pp.gap = P.gap.ptr;
+  pp.n_pairs = P.n_pairs;
+  pp.list = ListDev{e.n, e.first, e.contiguous ? nullptr : e.idx.ptr};
+  pp.blocks_per_pair = (int32_t)std::max<int64_t>(1, ceil_div(e.n, 256));
+  pp.d2 = (double*)(base + o_d2);
+  pp.d4 = (double*)(base + o_d4);
+  pp.fs = (double*)(base + o_fs);
+  pp.n_shells = S;
+  pp.kv = (const int4*)(base + o_kv);
+  pp.kv_off = (const int32_t*)(base + o_off);
+  pp.two_pi_over_l = S ? 6.283185307179586476925286766559 / (double)req->kvec_period : 0.0;
+  pp.gs = (unsigned long long*)(base + o_gs);
+  pp.n_bins = NB;
+  pp.bin_size = NB ? (double)(req->bin_max / (float)NB) : 1.0;
+  const int64_t blocks = P.n_pairs * pp.blocks_per_pair;
+  if (blocks > 0 && e.n > 0) {
+    KernelTimer kt(ctx, "disp_plain_kernel");
+    disp_plain_kernel<<<(unsigned)blocks, 256, 0, ctx->stream>>>(pp);
+    check_launch("disp_plain_kernel");
+    count_launch(ctx);
+  }
+  to_out(ctx, sum_d2, pp.d2, n_lg, out_flags);
+  to_out(ctx, sum_d4, pp.d4, n_lg, out_flags);
+  if (S) to_out(ctx, fs_sum, pp.fs, n_lg * S, out_flags);
+  if (NB) to_out(ctx, (unsigned long long*)gs_counts, pp.gs, n_lg * NB, out_flags);
+  if (atom_pairs) {
+    std::vector<int64_t> c(G);
+    for (int g = 0; g < G; ++g) c[g] = (int64_t)e.n * (P.gap_first[g + 1] - P.gap_first[g]);
+    if (out_flags == AMDAT_OUT_DEVICE)
+      AMDAT_CUDA(cudaMemcpyAsync(atom_pairs, c.data(), G * 8, cudaMemcpyHostToDevice, ctx->stream));
+    else
+      std::memcpy(atom_pairs, c.data(), G * 8);
+    AMDAT_CUDA(cudaStreamSynchronize(ctx->stream));
+  }
+  AMDAT_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+}  // namespace amdat
+
+// ---------------------------------------------------------------------------
+// prepared displacement plans (mixed path): device tables built once, a run is
+// pure stream work (memsets + persistent kernel + finalize per shell pass),
+// optionally captured in a CUDA graph; tile choice optionally autotuned
+// ---------------------------------------------------------------------------
+struct amdat_disp_plan {
+  int n_lists = 0, G = 0, S = 0, NB = 0, n_passes = 1, n_out = 2;
+  bool fullblock = false;
+  float bin_max = 0.f, period = 1.f;
+  amdat::ShellSet sh;
+  std::vector<int32_t> lsize;
+  std::vector<amdat::ListDev> ldev;
+  std::vector<int64_t> pairs;  // atom_pairs [list][gap]
+  int chunk = 0, blocks_per_sm = 0, n_items = 0;
+  double tuned_ms = 0.0;
+  // device: [items | item_first | schedule | lists | counters | kv | off | inv | part | d2 | d4 | fs | gs]
+  amdat::DevBuf<unsigned char> dev;
+  size_t o_items = 0, o_first = 0, o_sched = 0, o_lists = 0, o_counter = 0, o_kv = 0, o_off = 0,
+         o_inv = 0, o_part = 0, o_d2 = 0, o_d4 = 0, o_fs = 0, o_gs = 0, bytes = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  ~amdat_disp_plan() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+  }
+};
+
+namespace amdat {
+
+static void plan_tables(amdat_ctx* ctx, amdat_disp_plan& pl, const PairTable& P, int chunk,
+                        int blocks_per_sm) {
+  const int G = pl.G;
+  const size_t n_lg = (size_t)pl.n_lists * G;
+  std::vector<DispItem> items;
+  std::vector<int32_t> item_first(n_lg + 1, 0);
+  std::vector<int64_t> key;  // schedule key per item: (list, chunk, pair)
+  for (int l = 0; l < pl.n_lists; ++l) {
+    const int nch = (int)std::max<int64_t>(1, ceil_div(pl.lsize[l], chunk));
+    for (int g = 0; g < G; ++g) {
+      item_first[(size_t)l * G + g] = (int32_t)items.size();
+      if (pl.lsize[l] == 0) continue;
+      for (int pr = P.gap_first[g]; pr < P.gap_first[g + 1]; ++pr)
+        for (int c = 0; c < nch; ++c) {
+          const int a0 = (int)((int64_t)pl.lsize[l] * c / nch);
+          const int a1 = (int)((int64_t)pl.lsize[l] * (c + 1) / nch);
+          items.push_back(DispItem{l, pr, a0, a1});
+          key.push_back(((int64_t)l << 40) | ((int64_t)c << 20) | (int64_t)pr);
+        }
+    }
+  }
+  item_first[n_lg] = (int32_t)items.size();
+  // process all pairs of one (list, atom chunk) together: the chunk's frames
+  // are read from HBM once and reused from L2 by the other pairs
+  std::vector<int32_t> sched(items.size());
+  for (size_t i = 0; i < sched.size(); ++i) sched[i] = (int32_t)i;
+  std::stable_sort(sched.begin(), sched.end(), [&](int32_t a, int32_t b) { return key[a] < key[b]; });
+  pl.n_items = (int)items.size();
+  pl.chunk = chunk;
+  pl.blocks_per_sm = blocks_per_sm;
+  auto align = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  size_t o = 0;
+  pl.o_items = o; o = align(o + std::max<size_t>(items.size(), 1) * sizeof(DispItem));
+  pl.o_first = o; o = align(o + item_first.size() * 4);
+  pl.o_sched = o; o = align(o + std::max<size_t>(sched.size(), 1) * 4);
+  pl.o_lists = o; o = align(o + pl.ldev.size() * sizeof(ListDev));
+  pl.o_counter = o; o = align(o + 4 * (size_t)pl.n_passes);
+  pl.o_kv = o; o = align(o + std::max<size_t>(pl.sh.kv.size(), 1) * sizeof(int4));
+  pl.o_off = o; o = align(o + std::max<size_t>(pl.sh.off.size(), 1) * 4);
+  pl.o_inv = o; o = align(o + std::max<size_t>(pl.sh.inv_count.size(), 1) * 4);
+  pl.o_part = o; o = align(o + (size_t)std::max(pl.n_items, 1) * pl.n_out * 8);
+  pl.o_d2 = o; o = align(o + n_lg * 8);
+  pl.o_d4 = o; o = align(o + n_lg * 8);
+  pl.o_fs = o; o = align(o + n_lg * std::max(pl.S, 1) * 8);
+  pl.o_gs = o; o = align(o + n_lg * std::max(pl.NB, 1) * 8);
+  pl.bytes = o;
+  unsigned char* base = pl.dev.reserve(o);
+  std::vector<unsigned char> host(pl.o_part, 0);
+  std::memcpy(host.data() + pl.o_items, items.data(), items.size() * sizeof(DispItem));
+  std::memcpy(host.data() + pl.o_first, item_first.data(), item_first.size() * 4);
+  std::memcpy(host.data() + pl.o_sched, sched.data(), sched.size() * 4);
+  std::memcpy(host.data() + pl.o_lists, pl.ldev.data(), pl.ldev.size() * sizeof(ListDev));
+  if (pl.S) {
+    std::memcpy(host.data() + pl.o_kv, pl.sh.kv.data(), pl.sh.kv.size() * sizeof(int4));
+    std::memcpy(host.data() + pl.o_off, pl.sh.off.data(), pl.sh.off.size() * 4);
+    std::memcpy(host.data() + pl.o_inv, pl.sh.inv_count.data(), pl.sh.inv_count.size() * 4);
+  }
+  AMDAT_CUDA(cudaMemcpyAsync(base, host.data(), pl.o_part, cudaMemcpyHostToDevice, ctx->stream));
+  AMDAT_CUDA(cudaMemsetAsync(base + pl.o_d2, 0, pl.o_gs - pl.o_d2, ctx->stream));
+  AMDAT_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
+// every device operation of one run, in stream order (capturable)
+static void plan_launch(amdat_ctx* ctx, amdat_disp_plan& pl, const PairTable& P) {
+  unsigned char* base = pl.dev.ptr;
+  const size_t n_lg = (size_t)pl.n_lists * pl.G;
+  if (pl.NB) AMDAT_CUDA(cudaMemsetAsync(base + pl.o_gs, 0, n_lg * pl.NB * 8, ctx->stream));
+  if (pl.n_items == 0) {
+    AMDAT_CUDA(cudaMemsetAsync(base + pl.o_d2, 0, pl.o_gs - pl.o_d2, ctx->stream));
+    return;
+  }
+  AMDAT_CUDA(cudaMemsetAsync(base + pl.o_counter, 0, 4 * (size_t)pl.n_passes, ctx->stream));
+  for (int pass = 0; pass < pl.n_passes; ++pass) {
+    const int s0 = pass * MAX_FS;
+    const int nfs = pl.S ? std::min(MAX_FS, pl.S - s0) : 0;
+    DispParams p{};
+    p.u = ctx->u.ptr;
+    p.n_pad = ctx->n_pad;
+    p.t0 = P.t0.ptr;
+    p.t1 = P.t1.ptr;
+    p.gap = P.gap.ptr;
+    p.items = (const DispItem*)(base + pl.o_items);
+    p.n_items = pl.n_items;
+    p.lists = (const ListDev*)(base + pl.o_lists);
+    p.counter = (int32_t*)(base + pl.o_counter) + pass;
+    p.schedule = (const int32_t*)(base + pl.o_sched);
+    p.part = (double*)(base + pl.o_part);
+    p.n_out = pl.n_out;
+    p.want_moments = pass == 0;
+    p.gs = (unsigned long long*)(base + pl.o_gs);
+    p.n_gaps = pl.G;
+    p.n_bins = pass == 0 ? pl.NB : 0;
+    p.bin_size = pl.NB ? pl.bin_max / (float)pl.NB : 1.0f;
+    p.n_fs = nfs;
+    p.fs_mode = pl.S ? pl.sh.mode : 0;
+    p.kv = (const int4*)(base + pl.o_kv);
+    p.kv_off = (const int32_t*)(base + pl.o_off) + s0;
+    p.inv_count = (const float*)(base + pl.o_inv) + s0;
+    p.nmax = pl.sh.nmax;
+    p.period = pl.S ? pl.period : 1.0f;
+    const bool gs = p.n_bins > 0;
+    const int mode = nfs ? pl.sh.mode : 0;
+    const int threads = mode ? FS_THREADS : DISP_THREADS;
+    size_t shm = gs ? (size_t)((pl.NB + 3) & ~3) * 4 : 0;
+    if (mode == 2) shm += (size_t)3 * (pl.sh.nmax + 1) * threads * 4;
+    auto launch = [&](auto kernel) {
+      if (shm > 48 * 1024)
+        AMDAT_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+      static thread_local std::map<std::pair<const void*, size_t>, int> occ_cache;
+      const auto okey = std::make_pair((const void*)kernel, shm);
+      int occ = 0;
+      auto oit = occ_cache.find(okey);
+      if (oit != occ_cache.end()) {
+        occ = oit->second;
+      } else {
+        AMDAT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, threads, shm));
+        occ_cache[okey] = occ;
+      }
+      const int bps = std::max(1, std::min(occ, pl.blocks_per_sm));
+      const int grid = (int)std::min<int64_t>((int64_t)bps * ctx->n_sm, pl.n_items);
+      KernelTimer kt(ctx, "disp_mixed_kernel");
+      kernel<<<grid, threads, shm, ctx->stream>>>(p);
+      check_launch("disp_mixed_kernel");
+      count_launch(ctx);
+    };
+    if (mode == 0) { if (gs) launch(disp_mixed_kernel<0, true>); else launch(disp_mixed_kernel<0, false>); }
+    else if (mode == 1) { if (gs) launch(disp_mixed_kernel<1, true>); else launch(disp_mixed_kernel<1, false>); }
+    else { if (gs) launch(disp_mixed_kernel<2, true>); else launch(disp_mixed_kernel<2, false>); }
+    disp_finalize_kernel<<<(unsigned)n_lg, 256, 0, ctx->stream>>>(
+        p.part, pl.n_out, (const int32_t*)(base + pl.o_first), 0,
+        pass == 0 ? (double*)(base + pl.o_d2) : nullptr, pass == 0 ? (double*)(base + pl.o_d4) : nullptr,
+        pl.S ? (double*)(base + pl.o_fs) : nullptr, std::max(pl.S, 1), s0, nfs, pass == 0 ? 1 : 0);
+    check_launch("disp_finalize_kernel");
+    count_launch(ctx);
+  }
+}
+
+// ---- autotuner cache: JSON lines {"key": ..., "chunk": c, "blocks_per_sm": b, "ms": t}
+static std::map<std::string, std::pair<int, int>>& tune_cache() {
+  static std::map<std::string, std::pair<int, int>> c;
+  static bool loaded = false;
+  if (!loaded) {
+    loaded = true;
+    if (const char* f = std::getenv("AMDAT_TUNE_CACHE")) {
+      FILE* fp = std::fopen(f, "r");
+      if (fp) {
+        char line[512], key[256];
+        int ch = 0, bps = 0;
+        while (std::fgets(line, sizeof(line), fp))
+          if (std::sscanf(line, "{\"key\": \"%255[^\"]\", \"chunk\": %d, \"blocks_per_sm\": %d", key, &ch, &bps) == 3)
+            c[key] = {ch, bps};
+        std::fclose(fp);
+      }
+    }
+  }
+  return c;
+}
+
+static void tune_store(const std::string& key, int ch, int bps, double ms) {
+  tune_cache()[key] = {ch, bps};
+  if (const char* f = std::getenv("AMDAT_TUNE_CACHE")) {
+    FILE* fp = std::fopen(f, "a");
+    if (fp) {
+      std::fprintf(fp, "{\"key\": \"%s\", \"chunk\": %d, \"blocks_per_sm\": %d, \"ms\": %.6f}\n",
+                   key.c_str(), ch, bps, ms);
+      std::fclose(fp);
+    }
+  }
+}
+
+static amdat_disp_plan* plan_create(amdat_ctx* ctx, const amdat_disp_request* req,
+                                    const int32_t* lists, int32_t n_lists, int32_t flags) {
+  check_request(ctx, req);
+  AMDAT_REQUIRE(req->precision == AMDAT_MIXED, "plans run the mixed-precision path");
+  AMDAT_REQUIRE(lists != nullptr && n_lists >= 1, "need >= 1 list");
+  const PairTable& P = pair_table(ctx, req->fullblock != 0, false);
+  auto* pl = new amdat_disp_plan();
+  try {
+    pl->n_lists = n_lists;
+    pl->G = P.n_gaps;
+    pl->S = req->n_shells;
+    pl->NB = req->n_bins;
+    pl->fullblock = req->fullblock != 0;
+    pl->bin_max = req->bin_max;
+    pl->period = req->kvec_period;
+    if (pl->S) {
+      if (!octant_shells(req->shell_offsets, req->kvec_n, pl->S, pl->sh) || pl->sh.nmax > 48)
+        list_shells(req->shell_offsets, req->kvec_n, pl->S, pl->sh);
+    }
+    pl->n_passes = pl->S ? (int)ceil_div(pl->S, MAX_FS) : 1;
+    pl->n_out = 2 + (pl->S ? std::min(pl->S, MAX_FS) : 0);
+    int64_t total_atoms = 0;
+    for (int l = 0; l < n_lists; ++l) {
+      const ListEntry& e = list_entry(ctx, lists[l]);
+      pl->ldev.push_back(ListDev{e.n, e.first, e.contiguous ? nullptr : e.idx.ptr});
+      pl->lsize.push_back(e.n);
+      total_atoms += e.n;
+    }
+    pl->pairs.assign((size_t)n_lists * pl->G, 0);
+    for (int l = 0; l < n_lists; ++l)
+      for (int g = 0; g < pl->G; ++g)
+        pl->pairs[(size_t)l * pl->G + g] = (int64_t)pl->lsize[l] * (P.gap_first[g + 1] - P.gap_first[g]);
+    // default tile: full chunks stream memory; F_s or few pairs want smaller
+    // chunks to keep every SM busy
+    const int64_t want_items = (int64_t)ctx->n_sm * 16;
+    int64_t chunk = DISP_CHUNK;
+    if (P.n_pairs > 0 && total_atoms > 0)
+      chunk = std::max<int64_t>(pl->S ? 128 : 1024,
+                                std::min<int64_t>(DISP_CHUNK, ceil_div(total_atoms * P.n_pairs, want_items)));
+    int bps = pl->S ? 4 : 8;
+    char keybuf[256];
+    std::snprintf(keybuf, sizeof(keybuf), "sm%d_mode%d_S%d_NB%d_L%d_atoms%lld_pairs%lld", ctx->n_sm,
+                  pl->S ? pl->sh.mode : 0, pl->S, pl->NB, n_lists, (long long)total_atoms,
+                  (long long)P.n_pairs);
+    const std::string key(keybuf);
+    auto hit = tune_cache().find(key);
+    if (hit != tune_cache().end()) {
+      chunk = hit->second.first;
+      bps = hit->second.second;
+    } else if (flags & AMDAT_PLAN_AUTOTUNE) {
+      // time each candidate (warm-up + 3 runs, CUDA events) and keep the fastest
+      // candidates: F_s is compute bound (small chunks, fewer heavier blocks);
+      // MSD-only streams memory (large chunks, more resident blocks)
+      const std::vector<int> chunks = pl->S ? std::vector<int>{256, 512, 1024, 2048}
+                                            : std::vector<int>{1024, 2048, 4096, 8192};
+      const std::vector<int> bpss = pl->S ? std::vector<int>{2, 4} : std::vector<int>{4, 8};
+      cudaEvent_t a, b;
+      AMDAT_CUDA(cudaEventCreate(&a));
+      AMDAT_CUDA(cudaEventCreate(&b));
+      double best = 1e30;
+      int bc = (int)chunk, bb = bps;
+      for (int c : chunks) {
+        for (int bp : bpss) {
+          plan_tables(ctx, *pl, P, c, bp);
+          plan_launch(ctx, *pl, P);
+          AMDAT_CUDA(cudaEventRecord(a, ctx->stream));
+          for (int r = 0; r < 2; ++r) plan_launch(ctx, *pl, P);
+          AMDAT_CUDA(cudaEventRecord(b, ctx->stream));
+          AMDAT_CUDA(cudaEventSynchronize(b));
+          float ms = 0.f;
+          AMDAT_CUDA(cudaEventElapsedTime(&ms, a, b));
+          if (ms / 2 < best) {
+            best = ms / 2;
+            bc = c;
+            bb = bp;
+          }
+        }
+      }
+      cudaEventDestroy(a);
+      cudaEventDestroy(b);
+      chunk = bc;
+      bps = bb;
+      pl->tuned_ms = best;
+      tune_store(key, bc, bb, best);
+    }
+    plan_tables(ctx, *pl, P, (int)chunk, bps);
+    if (flags & AMDAT_PLAN_GRAPH) {
+      AMDAT_CUDA(cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+      const bool prof = ctx->profiling;
+      ctx->profiling = false;  // events are not recorded inside a graph
+      try {
+        plan_launch(ctx, *pl, P);
+      } catch (...) {
+        ctx->profiling = prof;
+        cudaGraph_t g;
+        cudaStreamEndCapture(ctx->stream, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+      }
+      ctx->profiling = prof;
+      AMDAT_CUDA(cudaStreamEndCapture(ctx->stream, &pl->graph));
+      AMDAT_CUDA(cudaGraphInstantiate(&pl->exec, pl->graph, 0));
+    }
+  } catch (...) {
+    delete pl;
+    throw;
+  }
+  return pl;
+}
+
+static void plan_run(amdat_ctx* ctx, amdat_disp_plan* pl) {
+  AMDAT_REQUIRE(pl != nullptr, "null plan");
+  const PairTable& P = pair_table(ctx, pl->fullblock, false);
+  if (pl->exec) {
+    KernelTimer kt(ctx, "disp_plan_graph");
+    AMDAT_CUDA(cudaGraphLaunch(pl->exec, ctx->stream));
+    count_launch(ctx, 2 * pl->n_passes);
+  } else {
+    plan_launch(ctx, *pl, P);
+  }
+}
+
+static void plan_read(amdat_ctx* ctx, amdat_disp_plan* pl, int32_t out_flags, double* sum_d2,
+                      double* sum_d4, int64_t* atom_pairs, double* fs_sum, int64_t* gs_counts) {
+  AMDAT_REQUIRE(out_flags == AMDAT_OUT_HOST || out_flags == AMDAT_OUT_DEVICE, "bad out_flags");
+  const size_t n_lg = (size_t)pl->n_lists * pl->G;
+  unsigned char* base = pl->dev.ptr;
+  to_out(ctx, sum_d2, (const double*)(base + pl->o_d2), n_lg, out_flags);
+  to_out(ctx, sum_d4, (const double*)(base + pl->o_d4), n_lg, out_flags);
+  if (pl->S) to_out(ctx, fs_sum, (const double*)(base + pl->o_fs), n_lg * pl->S, out_flags);
+  if (pl->NB) to_out(ctx, (unsigned long long*)gs_counts, (const unsigned long long*)(base + pl->o_gs), n_lg * pl->NB, out_flags);
+  if (atom_pairs) {
+    if (out_flags == AMDAT_OUT_DEVICE)
+      AMDAT_CUDA(cudaMemcpyAsync(atom_pairs, pl->pairs.data(), n_lg * 8, cudaMemcpyHostToDevice, ctx->stream));
+    else
+      std::memcpy(atom_pairs, pl->pairs.data(), n_lg * 8);
+  }
+  if (out_flags == AMDAT_OUT_HOST || atom_pairs) AMDAT_CUDA(cudaStreamSynchronize(ctx->stream));
+}
+
 static void disp_run_impl(amdat_ctx* ctx, const amdat_disp_request* req, const int32_t* lists,
                           int32_t n_lists, int32_t out_flags, double* sum_d2, double* sum_d4,
                           int64_t* atom_pairs, double* fs_sum, int64_t* gs_counts) {
   check_request(ctx, req);
-  AMDAT_REQUIRE(n_lists >= 1, "need >= 1 list");
   AMDAT_REQUIRE(out_flags == AMDAT_OUT_HOST || out_flags == AMDAT_OUT_DEVICE, "bad out_flags");
-  const PairTable& P = pair_table(ctx, req->fullblock != 0, false);
-  const int G = P.n_gaps;
-  const int S = req->n_shells;
-  const int NB = req->n_bins;
-
-  // list table and item table (list-major, pair-major, chunk)
-  std::vector<ListDev> ldev(n_lists);
-  std::vector<int32_t> lsize(n_lists);
-  for (int l = 0; l < n_lists; ++l) {
-    const ListEntry& e = list_entry(ctx, lists[l]);
-    ldev[l] = ListDev{e.n, e.first, e.contiguous ? nullptr : e.idx.ptr};
-    lsize[l] = e.n;
-  }
-  // atom_pairs: list size (membership is static) per pair of the gap
-  std::vector<int64_t> counts((size_t)n_lists * G, 0);
-  for (int l = 0; l < n_lists; ++l)
-    for (int g = 0; g < G; ++g)
-      counts[(size_t)l * G + g] = (int64_t)lsize[l] * (P.gap_first[g + 1] - P.gap_first[g]);
-
-  // scratch layout
-  const double h_unused = 0;
-  (void)h_unused;
-  double* d_out_d2 = nullptr;
-  double* d_out_d4 = nullptr;
-  double* d_out_fs = nullptr;
-  unsigned long long* d_out_gs = nullptr;
-  const size_t n_lg = (size_t)n_lists * G;
-
   if (req->precision == AMDAT_PLAIN_FP64) {
     AMDAT_REQUIRE(n_lists == 1, "the plain FP64 path runs one list per call");
-    ensure_fp64(ctx);
-    const size_t bytes = n_lg * (2 + S) * sizeof(double) + n_lg * NB * sizeof(unsigned long long) +
-                         (S ? (size_t)(req->shell_offsets[S]) * sizeof(int4) + (S + 1) * 4 : 0) + 256;
-    unsigned char* base = ctx->scratch.reserve(bytes);
-    AMDAT_CUDA(cudaMemsetAsync(base, 0, bytes, ctx->stream));
-    d_out_d2 = (double*)base;
-    d_out_d4 = d_out_d2 + n_lg;
-    d_out_fs = d_out_d4 + n_lg;
-    d_out_gs = (unsigned long long*)(d_out_fs + n_lg * S);
-    int4* d_kv = (int4*)(((uintptr_t)(d_out_gs + n_lg * NB) + 15) & ~(uintptr_t)15);
-    int32_t* d_off = nullptr;
-    if (S) {
-      ShellSet sh;
-      list_shells(req->shell_offsets, req->kvec_n, S, sh);
-      d_off = (int32_t*)(d_kv + sh.kv.size());
-      AMDAT_CUDA(cudaMemcpyAsync(d_kv, sh.kv.data(), sh.kv.size() * sizeof(int4), cudaMemcpyHostToDevice, ctx->stream));
-      AMDAT_CUDA(cudaMemcpyAsync(d_off, sh.off.data(), sh.off.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
-    }
-    PlainParams pp{};
-    pp.u = ctx->u64.ptr;
-    pp.n_pad = ctx->n_pad;
-    pp.t0 = P.t0.ptr;
-    pp.t1 = P.t1.ptr;
-    pp.gap = P.gap.ptr;
-    pp.n_pairs = P.n_pairs;
-    pp.list = ldev[0];
-    pp.blocks_per_pair = (int32_t)std::max<int64_t>(1, ceil_div(lsize[0], 256));
-    pp.d2 = d_out_d2;
-    pp.d4 = d_out_d4;
-    pp.fs = d_out_fs;
-    pp.n_shells = S;
-    pp.kv = d_kv;
-    pp.kv_off = d_off;
-    pp.two_pi_over_l = S ? 6.283185307179586476925286766559 / (double)req->kvec_period : 0.0;
-    pp.gs = d_out_gs;
-    pp.n_bins = NB;
-    pp.bin_size = NB ? (double)(req->bin_max / (float)NB) : 1.0;
-    const int64_t blocks = P.n_pairs * pp.blocks_per_pair;
-    if (blocks > 0 && lsize[0] > 0) {
-      KernelTimer kt(ctx, "disp_plain_kernel");
-      disp_plain_kernel<<<(unsigned)blocks, 256, 0, ctx->stream>>>(pp);
-      check_launch("disp_plain_kernel");
-      count_launch(ctx);
-    }
-  } else {
-    // ---- mixed path
-    static thread_local std::string sh_key;
-    static thread_local ShellSet sh_cached;
-    ShellSet sh;
-    if (S) {
-      std::string key((const char*)req->shell_offsets, sizeof(int32_t) * (S + 1));
-      key.append((const char*)req->kvec_n, sizeof(int32_t) * 3 * (size_t)req->shell_offsets[S]);
-      if (key == sh_key) {
-        sh = sh_cached;
-      } else {
-        if (!octant_shells(req->shell_offsets, req->kvec_n, S, sh) || sh.nmax > 48)
-          list_shells(req->shell_offsets, req->kvec_n, S, sh);
-        sh_key = std::move(key);
-        sh_cached = sh;
-      }
-    }
-    std::vector<DispItem> items;
-    std::vector<int32_t> item_first(n_lg + 1, 0);
-    // chunk size: full chunks stream memory efficiently; with F_s (compute
-    // bound) or few pairs, smaller chunks keep every SM busy
-    int64_t total_atoms = 0;
-    for (int l = 0; l < n_lists; ++l) total_atoms += lsize[l];
-    const int64_t want_items = (int64_t)ctx->n_sm * 16;
-    int64_t chunk = DISP_CHUNK;
-    if (P.n_pairs > 0 && total_atoms > 0) {
-      const int64_t by_fill = ceil_div(total_atoms * P.n_pairs, want_items);
-      chunk = std::max<int64_t>(S ? 128 : 1024, std::min<int64_t>(DISP_CHUNK, by_fill));
-    }
-    for (int l = 0; l < n_lists; ++l) {
-      const int nch = (int)std::max<int64_t>(1, ceil_div(lsize[l], chunk));
-      for (int g = 0; g < G; ++g) {
-        item_first[(size_t)l * G + g] = (int32_t)items.size();
-        if (lsize[l] == 0) continue;
-        for (int pr = P.gap_first[g]; pr < P.gap_first[g + 1]; ++pr)
-          for (int c = 0; c < nch; ++c) {
-            const int a0 = (int)((int64_t)lsize[l] * c / nch);
-            const int a1 = (int)((int64_t)lsize[l] * (c + 1) / nch);
-            items.push_back(DispItem{l, pr, a0, a1});
-          }
-      }
-    }
-    item_first[n_lg] = (int32_t)items.size();
-    const int n_items = (int)items.size();
-    const int n_passes = S ? (int)ceil_div(S, MAX_FS) : 1;
-    const int max_fs_pass = S ? std::min(S, MAX_FS) : 0;
-    const int n_out = 2 + max_fs_pass;
-
-    // scratch: [items | item_first | lists | counter | part | outputs | gs | kv | off | invc]
-    auto align = [](size_t x) { return (x + 255) & ~(size_t)255; };
-    size_t o = 0;
-    const size_t o_items = o; o = align(o + items.size() * sizeof(DispItem));
-    const size_t o_first = o; o = align(o + item_first.size() * 4);
-    const size_t o_lists = o; o = align(o + ldev.size() * sizeof(ListDev));
-    const size_t o_counter = o; o = align(o + 4 * (size_t)n_passes);
-    const size_t o_part = o; o = align(o + (size_t)std::max(n_items, 1) * n_out * sizeof(double));
-    const size_t o_d2 = o; o = align(o + n_lg * sizeof(double));
-    const size_t o_d4 = o; o = align(o + n_lg * sizeof(double));
-    const size_t o_fs = o; o = align(o + n_lg * std::max(S, 1) * sizeof(double));
-    const size_t o_gs = o; o = align(o + n_lg * std::max(NB, 1) * sizeof(unsigned long long));
-    const size_t o_kv = o; o = align(o + std::max<size_t>(sh.kv.size(), 1) * sizeof(int4));
-    const size_t o_off = o; o = align(o + std::max<size_t>(sh.off.size(), 1) * 4);
-    const size_t o_inv = o; o = align(o + std::max<size_t>(sh.inv_count.size(), 1) * 4);
-    unsigned char* base = ctx->scratch.reserve(o);
-    // host staging of the small tables in one buffer, one copy
-    std::vector<unsigned char> host(o_part, 0);
-    std::memcpy(host.data() + o_items, items.data(), items.size() * sizeof(DispItem));
-    std::memcpy(host.data() + o_first, item_first.data(), item_first.size() * 4);
-    std::memcpy(host.data() + o_lists, ldev.data(), ldev.size() * sizeof(ListDev));
-    AMDAT_CUDA(cudaMemcpyAsync(base, host.data(), o_part, cudaMemcpyHostToDevice, ctx->stream));
-    if (S) {
-      AMDAT_CUDA(cudaMemcpyAsync(base + o_kv, sh.kv.data(), sh.kv.size() * sizeof(int4), cudaMemcpyHostToDevice, ctx->stream));
-      AMDAT_CUDA(cudaMemcpyAsync(base + o_off, sh.off.data(), sh.off.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
-      AMDAT_CUDA(cudaMemcpyAsync(base + o_inv, sh.inv_count.data(), sh.inv_count.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
-    }
-    if (NB) AMDAT_CUDA(cudaMemsetAsync(base + o_gs, 0, n_lg * NB * sizeof(unsigned long long), ctx->stream));
-    d_out_d2 = (double*)(base + o_d2);
-    d_out_d4 = (double*)(base + o_d4);
-    d_out_fs = (double*)(base + o_fs);
-    d_out_gs = (unsigned long long*)(base + o_gs);
-    if (n_items == 0) {
-      AMDAT_CUDA(cudaMemsetAsync(base + o_d2, 0, o_gs - o_d2, ctx->stream));
-    }
-
-    for (int pass = 0; pass < n_passes && n_items > 0; ++pass) {
-      const int s0 = pass * MAX_FS;
-      const int nfs = S ? std::min(MAX_FS, S - s0) : 0;
-      DispParams p{};
-      p.u = ctx->u.ptr;
-      p.n_pad = ctx->n_pad;
-      p.t0 = P.t0.ptr;
-      p.t1 = P.t1.ptr;
-      p.gap = P.gap.ptr;
-      p.items = (const DispItem*)(base + o_items);
-      p.n_items = n_items;
-      p.lists = (const ListDev*)(base + o_lists);
-      p.counter = (int32_t*)(base + o_counter) + pass;
-      p.part = (double*)(base + o_part);
-      p.n_out = n_out;
-      p.want_moments = pass == 0;
-      p.gs = d_out_gs;
-      p.n_gaps = G;
-      p.n_bins = pass == 0 ? NB : 0;
-      p.bin_size = NB ? req->bin_max / (float)NB : 1.0f;
-      p.n_fs = nfs;
-      p.fs_mode = S ? sh.mode : 0;
-      p.kv = (const int4*)(base + o_kv);
-      p.kv_off = (const int32_t*)(base + o_off) + s0;
-      p.inv_count = (const float*)(base + o_inv) + s0;
-      p.nmax = sh.nmax;
-      p.period = S ? req->kvec_period : 1.0f;
-      AMDAT_CUDA(cudaMemsetAsync(p.counter, 0, 4, ctx->stream));
-      const bool gs = p.n_bins > 0;
-      const int mode = nfs ? sh.mode : 0;
-      const int threads = mode ? FS_THREADS : DISP_THREADS;
-      size_t shm = gs ? (size_t)((NB + 3) & ~3) * 4 : 0;
-      if (mode == 2) shm += (size_t)3 * (sh.nmax + 1) * threads * 4;
-      int blocks_per_sm = mode ? 4 : 8;
-      auto launch = [&](auto kernel) {
-        if (shm > 48 * 1024) AMDAT_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
-        // occupancy per (kernel, shared memory size), computed once
-        static thread_local std::map<std::pair<const void*, size_t>, int> occ_cache;
-        const auto okey = std::make_pair((const void*)kernel, shm);
-        int occ = 0;
-        auto oit = occ_cache.find(okey);
-        if (oit != occ_cache.end()) {
-          occ = oit->second;
-        } else {
-          AMDAT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel, threads, shm));
-          occ_cache[okey] = occ;
-        }
-        const int grid = (int)std::min<int64_t>((int64_t)std::max(1, std::min(occ, blocks_per_sm)) * ctx->n_sm, n_items);
-        KernelTimer kt(ctx, "disp_mixed_kernel");
-        kernel<<<grid, threads, shm, ctx->stream>>>(p);
-        check_launch("disp_mixed_kernel");
-        count_launch(ctx);
-      };
-      if (mode == 0) { if (gs) launch(disp_mixed_kernel<0, true>); else launch(disp_mixed_kernel<0, false>); }
-      else if (mode == 1) { if (gs) launch(disp_mixed_kernel<1, true>); else launch(disp_mixed_kernel<1, false>); }
-      else { if (gs) launch(disp_mixed_kernel<2, true>); else launch(disp_mixed_kernel<2, false>); }
-      disp_finalize_kernel<<<(unsigned)n_lg, 256, 0, ctx->stream>>>(
-          p.part, n_out, (const int32_t*)(base + o_first), 0, pass == 0 ? d_out_d2 : nullptr,
-          pass == 0 ? d_out_d4 : nullptr, S ? d_out_fs : nullptr, std::max(S, 1), s0, nfs,
-          pass == 0 ? 1 : 0);
-      check_launch("disp_finalize_kernel");
-      count_launch(ctx);
-    }
-    // lists with no members: zero outputs
-    for (int l = 0; l < n_lists; ++l)
-      if (lsize[l] == 0) {
-        AMDAT_CUDA(cudaMemsetAsync(d_out_d2 + (size_t)l * G, 0, G * sizeof(double), ctx->stream));
-        AMDAT_CUDA(cudaMemsetAsync(d_out_d4 + (size_t)l * G, 0, G * sizeof(double), ctx->stream));
-        if (S) AMDAT_CUDA(cudaMemsetAsync(d_out_fs + (size_t)l * G * S, 0, (size_t)G * S * sizeof(double), ctx->stream));
-      }
+    amdat_disp_request r = *req;
+    r.list = lists[0];
+    disp_plain(ctx, &r, out_flags, sum_d2, sum_d4, atom_pairs, fs_sum, gs_counts);
+    return;
   }
-  to_out(ctx, sum_d2, d_out_d2, n_lg, out_flags);
-  to_out(ctx, sum_d4, d_out_d4, n_lg, out_flags);
-  if (S) to_out(ctx, fs_sum, d_out_fs, n_lg * S, out_flags);
-  if (NB) to_out(ctx, (unsigned long long*)gs_counts, d_out_gs, n_lg * NB, out_flags);
-  if (atom_pairs) {
-    if (out_flags == AMDAT_OUT_DEVICE)
-      AMDAT_CUDA(cudaMemcpyAsync(atom_pairs, counts.data(), counts.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
-    else
-      std::memcpy(atom_pairs, counts.data(), counts.size() * 8);
-  }
+  std::unique_ptr<amdat_disp_plan> pl(plan_create(ctx, req, lists, n_lists, 0));
+  plan_run(ctx, pl.get());
+  plan_read(ctx, pl.get(), out_flags, sum_d2, sum_d4, atom_pairs, fs_sum, gs_counts);
   AMDAT_CUDA(cudaStreamSynchronize(ctx->stream));
 }
 
@@ -724,6 +909,54 @@ amdat_status amdat_disp_run_lists(amdat_ctx* ctx, const amdat_disp_request* req,
     check_ctx(ctx);
     AMDAT_REQUIRE(lists != nullptr && n_lists >= 1, "need >= 1 list");
     disp_run_impl(ctx, req, lists, n_lists, out_flags, sum_d2, sum_d4, atom_pairs, fs_sum, gs_counts);
+  });
+}
+
+amdat_status amdat_disp_plan_create(amdat_ctx* ctx, const amdat_disp_request* req,
+                                    const int32_t* lists, int32_t n_lists, int32_t flags,
+                                    amdat_disp_plan** plan) {
+  return guarded([&] {
+    check_ctx(ctx);
+    AMDAT_REQUIRE(plan != nullptr, "null plan pointer");
+    *plan = plan_create(ctx, req, lists, n_lists, flags);
+  });
+}
+
+amdat_status amdat_disp_plan_run(amdat_ctx* ctx, amdat_disp_plan* plan) {
+  return guarded([&] {
+    check_ctx(ctx);
+    plan_run(ctx, plan);
+  });
+}
+
+amdat_status amdat_disp_plan_read(amdat_ctx* ctx, amdat_disp_plan* plan, int32_t out_flags,
+                                  double* sum_d2, double* sum_d4, int64_t* atom_pairs,
+                                  double* fs_sum, int64_t* gs_counts) {
+  return guarded([&] {
+    check_ctx(ctx);
+    AMDAT_REQUIRE(plan != nullptr, "null plan");
+    plan_read(ctx, plan, out_flags, sum_d2, sum_d4, atom_pairs, fs_sum, gs_counts);
+  });
+}
+
+amdat_status amdat_disp_plan_info(amdat_disp_plan* plan, int32_t* chunk, int32_t* blocks_per_sm,
+                                  int64_t* n_items, double* tuned_ms) {
+  return guarded([&] {
+    AMDAT_REQUIRE(plan != nullptr, "null plan");
+    if (chunk) *chunk = plan->chunk;
+    if (blocks_per_sm) *blocks_per_sm = plan->blocks_per_sm;
+    if (n_items) *n_items = plan->n_items;
+    if (tuned_ms) *tuned_ms = plan->tuned_ms;
+  });
+}
+
+amdat_status amdat_disp_plan_destroy(amdat_ctx* ctx, amdat_disp_plan* plan) {
+  return guarded([&] {
+    if (ctx) {
+      check_ctx(ctx);
+      AMDAT_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
+    delete plan;
   });
 }
 

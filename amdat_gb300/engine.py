@@ -51,7 +51,11 @@ EXPORTED = [
     "amdat_wave_density_vectors", "amdat_wave_density_read", "amdat_wave_density_free",
     "amdat_isf_run", "amdat_structure_factor_run", "amdat_rdf_run", "amdat_vhd_run",
     "amdat_profile_reset", "amdat_profile_kernel", "amdat_run_script", "amdat_script_error",
+    "amdat_disp_plan_create", "amdat_disp_plan_run", "amdat_disp_plan_read", "amdat_disp_plan_info",
+    "amdat_disp_plan_destroy",
 ]
+
+PLAN_AUTOTUNE, PLAN_GRAPH = 1, 2
 
 _lib = None
 
@@ -291,6 +295,10 @@ class Engine:
                                     C.c_void_p(gs) if n_bins else None))
         del keep
 
+    def plan(self, lists, fullblock=0, shells=None, period=1.0, n_bins=0, bin_max=0.0, flags=0):
+        """Prepared many-list displacement run (amdat_disp_plan_*)."""
+        return DispPlan(self, lists, fullblock, shells, period, n_bins, bin_max, flags)
+
     # ---- Fourier densities
     def wave_density(self, list_h, kvec_n, period, frames, precision=MIXED) -> int:
         kv = _i32(kvec_n).reshape(-1)
@@ -364,3 +372,47 @@ class Engine:
         _check(lib().amdat_vhd_run(self._ctx, int(list1), int(list2), int(fullblock),
                                    C.c_float(max_distance), int(n_bins), OUT_HOST, _p(out)))
         return out
+
+
+class DispPlan:
+    """A prepared displacement run over many lists: run() is stream work only
+    (optionally a CUDA-graph replay), read() copies the results out."""
+
+    def __init__(self, eng, lists, fullblock, shells, period, n_bins, bin_max, flags):
+        self.eng = eng
+        req, self._keep = eng._disp_req(0, fullblock, MIXED, shells, period, n_bins, bin_max)
+        self.lists = _i32(lists)
+        self.S, self.NB, self.L, self.G = req.n_shells, int(n_bins), len(self.lists), eng.n_timegaps
+        self._plan = C.c_void_p()
+        _check(lib().amdat_disp_plan_create(eng.handle, C.byref(req), _p(self.lists), self.L,
+                                            int(flags), C.byref(self._plan)))
+
+    def run(self):
+        _check(lib().amdat_disp_plan_run(self.eng.handle, self._plan))
+
+    def read(self):
+        L, G, S, NB = self.L, self.G, self.S, self.NB
+        d2, d4 = np.zeros((L, G)), np.zeros((L, G))
+        cnt = np.zeros((L, G), np.int64)
+        fs = np.zeros((L, G, max(S, 1)))
+        gs = np.zeros((L, G, max(NB, 1)), np.int64)
+        _check(lib().amdat_disp_plan_read(self.eng.handle, self._plan, OUT_HOST, _p(d2), _p(d4),
+                                          _p(cnt), _p(fs) if S else None, _p(gs) if NB else None))
+        return dict(sum_d2=d2, sum_d4=d4, atom_pairs=cnt, fs_sum=fs[..., :S], gs_counts=gs[..., :NB])
+
+    def info(self):
+        ch, bps, ni, ms = C.c_int32(), C.c_int32(), C.c_int64(), C.c_double()
+        _check(lib().amdat_disp_plan_info(self._plan, C.byref(ch), C.byref(bps), C.byref(ni),
+                                          C.byref(ms)))
+        return dict(chunk=ch.value, blocks_per_sm=bps.value, n_items=ni.value, tuned_ms=ms.value)
+
+    def close(self):
+        if self._plan:
+            lib().amdat_disp_plan_destroy(self.eng.handle, self._plan)
+            self._plan = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -182,6 +182,30 @@ amdat_status amdat_disp_run_lists(amdat_ctx* ctx, const amdat_disp_request* req,
                                   double* fs_sum, int64_t* gs_counts);
 amdat_status amdat_set_scheme(amdat_ctx* ctx, const amdat_scheme* scheme);
 
+/* Prepared displacement runs (many lists, one persistent launch).  A plan
+ * builds its item tables on the device once; amdat_disp_plan_run is then pure
+ * stream work and does not synchronise.  AMDAT_PLAN_GRAPH captures the run in
+ * a CUDA graph (replayed by each plan_run); AMDAT_PLAN_AUTOTUNE times candidate
+ * atom-chunk sizes and blocks per SM and keeps the fastest (remembered per
+ * process and, when AMDAT_TUNE_CACHE names a file, across processes as JSON
+ * lines).  Results stay in the plan until amdat_disp_plan_read.  The plan
+ * refers to the context's trajectory, lists and scheme: rebuild it after
+ * changing them.  (The reference runs one Analysis copy per list, e.g.
+ * Bin_Static_Analysis, src/bin_static_analysis.h:69-111.) */
+#define AMDAT_PLAN_AUTOTUNE 1
+#define AMDAT_PLAN_GRAPH 2
+typedef struct amdat_disp_plan amdat_disp_plan;
+amdat_status amdat_disp_plan_create(amdat_ctx* ctx, const amdat_disp_request* req,
+                                    const int32_t* lists, int32_t n_lists, int32_t flags,
+                                    amdat_disp_plan** plan);
+amdat_status amdat_disp_plan_run(amdat_ctx* ctx, amdat_disp_plan* plan);
+amdat_status amdat_disp_plan_read(amdat_ctx* ctx, amdat_disp_plan* plan, int32_t out_flags,
+                                  double* sum_d2, double* sum_d4, int64_t* atom_pairs,
+                                  double* fs_sum, int64_t* gs_counts);
+amdat_status amdat_disp_plan_info(amdat_disp_plan* plan, int32_t* chunk, int32_t* blocks_per_sm,
+                                  int64_t* n_items, double* tuned_ms);
+amdat_status amdat_disp_plan_destroy(amdat_ctx* ctx, amdat_disp_plan* plan);
+
 /* ---------------------------------------------------------------------------
  * Fourier densities rho(k,t) = sum_j exp(i 2 pi n.r_j(t) / period)
  * ------------------------------------------------------------------------- */

@@ -202,3 +202,41 @@ def test_errors_are_status_codes(eng, engine_mod):
     with pytest.raises(engine_mod.AmdatError) as e:
         eng.disp(0)
     assert e.value.status == 2
+
+
+def test_plans_graph_and_autotune(eng, tmp_path, monkeypatch):
+    """A prepared many-list plan gives the single-list results; its CUDA-graph
+    replay and its autotuned tile give the same numbers run after run."""
+    traj, _, _ = load("lin_binary")
+    eng.upload(traj.unwrapped, traj.box)
+    eng.set_scheme(traj.scheme)
+    rng = np.random.default_rng(5)
+    perm = rng.permutation(traj.n_atoms)
+    handles = [eng.list(np.sort(perm[:n]).astype(np.int32)) for n in (3, 40, 250)]
+    shell = lattice_shell(7.0, 2.0, 2.6)
+    off = np.array([0, len(shell)], np.int32)
+    kw = dict(shells=(shell, off), period=7.0, n_bins=25, bin_max=1.0)
+    ref = [eng.disp(h, **kw) for h in handles]
+    plain = eng.plan(handles, **kw)
+    plain.run()
+    a = plain.read()
+    graph = eng.plan(handles, flags=2, **kw)
+    for _ in range(3):
+        graph.run()
+    b = graph.read()
+    cache = tmp_path / "tune.jsonl"
+    monkeypatch.setenv("AMDAT_TUNE_CACHE", str(cache))
+    tuned = eng.plan(handles, flags=3, **kw)
+    tuned.run()
+    c = tuned.read()
+    info = tuned.info()
+    assert info["chunk"] in (256, 512, 1024, 2048) and info["blocks_per_sm"] in (2, 4)
+    assert cache.exists() and '"chunk"' in cache.read_text()
+    for out in (a, b, c):
+        for i, r in enumerate(ref):
+            np.testing.assert_allclose(out["sum_d2"][i], r["sum_d2"], rtol=1e-7)
+            np.testing.assert_allclose(out["fs_sum"][i], r["fs_sum"], rtol=1e-6, atol=1e-9)
+            np.testing.assert_array_equal(out["gs_counts"][i], r["gs_counts"])
+            np.testing.assert_array_equal(out["atom_pairs"][i], r["atom_pairs"])
+    for p in (plain, graph, tuned):
+        p.close()
