@@ -30,6 +30,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 
@@ -369,16 +370,33 @@ struct LatticePlan {
 
 }  // namespace amdat
 namespace amdat {
+struct TcPlan;
+TcPlan* tc_plan_build(const std::vector<int32_t>& kvec);
+void tc_plan_free(TcPlan* p);
+void rhok_tc_run(amdat_ctx* ctx, const TcPlan& P, const int4* fx, int32_t n_list, int32_t n_frames,
+                 int32_t n_k, float2* rho);
+
 struct LatticePlanDev {
   std::vector<int32_t> kvec, shell_off;
   DevBuf<LatticeTile> tiles;
   DevBuf<int32_t> entry_k;
   int32_t n_tiles = 0;
+  TcPlan* tc = nullptr;  // tensor-core tiling, built at first use
+  ~LatticePlanDev() { tc_plan_free(tc); }
 };
 
 void lattice_plans_free(amdat_ctx* ctx) {
   for (auto& kv : ctx->lattice_plans) delete kv.second;
   ctx->lattice_plans.clear();
+}
+
+// tcgen05 kernel on compute capability 10.x unless AMDAT_RHOK_KERNEL=fp32
+static bool use_tensor_cores(amdat_ctx* ctx) {
+  const char* e = std::getenv("AMDAT_RHOK_KERNEL");
+  if (e && std::strcmp(e, "fp32") == 0) return false;
+  int major = 0;
+  AMDAT_CUDA(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, ctx->device));
+  return major == 10;
 }
 
 static LatticePlan plan_lattice(float kmax, float dk, float period) {
@@ -515,12 +533,18 @@ amdat_status amdat_wave_density_lattice(amdat_ctx* ctx, int32_t list, float kmax
         d->rho = rho_acquire(ctx, (size_t)n_frames * std::max(d->n_k, 1));
         DevBuf<int32_t> d_frames;
         int4* fx = fixed_turns(ctx, *d, e, period, d_frames);
-        dim3 grid((unsigned)P.n_tiles, (unsigned)n_frames);
-        KernelTimer kt(ctx, "rhok_lattice_kernel");
-        rhok_lattice_kernel<<<grid, LT_THREADS, 0, ctx->stream>>>(fx, e.n, P.tiles.ptr, P.entry_k.ptr,
-                                                                 d->n_k, d->rho->ptr);
-        check_launch("rhok_lattice_kernel");
-        count_launch(ctx);
+        if (use_tensor_cores(ctx)) {
+          LatticePlanDev& pw = *it->second;
+          if (!pw.tc) pw.tc = tc_plan_build(pw.kvec);
+          rhok_tc_run(ctx, *pw.tc, fx, e.n, n_frames, d->n_k, d->rho->ptr);
+        } else {
+          dim3 grid((unsigned)P.n_tiles, (unsigned)n_frames);
+          KernelTimer kt(ctx, "rhok_lattice_kernel");
+          rhok_lattice_kernel<<<grid, LT_THREADS, 0, ctx->stream>>>(fx, e.n, P.tiles.ptr, P.entry_k.ptr,
+                                                                   d->n_k, d->rho->ptr);
+          check_launch("rhok_lattice_kernel");
+          count_launch(ctx);
+        }
         AMDAT_CUDA(cudaStreamSynchronize(ctx->stream));
       }
     } catch (...) {
