@@ -52,7 +52,7 @@ EXPORTED = [
     "amdat_isf_run", "amdat_structure_factor_run", "amdat_rdf_run", "amdat_vhd_run",
     "amdat_profile_reset", "amdat_profile_kernel", "amdat_run_script", "amdat_script_error",
     "amdat_disp_plan_create", "amdat_disp_plan_run", "amdat_disp_plan_read", "amdat_disp_plan_info",
-    "amdat_disp_plan_destroy",
+    "amdat_disp_plan_destroy", "amdat_disp_moments_noalloc",
 ]
 
 PLAN_AUTOTUNE, PLAN_GRAPH = 1, 2

@@ -259,6 +259,26 @@ amdat_status amdat_vhd_run(amdat_ctx* ctx, int32_t list1, int32_t list2, int32_t
                            float max_distance, int32_t n_bins, int32_t out_flags, int64_t* counts);
 
 /* ---------------------------------------------------------------------------
+ * Displacement moments without device allocation (no counterpart in the
+ * reference).  For callers that cannot call cudaMalloc where they need an MSD
+ * (a memory pool or arena that owns the GPU's memory, plugin hosts that forbid
+ * allocation after start-up): per gap of the scheme, sums over every time pair
+ * and atom of |dr|^2 and |dr|^4, as amdat_disp_run gives for the list of all
+ * atoms.  The caller passes device coordinates [n_frames][n_atoms][3]
+ * (unwrapped, FP32), two device output arrays of n_timegaps doubles and a
+ * stream (NULL = legacy default stream, the device current on the calling
+ * thread).  No context is used and nothing is allocated: the temporaries live
+ * in a 16 MiB __device__ array that every GPU loading this library holds until
+ * exit.  The work must fit in it (about 500k time-pair x atom-chunk items):
+ * larger schemes return AMDAT_ERR_ARGUMENT.  The first call on a device looks
+ * up the array's address (and may load the module), so make it before any
+ * stream capture.  Calls share the array: calls whose GPU work overlaps race.
+ * ------------------------------------------------------------------------- */
+amdat_status amdat_disp_moments_noalloc(const amdat_scheme* scheme, int32_t fullblock,
+                                        const float* d_xyz, int32_t n_frames, int32_t n_atoms,
+                                        void* cuda_stream, double* d_sum_d2, double* d_sum_d4);
+
+/* ---------------------------------------------------------------------------
  * Input scripts: run an AMDAT input file's hot-path commands (system with a
  * custom dump, create_list, limit, msd, ngp, isfs, isf, structure_factor, rdf,
  * vhs, vhd) on one GPU and write the reference's output files.  Replaces

@@ -1,0 +1,52 @@
+"""amdat_disp_moments_noalloc: the displacement-moment entry point for callers
+that cannot allocate device memory (the caller owns the input and output
+buffers; the temporaries live in the library's fixed __device__ scratch).
+Its sums must match amdat_disp_run's (list of all atoms) to 1e-6 relative,
+call after call.  This file is collected last so a failure here does not stop
+the other GPU tests."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from amdat_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def test_noalloc_matches_disp_run(engine_mod):
+    import torch
+    E = engine_mod
+    scheme = synth.TimeScheme.exponential(6, 10, 1.3, 0, 0, 0.01)
+    traj = synth.random_walk(3000, 14.0, scheme, 0.4, seed=12)
+    eng = E.Engine(0)
+    eng.upload(traj.unwrapped, traj.box)
+    eng.set_scheme(scheme)
+    ref = eng.disp(0)
+    eng.close()
+    torch.cuda.set_device(0)
+    x = torch.from_numpy(np.ascontiguousarray(traj.unwrapped)).cuda()  # caller-owned input
+    G = len(ref["sum_d2"])
+    s = E.make_scheme(scheme)
+    for call in range(2):
+        d2 = torch.full((G,), -1.0, dtype=torch.float64, device="cuda")  # caller-owned outputs
+        d4 = torch.full((G,), -1.0, dtype=torch.float64, device="cuda")
+        st = E.lib().amdat_disp_moments_noalloc(C.byref(s), 0, C.c_void_p(x.data_ptr()),
+                                                traj.n_frames, traj.n_atoms, None,
+                                                C.c_void_p(d2.data_ptr()), C.c_void_p(d4.data_ptr()))
+        torch.cuda.synchronize()
+        assert st == 0, E.lib().amdat_last_error()
+        np.testing.assert_allclose(d2.cpu().numpy(), ref["sum_d2"], rtol=1e-6, atol=1e-12)
+        np.testing.assert_allclose(d4.cpu().numpy(), ref["sum_d4"], rtol=1e-6, atol=1e-14)
+
+
+def test_noalloc_rejects_oversized_work(engine_mod):
+    import torch
+    E = engine_mod
+    s = E.make_scheme(synth.TimeScheme.linear(5000, 1.0))   # ~12.5M time pairs
+    x = torch.zeros((2, 1, 3), dtype=torch.float32, device="cuda")
+    out = torch.zeros(5000, dtype=torch.float64, device="cuda")
+    st = E.lib().amdat_disp_moments_noalloc(C.byref(s), 0, C.c_void_p(x.data_ptr()), 5000, 1,
+                                            None, C.c_void_p(out.data_ptr()),
+                                            C.c_void_p(out.data_ptr()))
+    assert st == 1 and b"16 MiB" in E.lib().amdat_last_error()
