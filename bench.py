@@ -270,7 +270,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--frames", type=int, default=400, help="frames of the headline workload")
-    ap.add_argument("--only", default="", choices=["", "isf", "msd", "batched"],
+    ap.add_argument("--only", default="", choices=["", "isf", "msd", "batched", "pairs"],
                     help="run one workload only (profiling)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     args = ap.parse_args()
@@ -496,6 +496,43 @@ def main():
             info_msd=info_msd, info_fs=info_fs, launches=blaunch, plain_rate=plain_rate,
             alg_bytes=alg_bytes, nvec=int(shells[1][-1]), sum_n=int(sizes.sum()), npairs=npairs)
 
+    if args.only in ("", "pairs"):
+        # RDF + van Hove self/distinct: N=64000, L=42.3, 50 linear frames, sigma=0.1
+        from amdat_gb300 import synth
+        pscheme = synth.TimeScheme.linear(50, 1.0)
+        ptraj = synth.random_walk(64000, 42.3, pscheme, 0.1, seed=3, time_scaled=False)
+        eng.upload(ptraj.unwrapped, ptraj.box)
+        eng.set_scheme(pscheme)
+        frames = np.arange(50, dtype=np.int32)
+        eng.profile_reset(True)
+        eng.rdf(0, 0, frames[:2], 21.15, 500)  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        counts = eng.rdf(0, 0, frames, 21.15, 500)
+        rdf_s = time.perf_counter() - t0
+        n_rdf, ms_rdf = eng.profile_kernel("pair_hist_kernel")
+        gs_units = 64000.0 * int(E.scheme_counts(eng.scheme)[2])
+        eng.disp(0, n_bins=200, bin_max=5.0)
+        t0 = time.perf_counter()
+        out = eng.disp(0, n_bins=200, bin_max=5.0)
+        gs_s = time.perf_counter() - t0
+        # distinct van Hove: every time pair is N^2 pair distances; time the
+        # first 24 time pairs (gaps 0..) as a bounded sample
+        sub = synth.TimeScheme.linear(25, 1.0)
+        eng.upload(ptraj.unwrapped[:25], ptraj.box)
+        eng.set_scheme(sub)
+        npairs_sub = int(E.scheme_counts(eng.scheme)[2])
+        t0 = time.perf_counter()
+        eng.vhd(0, 0, 5.0, 200)
+        gd_s = time.perf_counter() - t0
+        eng.profile_reset(False)
+        n = 64000.0
+        result["pairs"] = dict(rdf_rate=50 * n * (n - 1) / rdf_s, rdf_ms=1e3 * rdf_s,
+                               rdf_kernel_ms=ms_rdf / max(n_rdf, 1) * 50 / 2,
+                               gs_rate=gs_units / gs_s, gs_ms=1e3 * gs_s,
+                               gd_rate=npairs_sub * n * (n - 1) / gd_s, gd_ms=1e3 * gd_s,
+                               gd_sample=npairs_sub, rdf_total=int(counts.sum()))
+
     # CPU baseline on rank 0 (bounded samples of both workloads)
     cpu = None
     if rank == 0 and not args.no_cpu and args.only in ("", "isf"):
@@ -609,6 +646,16 @@ def main():
         if "value" not in line:
             line.update({"value": b["units"] / (b["ms_fs"] / 1e3), "unit": "atom·time-pairs/s",
                          "ms_per_step": b["ms_fs"], "config": {"workload": line["batched"]["workload"]}})
+    if "pairs" in result:
+        q = result["pairs"]
+        line["pairs"] = {
+            "workload": "N=64000, L=42.3, 50 linear frames (sigma 0.1): RDF 500 bins to L/2 over all "
+                        "frames; G_s 200 bins to 5.0 over all 1226 time pairs; G_d 200 bins to 5.0 "
+                        f"on the first {q['gd_sample']} time pairs of a 25-frame scheme",
+            "rdf": {"value": q["rdf_rate"], "unit": "ordered pairs/s", "ms_per_step": q["rdf_ms"],
+                    "counted_pairs_in_range": q["rdf_total"]},
+            "vhs": {"value": q["gs_rate"], "unit": "atom·time-pairs/s", "ms_per_step": q["gs_ms"]},
+            "vhd": {"value": q["gd_rate"], "unit": "ordered pairs/s", "ms_per_step": q["gd_ms"]}}
     print(json.dumps(line), flush=True)
     eng.close()
 
