@@ -93,5 +93,47 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
     return LIB
 
 
+TORCH_SRC = os.path.join(PKG, "torch_ext", "amdat_torch.cpp")
+
+
+def torch_ext_path() -> str:
+    import sysconfig
+    return os.path.join(OUT, "amdat_torch" + sysconfig.get_config_var("EXT_SUFFIX"))
+
+
+def build_torch_ext(verbose: bool = False) -> str:
+    """The libtorch autograd extension (amdat_torch), compiled with g++ against
+    the installed torch and linked to libamdat_gb300.so (no ninja needed)."""
+    import sysconfig
+
+    import torch
+    from torch.utils import cpp_extension as ce
+
+    lib = build(verbose=verbose)
+    out = torch_ext_path()
+    deps = [TORCH_SRC, lib, os.path.join(REPO, "include", "amdat_gb300.h")]
+    if os.path.exists(out) and os.path.getmtime(out) >= max(os.path.getmtime(d) for d in deps):
+        return out
+    cuda = _cuda_home()
+    torch_lib = os.path.join(os.path.dirname(torch.__file__), "lib")
+    flags = ["-O2", "-std=c++17", "-fPIC", "-shared", "-w",
+             f"-D_GLIBCXX_USE_CXX11_ABI={int(torch._C._GLIBCXX_USE_CXX11_ABI)}",
+             "-DTORCH_EXTENSION_NAME=amdat_torch", "-DTORCH_API_INCLUDE_EXTENSION_H"]
+    abi = getattr(ce, "_get_pybind11_abi_build_flags", None)
+    if abi is not None:
+        flags += abi()
+    incs = []
+    for d in ce.include_paths("cuda") + [sysconfig.get_paths()["include"], os.path.join(REPO, "include"),
+                                         os.path.join(cuda, "include")]:
+        incs += ["-I", d]
+    libs = ["-L", torch_lib, "-lc10", "-lc10_cuda", "-ltorch", "-ltorch_cpu", "-ltorch_cuda",
+            "-ltorch_python", "-L", OUT, "-lamdat_gb300", f"-Wl,-rpath,{torch_lib}",
+            "-Wl,-rpath,$ORIGIN", "-L", os.path.join(cuda, "lib64"), "-lcudart"]
+    tmp = out + f".tmp{os.getpid()}"
+    _run(["g++"] + flags + incs + [TORCH_SRC, "-o", tmp] + libs)
+    os.replace(tmp, out)
+    return out
+
+
 if __name__ == "__main__":
     print(build(verbose=True))

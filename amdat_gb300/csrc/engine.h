@@ -113,6 +113,8 @@ struct Density {
   int32_t n_k = 0;
   int32_t n_frames = 0;
   int32_t n_shells = 0;
+  float period = 0.f;              // k = 2 pi n / period
+  int32_t n_list = 0;              // list size when the density was computed
   std::vector<int32_t> frames;     // system frame of each row
   std::vector<int32_t> kvec;       // [3*n_k] (lattice mode: shell-sorted)
   std::vector<int32_t> shell_off;  // lattice mode
@@ -176,6 +178,8 @@ void check_launch(const char* what);
 DevBuf<float2>* rho_acquire(amdat_ctx* ctx, size_t count);
 void rho_release(amdat_ctx* ctx, DevBuf<float2>* b);
 void lattice_plans_free(amdat_ctx* ctx);
+void fixed_turns_launch(amdat_ctx* ctx, const int32_t* d_frames, int32_t n_frames, const ListEntry& e,
+                        float period, int4* out);
 
 // RAII event pair around one kernel launch when profiling is enabled
 struct KernelTimer {

@@ -307,6 +307,19 @@ static int4* fixed_turns(amdat_ctx* ctx, const Density& d, const ListEntry& e, f
   return fx;
 }
 
+// fixed-point phases of a list's atoms in the given (device) frames, into out
+// [n_frames][n]; used by the adjoint kernels so they see the forward's phases
+void fixed_turns_launch(amdat_ctx* ctx, const int32_t* d_frames, int32_t n_frames,
+                        const ListEntry& e, float period, int4* out) {
+  const int64_t n = (int64_t)n_frames * e.n;
+  if (n == 0) return;
+  const int64_t blocks = std::min<int64_t>(ceil_div(n, 256), (int64_t)ctx->n_sm * 16);
+  fixed_turns_kernel<<<(unsigned)blocks, 256, 0, ctx->stream>>>(ctx->w.ptr, ctx->n_pad, n_frames, d_frames,
+                                                                view(e), 1.0 / (double)period, out);
+  check_launch("fixed_turns_kernel");
+  count_launch(ctx);
+}
+
 static int32_t store_density(amdat_ctx* ctx, Density* d) {
   const int32_t h = ctx->next_density++;
   ctx->densities[h] = d;
@@ -476,6 +489,8 @@ amdat_status amdat_wave_density(amdat_ctx* ctx, int32_t list, const int32_t* kve
     d->list = list;
     d->n_k = n_k;
     d->n_frames = n_frames;
+    d->period = period;
+    d->n_list = list_entry(ctx, list).n;
     d->frames.assign(frames, frames + n_frames);
     d->kvec.assign(kvec_n, kvec_n + 3 * (size_t)n_k);
     try {
@@ -523,6 +538,8 @@ amdat_status amdat_wave_density_lattice(amdat_ctx* ctx, int32_t list, float kmax
     d->n_k = (int32_t)(P.kvec.size() / 3);
     d->n_frames = n_frames;
     d->n_shells = (int32_t)P.shell_off.size() - 1;
+    d->period = period;
+    d->n_list = e.n;
     d->frames.assign(frames, frames + n_frames);
     d->kvec = P.kvec;
     d->shell_off = P.shell_off;

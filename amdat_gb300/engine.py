@@ -52,7 +52,8 @@ EXPORTED = [
     "amdat_isf_run", "amdat_structure_factor_run", "amdat_rdf_run", "amdat_vhd_run",
     "amdat_profile_reset", "amdat_profile_kernel", "amdat_run_script", "amdat_script_error",
     "amdat_disp_plan_create", "amdat_disp_plan_run", "amdat_disp_plan_read", "amdat_disp_plan_info",
-    "amdat_disp_plan_destroy", "amdat_disp_moments_noalloc",
+    "amdat_disp_plan_destroy", "amdat_disp_moments_noalloc", "amdat_gsmooth_run",
+    "amdat_gsmooth_adjoint", "amdat_structure_factor_adjoint",
 ]
 
 PLAN_AUTOTUNE, PLAN_GRAPH = 1, 2
@@ -372,6 +373,40 @@ class Engine:
         _check(lib().amdat_vhd_run(self._ctx, int(list1), int(list2), int(fullblock),
                                    C.c_float(max_distance), int(n_bins), OUT_HOST, _p(out)))
         return out
+
+
+    # ---- differentiable structure
+    def gsmooth(self, list_h, frames, sigma, r_max, n_bins, out_device=None):
+        """Gaussian-smoothed pair histogram h[n_bins] (FP64), summed over frames."""
+        fr = _i32(frames)
+        if out_device is not None:
+            _check(lib().amdat_gsmooth_run(self._ctx, int(list_h), _p(fr), len(fr), C.c_float(sigma),
+                                           C.c_float(r_max), int(n_bins), OUT_DEVICE,
+                                           C.c_void_p(out_device)))
+            return None
+        out = np.zeros(n_bins)
+        _check(lib().amdat_gsmooth_run(self._ctx, int(list_h), _p(fr), len(fr), C.c_float(sigma),
+                                       C.c_float(r_max), int(n_bins), OUT_HOST, _p(out)))
+        return out
+
+    def gsmooth_adjoint(self, list_h, frames, sigma, r_max, n_bins, dl_dh, n_list):
+        """dLoss/dr [n_frames][n_list][3] (FP32) for dLoss/dh = dl_dh."""
+        fr = _i32(frames)
+        w = np.ascontiguousarray(dl_dh, dtype=np.float64)
+        g = np.zeros((len(fr), n_list, 3), np.float32)
+        _check(lib().amdat_gsmooth_adjoint(self._ctx, int(list_h), _p(fr), len(fr), C.c_float(sigma),
+                                           C.c_float(r_max), int(n_bins), _p(w), OUT_HOST, _p(g)))
+        return g
+
+    def structure_factor_adjoint(self, density, shell_off, dl_ds, n_frames, n_list):
+        """dLoss/dr [n_frames][n_list][3] (FP32) of loss(S_raw) with dLoss/dS_raw = dl_ds,
+        S_raw the auto structure factor of the density (structure_factor(d, d, ...))."""
+        off = _i32(shell_off)
+        w = np.ascontiguousarray(dl_ds, dtype=np.float64)
+        g = np.zeros((n_frames, n_list, 3), np.float32)
+        _check(lib().amdat_structure_factor_adjoint(self._ctx, int(density), _p(off), len(off) - 1,
+                                                    _p(w), OUT_HOST, _p(g)))
+        return g
 
 
 class DispPlan:

@@ -114,8 +114,9 @@ amdat_status amdat_launch_count(amdat_ctx* ctx, int64_t* count);
  * CUDA events on the context's stream; amdat_profile_kernel returns the number
  * of launches and their total device time (ms) since the last reset.  Kernel
  * names: disp_mixed_kernel, disp_plain_kernel, rhok_list_kernel,
- * rhok_lattice_kernel, rhok_plain_kernel, isf_pairs_kernel, sk_frames_kernel,
- * pair_hist_kernel.  (No counterpart in the reference, which times commands
+ * rhok_lattice_kernel, rhok_tc_kernel, rhok_plain_kernel, isf_pairs_kernel,
+ * sk_frames_kernel, pair_hist_kernel, gsmooth_kernel, gsmooth_adjoint_kernel,
+ * sk_adjoint_columns_kernel, sk_adjoint_direct_kernel.  (No counterpart in the reference, which times commands
  * with time(NULL), e.g. src/control.cpp:2190-2196.) */
 amdat_status amdat_profile_reset(amdat_ctx* ctx, int32_t enable);
 amdat_status amdat_profile_kernel(amdat_ctx* ctx, const char* kernel, int64_t* launches,
@@ -257,6 +258,37 @@ amdat_status amdat_rdf_run(amdat_ctx* ctx, int32_t list1, int32_t list2, const i
  * counts[g][b]. */
 amdat_status amdat_vhd_run(amdat_ctx* ctx, int32_t list1, int32_t list2, int32_t fullblock,
                            float max_distance, int32_t n_bins, int32_t out_flags, int64_t* counts);
+
+/* ---------------------------------------------------------------------------
+ * Differentiable structure (no counterpart in the reference, whose nearest
+ * parts are the hard-binned RDF, src/radial_distribution_function.cpp:233-285,
+ * and Structure_Factor, src/structure_factor.cpp:201-320).
+ * ------------------------------------------------------------------------- */
+/* Gaussian-smoothed pair histogram of one list over the given frames:
+ * h[b] = sum_f sum_{i<j} exp(-(r_b - r_ij)^2 / 2 sigma^2) / (sqrt(2 pi) sigma),
+ * r_b = (b + 1/2) r_max / n_bins, r_ij the minimum-image distance of the wrapped
+ * coordinates, pairs with r_ij >= r_max + 6 sigma skipped (r_max + 6 sigma must
+ * not exceed half the box).  Bins b within ceil(6 sigma n_bins / r_max) of
+ * floor(r_ij n_bins / r_max) receive a pair's terms. */
+amdat_status amdat_gsmooth_run(amdat_ctx* ctx, int32_t list, const int32_t* frames, int32_t n_frames,
+                               float sigma, float r_max, int32_t n_bins, int32_t out_flags,
+                               double* h);
+/* Adjoint of amdat_gsmooth_run: given dl_dh[n_bins] = dLoss/dh, writes
+ * grad[f][i][3] = dLoss/dr_i(frames[f]) for the list's atoms (FP32).  The pair
+ * loop is recomputed.  io_flags = AMDAT_OUT_DEVICE: dl_dh and grad are device
+ * pointers. */
+amdat_status amdat_gsmooth_adjoint(amdat_ctx* ctx, int32_t list, const int32_t* frames,
+                                   int32_t n_frames, float sigma, float r_max, int32_t n_bins,
+                                   const double* dl_dh, int32_t io_flags, float* grad);
+/* Adjoint of the auto structure factor of one density:
+ * S_raw[s] = sum_f sum_{k in shell s} |rho_k(f)|^2 / H_s (what
+ * amdat_structure_factor_run(ctx, d, d, ...) gives).  Given dl_ds[n_shells],
+ * writes grad[f][i][3] = dLoss/dr_i for the density's frames and list atoms.
+ * The phases come from the context's current trajectory, which must hold the
+ * coordinates the density was computed from. */
+amdat_status amdat_structure_factor_adjoint(amdat_ctx* ctx, int32_t density,
+                                            const int32_t* shell_offsets, int32_t n_shells,
+                                            const double* dl_ds, int32_t io_flags, float* grad);
 
 /* ---------------------------------------------------------------------------
  * Displacement moments without device allocation (no counterpart in the

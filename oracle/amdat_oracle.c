@@ -721,3 +721,125 @@ void orc_rhok_parallel(const float* r, int32_t n_atoms, const int32_t* frames, i
     }
   }
 }
+
+/* ------------------------------------------------------------------------- */
+/* differentiable structure (FP64; no reference counterpart)                 */
+/* ------------------------------------------------------------------------- */
+#define SG_CUT 6.0
+#define INV_SQRT_2PI 0.39894228040143267794
+
+static double min_image_d(double d, double L) { return d - L * rint(d / L); }
+
+/* span of bins a pair touches, as the engine computes it (FP32 bin width) */
+static int sg_span(double sigma, double r_max, int32_t n_bins) {
+  float bin = (float)r_max / (float)n_bins;
+  return (int)ceil((double)(6.0f * (float)sigma / bin));
+}
+
+void orc_gsmooth(const float* r, int32_t n_atoms, const float* box, const int32_t* list,
+                 int32_t n_list, const int32_t* frames, int32_t n_frames, double sigma,
+                 double r_max, int32_t n_bins, double* h) {
+  const double bin = r_max / n_bins, cut = r_max + SG_CUT * sigma;
+  const int span = sg_span(sigma, r_max, n_bins);
+  for (int b = 0; b < n_bins; ++b) h[b] = 0;
+  for (int f = 0; f < n_frames; ++f) {
+    int t = frames[f];
+    for (int i = 0; i < n_list; ++i)
+      for (int j = i + 1; j < n_list; ++j) {
+        int a = list[i], c = list[j];
+        double d[3], r2 = 0;
+        for (int k = 0; k < 3; ++k) {
+          d[k] = min_image_d((double)POS(r, t, c, k) - (double)POS(r, t, a, k), box[k]);
+          r2 += d[k] * d[k];
+        }
+        if (r2 >= cut * cut) continue;
+        double rr = sqrt(r2);
+        int bc = (int)(rr / bin);
+        for (int b = bc - span; b <= bc + span; ++b) {
+          if (b < 0 || b >= n_bins) continue;
+          double x = (b + 0.5) * bin - rr;
+          h[b] += INV_SQRT_2PI / sigma * exp(-x * x / (2 * sigma * sigma));
+        }
+      }
+  }
+}
+
+void orc_gsmooth_grad(const float* r, int32_t n_atoms, const float* box, const int32_t* list,
+                      int32_t n_list, const int32_t* frames, int32_t n_frames, double sigma,
+                      double r_max, int32_t n_bins, const double* w, double* grad) {
+  const double bin = r_max / n_bins, cut = r_max + SG_CUT * sigma;
+  const int span = sg_span(sigma, r_max, n_bins);
+  for (int f = 0; f < n_frames; ++f) {
+    int t = frames[f];
+    for (int i = 0; i < n_list; ++i) {
+      double g[3] = {0, 0, 0};
+      for (int j = 0; j < n_list; ++j) {
+        if (j == i) continue;
+        int a = list[i], c = list[j];
+        double d[3], r2 = 0;
+        for (int k = 0; k < 3; ++k) {
+          d[k] = min_image_d((double)POS(r, t, a, k) - (double)POS(r, t, c, k), box[k]);
+          r2 += d[k] * d[k];
+        }
+        if (r2 >= cut * cut || r2 == 0) continue;
+        double rr = sqrt(r2), psi = 0;
+        int bc = (int)(rr / bin);
+        for (int b = bc - span; b <= bc + span; ++b) {
+          if (b < 0 || b >= n_bins) continue;
+          double x = (b + 0.5) * bin - rr;
+          psi += w[b] * x / (sigma * sigma) * INV_SQRT_2PI / sigma * exp(-x * x / (2 * sigma * sigma));
+        }
+        for (int k = 0; k < 3; ++k) g[k] += psi * d[k] / rr;
+      }
+      for (int k = 0; k < 3; ++k) grad[((size_t)f * n_list + i) * 3 + k] = g[k];
+    }
+  }
+}
+
+void orc_sk_grad(const float* r, int32_t n_atoms, const int32_t* list, int32_t n_list,
+                 const int32_t* frames, int32_t n_frames, const int32_t* kvec_n, int32_t n_k,
+                 const int32_t* off, int32_t n_shells, double box_len, const double* w,
+                 int32_t n_threads, double* grad) {
+  const double tpl = TWO_PI / box_len;
+  double* u = (double*)calloc(n_k > 0 ? n_k : 1, sizeof(double));
+  for (int s = 0; s < n_shells; ++s) {
+    int cnt = off[s + 1] - off[s];
+    for (int k = off[s]; k < off[s + 1]; ++k) u[k] = 2.0 * w[s] / cnt;
+  }
+  double* rho = (double*)malloc(sizeof(double) * 2 * (n_k > 0 ? n_k : 1));
+  for (int f = 0; f < n_frames; ++f) {
+    int t = frames[f];
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(n_threads > 0 ? n_threads : 1) schedule(static)
+#endif
+    for (int k = 0; k < n_k; ++k) {
+      double re = 0, im = 0;
+      for (int j = 0; j < n_list; ++j) {
+        int a = list[j];
+        double ph = tpl * ((double)kvec_n[3 * k] * POS(r, t, a, 0) + (double)kvec_n[3 * k + 1] * POS(r, t, a, 1) +
+                           (double)kvec_n[3 * k + 2] * POS(r, t, a, 2));
+        re += cos(ph);
+        im += sin(ph);
+      }
+      rho[2 * k] = re;
+      rho[2 * k + 1] = im;
+    }
+#ifdef _OPENMP
+#pragma omp parallel for num_threads(n_threads > 0 ? n_threads : 1) schedule(static)
+#endif
+    for (int j = 0; j < n_list; ++j) {
+      int a = list[j];
+      double g[3] = {0, 0, 0};
+      for (int k = 0; k < n_k; ++k) {
+        if (u[k] == 0) continue;
+        double ph = tpl * ((double)kvec_n[3 * k] * POS(r, t, a, 0) + (double)kvec_n[3 * k + 1] * POS(r, t, a, 1) +
+                           (double)kvec_n[3 * k + 2] * POS(r, t, a, 2));
+        double v = u[k] * (rho[2 * k + 1] * cos(ph) - rho[2 * k] * sin(ph)) * tpl;
+        for (int c = 0; c < 3; ++c) g[c] += v * kvec_n[3 * k + c];
+      }
+      for (int c = 0; c < 3; ++c) grad[((size_t)f * n_list + j) * 3 + c] = g[c];
+    }
+  }
+  free(rho);
+  free(u);
+}

@@ -106,6 +106,25 @@ void orc_rhok_parallel(const float* wrapped, int32_t n_atoms, const int32_t* fra
                        int32_t n_frames, const int32_t* kvec_n, int32_t n_k, double box_len,
                        int32_t n_threads, double* rho);
 
+/* Differentiable structure (no reference counterpart; restates the engine's
+ * definitions in FP64 from the FP32 wrapped coordinates).
+ * orc_gsmooth: h[b] = sum_f sum_{i<j} G(r_b - r_ij), G the normalised Gaussian
+ * of width sigma, r_b = (b+1/2) r_max/n_bins, minimum image, pairs with
+ * r_ij >= r_max + 6 sigma skipped, bins within ceil(6 sigma/bin) of floor(r_ij/bin).
+ * orc_gsmooth_grad: grad[f][i][3] = d(sum_b w[b] h[b]) / dr_i(frames[f]).
+ * orc_sk_grad: grad[f][i][3] = d(sum_s w[s] S_raw[s]) / dr_i(frames[f]) with
+ * S_raw[s] = sum_f sum_{k in s} |rho_k(f)|^2 / H_s, k = 2 pi n / box_len. */
+void orc_gsmooth(const float* wrapped, int32_t n_atoms, const float* box, const int32_t* list,
+                 int32_t n_list, const int32_t* frames, int32_t n_frames, double sigma,
+                 double r_max, int32_t n_bins, double* h);
+void orc_gsmooth_grad(const float* wrapped, int32_t n_atoms, const float* box, const int32_t* list,
+                      int32_t n_list, const int32_t* frames, int32_t n_frames, double sigma,
+                      double r_max, int32_t n_bins, const double* w, double* grad);
+void orc_sk_grad(const float* wrapped, int32_t n_atoms, const int32_t* list, int32_t n_list,
+                 const int32_t* frames, int32_t n_frames, const int32_t* kvec_n, int32_t n_k,
+                 const int32_t* shell_off, int32_t n_shells, double box_len, const double* w,
+                 int32_t n_threads, double* grad);
+
 #ifdef __cplusplus
 }
 #endif

@@ -240,3 +240,39 @@ def rhok_parallel(wrapped, frames, kvec_n, box_len, n_threads):
     lib().orc_rhok_parallel(_p(r), r.shape[1], _p(fr), len(fr), _p(kv), nk, C.c_double(box_len),
                             int(n_threads), _p(out))
     return out
+
+
+def gsmooth(wrapped, box, lst, frames, sigma, r_max, n_bins):
+    """FP64 Gaussian-smoothed pair histogram (the engine's amdat_gsmooth_run)."""
+    r = _f32(wrapped)
+    bx = _f32(box)
+    lst, fr = _i32(lst), _i32(frames)
+    h = np.zeros(n_bins)
+    lib().orc_gsmooth(_p(r), r.shape[1], _p(bx), _p(lst), len(lst), _p(fr), len(fr),
+                      C.c_double(sigma), C.c_double(r_max), int(n_bins), _p(h))
+    return h
+
+
+def gsmooth_grad(wrapped, box, lst, frames, sigma, r_max, n_bins, w):
+    """FP64 gradient of sum_b w[b] h[b] with respect to the list's positions."""
+    r = _f32(wrapped)
+    bx = _f32(box)
+    lst, fr = _i32(lst), _i32(frames)
+    ww = np.ascontiguousarray(w, np.float64)
+    g = np.zeros((len(fr), len(lst), 3))
+    lib().orc_gsmooth_grad(_p(r), r.shape[1], _p(bx), _p(lst), len(lst), _p(fr), len(fr),
+                           C.c_double(sigma), C.c_double(r_max), int(n_bins), _p(ww), _p(g))
+    return g
+
+
+def sk_grad(wrapped, lst, frames, kvec_n, shell_off, box_len, w, n_threads=1):
+    """FP64 gradient of sum_s w[s] S_raw[s], S_raw[s] = sum_f sum_{k in s} |rho_k|^2 / H_s."""
+    r = _f32(wrapped)
+    lst, fr = _i32(lst), _i32(frames)
+    kv = _i32(kvec_n).reshape(-1)
+    off = _i32(shell_off)
+    ww = np.ascontiguousarray(w, np.float64)
+    g = np.zeros((len(fr), len(lst), 3))
+    lib().orc_sk_grad(_p(r), r.shape[1], _p(lst), len(lst), _p(fr), len(fr), _p(kv), len(kv) // 3,
+                      _p(off), len(off) - 1, C.c_double(box_len), _p(ww), int(n_threads), _p(g))
+    return g
