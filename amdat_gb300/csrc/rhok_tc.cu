@@ -4,23 +4,30 @@
 // GEMM with the atoms as the reduction axis.  As a real GEMM per tile:
 //   A (128 x 2J): rows 0..63   = [Wr, -Wi] of 64 (nx,ny) rows (8 nx x 8 ny),
 //                 rows 64..127 = [Wi,  Wr]           (k = 2j, 2j+1 per atom j)
-//   B ( 64 x 2J): [Zr, Zi] for 64 consecutive nz
-//   D = A B^T  (128 x 64): rows 0..63 = Re rho, rows 64..127 = Im rho.
+//   B (  n x 2J): [Zr, Zi] for n consecutive nz (n <= 128, a multiple of 16,
+//                 sized per tile to the nz extent of its 64 rows)
+//   D = A B^T  (128 x n): rows 0..63 = Re rho, rows 64..127 = Im rho.
 // Operands are FP16 split into hi + lo parts (x = hi + lo to ~2^-22), and each
-// chunk runs three tcgen05.mma passes, hi*hi + hi*lo + lo*hi, accumulating in
-// FP32 tensor memory; after every TC_GROUP chunks (64 atoms) the accumulator
-// is drained into Kahan-compensated FP32 registers (the tensor core's FP32
-// accumulation drops low bits as the accumulator grows, so it never spans more
-// than 64 atoms), double-buffered so the next MMAs overlap the drain.  The phases are the exact fixed-point phases of
-// the FP32 kernels (fraction of the box in units of 2^-31 turns).
+// chunk of 32 atoms runs three tcgen05.mma passes, hi*lo + lo*hi + hi*hi (small
+// terms first), accumulating in FP32 tensor memory.  The tensor core's FP32
+// accumulation drops low bits as the accumulator grows, so an accumulation
+// never spans more than TC_GROUP chunks (64 atoms): the accumulator is then
+// drained into Kahan-compensated sums that also live in tensor memory.  The
+// phases are the exact fixed-point phases of the FP32 kernels (fraction of the
+// box in units of 2^-31 turns).
 //
 // Per frame batch, zgen_kernel precomputes the B operands (Z hi/lo in the
-// K-major core-matrix layout, one 16 KB blob per (frame, nz block, 32-atom
-// chunk)); the main kernel streams them with 1-D bulk copies (cp.async.bulk)
-// into a two-stage shared-memory ring and builds A from per-chunk X/Y phase
-// tables.  One thread issues the MMAs; mbarriers order bulk copy -> MMA ->
-// stage reuse and MMA -> tensor-memory drain; every wait is bounded and a
-// timeout is reported through an error word.
+// K-major core-matrix layout, one blob per (frame, nz window, chunk)).  The
+// main kernel is warp-specialised, one CTA per SM, 512 TMEM columns:
+//   warps 0-3   drain: TMEM accumulator -> Kahan (s, c) columns, then the epilogue
+//   warp 4      producer: bulk copies (cp.async.bulk) of Z into a 3-stage ring
+//   warp 5      MMA issuer: 12 tcgen05.mma per chunk into one of two accumulators
+//   warps 6-13  builders: X/Y phase tables (sincospif) and the A operand (W
+//               products, FP16 split, K-major stores) into a 2-stage ring
+// Hand-offs are mbarriers (bulk-copy transactions, tcgen05.commit, thread
+// arrivals); every wait is bounded, and a timeout makes every role stop, wait
+// for its own copies and MMAs, free tensor memory and report through an error
+// word.
 #include <cuda_fp16.h>
 
 #include <algorithm>
@@ -36,28 +43,43 @@ namespace amdat {
 constexpr int TC_J = 32;                      // atoms per chunk
 constexpr int TC_K = 2 * TC_J;                // real K per chunk
 constexpr int TC_ROWS = 64;                   // complex rows (8 nx x 8 ny)
-constexpr int TC_NZ = 64;                     // nz columns per tile (MMA N)
+constexpr int TC_NMAX = 128;                  // widest nz window (MMA N)
 constexpr int TC_M = 2 * TC_ROWS;             // MMA M = 128
-constexpr int TC_THREADS = 256;
-constexpr uint32_t TC_A_BYTES = TC_M * TC_K * 2;    // 16 KB (one of hi / lo)
-constexpr uint32_t TC_B_BYTES = TC_NZ * TC_K * 2;   // 8 KB (one of hi / lo)
-constexpr uint32_t TC_BLOB = 2 * TC_B_BYTES;        // Z hi + lo per (frame, nz block, chunk)
-constexpr uint32_t TC_WAIT = 1u << 22;              // mbarrier polls (~0.5 s bound)
-constexpr int TC_GROUP = 2;                          // chunks per tensor-memory accumulation
+constexpr int TC_GROUP = 2;                   // chunks per tensor-memory accumulation
+constexpr int TC_SZ = 3;                      // Z ring stages
+constexpr int TC_SA = 2;                      // A ring stages
+constexpr int TC_PRODUCER_WARP = 4;
+constexpr int TC_MMA_WARP = 5;
+constexpr int TC_BUILD_WARP0 = 6;
+constexpr int TC_BUILDERS = 256;              // 8 builder warps
+constexpr int TC_DRAINERS = 128;              // warps 0-3, one per TMEM lane quadrant
+constexpr int TC_THREADS = 32 * TC_BUILD_WARP0 + TC_BUILDERS;  // 448
+constexpr uint32_t TC_A_BYTES = TC_M * TC_K * 2;      // 16 KB (one of hi / lo)
+constexpr uint32_t TC_ZHALF = TC_NMAX * TC_K * 2;     // 16 KB (one of hi / lo, widest window)
+constexpr uint32_t TC_WAIT = 1u << 22;                // mbarrier polls (~0.5 s bound)
+// tensor-memory columns: two accumulators, then the Kahan sums and compensations
+constexpr uint32_t TC_COL_ACC = 0, TC_COL_S = 2 * TC_NMAX, TC_COL_C = 3 * TC_NMAX;
+constexpr uint32_t TC_TMEM_COLS = 4 * TC_NMAX;        // 512
 
 struct TcTile {
-  int32_t nx0, ny0, zblk, entry0;  // entry map: TC_ROWS * TC_NZ ints from entry0
+  int32_t nx0, ny0, zblk, entry0;  // entry map: TC_ROWS * n ints from entry0
+  int32_t n, pad0, pad1, pad2;     // MMA N of this tile (multiple of 16, <= TC_NMAX)
 };
 
 struct TcSmem {
-  unsigned char a[2][2][TC_A_BYTES];  // [stage][hi|lo]
-  unsigned char b[2][TC_BLOB];        // [stage] hi then lo
-  float2 xy[2][TC_J * 16];            // [stage][atom*16 + swizzled(8 X then 8 Y)]
-  uint64_t mbar_tma[2];
-  uint64_t mbar_mma[2];
+  unsigned char z[TC_SZ][2 * TC_ZHALF];  // [stage] hi then lo; the epilogue stages D here
+  unsigned char a[TC_SA][2][TC_A_BYTES]; // [stage][hi|lo]
+  float2 xy[2][TC_J * 16];               // [chunk parity][atom*16 + swizzled(8 X then 8 Y)]
+  uint64_t full_z[TC_SZ], empty_z[TC_SZ];
+  uint64_t full_a[TC_SA], empty_a[TC_SA];
+  uint64_t full_acc[2], empty_acc[2];
+  uint64_t mma_done;
   uint32_t tmem;
-  int bad;
+  volatile int bad;        // any role gave up
+  int build_stop[2];       // chunk parity: written by builder 0 before a builder barrier
+  int z_issued, z_landed;  // bulk copies issued / seen complete
 };
+static_assert(sizeof(float) * TC_M * (TC_NMAX + 1) <= sizeof(((TcSmem*)0)->z), "D staging must fit the Z ring");
 
 __device__ __forceinline__ void tc_split(float x, __half& hi, __half& lo) {
   hi = __float2half_rn(x);
@@ -68,24 +90,25 @@ __device__ __forceinline__ void tc_phase(int32_t ph, float* s, float* c) {
   sincospif(__fmul_rn((float)ph, 9.313225746154785e-10f), s, c);  // ph * 2^-30 * pi
 }
 
-// Z operands of one frame batch: blob (f, zblk, chunk) = [hi 8 KB][lo 8 KB],
-// each a 64 (nz) x 64 (k) K-major tile; k = 2j -> Re Z_j, 2j+1 -> Im Z_j
+// Z operands of one frame batch: blob (f, zblk, chunk) = [hi][lo], each an
+// nzw (nz) x 64 (k) K-major tile; k = 2j -> Re Z_j, 2j+1 -> Im Z_j
 __global__ void __launch_bounds__(256)
     zgen_kernel(const int4* __restrict__ fx, int32_t n_list, int32_t n_chunks, int32_t n_zblk,
-                unsigned char* __restrict__ zbuf) {
+                int32_t nzw, unsigned char* __restrict__ zbuf) {
   const int blob = blockIdx.x;
   const int c = blob % n_chunks;
   const int zb = (blob / n_chunks) % n_zblk;
   const int f = blob / (n_chunks * n_zblk);
-  unsigned char* hi = zbuf + (size_t)blob * TC_BLOB;
-  unsigned char* lo = hi + TC_B_BYTES;
+  const uint32_t half = (uint32_t)nzw * TC_K * 2;
+  unsigned char* hi = zbuf + (size_t)blob * 2 * half;
+  unsigned char* lo = hi + half;
   const int4* F = fx + (int64_t)f * n_list;
-  for (int e = threadIdx.x; e < TC_NZ * TC_J; e += blockDim.x) {
-    const int col = e % TC_NZ, j = e / TC_NZ;
+  for (int e = threadIdx.x; e < nzw * TC_J; e += blockDim.x) {
+    const int col = e % nzw, j = e / nzw;
     const int a = c * TC_J + j;
     float s = 0.f, co = 0.f;
     if (a < n_list) {
-      const int32_t nz = zb * TC_NZ + col;
+      const int32_t nz = zb * nzw + col;
       tc_phase((int32_t)((uint32_t)nz * (uint32_t)F[a].z), &s, &co);
     }
     __half rh, rl, ih, il;
@@ -101,130 +124,96 @@ __global__ void __launch_bounds__(256)
 // spreads a warp's reads (8 rows x 4 atoms) over all banks
 __device__ __forceinline__ int xy_slot(int j, int m) { return j * 16 + ((m + 4 * (j & 3)) & 15); }
 
-struct KCf {
-  float s, c;
-};
+// warp-uniform bounded wait: lane 0 polls, the warp shares the outcome
+__device__ __forceinline__ bool warp_wait(uint64_t* mbar, uint32_t parity) {
+  bool ok = true;
+  if ((threadIdx.x & 31) == 0) ok = umma::mbar_wait(mbar, parity, TC_WAIT);
+  return __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
+}
 
-__global__ void __launch_bounds__(TC_THREADS, 2)
+__global__ void __launch_bounds__(TC_THREADS, 1)
     rhok_tc_kernel(const int4* __restrict__ fx, int32_t n_list, int32_t n_chunks, int32_t n_zblk,
-                   const TcTile* __restrict__ tiles, const int32_t* __restrict__ entry_k,
+                   int32_t nzw, const TcTile* __restrict__ tiles, const int32_t* __restrict__ entry_k,
                    const unsigned char* __restrict__ zbuf, int32_t frame0, int32_t n_k,
                    float2* __restrict__ rho, int* __restrict__ err) {
-  extern __shared__ __align__(1024) unsigned char smem_raw[];
-  TcSmem& S = *reinterpret_cast<TcSmem*>(smem_raw);
+  extern __shared__ unsigned char smem_raw[];
+  TcSmem& S = *reinterpret_cast<TcSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
   const TcTile T = tiles[blockIdx.x];
   const int fl = blockIdx.y;  // frame within the batch
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const int4* F = fx + (int64_t)fl * n_list;
-  const unsigned char* Z = zbuf + ((size_t)fl * n_zblk + T.zblk) * (size_t)n_chunks * TC_BLOB;
+  const int n = T.n;
+  const uint32_t zhalf = (uint32_t)nzw * TC_K * 2;
+  const unsigned char* Z = zbuf + ((size_t)fl * n_zblk + T.zblk) * (size_t)n_chunks * 2 * zhalf;
+  const int n_groups = (n_chunks + TC_GROUP - 1) / TC_GROUP;
 
   if (tid == 0) {
-    umma::mbar_init(&S.mbar_tma[0], 1);
-    umma::mbar_init(&S.mbar_tma[1], 1);
-    umma::mbar_init(&S.mbar_mma[0], 1);
-    umma::mbar_init(&S.mbar_mma[1], 1);
+    for (int s = 0; s < TC_SZ; ++s) {
+      umma::mbar_init(&S.full_z[s], 1);
+      umma::mbar_init(&S.empty_z[s], 1);
+    }
+    for (int s = 0; s < TC_SA; ++s) {
+      umma::mbar_init(&S.full_a[s], TC_BUILDERS);
+      umma::mbar_init(&S.empty_a[s], 1);
+    }
+    for (int b = 0; b < 2; ++b) {
+      umma::mbar_init(&S.full_acc[b], 1);
+      umma::mbar_init(&S.empty_acc[b], TC_DRAINERS);
+    }
+    umma::mbar_init(&S.mma_done, 1);
     umma::fence_mbarrier_init();
     S.bad = 0;
+    S.build_stop[0] = S.build_stop[1] = 0;
+    S.z_issued = 0;
+    S.z_landed = 0;
   }
   if (warp == 0) {
-    umma::tmem_alloc(&S.tmem, 2 * TC_NZ);  // two 64-column accumulators
+    umma::tmem_alloc(&S.tmem, TC_TMEM_COLS);
     umma::tmem_relinquish();
   }
   umma::fence_before_sync();
   __syncthreads();
   umma::fence_after_sync();
   const uint32_t tmem = S.tmem;
-  // this thread's accumulator slice: TMEM lanes 32*(warp%4)+lane, columns 32*(warp/4)..+31
-  const uint32_t t_lane = (uint32_t)(32 * (warp & 3)) << 16;
-  const uint32_t t_col = (uint32_t)(32 * (warp >> 2));
-  KCf acc[32];
-#pragma unroll
-  for (int i = 0; i < 32; ++i) acc[i] = KCf{0.f, 0.f};
-  const uint32_t idesc = umma::idesc_f16_f32(TC_M, TC_NZ);
-  constexpr uint32_t LBO = 128, SBO = (TC_K / 8) * 128;
 
-  auto drain = [&](int buf) {
-    umma::fence_after_sync();
-    uint32_t r[32];
-    umma::tmem_ld_32x32b_x32(tmem + t_lane + (uint32_t)(buf * TC_NZ) + t_col, r);
-    umma::tmem_ld_wait();
-#pragma unroll
-    for (int i = 0; i < 32; ++i) {
-      const float v = __uint_as_float(r[i]);
-      const float y = __fsub_rn(v, acc[i].c);
-      const float t = __fadd_rn(acc[i].s, y);
-      acc[i].c = __fsub_rn(__fsub_rn(t, acc[i].s), y);
-      acc[i].s = t;
-    }
-    umma::fence_before_sync();
-  };
-
-  // X (8) and Y (8) phase tables of chunk cc's atoms, into xy[cc & 1]
-  auto build_xy = [&](int cc) {
-    for (int e = tid; e < TC_J * 16; e += TC_THREADS) {
-      const int j = e >> 4, m = e & 15;
-      const int a = cc * TC_J + j;
-      float sn = 0.f, cs = 0.f;
-      if (a < n_list) {
-        const int4 q = F[a];
-        const int32_t ph = m < 8 ? (int32_t)((uint32_t)(T.nx0 + m) * (uint32_t)q.x)
-                                 : (int32_t)((uint32_t)(T.ny0 + m - 8) * (uint32_t)q.y);
-        tc_phase(ph, &sn, &cs);
+  if (warp == TC_PRODUCER_WARP) {
+    // ---- producer: Z(c) into ring stage c % TC_SZ once the MMAs of c - TC_SZ are done
+    if (lane == 0) {
+      int c = 0;
+      for (; c < n_chunks; ++c) {
+        const int s = c % TC_SZ;
+        if (S.bad || !umma::mbar_wait(&S.empty_z[s], ((c / TC_SZ) & 1) ^ 1, TC_WAIT)) {
+          S.bad = 1;
+          break;
+        }
+        const unsigned char* src = Z + (size_t)c * 2 * zhalf;
+        umma::mbar_expect_tx(&S.full_z[s], 2u * n * TC_K * 2);
+        umma::bulk_g2s(S.z[s], src, (uint32_t)n * TC_K * 2, &S.full_z[s]);
+        umma::bulk_g2s(S.z[s] + TC_ZHALF, src + zhalf, (uint32_t)n * TC_K * 2, &S.full_z[s]);
       }
-      S.xy[cc & 1][xy_slot(j, m)] = make_float2(cs, sn);
+      S.z_issued = c;
     }
-  };
-  // prologue: Z operands of chunks 0 and 1 in flight, X/Y of chunk 0
-  if (tid == 0)
-    for (int cc = 0; cc < 2 && cc < n_chunks; ++cc) {
-      umma::mbar_expect_tx(&S.mbar_tma[cc], TC_BLOB);
-      umma::bulk_g2s(S.b[cc], Z + (size_t)cc * TC_BLOB, TC_BLOB, &S.mbar_tma[cc]);
-    }
-  build_xy(0);
-  __syncthreads();
-
-  // Pipeline per chunk c (stage s = c & 1, accumulator s):
-  //   all threads: A(c) into stage s, X/Y of chunk c+1        | MMA(c-1) runs
-  //   thread 0:    wait Z(c); issue MMA(c); wait MMA(c-1);
-  //                bulk-copy Z(c+1) into stage s^1 (now free)
-  //   all threads: drain accumulator s^1 (chunk c-1)           | MMA(c) runs
-  int c = 0;
-  for (; c < n_chunks; ++c) {
-    const int s = c & 1;
-    // A operand: lane = (row % 8) * 4 + (atom % 4), conflict-free 4-byte stores
-#pragma unroll 2
-    for (int it = 0; it < 8; ++it) {
-      const int combo = warp * 8 + it;  // 0..63
-      const int rg = combo >> 3, jg = combo & 7;
-      const int r = rg * 8 + (lane >> 2);   // complex row: nx = r % 8, ny = r / 8
-      const int j = jg * 4 + (lane & 3);
-      const float2 x = S.xy[s][xy_slot(j, r & 7)], y = S.xy[s][xy_slot(j, 8 + (r >> 3))];
-      const float wr = fmaf(x.x, y.x, -x.y * y.y), wi = fmaf(x.x, y.y, x.y * y.x);
-      // hi = fp16(w), lo = fp16(w - hi), both as (re, im) half2 pairs
-      const __half2 hi = __floats2half2_rn(wr, wi);
-      const float2 hb = __half22float2(hi);
-      const __half2 lo = __floats2half2_rn(__fsub_rn(wr, hb.x), __fsub_rn(wi, hb.y));
-      const uint32_t h = *reinterpret_cast<const uint32_t*>(&hi);
-      const uint32_t l = *reinterpret_cast<const uint32_t*>(&lo);
-      const uint32_t o_re = umma::kmajor_offset(r, 2 * j, TC_K);
-      const uint32_t o_im = umma::kmajor_offset(TC_ROWS + r, 2 * j, TC_K);
-      // real rows (Wr, -Wi): flip the sign of the high half; imaginary rows (Wi, Wr): swap halves
-      *reinterpret_cast<uint32_t*>(S.a[s][0] + o_re) = h ^ 0x80000000u;
-      *reinterpret_cast<uint32_t*>(S.a[s][1] + o_re) = l ^ 0x80000000u;
-      *reinterpret_cast<uint32_t*>(S.a[s][0] + o_im) = __byte_perm(h, 0, 0x1032);
-      *reinterpret_cast<uint32_t*>(S.a[s][1] + o_im) = __byte_perm(l, 0, 0x1032);
-    }
-    if (c + 1 < n_chunks) build_xy(c + 1);
-    umma::fence_proxy_async_smem();
-    __syncthreads();
-    if (tid == 0) {
-      if (!umma::mbar_wait(&S.mbar_tma[s], (c >> 1) & 1, TC_WAIT)) {
-        S.bad = 1;
-      } else {
+  } else if (warp == TC_MMA_WARP) {
+    // ---- MMA issuer
+    if (lane == 0) {
+      const uint32_t idesc = umma::idesc_f16_f32(TC_M, n);
+      constexpr uint32_t LBO = 128, SBO = (TC_K / 8) * 128;
+      bool ok = true;
+      for (int c = 0; c < n_chunks; ++c) {
+        const int sz = c % TC_SZ, sa = c % TC_SA, g = c / TC_GROUP, buf = g & 1;
+        if (S.bad || !umma::mbar_wait(&S.full_z[sz], (c / TC_SZ) & 1, TC_WAIT)) {
+          ok = false;
+          break;
+        }
+        S.z_landed = c + 1;
+        if (!umma::mbar_wait(&S.full_a[sa], (c / TC_SA) & 1, TC_WAIT) ||
+            (c % TC_GROUP == 0 && !umma::mbar_wait(&S.empty_acc[buf], ((g >> 1) & 1) ^ 1, TC_WAIT))) {
+          ok = false;
+          break;
+        }
         umma::fence_after_sync();
-        const uint32_t d = tmem + (uint32_t)(((c / TC_GROUP) & 1) * TC_NZ);
-        const uint32_t a_hi = umma::smem_addr(S.a[s][0]), a_lo = umma::smem_addr(S.a[s][1]);
-        const uint32_t b_hi = umma::smem_addr(S.b[s]), b_lo = b_hi + TC_B_BYTES;
+        const uint32_t d = tmem + TC_COL_ACC + (uint32_t)(buf * TC_NMAX);
+        const uint32_t a_hi = umma::smem_addr(S.a[sa][0]), a_lo = umma::smem_addr(S.a[sa][1]);
+        const uint32_t b_hi = umma::smem_addr(S.z[sz]), b_lo = b_hi + TC_ZHALF;
         // small cross terms first, then hi*hi, so the accumulator is still small
         // while the 2^-11-sized terms are added
         const uint32_t pa[3] = {a_hi, a_lo, a_hi}, pb[3] = {b_lo, b_hi, b_hi};
@@ -235,55 +224,159 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
             umma::mma_f16(d, umma::smem_desc(pa[pass] + ks * 256, LBO, SBO),
                           umma::smem_desc(pb[pass] + ks * 256, LBO, SBO), idesc,
                           (c % TC_GROUP == 0 && pass == 0 && ks == 0) ? 0u : 1u);
-        umma::mma_commit(&S.mbar_mma[s]);
+        umma::mma_commit(&S.empty_z[sz]);
+        umma::mma_commit(&S.empty_a[sa]);
+        if (c % TC_GROUP == TC_GROUP - 1 || c == n_chunks - 1) umma::mma_commit(&S.full_acc[buf]);
       }
-      if (!S.bad && c >= 1) {
-        if (!umma::mbar_wait(&S.mbar_mma[s ^ 1], ((c - 1) >> 1) & 1, TC_WAIT)) {
-          S.bad = 1;
-        } else if (c + 1 < n_chunks) {
-          umma::mbar_expect_tx(&S.mbar_tma[s ^ 1], TC_BLOB);
-          umma::bulk_g2s(S.b[s ^ 1], Z + (size_t)(c + 1) * TC_BLOB, TC_BLOB, &S.mbar_tma[s ^ 1]);
+      if (!ok) S.bad = 1;
+      // every MMA this thread issued has finished once mma_done completes
+      umma::mma_commit(&S.mma_done);
+      if (!umma::mbar_wait(&S.mma_done, 0, TC_WAIT)) S.bad = 1;
+    }
+  } else if (warp < 4) {
+    // ---- drain: accumulator of group g -> Kahan sums (s, c) in tensor memory
+    const uint32_t lanes = (uint32_t)(32 * warp) << 16;
+    bool ok = true;
+    for (int g = 0; g < n_groups; ++g) {
+      const int buf = g & 1;
+      if (S.bad || !warp_wait(&S.full_acc[buf], (g >> 1) & 1)) {
+        ok = false;
+        break;
+      }
+      umma::fence_after_sync();
+      for (int cb = 0; cb < n; cb += 16) {
+        uint32_t v[16], s[16], cc[16];
+        umma::tmem_ld_32x32b_x16(tmem + lanes + TC_COL_ACC + (uint32_t)(buf * TC_NMAX + cb), v);
+        if (g > 0) {
+          umma::tmem_ld_32x32b_x16(tmem + lanes + TC_COL_S + (uint32_t)cb, s);
+          umma::tmem_ld_32x32b_x16(tmem + lanes + TC_COL_C + (uint32_t)cb, cc);
         }
+        umma::tmem_ld_wait();
+        if (g == 0) {
+#pragma unroll
+          for (int i = 0; i < 16; ++i) {
+            s[i] = v[i];
+            cc[i] = 0u;
+          }
+        } else {
+#pragma unroll
+          for (int i = 0; i < 16; ++i) {
+            const float sv = __uint_as_float(s[i]), cv = __uint_as_float(cc[i]);
+            const float y = __fsub_rn(__uint_as_float(v[i]), cv);
+            const float t = __fadd_rn(sv, y);
+            cc[i] = __float_as_uint(__fsub_rn(__fsub_rn(t, sv), y));
+            s[i] = __float_as_uint(t);
+          }
+        }
+        umma::tmem_st_32x32b_x16(tmem + lanes + TC_COL_S + (uint32_t)cb, s);
+        umma::tmem_st_32x32b_x16(tmem + lanes + TC_COL_C + (uint32_t)cb, cc);
+      }
+      umma::tmem_st_wait();
+      umma::fence_before_sync();
+      umma::mbar_arrive(&S.empty_acc[buf]);
+    }
+    if (ok && n_groups > 0) {
+      // epilogue: s - c into the D staging area (the Z ring is idle: every copy
+      // was consumed by an MMA that completed before the last group's commit)
+      constexpr int DP = TC_NMAX + 1;
+      float* D = reinterpret_cast<float*>(S.z[0]);
+      const int row = 32 * warp + lane;
+      for (int cb = 0; cb < n; cb += 16) {
+        uint32_t s[16], cc[16];
+        umma::tmem_ld_32x32b_x16(tmem + lanes + TC_COL_S + (uint32_t)cb, s);
+        umma::tmem_ld_32x32b_x16(tmem + lanes + TC_COL_C + (uint32_t)cb, cc);
+        umma::tmem_ld_wait();
+#pragma unroll
+        for (int i = 0; i < 16; ++i)
+          D[row * DP + cb + i] = __fsub_rn(__uint_as_float(s[i]), __uint_as_float(cc[i]));
       }
     }
-    __syncthreads();
-    if (S.bad) break;
-    // a new accumulation group started: drain the previous group's buffer
-    if (c % TC_GROUP == 0 && c >= 1) drain(((c / TC_GROUP) & 1) ^ 1);
+    if (!ok) S.bad = 1;
+  } else {
+    // ---- builders: X/Y tables of chunk c, then A(c) = W products into stage c % TC_SA
+    const int btid = tid - 32 * TC_BUILD_WARP0;
+    const int bw = btid >> 5;
+    const int4* F = fx + (int64_t)fl * n_list;
+    for (int c = 0; c < n_chunks; ++c) {
+      const int sa = c % TC_SA;
+      float2* xy = S.xy[c & 1];
+      for (int e = btid; e < TC_J * 16; e += TC_BUILDERS) {
+        const int j = e >> 4, m = e & 15;
+        const int a = c * TC_J + j;
+        float sn = 0.f, cs = 0.f;
+        if (a < n_list) {
+          const int4 q = F[a];
+          const int32_t ph = m < 8 ? (int32_t)((uint32_t)(T.nx0 + m) * (uint32_t)q.x)
+                                   : (int32_t)((uint32_t)(T.ny0 + m - 8) * (uint32_t)q.y);
+          tc_phase(ph, &sn, &cs);
+        }
+        xy[xy_slot(j, m)] = make_float2(cs, sn);
+      }
+      // builder 0 decides for all builders; the flag alternates with the chunk
+      // parity so a slow reader of chunk c never sees chunk c+1's decision
+      if (btid == 0) {
+        const bool free_stage = !S.bad && umma::mbar_wait(&S.empty_a[sa], ((c / TC_SA) & 1) ^ 1, TC_WAIT);
+        S.build_stop[c & 1] = free_stage ? 0 : 1;
+      }
+      __syncwarp();
+      umma::named_barrier(1, TC_BUILDERS);
+      if (*(volatile int*)&S.build_stop[c & 1]) {
+        if (btid == 0) S.bad = 1;
+        break;
+      }
+      // A operand: lane = (row % 8) * 4 + (atom % 4), conflict-free 4-byte stores
+#pragma unroll 2
+      for (int it = 0; it < 8; ++it) {
+        const int combo = bw * 8 + it;  // 0..63
+        const int rg = combo >> 3, jg = combo & 7;
+        const int r = rg * 8 + (lane >> 2);   // complex row: nx = r % 8, ny = r / 8
+        const int j = jg * 4 + (lane & 3);
+        const float2 x = xy[xy_slot(j, r & 7)], y = xy[xy_slot(j, 8 + (r >> 3))];
+        const float wr = fmaf(x.x, y.x, -x.y * y.y), wi = fmaf(x.x, y.y, x.y * y.x);
+        // hi = fp16(w), lo = fp16(w - hi), both as (re, im) half2 pairs
+        const __half2 hi = __floats2half2_rn(wr, wi);
+        const float2 hb = __half22float2(hi);
+        const __half2 lo = __floats2half2_rn(__fsub_rn(wr, hb.x), __fsub_rn(wi, hb.y));
+        const uint32_t h = *reinterpret_cast<const uint32_t*>(&hi);
+        const uint32_t l = *reinterpret_cast<const uint32_t*>(&lo);
+        const uint32_t o_re = umma::kmajor_offset(r, 2 * j, TC_K);
+        const uint32_t o_im = umma::kmajor_offset(TC_ROWS + r, 2 * j, TC_K);
+        // real rows (Wr, -Wi): flip the sign of the high half; imaginary rows (Wi, Wr): swap halves
+        *reinterpret_cast<uint32_t*>(S.a[sa][0] + o_re) = h ^ 0x80000000u;
+        *reinterpret_cast<uint32_t*>(S.a[sa][1] + o_re) = l ^ 0x80000000u;
+        *reinterpret_cast<uint32_t*>(S.a[sa][0] + o_im) = __byte_perm(h, 0, 0x1032);
+        *reinterpret_cast<uint32_t*>(S.a[sa][1] + o_im) = __byte_perm(l, 0, 0x1032);
+      }
+      umma::fence_proxy_async_smem();
+      umma::mbar_arrive(&S.full_a[sa]);
+    }
   }
+
   __syncthreads();
-  const int last = c - 1;
-  if (!S.bad && last >= 0) {
-    if (tid == 0 && !umma::mbar_wait(&S.mbar_mma[last & 1], (last >> 1) & 1, TC_WAIT)) S.bad = 1;
-    __syncthreads();
-    if (!S.bad) drain((last / TC_GROUP) & 1);
-  }
-  __syncthreads();
-  if (!S.bad) {
-    // stage D through shared memory (reusing the A buffers) to pair Re / Im rows
-    constexpr int DP = TC_NZ + 1;  // padded row: lanes of a warp hit different banks
-    float* D = reinterpret_cast<float*>(S.a[0][0]);  // [128][DP]: 33 KB from the start of the A buffers
-    const int row = 32 * (warp & 3) + lane;
-#pragma unroll
-    for (int i = 0; i < 32; ++i) D[row * DP + t_col + i] = __fsub_rn(acc[i].s, acc[i].c);
-    __syncthreads();
+  if (S.bad) {
+    // copies still in flight land before the block exits
+    if (tid == 32 * TC_PRODUCER_WARP)
+      for (int c = S.z_landed; c < S.z_issued; ++c)
+        umma::mbar_wait(&S.full_z[c % TC_SZ], (c / TC_SZ) & 1, TC_WAIT);
+    if (tid == 0) atomicExch(err, 1);
+  } else if (n_groups > 0) {
+    constexpr int DP = TC_NMAX + 1;
+    const float* D = reinterpret_cast<const float*>(S.z[0]);
     const int32_t* E = entry_k + T.entry0;
     float2* out = rho + (int64_t)(frame0 + fl) * n_k;
-    for (int e = tid; e < TC_ROWS * TC_NZ; e += TC_THREADS) {
+    for (int e = tid; e < TC_ROWS * n; e += TC_THREADS) {
       const int k = E[e];
       if (k >= 0) {
-        const int r = e / TC_NZ, col = e % TC_NZ;
+        const int r = e / n, col = e % n;
         out[k] = make_float2(D[r * DP + col], D[(TC_ROWS + r) * DP + col]);
       }
     }
-  } else if (tid == 0) {
-    atomicExch(err, 1);
   }
   umma::fence_before_sync();
   __syncthreads();
   if (warp == 0) {
     umma::fence_after_sync();
-    umma::tmem_dealloc(tmem, 2 * TC_NZ);
+    umma::tmem_dealloc(tmem, TC_TMEM_COLS);
   }
 }
 
@@ -293,7 +386,8 @@ __global__ void __launch_bounds__(TC_THREADS, 2)
 struct TcPlan {
   DevBuf<TcTile> tiles;
   DevBuf<int32_t> entry_k;
-  int32_t n_tiles = 0, n_zblk = 0;
+  int32_t n_tiles = 0, n_zblk = 0, nzw = 0;
+  int64_t entries = 0;  // rows x columns computed per frame and atom, padding included
 };
 
 static bool tc_half_space(int nx, int ny, int nz) {
@@ -311,31 +405,43 @@ TcPlan* tc_plan_build(const std::vector<int32_t>& kvec) {
     AMDAT_REQUIRE(z >= 0 && tc_half_space(kvec[3 * k], kvec[3 * k + 1], z), "lattice vector outside the half space");
     index[((size_t)x * W + y) * H + z] = k;
   }
+  // nz windows: one window of the smallest multiple of 16 covering 0..nmax, or
+  // windows of TC_NMAX; each tile's width is trimmed to its rows' extent
+  const int nzw = std::min(TC_NMAX, (nmax + 1 + 15) / 16 * 16);
+  const int n_zblk = (nmax + nzw) / nzw;
   std::vector<TcTile> tiles;
   std::vector<int32_t> entries;
-  const int n_zblk = (nmax + TC_NZ) / TC_NZ;
+  int64_t computed = 0;
   for (int x0 = -nmax; x0 <= nmax; x0 += 8)
     for (int y0 = -nmax; y0 <= nmax; y0 += 8)
       for (int zb = 0; zb < n_zblk; ++zb) {
-        std::vector<int32_t> e(TC_ROWS * TC_NZ, -1);
-        bool any = false;
+        int last = -1;
         for (int r = 0; r < TC_ROWS; ++r)
-          for (int c = 0; c < TC_NZ; ++c) {
-            const int nx = x0 + (r & 7), ny = y0 + (r >> 3), nz = zb * TC_NZ + c;
+          for (int c = 0; c < nzw; ++c) {
+            const int nx = x0 + (r & 7), ny = y0 + (r >> 3), nz = zb * nzw + c;
             if (nx > nmax || ny > nmax || nz > nmax) continue;
-            const int k = index[((size_t)(nx + nmax) * W + (ny + nmax)) * H + nz];
-            if (k >= 0) {
-              e[r * TC_NZ + c] = k;
-              any = true;
-            }
+            if (index[((size_t)(nx + nmax) * W + (ny + nmax)) * H + nz] >= 0) last = std::max(last, c);
           }
-        if (!any) continue;
-        tiles.push_back(TcTile{x0, y0, zb, (int32_t)entries.size()});
-        entries.insert(entries.end(), e.begin(), e.end());
+        if (last < 0) continue;
+        const int n = (last + 1 + 15) / 16 * 16;
+        const int32_t e0 = (int32_t)entries.size();
+        for (int r = 0; r < TC_ROWS; ++r)
+          for (int c = 0; c < n; ++c) {
+            const int nx = x0 + (r & 7), ny = y0 + (r >> 3), nz = zb * nzw + c;
+            int k = -1;
+            if (nx <= nmax && ny <= nmax && nz <= nmax)
+              k = index[((size_t)(nx + nmax) * W + (ny + nmax)) * H + nz];
+            entries.push_back(k);
+          }
+        tiles.push_back(TcTile{x0, y0, zb, e0, n, 0, 0, 0});
+        computed += (int64_t)TC_ROWS * n;
       }
+  AMDAT_REQUIRE(entries.size() < (size_t)INT32_MAX, "lattice too large for the tensor-core tiling");
   auto* p = new TcPlan();
   p->n_tiles = (int32_t)tiles.size();
   p->n_zblk = n_zblk;
+  p->nzw = nzw;
+  p->entries = computed;
   p->tiles.reserve(std::max<size_t>(tiles.size(), 1));
   p->entry_k.reserve(std::max<size_t>(entries.size(), 1));
   if (!tiles.empty()) {
@@ -347,12 +453,15 @@ TcPlan* tc_plan_build(const std::vector<int32_t>& kvec) {
 
 void tc_plan_free(TcPlan* p) { delete p; }
 
+int64_t tc_plan_entries(const TcPlan& p) { return p.entries; }
+
 // rho[f][k] for frames 0..n_frames-1 of fx ([n_frames][n_list] fixed-point phases)
 void rhok_tc_run(amdat_ctx* ctx, const TcPlan& P, const int4* fx, int32_t n_list, int32_t n_frames,
                  int32_t n_k, float2* rho) {
   if (P.n_tiles == 0 || n_list == 0 || n_frames == 0) return;
   const int32_t n_chunks = (int32_t)ceil_div(n_list, TC_J);
-  const size_t per_frame = (size_t)P.n_zblk * n_chunks * TC_BLOB;
+  const size_t blob = (size_t)2 * P.nzw * TC_K * 2;
+  const size_t per_frame = (size_t)P.n_zblk * n_chunks * blob;
   // frame batches bound the Z-operand buffer to ~1 GB
   const int32_t batch = (int32_t)std::max<size_t>(1, std::min<size_t>(n_frames, (size_t)(1u << 30) / per_frame));
   unsigned char* zbuf = ctx->scratch.reserve(per_frame * batch + 256);
@@ -363,13 +472,13 @@ void rhok_tc_run(amdat_ctx* ctx, const TcPlan& P, const int4* fx, int32_t n_list
   for (int32_t f0 = 0; f0 < n_frames; f0 += batch) {
     const int32_t nb = std::min(batch, n_frames - f0);
     zgen_kernel<<<(unsigned)(nb * P.n_zblk * n_chunks), 256, 0, ctx->stream>>>(
-        fx + (int64_t)f0 * n_list, n_list, n_chunks, P.n_zblk, zbuf);
+        fx + (int64_t)f0 * n_list, n_list, n_chunks, P.n_zblk, P.nzw, zbuf);
     check_launch("zgen_kernel");
     count_launch(ctx);
     KernelTimer kt(ctx, "rhok_tc_kernel");
     dim3 grid((unsigned)P.n_tiles, (unsigned)nb);
     rhok_tc_kernel<<<grid, TC_THREADS, shm, ctx->stream>>>(fx + (int64_t)f0 * n_list, n_list, n_chunks,
-                                                          P.n_zblk, P.tiles.ptr, P.entry_k.ptr, zbuf,
+                                                          P.n_zblk, P.nzw, P.tiles.ptr, P.entry_k.ptr, zbuf,
                                                           f0, n_k, rho, d_err);
     check_launch("rhok_tc_kernel");
     count_launch(ctx);

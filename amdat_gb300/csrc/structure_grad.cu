@@ -8,7 +8,8 @@
 // Smoothed pair histogram of one list, bin centres r_b = (b + 1/2) r_max / n_bins:
 //     h_b = sum_t sum_{i<j} G(r_b - r_ij),  G(x) = exp(-x^2 / 2 sigma^2) / (sqrt(2 pi) sigma)
 // with r_ij the minimum-image distance (FP32, d - L rint(d / L)) and pairs
-// beyond r_max + 6 sigma skipped.  Adjoint for w_b = dLoss/dh_b:
+// beyond r_max + 6 sigma skipped; each term is rounded to a fixed-point integer
+// (relative step below 1e-9 of the largest term) and summed exactly.  Adjoint for w_b = dLoss/dh_b:
 //     psi(r) = sum_b w_b (r_b - r) / sigma^2 G(r_b - r)
 //     dLoss/dr_i(t) = sum_{j != i} psi(r_ij) (r_i - r_j) / r_ij
 // with the pair loop recomputed (nothing is stored between the passes).  A
@@ -81,19 +82,19 @@ __device__ __forceinline__ void stage_atoms(const SGParams& p, const float* P, i
   }
 }
 
-// forward: unordered pairs j > i.  Contributions go to an FP32 shared histogram
-// (native shared atomics), folded into an FP64 one after every partner tile, so
-// no FP32 bin ever holds more than one tile's worth of terms.
-__global__ void __launch_bounds__(SG_THREADS) gsmooth_kernel(SGParams p) {
-  extern __shared__ double sh_d[];  // [n_bins] FP64, then [n_bins] FP32
-  float* sh_f = (float*)(sh_d + p.n_bins);
+// forward: unordered pairs j > i.  Each Gaussian term is rounded once to a
+// fixed-point integer (scale 2^q chosen by the host so that a block's sum
+// cannot overflow 63 bits) and added with 64-bit shared-memory integer
+// atomics: the block histogram is exact and independent of the order of the
+// additions, so the forward is deterministic and finite differences of it
+// see only the terms that change.
+__global__ void __launch_bounds__(SG_THREADS) gsmooth_kernel(SGParams p, float qscale) {
+  extern __shared__ double sh_d[];  // [n_bins] as unsigned 64-bit fixed point
+  unsigned long long* sh_q = reinterpret_cast<unsigned long long*>(sh_d);
   __shared__ float sx[SG_JT], sy[SG_JT], sz[SG_JT];
   const int f = blockIdx.y;
   const float* P = p.w + (int64_t)p.frames[f] * 3 * p.n_pad;
-  for (int b = threadIdx.x; b < p.n_bins; b += blockDim.x) {
-    sh_d[b] = 0.0;
-    sh_f[b] = 0.f;
-  }
+  for (int b = threadIdx.x; b < p.n_bins; b += blockDim.x) sh_q[b] = 0ull;
   const int i0 = blockIdx.x * SG_THREADS, i = i0 + threadIdx.x;
   const bool live = i < p.lst.n;
   float xi = 0.f, yi = 0.f, zi = 0.f;
@@ -104,38 +105,33 @@ __global__ void __launch_bounds__(SG_THREADS) gsmooth_kernel(SGParams p) {
     zi = P[2 * p.n_pad + a];
   }
   const float inv2s2 = 0.5f / (p.sigma * p.sigma);
-  const float norm = INV_SQRT_2PI / p.sigma;
+  const float qnorm = qscale * INV_SQRT_2PI / p.sigma;
   const float inv_bin = 1.0f / p.bin;
   for (int j0 = i0; j0 < p.lst.n; j0 += SG_JT) {
     const int nj = min(SG_JT, p.lst.n - j0);
     __syncthreads();
     stage_atoms(p, P, j0, nj, sx, sy, sz);
     __syncthreads();
-    if (live) {
-      for (int t = max(0, i + 1 - j0); t < nj; ++t) {
-        const float dx = min_image(sx[t] - xi, p.box.x, p.inv_box.x);
-        const float dy = min_image(sy[t] - yi, p.box.y, p.inv_box.y);
-        const float dz = min_image(sz[t] - zi, p.box.z, p.inv_box.z);
-        const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-        if (r2 >= p.cut2) continue;
-        const float r = sqrtf(r2);
-        const int bc = (int)(r * inv_bin);
-        const int b1 = min(p.n_bins - 1, bc + p.span);
-        for (int b = max(0, bc - p.span); b <= b1; ++b) {
-          const float x = fmaf((float)b + 0.5f, p.bin, -r);
-          atomicAdd(sh_f + b, norm * __expf(-x * x * inv2s2));
-        }
+    if (!live) continue;
+    for (int t = max(0, i + 1 - j0); t < nj; ++t) {
+      const float dx = min_image(sx[t] - xi, p.box.x, p.inv_box.x);
+      const float dy = min_image(sy[t] - yi, p.box.y, p.inv_box.y);
+      const float dz = min_image(sz[t] - zi, p.box.z, p.inv_box.z);
+      const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+      if (r2 >= p.cut2) continue;
+      const float r = sqrtf(r2);
+      const int bc = (int)(r * inv_bin);
+      const int b1 = min(p.n_bins - 1, bc + p.span);
+      for (int b = max(0, bc - p.span); b <= b1; ++b) {
+        const float x = fmaf((float)b + 0.5f, p.bin, -r);
+        atomicAdd(sh_q + b, (unsigned long long)__float2ll_rn(qnorm * __expf(-x * x * inv2s2)));
       }
-    }
-    __syncthreads();
-    for (int b = threadIdx.x; b < p.n_bins; b += blockDim.x) {
-      sh_d[b] += (double)sh_f[b];
-      sh_f[b] = 0.f;
     }
   }
   __syncthreads();
+  const double inv_q = 1.0 / (double)qscale;
   for (int b = threadIdx.x; b < p.n_bins; b += blockDim.x)
-    if (sh_d[b] != 0.0) atomicAdd(p.h + b, sh_d[b]);
+    if (sh_q[b]) atomicAdd(p.h + b, (double)sh_q[b] * inv_q);
 }
 
 // adjoint: thread per atom i, every j != i, single writer per gradient element
@@ -507,11 +503,15 @@ amdat_status amdat_gsmooth_run(amdat_ctx* ctx, int32_t list, const int32_t* fram
     if (e.n > 1) {
       SGParams p = sg_params(ctx, e, d_frames, sigma, r_max, n_bins);
       p.h = d_h;
-      const size_t shm = (size_t)n_bins * 12;
+      // fixed-point scale: a block's bin collects at most SG_THREADS * n terms
+      // of at most 1/(sqrt(2 pi) sigma); keep that below 2^62
+      const double bound = (double)SG_THREADS * (double)e.n * (double)INV_SQRT_2PI / (double)sigma;
+      const float qscale = (float)std::ldexp(1.0, (int)std::floor(std::log2(std::ldexp(1.0, 62) / bound)));
+      const size_t shm = (size_t)n_bins * 8;
       set_smem((const void*)gsmooth_kernel, shm);
       dim3 grid((unsigned)ceil_div(e.n, SG_THREADS), (unsigned)n_frames);
       KernelTimer kt(ctx, "gsmooth_kernel");
-      gsmooth_kernel<<<grid, SG_THREADS, shm, ctx->stream>>>(p);
+      gsmooth_kernel<<<grid, SG_THREADS, shm, ctx->stream>>>(p, qscale);
       check_launch("gsmooth_kernel");
       count_launch(ctx);
     }

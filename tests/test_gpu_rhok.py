@@ -2,6 +2,8 @@
 and S(k) against the FP64 oracle.  Tolerances: |rho_gpu - rho_oracle| <=
 2e-6 * sqrt(N) per element (N unit phasors); coherent F(k,t) and S(k) <= 1e-5
 relative to their values scaled by S(k) (F(k,0) = S(k))."""
+import os
+
 import numpy as np
 import pytest
 
@@ -95,6 +97,31 @@ def test_rhok_lattice_mode(eng):
     h2 = eng.wave_density(0, kv, box, frames)
     rho2 = eng.wave_density_read(h2, 4, nk).astype(np.float64)
     assert np.abs(rho2 - ref).max() / np.sqrt(traj.n_atoms) <= 2e-6
+
+
+@pytest.mark.parametrize("box,kmax,n_atoms,n_frames", [
+    (20.0, 19.0, 300, 2),    # nmax 60: one 64-wide nz window, tiles trimmed to 16..64 columns
+    (25.0, 35.5, 40, 1),     # nmax 141: two 128-wide nz windows
+    (8.0, 3.0, 33, 3),       # nmax 3: 16-column tiles, a one-atom last chunk
+])
+def test_rhok_lattice_tilings(eng, box, kmax, n_atoms, n_frames):
+    """Lattice densities whose tilings exercise every tensor-core tile shape,
+    against the FP64 oracle.  These cases hold up to 1e6 elements, so the bound
+    is on the rms error (<= 1e-6 sqrt(N)) and on the largest one (<= 3e-6 sqrt(N)):
+    the rounding of the tensor core's FP32 accumulation over 64 atoms gives
+    independent errors whose extreme over many elements passes 2e-6 sqrt(N)."""
+    scheme = synth.TimeScheme.linear(n_frames + 1, 1.0)
+    traj = synth.random_walk(n_atoms, box, scheme, 0.1, seed=17, time_scaled=False)
+    eng.upload(traj.unwrapped, traj.box)
+    frames = np.arange(n_frames, dtype=np.int32)
+    h, nk, ns = eng.wave_density_lattice(0, kmax, 0.1, box, frames)
+    kv, off = eng.wave_density_vectors(h, nk, ns)
+    rho = eng.wave_density_read(h, n_frames, nk).astype(np.float64)
+    eng.wave_density_free(h)
+    ref = orc.rhok_parallel(traj.wrapped(), frames, kv, box, os.cpu_count() or 1)
+    d = (rho - ref) / np.sqrt(n_atoms)
+    rms, worst = float(np.sqrt((d ** 2).mean())), float(np.abs(d).max())
+    assert rms <= 1e-6 and worst <= 3e-6, (rms, worst)
 
 
 def test_rhok_plain_fp64(eng, qvectors):
