@@ -288,6 +288,34 @@ __global__ void disp_finalize_kernel(const double* __restrict__ part, int32_t n_
   (void)k_begin;
 }
 
+// Sums each list's membership classes into the list's outputs (one block per
+// (list, gap); classes in ascending order, FP64; G_s counts as integers).
+__global__ void disp_combine_kernel(int32_t G, int32_t S, int32_t NB, const int32_t* __restrict__ lu_off,
+                                    const int32_t* __restrict__ lu_units, const double* __restrict__ ud2,
+                                    const double* __restrict__ ud4, const double* __restrict__ ufs,
+                                    const unsigned long long* __restrict__ ugs, double* __restrict__ d2,
+                                    double* __restrict__ d4, double* __restrict__ fs,
+                                    unsigned long long* __restrict__ gs) {
+  const int lg = blockIdx.x, l = lg / G, g = lg % G;
+  const int u0 = lu_off[l], u1 = lu_off[l + 1];
+  const int S1 = S > 0 ? S : 1;
+  for (int k = threadIdx.x; k < 2 + S; k += blockDim.x) {
+    double acc = 0.0;
+    for (int i = u0; i < u1; ++i) {
+      const int64_t ug = (int64_t)lu_units[i] * G + g;
+      acc += k == 0 ? ud2[ug] : (k == 1 ? ud4[ug] : ufs[ug * S1 + (k - 2)]);
+    }
+    if (k == 0) d2[lg] = acc;
+    else if (k == 1) d4[lg] = acc;
+    else fs[(int64_t)lg * S1 + (k - 2)] = acc;
+  }
+  for (int b = threadIdx.x; b < NB; b += blockDim.x) {
+    unsigned long long c = 0ull;
+    for (int i = u0; i < u1; ++i) c += ugs[((int64_t)lu_units[i] * G + g) * NB + b];
+    gs[(int64_t)lg * NB + b] = c;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // plain FP64 path: one thread per (pair, atom), FP64 arithmetic, direct cos,
 // block reduction then one FP64 atomic per block and output
@@ -538,14 +566,22 @@ struct amdat_disp_plan {
   float bin_max = 0.f, period = 1.f;
   amdat::ShellSet sh;
   std::vector<int32_t> lsize;
-  std::vector<amdat::ListDev> ldev;
   std::vector<int64_t> pairs;  // atom_pairs [list][gap]
+  // work units: the lists themselves, or membership classes shared by lists
+  bool classes = false;
+  int n_units = 0;
+  std::vector<int32_t> usize;
+  std::vector<amdat::ListDev> udev;
+  std::vector<int32_t> lu_off, lu_units;  // list -> its units (CSR, ascending)
+  amdat::DevBuf<int32_t> class_idx;       // atoms of gathered classes
   int chunk = 0, blocks_per_sm = 0, n_items = 0;
   double tuned_ms = 0.0;
-  // device: [items | item_first | schedule | lists | counters | kv | off | inv | part | d2 | d4 | fs | gs]
+  // device: [items | item_first | schedule | units | counters | kv | off | inv | lu_off | lu_units |
+  //          part | unit d2 | d4 | fs | gs | list d2 | d4 | fs | gs]
   amdat::DevBuf<unsigned char> dev;
   size_t o_items = 0, o_first = 0, o_sched = 0, o_lists = 0, o_counter = 0, o_kv = 0, o_off = 0,
-         o_inv = 0, o_part = 0, o_d2 = 0, o_d4 = 0, o_fs = 0, o_gs = 0, bytes = 0;
+         o_inv = 0, o_luo = 0, o_luu = 0, o_part = 0, o_ud2 = 0, o_ud4 = 0, o_ufs = 0, o_ugs = 0,
+         o_d2 = 0, o_d4 = 0, o_fs = 0, o_gs = 0, bytes = 0;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   ~amdat_disp_plan() {
@@ -559,26 +595,26 @@ namespace amdat {
 static void plan_tables(amdat_ctx* ctx, amdat_disp_plan& pl, const PairTable& P, int chunk,
                         int blocks_per_sm) {
   const int G = pl.G;
-  const size_t n_lg = (size_t)pl.n_lists * G;
+  const size_t n_ug = (size_t)pl.n_units * G, n_lg = (size_t)pl.n_lists * G;
   std::vector<DispItem> items;
-  std::vector<int32_t> item_first(n_lg + 1, 0);
-  std::vector<int64_t> key;  // schedule key per item: (list, chunk, pair)
-  for (int l = 0; l < pl.n_lists; ++l) {
-    const int nch = (int)std::max<int64_t>(1, ceil_div(pl.lsize[l], chunk));
+  std::vector<int32_t> item_first(n_ug + 1, 0);
+  std::vector<int64_t> key;  // schedule key per item: (unit, chunk, pair)
+  for (int u = 0; u < pl.n_units; ++u) {
+    const int nch = (int)std::max<int64_t>(1, ceil_div(pl.usize[u], chunk));
     for (int g = 0; g < G; ++g) {
-      item_first[(size_t)l * G + g] = (int32_t)items.size();
-      if (pl.lsize[l] == 0) continue;
+      item_first[(size_t)u * G + g] = (int32_t)items.size();
+      if (pl.usize[u] == 0) continue;
       for (int pr = P.gap_first[g]; pr < P.gap_first[g + 1]; ++pr)
         for (int c = 0; c < nch; ++c) {
-          const int a0 = (int)((int64_t)pl.lsize[l] * c / nch);
-          const int a1 = (int)((int64_t)pl.lsize[l] * (c + 1) / nch);
-          items.push_back(DispItem{l, pr, a0, a1});
-          key.push_back(((int64_t)l << 40) | ((int64_t)c << 20) | (int64_t)pr);
+          const int a0 = (int)((int64_t)pl.usize[u] * c / nch);
+          const int a1 = (int)((int64_t)pl.usize[u] * (c + 1) / nch);
+          items.push_back(DispItem{u, pr, a0, a1});
+          key.push_back(((int64_t)u << 40) | ((int64_t)c << 20) | (int64_t)pr);
         }
     }
   }
-  item_first[n_lg] = (int32_t)items.size();
-  // process all pairs of one (list, atom chunk) together: the chunk's frames
+  item_first[n_ug] = (int32_t)items.size();
+  // process all pairs of one (unit, atom chunk) together: the chunk's frames
   // are read from HBM once and reused from L2 by the other pairs
   std::vector<int32_t> sched(items.size());
   for (size_t i = 0; i < sched.size(); ++i) sched[i] = (int32_t)i;
@@ -587,44 +623,62 @@ static void plan_tables(amdat_ctx* ctx, amdat_disp_plan& pl, const PairTable& P,
   pl.chunk = chunk;
   pl.blocks_per_sm = blocks_per_sm;
   auto align = [](size_t x) { return (x + 255) & ~(size_t)255; };
+  const size_t S1 = (size_t)std::max(pl.S, 1), NB1 = (size_t)std::max(pl.NB, 1);
   size_t o = 0;
   pl.o_items = o; o = align(o + std::max<size_t>(items.size(), 1) * sizeof(DispItem));
   pl.o_first = o; o = align(o + item_first.size() * 4);
   pl.o_sched = o; o = align(o + std::max<size_t>(sched.size(), 1) * 4);
-  pl.o_lists = o; o = align(o + pl.ldev.size() * sizeof(ListDev));
+  pl.o_lists = o; o = align(o + pl.udev.size() * sizeof(ListDev));
   pl.o_counter = o; o = align(o + 4 * (size_t)pl.n_passes);
   pl.o_kv = o; o = align(o + std::max<size_t>(pl.sh.kv.size(), 1) * sizeof(int4));
   pl.o_off = o; o = align(o + std::max<size_t>(pl.sh.off.size(), 1) * 4);
   pl.o_inv = o; o = align(o + std::max<size_t>(pl.sh.inv_count.size(), 1) * 4);
+  pl.o_luo = o; o = align(o + std::max<size_t>(pl.lu_off.size(), 1) * 4);
+  pl.o_luu = o; o = align(o + std::max<size_t>(pl.lu_units.size(), 1) * 4);
   pl.o_part = o; o = align(o + (size_t)std::max(pl.n_items, 1) * pl.n_out * 8);
-  pl.o_d2 = o; o = align(o + n_lg * 8);
-  pl.o_d4 = o; o = align(o + n_lg * 8);
-  pl.o_fs = o; o = align(o + n_lg * std::max(pl.S, 1) * 8);
-  pl.o_gs = o; o = align(o + n_lg * std::max(pl.NB, 1) * 8);
+  pl.o_ud2 = o; o = align(o + n_ug * 8);
+  pl.o_ud4 = o; o = align(o + n_ug * 8);
+  pl.o_ufs = o; o = align(o + n_ug * S1 * 8);
+  pl.o_ugs = o; o = align(o + n_ug * NB1 * 8);
+  if (pl.classes) {
+    pl.o_d2 = o; o = align(o + n_lg * 8);
+    pl.o_d4 = o; o = align(o + n_lg * 8);
+    pl.o_fs = o; o = align(o + n_lg * S1 * 8);
+    pl.o_gs = o; o = align(o + n_lg * NB1 * 8);
+  } else {
+    pl.o_d2 = pl.o_ud2;
+    pl.o_d4 = pl.o_ud4;
+    pl.o_fs = pl.o_ufs;
+    pl.o_gs = pl.o_ugs;
+  }
   pl.bytes = o;
   unsigned char* base = pl.dev.reserve(o);
   std::vector<unsigned char> host(pl.o_part, 0);
   std::memcpy(host.data() + pl.o_items, items.data(), items.size() * sizeof(DispItem));
   std::memcpy(host.data() + pl.o_first, item_first.data(), item_first.size() * 4);
   std::memcpy(host.data() + pl.o_sched, sched.data(), sched.size() * 4);
-  std::memcpy(host.data() + pl.o_lists, pl.ldev.data(), pl.ldev.size() * sizeof(ListDev));
+  std::memcpy(host.data() + pl.o_lists, pl.udev.data(), pl.udev.size() * sizeof(ListDev));
   if (pl.S) {
     std::memcpy(host.data() + pl.o_kv, pl.sh.kv.data(), pl.sh.kv.size() * sizeof(int4));
     std::memcpy(host.data() + pl.o_off, pl.sh.off.data(), pl.sh.off.size() * 4);
     std::memcpy(host.data() + pl.o_inv, pl.sh.inv_count.data(), pl.sh.inv_count.size() * 4);
   }
+  if (pl.classes) {
+    std::memcpy(host.data() + pl.o_luo, pl.lu_off.data(), pl.lu_off.size() * 4);
+    std::memcpy(host.data() + pl.o_luu, pl.lu_units.data(), pl.lu_units.size() * 4);
+  }
   AMDAT_CUDA(cudaMemcpyAsync(base, host.data(), pl.o_part, cudaMemcpyHostToDevice, ctx->stream));
-  AMDAT_CUDA(cudaMemsetAsync(base + pl.o_d2, 0, pl.o_gs - pl.o_d2, ctx->stream));
+  AMDAT_CUDA(cudaMemsetAsync(base + pl.o_ud2, 0, o - pl.o_ud2, ctx->stream));
   AMDAT_CUDA(cudaStreamSynchronize(ctx->stream));
 }
 
 // every device operation of one run, in stream order (capturable)
 static void plan_launch(amdat_ctx* ctx, amdat_disp_plan& pl, const PairTable& P) {
   unsigned char* base = pl.dev.ptr;
-  const size_t n_lg = (size_t)pl.n_lists * pl.G;
-  if (pl.NB) AMDAT_CUDA(cudaMemsetAsync(base + pl.o_gs, 0, n_lg * pl.NB * 8, ctx->stream));
+  const size_t n_ug = (size_t)pl.n_units * pl.G, n_lg = (size_t)pl.n_lists * pl.G;
+  if (pl.NB) AMDAT_CUDA(cudaMemsetAsync(base + pl.o_ugs, 0, n_ug * pl.NB * 8, ctx->stream));
   if (pl.n_items == 0) {
-    AMDAT_CUDA(cudaMemsetAsync(base + pl.o_d2, 0, pl.o_gs - pl.o_d2, ctx->stream));
+    AMDAT_CUDA(cudaMemsetAsync(base + pl.o_ud2, 0, pl.bytes - pl.o_ud2, ctx->stream));
     return;
   }
   AMDAT_CUDA(cudaMemsetAsync(base + pl.o_counter, 0, 4 * (size_t)pl.n_passes, ctx->stream));
@@ -645,7 +699,7 @@ static void plan_launch(amdat_ctx* ctx, amdat_disp_plan& pl, const PairTable& P)
     p.part = (double*)(base + pl.o_part);
     p.n_out = pl.n_out;
     p.want_moments = pass == 0;
-    p.gs = (unsigned long long*)(base + pl.o_gs);
+    p.gs = (unsigned long long*)(base + pl.o_ugs);
     p.n_gaps = pl.G;
     p.n_bins = pass == 0 ? pl.NB : 0;
     p.bin_size = pl.NB ? pl.bin_max / (float)pl.NB : 1.0f;
@@ -684,11 +738,20 @@ static void plan_launch(amdat_ctx* ctx, amdat_disp_plan& pl, const PairTable& P)
     if (mode == 0) { if (gs) launch(disp_mixed_kernel<0, true>); else launch(disp_mixed_kernel<0, false>); }
     else if (mode == 1) { if (gs) launch(disp_mixed_kernel<1, true>); else launch(disp_mixed_kernel<1, false>); }
     else { if (gs) launch(disp_mixed_kernel<2, true>); else launch(disp_mixed_kernel<2, false>); }
-    disp_finalize_kernel<<<(unsigned)n_lg, 256, 0, ctx->stream>>>(
+    disp_finalize_kernel<<<(unsigned)n_ug, 256, 0, ctx->stream>>>(
         p.part, pl.n_out, (const int32_t*)(base + pl.o_first), 0,
-        pass == 0 ? (double*)(base + pl.o_d2) : nullptr, pass == 0 ? (double*)(base + pl.o_d4) : nullptr,
-        pl.S ? (double*)(base + pl.o_fs) : nullptr, std::max(pl.S, 1), s0, nfs, pass == 0 ? 1 : 0);
+        pass == 0 ? (double*)(base + pl.o_ud2) : nullptr, pass == 0 ? (double*)(base + pl.o_ud4) : nullptr,
+        pl.S ? (double*)(base + pl.o_ufs) : nullptr, std::max(pl.S, 1), s0, nfs, pass == 0 ? 1 : 0);
     check_launch("disp_finalize_kernel");
+    count_launch(ctx);
+  }
+  if (pl.classes) {
+    disp_combine_kernel<<<(unsigned)n_lg, 128, 0, ctx->stream>>>(
+        pl.G, pl.S, pl.NB, (const int32_t*)(base + pl.o_luo), (const int32_t*)(base + pl.o_luu),
+        (const double*)(base + pl.o_ud2), (const double*)(base + pl.o_ud4), (const double*)(base + pl.o_ufs),
+        (const unsigned long long*)(base + pl.o_ugs), (double*)(base + pl.o_d2), (double*)(base + pl.o_d4),
+        (double*)(base + pl.o_fs), (unsigned long long*)(base + pl.o_gs));
+    check_launch("disp_combine_kernel");
     count_launch(ctx);
   }
 }
@@ -726,6 +789,85 @@ static void tune_store(const std::string& key, int ch, int bps, double ms) {
   }
 }
 
+// Membership classes of a plan's lists: atoms that belong to exactly the same
+// lists form one class.  Adopted when the classes stream at most 4/5 of the
+// lists' atoms and there are at most four classes per list; otherwise the
+// lists stay the work units.
+static void plan_classes(amdat_ctx* ctx, amdat_disp_plan& pl, const int32_t* lists) {
+  const int L = pl.n_lists;
+  const int words = (L + 63) / 64;
+  const int64_t N = ctx->n_atoms;
+  int64_t list_atoms = 0;
+  for (int l = 0; l < L; ++l) list_atoms += pl.lsize[l];
+  if (list_atoms == 0) return;
+  std::vector<uint64_t> mask((size_t)N * words, 0ull);
+  std::vector<int32_t> buf;
+  for (int l = 0; l < L; ++l) {
+    const ListEntry& e = list_entry(ctx, lists[l]);
+    if (e.n == 0) continue;
+    const int32_t* a = nullptr;
+    if (!e.contiguous) {
+      buf.resize(e.n);
+      AMDAT_CUDA(cudaMemcpy(buf.data(), e.idx.ptr, (size_t)e.n * 4, cudaMemcpyDeviceToHost));
+      a = buf.data();
+    }
+    for (int i = 0; i < e.n; ++i) {
+      const int64_t atom = a ? a[i] : (int64_t)e.first + i;
+      mask[(size_t)atom * words + l / 64] |= 1ull << (l % 64);
+    }
+  }
+  std::vector<int32_t> members;
+  for (int64_t a = 0; a < N; ++a)
+    for (int w = 0; w < words; ++w)
+      if (mask[(size_t)a * words + w]) {
+        members.push_back((int32_t)a);
+        break;
+      }
+  auto less = [&](int32_t x, int32_t y) {
+    for (int w = words - 1; w >= 0; --w) {
+      const uint64_t mx = mask[(size_t)x * words + w], my = mask[(size_t)y * words + w];
+      if (mx != my) return mx < my;
+    }
+    return x < y;
+  };
+  std::sort(members.begin(), members.end(), less);
+  auto same = [&](int32_t x, int32_t y) {
+    for (int w = 0; w < words; ++w)
+      if (mask[(size_t)x * words + w] != mask[(size_t)y * words + w]) return false;
+    return true;
+  };
+  std::vector<int32_t> start;
+  for (size_t i = 0; i < members.size(); ++i)
+    if (i == 0 || !same(members[i - 1], members[i])) start.push_back((int32_t)i);
+  const int n_cls = (int)start.size();
+  start.push_back((int32_t)members.size());
+  if ((int64_t)members.size() * 5 > list_atoms * 4 || n_cls > 4 * L) return;
+  // adopt: class atoms ascending (members are sorted by mask, then atom)
+  pl.classes = true;
+  pl.n_units = n_cls;
+  pl.usize.assign(n_cls, 0);
+  pl.udev.assign(n_cls, ListDev{0, 0, nullptr});
+  pl.class_idx.reserve(std::max<size_t>(members.size(), 1));
+  AMDAT_CUDA(cudaMemcpy(pl.class_idx.ptr, members.data(), members.size() * 4, cudaMemcpyHostToDevice));
+  std::vector<std::vector<int32_t>> per_list(L);
+  for (int c = 0; c < n_cls; ++c) {
+    const int32_t b = start[c], e = start[c + 1];
+    pl.usize[c] = e - b;
+    const bool contiguous = members[e - 1] - members[b] == e - 1 - b;
+    pl.udev[c] = contiguous ? ListDev{e - b, members[b], nullptr} : ListDev{e - b, 0, pl.class_idx.ptr + b};
+    const int32_t rep = members[b];
+    for (int l = 0; l < L; ++l)
+      if (mask[(size_t)rep * words + l / 64] >> (l % 64) & 1ull) per_list[l].push_back(c);
+  }
+  pl.lu_off.assign(L + 1, 0);
+  pl.lu_units.clear();
+  for (int l = 0; l < L; ++l) {
+    pl.lu_off[l] = (int32_t)pl.lu_units.size();
+    pl.lu_units.insert(pl.lu_units.end(), per_list[l].begin(), per_list[l].end());
+  }
+  pl.lu_off[L] = (int32_t)pl.lu_units.size();
+}
+
 static amdat_disp_plan* plan_create(amdat_ctx* ctx, const amdat_disp_request* req,
                                     const int32_t* lists, int32_t n_lists, int32_t flags) {
   check_request(ctx, req);
@@ -750,10 +892,15 @@ static amdat_disp_plan* plan_create(amdat_ctx* ctx, const amdat_disp_request* re
     int64_t total_atoms = 0;
     for (int l = 0; l < n_lists; ++l) {
       const ListEntry& e = list_entry(ctx, lists[l]);
-      pl->ldev.push_back(ListDev{e.n, e.first, e.contiguous ? nullptr : e.idx.ptr});
+      pl->udev.push_back(ListDev{e.n, e.first, e.contiguous ? nullptr : e.idx.ptr});
       pl->lsize.push_back(e.n);
+      pl->usize.push_back(e.n);
       total_atoms += e.n;
     }
+    pl->n_units = n_lists;
+    if (n_lists > 1 && !(flags & AMDAT_PLAN_NO_SHARING)) plan_classes(ctx, *pl, lists);
+    int64_t unit_atoms = 0;
+    for (int u = 0; u < pl->n_units; ++u) unit_atoms += pl->usize[u];
     pl->pairs.assign((size_t)n_lists * pl->G, 0);
     for (int l = 0; l < n_lists; ++l)
       for (int g = 0; g < pl->G; ++g)
@@ -762,14 +909,14 @@ static amdat_disp_plan* plan_create(amdat_ctx* ctx, const amdat_disp_request* re
     // chunks to keep every SM busy
     const int64_t want_items = (int64_t)ctx->n_sm * 16;
     int64_t chunk = DISP_CHUNK;
-    if (P.n_pairs > 0 && total_atoms > 0)
+    if (P.n_pairs > 0 && unit_atoms > 0)
       chunk = std::max<int64_t>(pl->S ? 128 : 1024,
-                                std::min<int64_t>(DISP_CHUNK, ceil_div(total_atoms * P.n_pairs, want_items)));
+                                std::min<int64_t>(DISP_CHUNK, ceil_div(unit_atoms * P.n_pairs, want_items)));
     int bps = pl->S ? 4 : 8;
     char keybuf[256];
-    std::snprintf(keybuf, sizeof(keybuf), "sm%d_mode%d_S%d_NB%d_L%d_atoms%lld_pairs%lld", ctx->n_sm,
-                  pl->S ? pl->sh.mode : 0, pl->S, pl->NB, n_lists, (long long)total_atoms,
-                  (long long)P.n_pairs);
+    std::snprintf(keybuf, sizeof(keybuf), "sm%d_mode%d_S%d_NB%d_L%d_U%d_atoms%lld_unit%lld_pairs%lld",
+                  ctx->n_sm, pl->S ? pl->sh.mode : 0, pl->S, pl->NB, n_lists, pl->n_units,
+                  (long long)total_atoms, (long long)unit_atoms, (long long)P.n_pairs);
     const std::string key(keybuf);
     auto hit = tune_cache().find(key);
     if (hit != tune_cache().end()) {
@@ -947,6 +1094,19 @@ amdat_status amdat_disp_plan_info(amdat_disp_plan* plan, int32_t* chunk, int32_t
     if (blocks_per_sm) *blocks_per_sm = plan->blocks_per_sm;
     if (n_items) *n_items = plan->n_items;
     if (tuned_ms) *tuned_ms = plan->tuned_ms;
+  });
+}
+
+amdat_status amdat_disp_plan_sharing(amdat_disp_plan* plan, int32_t* n_units, int64_t* unit_atoms,
+                                     int64_t* list_atoms) {
+  return guarded([&] {
+    AMDAT_REQUIRE(plan != nullptr, "null plan");
+    int64_t ua = 0, la = 0;
+    for (int32_t v : plan->usize) ua += v;
+    for (int32_t v : plan->lsize) la += v;
+    if (n_units) *n_units = plan->n_units;
+    if (unit_atoms) *unit_atoms = ua;
+    if (list_atoms) *list_atoms = la;
   });
 }
 

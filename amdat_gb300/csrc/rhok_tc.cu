@@ -51,12 +51,14 @@ constexpr int TC_SA = 2;                      // A ring stages
 constexpr int TC_PRODUCER_WARP = 4;
 constexpr int TC_MMA_WARP = 5;
 constexpr int TC_BUILD_WARP0 = 6;
-constexpr int TC_BUILDERS = 256;              // 8 builder warps
+constexpr int TC_BUILDERS = 512;              // 16 builder warps
 constexpr int TC_DRAINERS = 128;              // warps 0-3, one per TMEM lane quadrant
-constexpr int TC_THREADS = 32 * TC_BUILD_WARP0 + TC_BUILDERS;  // 448
+constexpr int TC_THREADS = 32 * TC_BUILD_WARP0 + TC_BUILDERS;  // 704
 constexpr uint32_t TC_A_BYTES = TC_M * TC_K * 2;      // 16 KB (one of hi / lo)
 constexpr uint32_t TC_ZHALF = TC_NMAX * TC_K * 2;     // 16 KB (one of hi / lo, widest window)
-constexpr uint32_t TC_WAIT = 1u << 22;                // mbarrier polls (~0.5 s bound)
+constexpr uint32_t TC_XYB = TC_J * 8 * sizeof(float2);  // 2 KB: 8 phases of 32 atoms (X or Y)
+constexpr uint32_t TC_STAGE = 2 * TC_ZHALF + 2 * TC_XYB;  // Z hi, Z lo, X, Y
+constexpr uint32_t TC_WAIT = 1u << 19;                // try_wait calls of <= 1 us (~0.5 s bound)
 // tensor-memory columns: two accumulators, then the Kahan sums and compensations
 constexpr uint32_t TC_COL_ACC = 0, TC_COL_S = 2 * TC_NMAX, TC_COL_C = 3 * TC_NMAX;
 constexpr uint32_t TC_TMEM_COLS = 4 * TC_NMAX;        // 512
@@ -67,16 +69,14 @@ struct TcTile {
 };
 
 struct TcSmem {
-  unsigned char z[TC_SZ][2 * TC_ZHALF];  // [stage] hi then lo; the epilogue stages D here
+  unsigned char z[TC_SZ][TC_STAGE];     // [stage] Z hi, Z lo, X, Y; the epilogue stages D here
   unsigned char a[TC_SA][2][TC_A_BYTES]; // [stage][hi|lo]
-  float2 xy[2][TC_J * 16];               // [chunk parity][atom*16 + swizzled(8 X then 8 Y)]
   uint64_t full_z[TC_SZ], empty_z[TC_SZ];
   uint64_t full_a[TC_SA], empty_a[TC_SA];
   uint64_t full_acc[2], empty_acc[2];
   uint64_t mma_done;
   uint32_t tmem;
   volatile int bad;        // any role gave up
-  int build_stop[2];       // chunk parity: written by builder 0 before a builder barrier
   int z_issued, z_landed;  // bulk copies issued / seen complete
 };
 static_assert(sizeof(float) * TC_M * (TC_NMAX + 1) <= sizeof(((TcSmem*)0)->z), "D staging must fit the Z ring");
@@ -120,22 +120,50 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// X/Y table slot of (atom j, entry m): rotating the 16 entries by 4*(j%4)
-// spreads a warp's reads (8 rows x 4 atoms) over all banks
-__device__ __forceinline__ int xy_slot(int j, int m) { return j * 16 + ((m + 4 * (j & 3)) & 15); }
+// X/Y table slot of (atom j, entry m) inside a 32-atom block: rotating each
+// atom's 8 entries by 2*(j%4) makes a warp's reads (8 entries x 4 atoms,
+// 8-byte words) free of bank conflicts
+__device__ __forceinline__ int xy_slot(int j, int m) { return j * 8 + ((m + 2 * (j & 3)) & 7); }
 
-// warp-uniform bounded wait: lane 0 polls, the warp shares the outcome
-__device__ __forceinline__ bool warp_wait(uint64_t* mbar, uint32_t parity) {
+// X and Y phase tables of one frame batch: for axis a (0 = x, 1 = y), block b
+// of 8 lattice indices (n = -nmax + 8 b + m) and chunk c of 32 atoms, a 2 KB
+// block at ((f * 2 + a) * n_blk + b) * n_chunks + c holding exp(i 2 pi n q_a)
+__global__ void __launch_bounds__(256)
+    xygen_kernel(const int4* __restrict__ fx, int32_t n_list, int32_t n_chunks, int32_t n_blk,
+                 int32_t nmax, float2* __restrict__ xybuf) {
+  const int blk = blockIdx.x;  // ((f * 2 + axis) * n_blk + b) * n_chunks + c
+  const int c = blk % n_chunks;
+  const int b = (blk / n_chunks) % n_blk;
+  const int axis = (blk / (n_chunks * n_blk)) & 1;
+  const int f = blk / (n_chunks * n_blk * 2);
+  float2* out = xybuf + (size_t)blk * (TC_J * 8);
+  const int4* F = fx + (int64_t)f * n_list;
+  for (int e = threadIdx.x; e < TC_J * 8; e += blockDim.x) {
+    const int j = e >> 3, m = e & 7;
+    const int a = c * TC_J + j;
+    float sn = 0.f, cs = 0.f;
+    if (a < n_list) {
+      const int32_t q = axis ? F[a].y : F[a].x;
+      const int32_t n = -nmax + 8 * b + m;
+      tc_phase((int32_t)((uint32_t)n * (uint32_t)q), &sn, &cs);
+    }
+    out[xy_slot(j, m)] = make_float2(cs, sn);
+  }
+}
+
+// warp-uniform bounded wait: lane 0 reads the block's error flag and polls,
+// the warp shares the outcome (false: give up)
+__device__ __forceinline__ bool warp_wait(uint64_t* mbar, uint32_t parity, volatile int* bad) {
   bool ok = true;
-  if ((threadIdx.x & 31) == 0) ok = umma::mbar_wait(mbar, parity, TC_WAIT);
+  if ((threadIdx.x & 31) == 0) ok = !*bad && umma::mbar_wait(mbar, parity, TC_WAIT);
   return __shfl_sync(0xffffffffu, ok ? 1 : 0, 0) != 0;
 }
 
 __global__ void __launch_bounds__(TC_THREADS, 1)
-    rhok_tc_kernel(const int4* __restrict__ fx, int32_t n_list, int32_t n_chunks, int32_t n_zblk,
-                   int32_t nzw, const TcTile* __restrict__ tiles, const int32_t* __restrict__ entry_k,
-                   const unsigned char* __restrict__ zbuf, int32_t frame0, int32_t n_k,
-                   float2* __restrict__ rho, int* __restrict__ err) {
+    rhok_tc_kernel(int32_t n_list, int32_t n_chunks, int32_t n_zblk, int32_t nzw, int32_t n_blk,
+                   int32_t nmax, const TcTile* __restrict__ tiles, const int32_t* __restrict__ entry_k,
+                   const unsigned char* __restrict__ zbuf, const float2* __restrict__ xybuf,
+                   int32_t frame0, int32_t n_k, float2* __restrict__ rho, int* __restrict__ err) {
   extern __shared__ unsigned char smem_raw[];
   TcSmem& S = *reinterpret_cast<TcSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
   const TcTile T = tiles[blockIdx.x];
@@ -144,6 +172,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const int n = T.n;
   const uint32_t zhalf = (uint32_t)nzw * TC_K * 2;
   const unsigned char* Z = zbuf + ((size_t)fl * n_zblk + T.zblk) * (size_t)n_chunks * 2 * zhalf;
+  const float2* XT = xybuf + (((size_t)fl * 2 + 0) * n_blk + (T.nx0 + nmax) / 8) * (size_t)n_chunks * (TC_J * 8);
+  const float2* YT = xybuf + (((size_t)fl * 2 + 1) * n_blk + (T.ny0 + nmax) / 8) * (size_t)n_chunks * (TC_J * 8);
   const int n_groups = (n_chunks + TC_GROUP - 1) / TC_GROUP;
 
   if (tid == 0) {
@@ -162,7 +192,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     umma::mbar_init(&S.mma_done, 1);
     umma::fence_mbarrier_init();
     S.bad = 0;
-    S.build_stop[0] = S.build_stop[1] = 0;
     S.z_issued = 0;
     S.z_landed = 0;
   }
@@ -186,9 +215,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           break;
         }
         const unsigned char* src = Z + (size_t)c * 2 * zhalf;
-        umma::mbar_expect_tx(&S.full_z[s], 2u * n * TC_K * 2);
+        umma::mbar_expect_tx(&S.full_z[s], 2u * n * TC_K * 2 + 2 * TC_XYB);
         umma::bulk_g2s(S.z[s], src, (uint32_t)n * TC_K * 2, &S.full_z[s]);
         umma::bulk_g2s(S.z[s] + TC_ZHALF, src + zhalf, (uint32_t)n * TC_K * 2, &S.full_z[s]);
+        umma::bulk_g2s(S.z[s] + 2 * TC_ZHALF, XT + (size_t)c * (TC_J * 8), TC_XYB, &S.full_z[s]);
+        umma::bulk_g2s(S.z[s] + 2 * TC_ZHALF + TC_XYB, YT + (size_t)c * (TC_J * 8), TC_XYB, &S.full_z[s]);
       }
       S.z_issued = c;
     }
@@ -239,7 +270,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     bool ok = true;
     for (int g = 0; g < n_groups; ++g) {
       const int buf = g & 1;
-      if (S.bad || !warp_wait(&S.full_acc[buf], (g >> 1) & 1)) {
+      if (!warp_wait(&S.full_acc[buf], (g >> 1) & 1, &S.bad)) {
         ok = false;
         break;
       }
@@ -293,45 +324,28 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
     if (!ok) S.bad = 1;
   } else {
-    // ---- builders: X/Y tables of chunk c, then A(c) = W products into stage c % TC_SA
+    // ---- builders: A(c) = W products of the streamed X/Y tables into stage c % TC_SA.
+    // Each warp waits for itself (lane 0 polls, the warp shares the outcome), so
+    // warps run ahead or behind one another within the ring's slack.
     const int btid = tid - 32 * TC_BUILD_WARP0;
     const int bw = btid >> 5;
-    const int4* F = fx + (int64_t)fl * n_list;
     for (int c = 0; c < n_chunks; ++c) {
-      const int sa = c % TC_SA;
-      float2* xy = S.xy[c & 1];
-      for (int e = btid; e < TC_J * 16; e += TC_BUILDERS) {
-        const int j = e >> 4, m = e & 15;
-        const int a = c * TC_J + j;
-        float sn = 0.f, cs = 0.f;
-        if (a < n_list) {
-          const int4 q = F[a];
-          const int32_t ph = m < 8 ? (int32_t)((uint32_t)(T.nx0 + m) * (uint32_t)q.x)
-                                   : (int32_t)((uint32_t)(T.ny0 + m - 8) * (uint32_t)q.y);
-          tc_phase(ph, &sn, &cs);
-        }
-        xy[xy_slot(j, m)] = make_float2(cs, sn);
-      }
-      // builder 0 decides for all builders; the flag alternates with the chunk
-      // parity so a slow reader of chunk c never sees chunk c+1's decision
-      if (btid == 0) {
-        const bool free_stage = !S.bad && umma::mbar_wait(&S.empty_a[sa], ((c / TC_SA) & 1) ^ 1, TC_WAIT);
-        S.build_stop[c & 1] = free_stage ? 0 : 1;
-      }
-      __syncwarp();
-      umma::named_barrier(1, TC_BUILDERS);
-      if (*(volatile int*)&S.build_stop[c & 1]) {
-        if (btid == 0) S.bad = 1;
+      const int sa = c % TC_SA, sz = c % TC_SZ;
+      if (!warp_wait(&S.empty_a[sa], ((c / TC_SA) & 1) ^ 1, &S.bad) ||
+          !warp_wait(&S.full_z[sz], (c / TC_SZ) & 1, &S.bad)) {
+        if (lane == 0) S.bad = 1;
         break;
       }
+      const float2* X = reinterpret_cast<const float2*>(S.z[sz] + 2 * TC_ZHALF);
+      const float2* Y = X + TC_J * 8;
       // A operand: lane = (row % 8) * 4 + (atom % 4), conflict-free 4-byte stores
-#pragma unroll 2
-      for (int it = 0; it < 8; ++it) {
-        const int combo = bw * 8 + it;  // 0..63
+#pragma unroll
+      for (int it = 0; it < 4; ++it) {
+        const int combo = bw * 4 + it;  // 0..63
         const int rg = combo >> 3, jg = combo & 7;
         const int r = rg * 8 + (lane >> 2);   // complex row: nx = r % 8, ny = r / 8
         const int j = jg * 4 + (lane & 3);
-        const float2 x = xy[xy_slot(j, r & 7)], y = xy[xy_slot(j, 8 + (r >> 3))];
+        const float2 x = X[xy_slot(j, r & 7)], y = Y[xy_slot(j, r >> 3)];
         const float wr = fmaf(x.x, y.x, -x.y * y.y), wi = fmaf(x.x, y.y, x.y * y.x);
         // hi = fp16(w), lo = fp16(w - hi), both as (re, im) half2 pairs
         const __half2 hi = __floats2half2_rn(wr, wi);
@@ -340,7 +354,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         const uint32_t h = *reinterpret_cast<const uint32_t*>(&hi);
         const uint32_t l = *reinterpret_cast<const uint32_t*>(&lo);
         const uint32_t o_re = umma::kmajor_offset(r, 2 * j, TC_K);
-        const uint32_t o_im = umma::kmajor_offset(TC_ROWS + r, 2 * j, TC_K);
+        const uint32_t o_im = o_re + (uint32_t)(TC_ROWS / 8) * (TC_K / 8) * 128;  // row r + 64
         // real rows (Wr, -Wi): flip the sign of the high half; imaginary rows (Wi, Wr): swap halves
         *reinterpret_cast<uint32_t*>(S.a[sa][0] + o_re) = h ^ 0x80000000u;
         *reinterpret_cast<uint32_t*>(S.a[sa][1] + o_re) = l ^ 0x80000000u;
@@ -386,7 +400,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 struct TcPlan {
   DevBuf<TcTile> tiles;
   DevBuf<int32_t> entry_k;
-  int32_t n_tiles = 0, n_zblk = 0, nzw = 0;
+  int32_t n_tiles = 0, n_zblk = 0, nzw = 0, nmax = 0;
   int64_t entries = 0;  // rows x columns computed per frame and atom, padding included
 };
 
@@ -441,6 +455,7 @@ TcPlan* tc_plan_build(const std::vector<int32_t>& kvec) {
   p->n_tiles = (int32_t)tiles.size();
   p->n_zblk = n_zblk;
   p->nzw = nzw;
+  p->nmax = nmax;
   p->entries = computed;
   p->tiles.reserve(std::max<size_t>(tiles.size(), 1));
   p->entry_k.reserve(std::max<size_t>(entries.size(), 1));
@@ -460,11 +475,15 @@ void rhok_tc_run(amdat_ctx* ctx, const TcPlan& P, const int4* fx, int32_t n_list
                  int32_t n_k, float2* rho) {
   if (P.n_tiles == 0 || n_list == 0 || n_frames == 0) return;
   const int32_t n_chunks = (int32_t)ceil_div(n_list, TC_J);
-  const size_t blob = (size_t)2 * P.nzw * TC_K * 2;
-  const size_t per_frame = (size_t)P.n_zblk * n_chunks * blob;
-  // frame batches bound the Z-operand buffer to ~1 GB
+  const int32_t n_blk = 2 * P.nmax / 8 + 1;  // 8-index blocks from -nmax covering the tiles
+  const size_t zblob = (size_t)2 * P.nzw * TC_K * 2;
+  const size_t z_frame = (size_t)P.n_zblk * n_chunks * zblob;
+  const size_t xy_frame = (size_t)2 * n_blk * n_chunks * TC_XYB;
+  const size_t per_frame = z_frame + xy_frame;
+  // frame batches bound the operand buffers to ~1 GB
   const int32_t batch = (int32_t)std::max<size_t>(1, std::min<size_t>(n_frames, (size_t)(1u << 30) / per_frame));
   unsigned char* zbuf = ctx->scratch.reserve(per_frame * batch + 256);
+  float2* xybuf = reinterpret_cast<float2*>(zbuf + z_frame * batch);
   int* d_err = (int*)(zbuf + per_frame * batch);
   AMDAT_CUDA(cudaMemsetAsync(d_err, 0, sizeof(int), ctx->stream));
   const size_t shm = sizeof(TcSmem) + 1024;
@@ -475,11 +494,15 @@ void rhok_tc_run(amdat_ctx* ctx, const TcPlan& P, const int4* fx, int32_t n_list
         fx + (int64_t)f0 * n_list, n_list, n_chunks, P.n_zblk, P.nzw, zbuf);
     check_launch("zgen_kernel");
     count_launch(ctx);
+    xygen_kernel<<<(unsigned)(nb * 2 * n_blk * n_chunks), 256, 0, ctx->stream>>>(
+        fx + (int64_t)f0 * n_list, n_list, n_chunks, n_blk, P.nmax, xybuf);
+    check_launch("xygen_kernel");
+    count_launch(ctx);
     KernelTimer kt(ctx, "rhok_tc_kernel");
     dim3 grid((unsigned)P.n_tiles, (unsigned)nb);
-    rhok_tc_kernel<<<grid, TC_THREADS, shm, ctx->stream>>>(fx + (int64_t)f0 * n_list, n_list, n_chunks,
-                                                          P.n_zblk, P.nzw, P.tiles.ptr, P.entry_k.ptr, zbuf,
-                                                          f0, n_k, rho, d_err);
+    rhok_tc_kernel<<<grid, TC_THREADS, shm, ctx->stream>>>(n_list, n_chunks, P.n_zblk, P.nzw, n_blk, P.nmax,
+                                                          P.tiles.ptr, P.entry_k.ptr, zbuf, xybuf, f0, n_k,
+                                                          rho, d_err);
     check_launch("rhok_tc_kernel");
     count_launch(ctx);
   }

@@ -23,7 +23,7 @@
 //   sk_adjoint_columns_kernel  vectors grouped into lattice columns (fixed nx, ny,
 //                              consecutive nz): exp(i k.r) is advanced along nz by
 //                              one complex multiplication per vector, re-anchored
-//                              from the exact fixed-point phase every 32 steps.
+//                              from the exact fixed-point phase every 64 steps.
 //                              Used when the columns average >= 8 vectors (the
 //                              |k| <= kmax lattice densities).
 //   sk_adjoint_direct_kernel   one sincospif per (atom, vector) for arbitrary
@@ -239,7 +239,7 @@ constexpr int SKC_APT = 4;                           // atoms per thread
 constexpr int SKC_ATOMS = SKC_THREADS * SKC_APT;     // atoms per block
 constexpr int SKC_SLOTS = 2048;                      // coefficient slots per chunk
 constexpr int SKC_COLS = 512;                        // columns per chunk
-constexpr int SKC_ANCHOR = 32;                       // exact re-anchoring interval along nz
+constexpr int SKC_ANCHOR = 64;                       // exact re-anchoring interval along nz
 
 __global__ void __launch_bounds__(SKC_THREADS)
     sk_adjoint_columns_kernel(const int4* __restrict__ fx /*[F][n]*/, int32_t n,
@@ -286,6 +286,7 @@ __global__ void __launch_bounds__(SKC_THREADS)
           phase_sc(ph, &ei[a], &er[a]);
         }
         float nz = (float)(col.nz0 + m0);
+#pragma unroll 4
         for (int m = m0; m < m1; ++m) {
           const float2 cc = s_c[slot + m];
 #pragma unroll

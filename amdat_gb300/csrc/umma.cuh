@@ -155,14 +155,24 @@ __device__ __forceinline__ bool mbar_test(uint64_t* mbar, uint32_t parity) {
       : "=r"(ok) : "r"(smem_addr(mbar)), "r"(parity) : "memory");
   return ok != 0;
 }
-// bounded wait for the phase with the given parity: polls with a short sleep
-// between tests, so the total wait is bounded by max_iter * ~0.1 us; false on
-// timeout (the caller reports an error instead of hanging)
-__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, uint32_t max_iter) {
-  for (uint32_t i = 0; i < max_iter; ++i) {
-    if (mbar_test(mbar, parity)) return true;
-    if (i > 64) __nanosleep(64);
-  }
+// bounded wait for the phase with the given parity.  Each mbarrier.try_wait
+// suspends the thread in hardware until the phase completes or the given
+// time hint (ns) elapses, so a waiting warp takes no issue slots; the total
+// wait is bounded by max_iter * hint_ns.  false on timeout (the caller reports
+// an error instead of hanging).
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* mbar, uint32_t parity, uint32_t hint_ns) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok) : "r"(smem_addr(mbar)), "r"(parity), "r"(hint_ns) : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, uint32_t max_iter,
+                                          uint32_t hint_ns = 1000) {
+  for (uint32_t i = 0; i < max_iter; ++i)
+    if (mbar_try_wait(mbar, parity, hint_ns)) return true;
   return false;
 }
 

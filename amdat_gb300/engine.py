@@ -52,11 +52,12 @@ EXPORTED = [
     "amdat_isf_run", "amdat_structure_factor_run", "amdat_rdf_run", "amdat_vhd_run",
     "amdat_profile_reset", "amdat_profile_kernel", "amdat_run_script", "amdat_script_error",
     "amdat_disp_plan_create", "amdat_disp_plan_run", "amdat_disp_plan_read", "amdat_disp_plan_info",
-    "amdat_disp_plan_destroy", "amdat_disp_moments_noalloc", "amdat_gsmooth_run",
+    "amdat_disp_plan_destroy", "amdat_disp_plan_sharing", "amdat_disp_moments_noalloc",
+    "amdat_gsmooth_run",
     "amdat_gsmooth_adjoint", "amdat_structure_factor_adjoint",
 ]
 
-PLAN_AUTOTUNE, PLAN_GRAPH = 1, 2
+PLAN_AUTOTUNE, PLAN_GRAPH, PLAN_NO_SHARING = 1, 2, 4
 
 _lib = None
 
@@ -440,6 +441,12 @@ class DispPlan:
         _check(lib().amdat_disp_plan_info(self._plan, C.byref(ch), C.byref(bps), C.byref(ni),
                                           C.byref(ms)))
         return dict(chunk=ch.value, blocks_per_sm=bps.value, n_items=ni.value, tuned_ms=ms.value)
+
+    def sharing(self):
+        """(work units, atoms streamed per time pair, sum of the list sizes)"""
+        nu, ua, la = C.c_int32(), C.c_int64(), C.c_int64()
+        _check(lib().amdat_disp_plan_sharing(self._plan, C.byref(nu), C.byref(ua), C.byref(la)))
+        return dict(n_units=nu.value, unit_atoms=ua.value, list_atoms=la.value)
 
     def close(self):
         if self._plan:

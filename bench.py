@@ -353,10 +353,11 @@ def structure_bench(torch, stream, device, args, n_atoms=100000, box=48.9, frame
         r = frames * n_atoms * nk / (kern["sk_adjoint_columns_kernel"] / 1e3)
         out["sk_adjoint_atom_k_per_s"] = r
         out["sk_adjoint_roofline"] = {
-            "bound": "fp32", "achieved": 8 * r / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
-            "frac": 8 * r / 1e12 / fp32_peak,
-            "rule": "8 flops per atom x vector (2 FMA Im(c e), 1 add, 1 FMA nz weight, 4 for the "
-                    "phase rotation); peak = 2 x 128 FP32 lanes x SMs x 2.07 GHz"}
+            "bound": "fp32", "achieved": 12 * r / 1e12, "peak": fp32_peak, "unit": "TFLOP/s",
+            "frac": 12 * r / 1e12 / fp32_peak,
+            "rule": "12 flops per atom x vector: Im(c e) (mul + fma = 3), shell sum (1), nz-weighted "
+                    "sum (fma = 2), phase rotation (2 mul + 2 fma = 6); peak = 2 flops x 128 FP32 "
+                    "lanes x SMs x 2.07 GHz"}
     return out
 
 
@@ -573,8 +574,17 @@ def main():
         ms_fs = max_over_ranks(time_plan(p_fs, max(2, args.steps)))
         blaunch = eng.launch_count() - l0
         info_msd, info_fs = p_msd.info(), p_fs.info()
+        share = p_msd.sharing()
         p_msd.close()
         p_fs.close()
+        # the same lists without work sharing (one unit of work per list)
+        ns_flags = E.PLAN_AUTOTUNE | E.PLAN_GRAPH | E.PLAN_NO_SHARING
+        p_ns = eng.plan(nested, flags=ns_flags)
+        ms_msd_ns = max_over_ranks(time_plan(p_ns, 10))
+        p_ns.close()
+        p_fs_ns = eng.plan(nested, shells=shells, period=L, flags=ns_flags)
+        ms_fs_ns = max_over_ranks(time_plan(p_fs_ns, 1))
+        p_fs_ns.close()
         # gathered layout (original atom order, index lists) for comparison
         eng.upload(btraj.unwrapped, btraj.box)
         eng.set_scheme(bscheme)
@@ -588,10 +598,12 @@ def main():
         eng.disp(big, shells=shells, period=L, precision=1)
         plain_rate = float(sizes[-1]) * npairs / (time.perf_counter() - t1)
         alg_bytes = float(sizes.sum()) * frames_used * 12
+        unit_bytes = float(share["unit_atoms"]) * frames_used * 12
         result["batched"] = dict(
             ms_msd=ms_msd, ms_fs=ms_fs, ms_gathered=ms_g, units=units, tune_s=tune_s,
             info_msd=info_msd, info_fs=info_fs, launches=blaunch, plain_rate=plain_rate,
-            alg_bytes=alg_bytes, nvec=int(shells[1][-1]), sum_n=int(sizes.sum()), npairs=npairs)
+            alg_bytes=alg_bytes, unit_bytes=unit_bytes, share=share, ms_msd_ns=ms_msd_ns,
+            ms_fs_ns=ms_fs_ns, nvec=int(shells[1][-1]), sum_n=int(sizes.sum()), npairs=npairs)
 
     if args.only in ("", "pairs"):
         # RDF + van Hove self/distinct: N=64000, L=42.3, 50 linear frames, sigma=0.1
@@ -722,22 +734,35 @@ def main():
     if "batched" in result:
         b = result["batched"]
         hbm = peaks.get("hbm_gbs", 6699.5)
-        gbs = b["alg_bytes"] / (b["ms_msd"] / 1e3) / 1e9
+        gbs = b["unit_bytes"] / (b["ms_msd"] / 1e3) / 1e9
+        gbs_ns = b["alg_bytes"] / (b["ms_msd_ns"] / 1e3) / 1e9
         line["batched"] = {
             "workload": f"64 lists (log-uniform 100..50000, nested prefixes of one permutation, "
                         f"sum N = {b['sum_n']}) of a 200000-atom walk, exponential 12x30 base 1.25, "
                         f"{b['npairs']} time pairs; one persistent launch per pass, CUDA graph, "
                         f"autotuned tiles",
+            "sharing": {"units": b["share"]["n_units"], "unit_atoms": b["share"]["unit_atoms"],
+                        "list_atoms": b["share"]["list_atoms"],
+                        "rule": "membership classes: atoms in exactly the same lists are one unit, "
+                                "processed once per time pair; list sums are sums of their classes"},
             "msd_ngp": {"value": b["units"] / (b["ms_msd"] / 1e3), "unit": "atom·time-pairs/s",
                         "ms_per_step": b["ms_msd"], "tile": b["info_msd"],
                         "roofline": {"bound": "hbm", "achieved": gbs, "peak": hbm, "unit": "GB/s",
-                                     "frac": gbs / hbm,
-                                     "algorithmic_bytes": b["alg_bytes"],
-                                     "bytes_rule": "sum_l N_l x 361 frames x 12 B (each list's "
-                                                   "trajectory once)"},
+                                     "frac": gbs / hbm, "algorithmic_bytes": b["unit_bytes"],
+                                     "bytes_rule": "unit atoms x 361 frames x 12 B (each shared "
+                                                   "unit's trajectory once)"},
+                        "per_list": {"value": b["units"] / (b["ms_msd_ns"] / 1e3),
+                                     "ms_per_step": b["ms_msd_ns"],
+                                     "roofline": {"bound": "hbm", "achieved": gbs_ns, "peak": hbm,
+                                                  "unit": "GB/s", "frac": gbs_ns / hbm,
+                                                  "algorithmic_bytes": b["alg_bytes"],
+                                                  "bytes_rule": "sum_l N_l x 361 frames x 12 B "
+                                                                "(each list's trajectory once)"}},
                         "gathered_layout_ms": b["ms_gathered"]},
             "msd_ngp_fs": {"value": b["units"] / (b["ms_fs"] / 1e3), "unit": "atom·time-pairs/s",
                            "ms_per_step": b["ms_fs"], "tile": b["info_fs"],
+                           "per_list": {"value": b["units"] / (b["ms_fs_ns"] / 1e3),
+                                        "ms_per_step": b["ms_fs_ns"]},
                            "shells": "reference q-vector shells m=10,20,40,60,80 "
                                      f"({b['nvec']} vectors), L=61.9",
                            "fp64_plain_largest_list": b["plain_rate"],

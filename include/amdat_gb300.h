@@ -195,6 +195,13 @@ amdat_status amdat_set_scheme(amdat_ctx* ctx, const amdat_scheme* scheme);
  * Bin_Static_Analysis, src/bin_static_analysis.h:69-111.) */
 #define AMDAT_PLAN_AUTOTUNE 1
 #define AMDAT_PLAN_GRAPH 2
+/* Lists that overlap (nested lists, bins plus their union, ...) share work:
+ * atoms are grouped into membership classes (atoms that belong to exactly the
+ * same lists), every class is processed once per time pair, and each list's
+ * sums are the sums of its classes (in a fixed order, FP64).  Used when it
+ * removes at least a fifth of the atom-pair terms and yields at most four
+ * classes per list; AMDAT_PLAN_NO_SHARING keeps one unit of work per list. */
+#define AMDAT_PLAN_NO_SHARING 4
 typedef struct amdat_disp_plan amdat_disp_plan;
 amdat_status amdat_disp_plan_create(amdat_ctx* ctx, const amdat_disp_request* req,
                                     const int32_t* lists, int32_t n_lists, int32_t flags,
@@ -205,6 +212,11 @@ amdat_status amdat_disp_plan_read(amdat_ctx* ctx, amdat_disp_plan* plan, int32_t
                                   double* fs_sum, int64_t* gs_counts);
 amdat_status amdat_disp_plan_info(amdat_disp_plan* plan, int32_t* chunk, int32_t* blocks_per_sm,
                                   int64_t* n_items, double* tuned_ms);
+/* Work sharing of a plan: the number of work units (membership classes, or
+ * the lists themselves) and the atoms streamed per time pair (the sum of the
+ * units' sizes, against the sum of the lists' sizes). */
+amdat_status amdat_disp_plan_sharing(amdat_disp_plan* plan, int32_t* n_units, int64_t* unit_atoms,
+                                     int64_t* list_atoms);
 amdat_status amdat_disp_plan_destroy(amdat_ctx* ctx, amdat_disp_plan* plan);
 
 /* ---------------------------------------------------------------------------

@@ -178,9 +178,55 @@ def test_many_lists_one_launch(eng):
     batch = eng.disp_lists(handles, shells=(shell, off), period=7.0, n_bins=30, bin_max=1.0)
     for i, h in enumerate(handles):
         one = eng.disp(h, shells=(shell, off), period=7.0, n_bins=30, bin_max=1.0)
-        np.testing.assert_allclose(batch["sum_d2"][i], one["sum_d2"], rtol=1e-12)
-        np.testing.assert_allclose(batch["fs_sum"][i], one["fs_sum"], rtol=1e-12, atol=1e-12)
+        # nested lists share work through membership classes: the sums differ
+        # from the single-list ones only in summation order
+        np.testing.assert_allclose(batch["sum_d2"][i], one["sum_d2"], rtol=1e-9)
+        np.testing.assert_allclose(batch["fs_sum"][i], one["fs_sum"], rtol=1e-9, atol=1e-9)
         np.testing.assert_array_equal(batch["gs_counts"][i], one["gs_counts"])
+
+
+@pytest.mark.parametrize("layout", ["nested", "bins_and_union", "random_overlap", "disjoint"])
+def test_plan_sharing_matches_per_list(eng, engine_mod, layout):
+    """Membership-class sharing gives the per-list results (summation order
+    aside) and is adopted only where it removes work."""
+    traj, _, _ = load("lin_binary")
+    eng.upload(traj.unwrapped, traj.box)
+    eng.set_scheme(traj.scheme)
+    n = traj.n_atoms
+    rng = np.random.default_rng(11)
+    perm = rng.permutation(n)
+    if layout == "nested":
+        sets = [np.sort(perm[:k]) for k in (5, 30, 31, 120, n)]
+    elif layout == "bins_and_union":
+        bins = np.array_split(perm, 4)
+        sets = [np.sort(b) for b in bins] + [np.arange(n)]
+    elif layout == "random_overlap":
+        sets = [np.sort(rng.choice(n, size=n // 2, replace=False)) for _ in range(9)]
+    else:
+        sets = [np.sort(b) for b in np.array_split(perm, 3)]
+    handles = [eng.list(a.astype(np.int32)) for a in sets]
+    shell = lattice_shell(7.0, 2.0, 2.6)
+    off = np.array([0, len(shell)], np.int32)
+    kw = dict(shells=(shell, off), period=7.0, n_bins=25, bin_max=1.0)
+    shared = eng.plan(handles, flags=2, **kw)
+    alone = eng.plan(handles, flags=2 | engine_mod.PLAN_NO_SHARING, **kw)
+    shared.run()
+    alone.run()
+    a, b = shared.read(), alone.read()
+    sh, sb = shared.sharing(), alone.sharing()
+    total = sum(len(x) for x in sets)
+    assert sb == dict(n_units=len(sets), unit_atoms=total, list_atoms=total)
+    if layout in ("nested", "bins_and_union"):
+        assert sh["unit_atoms"] == n and sh["n_units"] < 2 * len(sets)
+    else:
+        assert sh == sb
+    np.testing.assert_allclose(a["sum_d2"], b["sum_d2"], rtol=1e-9)
+    np.testing.assert_allclose(a["sum_d4"], b["sum_d4"], rtol=1e-9)
+    np.testing.assert_allclose(a["fs_sum"], b["fs_sum"], rtol=1e-9, atol=1e-9)
+    np.testing.assert_array_equal(a["gs_counts"], b["gs_counts"])
+    np.testing.assert_array_equal(a["atom_pairs"], b["atom_pairs"])
+    shared.close()
+    alone.close()
 
 
 def test_errors_are_status_codes(eng, engine_mod):
