@@ -53,7 +53,7 @@ EXPORTED = [
     "amdat_profile_reset", "amdat_profile_kernel", "amdat_run_script", "amdat_script_error",
     "amdat_disp_plan_create", "amdat_disp_plan_run", "amdat_disp_plan_read", "amdat_disp_plan_info",
     "amdat_disp_plan_destroy", "amdat_disp_plan_sharing", "amdat_disp_moments_noalloc",
-    "amdat_gsmooth_run",
+    "amdat_gsmooth_run", "amdat_disp_axes_run",
     "amdat_gsmooth_adjoint", "amdat_structure_factor_adjoint",
 ]
 
@@ -296,6 +296,18 @@ class Engine:
                                     C.c_void_p(fs) if req.n_shells else None,
                                     C.c_void_p(gs) if n_bins else None))
         del keep
+
+    def disp_axes(self, list_h=0, fullblock=0, gap=-1, n_bins=0, bin_size=1.0):
+        """Per-axis sums [G][6] (dx, dy, dz, dx^2, dy^2, dz^2), sum |dr|^4, atom-pair
+        counts and the |dr|^2 histogram (top bin = overflow) (amdat_disp_axes_run)."""
+        G = self.n_timegaps
+        ax, d4 = np.zeros((G, 6)), np.zeros(G)
+        cnt = np.zeros(G, np.int64)
+        h = np.zeros((G, max(n_bins, 1)), np.int64)
+        _check(lib().amdat_disp_axes_run(self._ctx, int(list_h), int(fullblock), int(gap), int(n_bins),
+                                         C.c_float(bin_size), OUT_HOST, _p(ax), _p(d4), _p(cnt),
+                                         _p(h) if n_bins else None))
+        return dict(axis_sums=ax, sum_d4=d4, atom_pairs=cnt, d2_counts=h[:, :n_bins])
 
     def plan(self, lists, fullblock=0, shells=None, period=1.0, n_bins=0, bin_max=0.0, flags=0):
         """Prepared many-list displacement run (amdat_disp_plan_*)."""

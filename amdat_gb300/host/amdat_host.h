@@ -173,6 +173,59 @@ class Incoherent_Scattering_Function : public Analysis {
   std::vector<float> corr_;  // [gap][shell]
 };
 
+// Mean_Square_Displacement_2D (src/mean_square_displacement_2d.cpp:79-199):
+// msd in one plane ("xy", "xz" or "yz")
+class Mean_Square_Displacement_2D : public Analysis {
+ public:
+  Mean_Square_Displacement_2D(System* sys, const std::string& plane);
+  void analyze(Trajectory_List* list) override;
+  void write(const std::string& file) const override;
+
+ private:
+  std::string plane_;
+  int a_ = 0, b_ = 1;  // axes of the plane
+  std::vector<float> msd_;
+};
+
+// Mean_Displacement (src/mean_displacement.cpp:149-199): mean vector displacement
+class Mean_Displacement : public Analysis {
+ public:
+  explicit Mean_Displacement(System* sys);
+  void analyze(Trajectory_List* list) override;
+  void write(const std::string& file) const override;
+
+ private:
+  std::vector<float> md_;  // [gap][3]
+};
+
+// DebyeWaller_Dist (src/debyewaller_dist.cpp:14-99, command u2dist): the
+// distribution of |dr|^2 at one time gap, its mean and variance; bins+1 bins of
+// maxvalue/bins, the top one collecting the overflow
+class DebyeWaller_Dist : public Analysis {
+ public:
+  DebyeWaller_Dist(System* sys, int bins, float maxvalue, int time_index);
+  void analyze(Trajectory_List* list) override;
+  void write(const std::string& file) const override;
+
+ protected:
+  int n_bins_, time_index_;
+  float binsize_, time_;
+  float mean_ = 0.f, variance_ = 0.f;
+  std::vector<float> dist_;
+};
+
+// Displacement_Distribution (src/displacement_distribution.cpp:17-141, command
+// displacement_dist): the same statistics; the power is only printed, as in
+// the reference (its kernel squares the displacement whatever the power)
+class Displacement_Distribution : public DebyeWaller_Dist {
+ public:
+  Displacement_Distribution(System* sys, float power, int bins, float maxvalue, int time_index);
+  void write(const std::string& file) const override;
+
+ private:
+  float power_;
+};
+
 // Van_Hove_Self (src/van_hove_self.cpp:45-103 + space_time_correlation_function.cpp)
 class Van_Hove_Self : public Analysis {
  public:

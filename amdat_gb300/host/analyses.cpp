@@ -93,6 +93,128 @@ void Mean_Square_Displacement::write(const std::string& file) const {
     out << system->timegaps()[g] << "\t" << Num{msd_[g]} << "\n";
 }
 
+// --- sibling displacement analyses ---------------------------------------
+namespace {
+struct AxesOut {
+  std::vector<double> ax, d4;
+  std::vector<int64_t> pairs, counts;
+};
+AxesOut axes(System* sys, int list, int gap, int n_bins, float bin_size) {
+  const int G = sys->n_timegaps();
+  AxesOut o;
+  o.ax.assign((size_t)G * 6, 0);
+  o.d4.assign(G, 0);
+  o.pairs.assign(G, 0);
+  o.counts.assign((size_t)G * std::max(n_bins, 1), 0);
+  check(amdat_disp_axes_run(sys->ctx(), list, 0, gap, n_bins, bin_size, AMDAT_OUT_HOST, o.ax.data(),
+                            o.d4.data(), o.pairs.data(), n_bins ? o.counts.data() : nullptr),
+        "displacement axes run");
+  return o;
+}
+}  // namespace
+
+Mean_Square_Displacement_2D::Mean_Square_Displacement_2D(System* sys, const std::string& plane)
+    : plane_(plane) {
+  system = sys;
+  if (plane == "xy") a_ = 0, b_ = 1;
+  else if (plane == "xz") a_ = 0, b_ = 2;
+  else if (plane == "yz") a_ = 1, b_ = 2;
+  else throw Error(AMDAT_ERR_ARGUMENT, "Error: plane command " + plane + " not understood.");
+}
+
+void Mean_Square_Displacement_2D::analyze(Trajectory_List* list) {
+  // displacement_list(this) with fullblock false; msd /= weighting (list sizes summed)
+  const AxesOut o = axes(system, list->handle(), -1, 0, 1.f);
+  const int G = system->n_timegaps();
+  msd_.assign(G, 0.f);
+  for (int g = 0; g < G; ++g)
+    msd_[g] = (float)((o.ax[(size_t)g * 6 + 3 + a_] + o.ax[(size_t)g * 6 + 3 + b_]) / (double)o.pairs[g]);
+}
+
+void Mean_Square_Displacement_2D::write(const std::string& file) const {
+  std::ofstream out = open_out(file);
+  out << "2-D mean square displacement data for " << plane_ << " plane created by AMDAT v." << SEMVER
+      << "\n";
+  for (int g = 0; g < system->n_timegaps(); ++g)
+    out << system->timegaps()[g] << "\t" << Num{msd_[g]} << "\n";
+}
+
+Mean_Displacement::Mean_Displacement(System* sys) { system = sys; }
+
+void Mean_Displacement::analyze(Trajectory_List* list) {
+  const AxesOut o = axes(system, list->handle(), -1, 0, 1.f);
+  const int G = system->n_timegaps();
+  md_.assign((size_t)G * 3, 0.f);
+  for (int g = 0; g < G; ++g)
+    for (int c = 0; c < 3; ++c) md_[(size_t)g * 3 + c] = (float)(o.ax[(size_t)g * 6 + c] / (double)o.pairs[g]);
+}
+
+void Mean_Displacement::write(const std::string& file) const {
+  std::ofstream out = open_out(file);
+  out << "Mean displacement data created by AMDAT v." << SEMVER << "\n";
+  for (int g = 0; g < system->n_timegaps(); ++g)
+    out << system->timegaps()[g] << "\t" << Num{md_[(size_t)g * 3]} << "\t" << Num{md_[(size_t)g * 3 + 1]}
+        << "\t" << Num{md_[(size_t)g * 3 + 2]} << "\n";
+}
+
+DebyeWaller_Dist::DebyeWaller_Dist(System* sys, int bins, float maxvalue, int time_index)
+    : n_bins_(bins + 1), time_index_(time_index), binsize_(maxvalue / (float)bins) {
+  system = sys;
+  if (bins < 1) throw Error(AMDAT_ERR_ARGUMENT, "need at least one bin");
+  if (time_index < 0 || time_index >= sys->n_timegaps())
+    throw Error(AMDAT_ERR_ARGUMENT, "Requested timegap out of range.");
+  time_ = sys->timegaps()[time_index];
+}
+
+void DebyeWaller_Dist::analyze(Trajectory_List* list) {
+  // displacement_list(this, t, false); every atom-pair term is weighted by
+  // 1/timegap_weighting()[t] (fullblock default 1) and the int atomcount
+  // accumulates n/w per pair with truncation, as in the reference
+  // (debyewaller_dist.cpp:50-99)
+  const AxesOut o = axes(system, list->handle(), time_index_, n_bins_, binsize_);
+  std::vector<int32_t> tw(system->n_timegaps());
+  check(amdat_scheme_weighting(&system->scheme(), 1, tw.data()), "timegap weighting");
+  const float w = (float)tw[time_index_];
+  const int n = list->show_n_trajectories();
+  const int64_t pairs = n > 0 ? o.pairs[time_index_] / n : 0;
+  int atomcount = 0;
+  for (int64_t p = 0; p < pairs; ++p) atomcount = (int)((float)atomcount + (float)n / w);
+  const size_t g6 = (size_t)time_index_ * 6;
+  const double sum_u2 = o.ax[g6 + 3] + o.ax[g6 + 4] + o.ax[g6 + 5];
+  const float mean = (float)(sum_u2 / (double)w) / (float)atomcount;
+  const float square = (float)(o.d4[time_index_] / (double)w);
+  mean_ = mean;
+  variance_ = square / (float)atomcount - mean * mean;
+  dist_.assign(n_bins_, 0.f);
+  for (int b = 0; b < n_bins_; ++b)
+    dist_[b] = (float)((double)o.counts[(size_t)time_index_ * n_bins_ + b] / (double)w) / (float)atomcount;
+}
+
+void DebyeWaller_Dist::write(const std::string& file) const {
+  std::ofstream out = open_out(file);
+  out << "MSD distribution created by AMDAT v." << SEMVER << "\n";
+  out << "MSD time = " << time_ << "\n";
+  out << "Mean_stiffness\t" << Num{mean_} << "\n";
+  out << "Variance\t" << Num{variance_} << "\n\n";
+  for (int b = 0; b < n_bins_; ++b) out << ((float)b + 0.5) * binsize_ << "\t" << Num{dist_[b]} << "\n";
+  out << "Last bin includes overflow.";
+}
+
+Displacement_Distribution::Displacement_Distribution(System* sys, float power, int bins, float maxvalue,
+                                                     int time_index)
+    : DebyeWaller_Dist(sys, bins, maxvalue, time_index), power_(power) {}
+
+void Displacement_Distribution::write(const std::string& file) const {
+  std::ofstream out = open_out(file);
+  out << "Particle displacement distribution to the " << power_ << " power created by AMDAT v." << SEMVER
+      << "\n";
+  out << "Last bin includes overflow.";
+  out << "time = " << time_ << "\n";
+  out << "Mean\t" << Num{mean_} << "\n";
+  out << "Variance\t" << Num{variance_} << "\n\n";
+  for (int b = 0; b < n_bins_; ++b) out << ((float)b + 0.5) * binsize_ << "\t" << Num{dist_[b]} << "\n";
+}
+
 // --- NGP -------------------------------------------------------------------
 Non_Gaussian_Parameter::Non_Gaussian_Parameter(System* sys) { system = sys; }
 

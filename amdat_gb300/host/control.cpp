@@ -136,6 +136,24 @@ class Control {
       pathcheck(a[1]);
       Mean_Square_Displacement m(&sys());
       analyze_write(m, a[1]);
+    } else if (cmd == "msd_2d") {
+      argcheck(a, 3, 3);
+      Mean_Square_Displacement_2D m(&sys(), a[2]);
+      analyze_write(m, a[1]);
+    } else if (cmd == "mean_displacement") {
+      argcheck(a, 2, 2);
+      Mean_Displacement m(&sys());
+      analyze_write(m, a[1]);
+    } else if (cmd == "u2dist") {
+      argcheck(a, 5, 5);
+      DebyeWaller_Dist d(&sys(), std::atoi(a[2].c_str()), (float)std::atof(a[3].c_str()),
+                         std::atoi(a[4].c_str()));
+      analyze_write(d, a[1]);
+    } else if (cmd == "displacement_dist") {
+      argcheck(a, 6, 6);
+      Displacement_Distribution d(&sys(), (float)std::atof(a[2].c_str()), std::atoi(a[3].c_str()),
+                                  (float)std::atof(a[4].c_str()), std::atoi(a[5].c_str()));
+      analyze_write(d, a[1]);
     } else if (cmd == "ngp") {
       argcheck(a, 2, 2);
       pathcheck(a[1]);

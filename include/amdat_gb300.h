@@ -116,7 +116,7 @@ amdat_status amdat_launch_count(amdat_ctx* ctx, int64_t* count);
  * names: disp_mixed_kernel, disp_plain_kernel, rhok_list_kernel,
  * rhok_lattice_kernel, rhok_tc_kernel, rhok_plain_kernel, isf_pairs_kernel,
  * sk_frames_kernel, pair_hist_kernel, gsmooth_kernel, gsmooth_adjoint_kernel,
- * sk_adjoint_columns_kernel, sk_adjoint_direct_kernel.  (No counterpart in the reference, which times commands
+ * sk_adjoint_columns_kernel, sk_adjoint_direct_kernel, disp_axes_kernel.  (No counterpart in the reference, which times commands
  * with time(NULL), e.g. src/control.cpp:2190-2196.) */
 amdat_status amdat_profile_reset(amdat_ctx* ctx, int32_t enable);
 amdat_status amdat_profile_kernel(amdat_ctx* ctx, const char* kernel, int64_t* launches,
@@ -182,6 +182,25 @@ amdat_status amdat_disp_run_lists(amdat_ctx* ctx, const amdat_disp_request* req,
                                   double* sum_d2, double* sum_d4, int64_t* atom_pairs,
                                   double* fs_sum, int64_t* gs_counts);
 amdat_status amdat_set_scheme(amdat_ctx* ctx, const amdat_scheme* scheme);
+
+/* Per-axis displacement sums and the |dr|^2 distribution of one list over the
+ * time pairs of the scheme: every gap (gap = -1) or one gap's pairs (the
+ * single-gap displacement_list, src/system.cpp:4349-4412).  Per gap g:
+ *   axis_sums[g][6]  sums of dx, dy, dz, dx^2, dy^2, dz^2
+ *   sum_d4[g]        sum of |dr|^4
+ *   atom_pairs[g]    number of (atom, time pair) terms (0 for gaps not run)
+ *   d2_counts[g][b]  histogram of u2 = float(|dr|^2) in the reference's FP32
+ *                    chain, b = int(u2 / bin_size), the top bin (n_bins - 1)
+ *                    collecting everything beyond it; n_bins = 0 disables it.
+ * Any output may be NULL.  Replaces the per-atom kernels of
+ * Mean_Square_Displacement_2D (src/mean_square_displacement_2d.cpp:143),
+ * Mean_Displacement (src/mean_displacement.cpp:163), DebyeWaller_Dist
+ * (src/debyewaller_dist.cpp:64) and Displacement_Distribution
+ * (src/displacement_distribution.cpp:69). */
+amdat_status amdat_disp_axes_run(amdat_ctx* ctx, int32_t list, int32_t fullblock, int32_t gap,
+                                 int32_t n_bins, float bin_size, int32_t out_flags,
+                                 double* axis_sums, double* sum_d4, int64_t* atom_pairs,
+                                 int64_t* d2_counts);
 
 /* Prepared displacement runs (many lists, one persistent launch).  A plan
  * builds its item tables on the device once; amdat_disp_plan_run is then pure

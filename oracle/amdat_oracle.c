@@ -843,3 +843,139 @@ void orc_sk_grad(const float* r, int32_t n_atoms, const int32_t* list, int32_t n
   free(rho);
   free(u);
 }
+
+/* ------------------------------------------------------------------------- */
+/* sibling displacement analyses                                             */
+/* ------------------------------------------------------------------------- */
+
+void orc_msd2d(const orc_scheme* s, const float* u, int32_t n_atoms, const int32_t* list,
+               int32_t n_list, int32_t plane, int32_t mode, double* msd) {
+  const int G = orc_n_timegaps(s);
+  const int ca = plane == 2 ? 1 : 0, cb = plane == 0 ? 1 : 2;
+  pairs_t p = make_pairs(s, 0, 0); /* analyze(): displacement_list(this) with fullblock false */
+  int64_t* w = (int64_t*)calloc(G, sizeof(int64_t));
+  if (mode == ORC_REF32) {
+    float* m = (float*)calloc(G, sizeof(float));
+    for (int64_t i = 0; i < p.n; ++i) {
+      int g = p.gap[i];
+      w[g] += n_list;
+      for (int j = 0; j < n_list; ++j) {
+        float a = POS(u, p.t1[i], list[j], ca) - POS(u, p.t0[i], list[j], ca);
+        float b = POS(u, p.t1[i], list[j], cb) - POS(u, p.t0[i], list[j], cb);
+        float d = sqrtf(a * a + b * b);
+        m[g] += d * d;
+      }
+    }
+    for (int g = 0; g < G; ++g) msd[g] = m[g] / (float)w[g];
+    free(m);
+  } else {
+    double* m = (double*)calloc(G, sizeof(double));
+    for (int64_t i = 0; i < p.n; ++i) {
+      int g = p.gap[i];
+      w[g] += n_list;
+      for (int j = 0; j < n_list; ++j) {
+        double a = (double)POS(u, p.t1[i], list[j], ca) - (double)POS(u, p.t0[i], list[j], ca);
+        double b = (double)POS(u, p.t1[i], list[j], cb) - (double)POS(u, p.t0[i], list[j], cb);
+        m[g] += a * a + b * b;
+      }
+    }
+    for (int g = 0; g < G; ++g) msd[g] = m[g] / (double)w[g];
+    free(m);
+  }
+  free(w);
+  free_pairs(&p);
+}
+
+void orc_mean_disp(const orc_scheme* s, const float* u, int32_t n_atoms, const int32_t* list,
+                   int32_t n_list, int32_t mode, double* md) {
+  const int G = orc_n_timegaps(s);
+  pairs_t p = make_pairs(s, 0, 0);
+  int64_t* w = (int64_t*)calloc(G, sizeof(int64_t));
+  if (mode == ORC_REF32) {
+    float* m = (float*)calloc((size_t)G * 3, sizeof(float));
+    for (int64_t i = 0; i < p.n; ++i) {
+      int g = p.gap[i];
+      w[g] += n_list;
+      for (int j = 0; j < n_list; ++j)
+        for (int c = 0; c < 3; ++c) m[3 * g + c] += POS(u, p.t1[i], list[j], c) - POS(u, p.t0[i], list[j], c);
+    }
+    for (int g = 0; g < G; ++g)
+      for (int c = 0; c < 3; ++c) md[3 * g + c] = m[3 * g + c] / (float)w[g];
+    free(m);
+  } else {
+    double* m = (double*)calloc((size_t)G * 3, sizeof(double));
+    for (int64_t i = 0; i < p.n; ++i) {
+      int g = p.gap[i];
+      w[g] += n_list;
+      for (int j = 0; j < n_list; ++j)
+        for (int c = 0; c < 3; ++c)
+          m[3 * g + c] += (double)POS(u, p.t1[i], list[j], c) - (double)POS(u, p.t0[i], list[j], c);
+    }
+    for (int g = 0; g < G; ++g)
+      for (int c = 0; c < 3; ++c) md[3 * g + c] = m[3 * g + c] / (double)w[g];
+    free(m);
+  }
+  free(w);
+  free_pairs(&p);
+}
+
+void orc_u2dist(const orc_scheme* s, const float* u, int32_t n_atoms, const int32_t* list,
+                int32_t n_list, int32_t gap, int32_t bins, float maxvalue, int32_t mode,
+                double* mean_out, double* var_out, double* dist_out) {
+  const int G = orc_n_timegaps(s);
+  const int nb = bins + 1;
+  const float binsize = maxvalue / bins;
+  int32_t* tw = (int32_t*)malloc(sizeof(int32_t) * G);
+  orc_timegap_weighting(s, 1, tw); /* timegap_weighting() defaults to fullblock = 1 */
+  const float w = (float)tw[gap];
+  pairs_t p = make_pairs(s, 0, 0); /* displacement_list(this, t, false): gap t's pairs */
+  if (mode == ORC_REF32) {
+    float mean = 0, sq = 0;
+    int count = 0; /* int atomcount: each pair's n / w is added and truncated */
+    float* dist = (float*)calloc(nb, sizeof(float));
+    for (int64_t i = 0; i < p.n; ++i) {
+      if (p.gap[i] != gap) continue;
+      count = (int)((float)count + (float)n_list / w);
+      for (int j = 0; j < n_list; ++j) {
+        float msd = (float)pow(dist32(u, n_atoms, list[j], p.t0[i], p.t1[i]), 2.0);
+        mean += msd / w;
+        sq += msd * msd / w;
+        int idx = (int)(msd / binsize);
+        if (idx >= nb) idx = nb - 1;
+        dist[idx] += 1.0 / w;
+      }
+    }
+    mean /= count;
+    float var = sq / count - mean * mean;
+    for (int b = 0; b < nb; ++b) dist_out[b] = dist[b] / count;
+    *mean_out = mean;
+    *var_out = var;
+    free(dist);
+  } else {
+    /* FP64 sums, the reference's normalisation (int atomcount, 1/w weights) */
+    double sum = 0, sum2 = 0;
+    int count = 0;
+    double* dist = (double*)calloc(nb, sizeof(double));
+    for (int64_t i = 0; i < p.n; ++i) {
+      if (p.gap[i] != gap) continue;
+      count = (int)((float)count + (float)n_list / w);
+      for (int j = 0; j < n_list; ++j) {
+        float d = dist32(u, n_atoms, list[j], p.t0[i], p.t1[i]);
+        float msd = (float)((double)d * (double)d);
+        double d2 = dist2_64(u, n_atoms, list[j], p.t0[i], p.t1[i]);
+        sum += d2;
+        sum2 += d2 * d2;
+        int idx = (int)(msd / binsize);
+        if (idx >= nb) idx = nb - 1;
+        dist[idx] += 1.0;
+      }
+    }
+    double mean = sum / w / count;
+    *mean_out = mean;
+    *var_out = sum2 / w / count - mean * mean;
+    for (int b = 0; b < nb; ++b) dist_out[b] = dist[b] / w / count;
+    free(dist);
+  }
+  free(tw);
+  free_pairs(&p);
+}

@@ -125,6 +125,28 @@ void orc_sk_grad(const float* wrapped, int32_t n_atoms, const int32_t* list, int
                  const int32_t* shell_off, int32_t n_shells, double box_len, const double* w,
                  int32_t n_threads, double* grad);
 
+/* Sibling displacement analyses (same scheduler, other per-atom kernels).
+ * orc_msd2d: Mean_Square_Displacement_2D (mean_square_displacement_2d.cpp:114-199):
+ *   msd[g] += |dr_plane|^2, |dr_plane| = sqrt(a*a + b*b) in FP32 (coordinate.h:56),
+ *   divided by the summed list sizes; plane 0 = xy, 1 = xz, 2 = yz.
+ * orc_mean_disp: Mean_Displacement (mean_displacement.cpp:149-199): md[g][3] +=
+ *   u(t1) - u(t0) (FP32 Coordinate), divided by the summed list sizes.
+ * orc_u2dist: DebyeWaller_Dist (debyewaller_dist.cpp:14-99) and
+ *   Displacement_Distribution (displacement_distribution.cpp:17-83) at one gap:
+ *   u2 = float(pow(|dr|, 2)), mean and variance of u2 and its histogram of
+ *   bins+1 bins of maxvalue/bins (top bin = overflow), all weighted by
+ *   1/timegap_weighting(fullblock=1)[gap] and normalised by the reference's
+ *   int atomcount (each pair adds n/w, truncated), with FP32 (REF32) or FP64
+ *   (F64) sums.
+ * mode REF32 = the reference's FP32 accumulators and order; F64 = FP64. */
+void orc_msd2d(const orc_scheme* s, const float* unwrapped, int32_t n_atoms, const int32_t* list,
+               int32_t n_list, int32_t plane, int32_t mode, double* msd);
+void orc_mean_disp(const orc_scheme* s, const float* unwrapped, int32_t n_atoms, const int32_t* list,
+                   int32_t n_list, int32_t mode, double* md);
+void orc_u2dist(const orc_scheme* s, const float* unwrapped, int32_t n_atoms, const int32_t* list,
+                int32_t n_list, int32_t gap, int32_t bins, float maxvalue, int32_t mode,
+                double* mean, double* variance, double* dist);
+
 #ifdef __cplusplus
 }
 #endif

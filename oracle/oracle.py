@@ -276,3 +276,32 @@ def sk_grad(wrapped, lst, frames, kvec_n, shell_off, box_len, w, n_threads=1):
     lib().orc_sk_grad(_p(r), r.shape[1], _p(lst), len(lst), _p(fr), len(fr), _p(kv), len(kv) // 3,
                       _p(off), len(off) - 1, C.c_double(box_len), _p(ww), int(n_threads), _p(g))
     return g
+
+
+def msd2d(s, unwrapped, lst, plane, mode=F64):
+    """Mean_Square_Displacement_2D: plane 0 = xy, 1 = xz, 2 = yz."""
+    u = _f32(unwrapped)
+    lst = _i32(lst)
+    out = np.zeros(n_timegaps(s))
+    lib().orc_msd2d(C.byref(s), _p(u), u.shape[1], _p(lst), len(lst), int(plane), mode, _p(out))
+    return out
+
+
+def mean_disp(s, unwrapped, lst, mode=F64):
+    """Mean_Displacement: [G][3]."""
+    u = _f32(unwrapped)
+    lst = _i32(lst)
+    out = np.zeros((n_timegaps(s), 3))
+    lib().orc_mean_disp(C.byref(s), _p(u), u.shape[1], _p(lst), len(lst), mode, _p(out))
+    return out
+
+
+def u2dist(s, unwrapped, lst, gap, bins, maxvalue, mode=F64):
+    """DebyeWaller_Dist / Displacement_Distribution at one gap: (mean, variance, dist[bins+1])."""
+    u = _f32(unwrapped)
+    lst = _i32(lst)
+    m, v = C.c_double(), C.c_double()
+    dist = np.zeros(bins + 1)
+    lib().orc_u2dist(C.byref(s), _p(u), u.shape[1], _p(lst), len(lst), int(gap), int(bins),
+                     C.c_float(maxvalue), mode, C.byref(m), C.byref(v), _p(dist))
+    return m.value, v.value, dist

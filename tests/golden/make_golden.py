@@ -102,6 +102,48 @@ list all
 isf ./isf.dat auto symmetric xyz 1 0 8
 list all
 """),
+    # sibling displacement analyses on the same scheduler (exponential and linear)
+    "siblings": dict(
+        n=150, box=6.5, sigma=0.4, seed=44, fractions=(0.7, 0.3),
+        scheme=synth.TimeScheme.exponential(4, 8, 1.3, 0, 0, 0.005),
+        commands="""create_list all
+all
+create_list b
+type_system 2
+msd_2d ./msd2d_xy.dat xy
+list all
+msd_2d ./msd2d_yz.dat yz
+list b
+mean_displacement ./md.dat
+list all
+u2dist ./u2_in_block.dat 40 2.0 5
+list all
+u2dist ./u2_cross.dat 25 3.0 9
+list b
+u2dist ./u2_last.dat 30 4.0 11
+list all
+displacement_dist ./dd.dat 2 30 1.5 3
+list all
+limit 2
+u2dist ./u2_lim.dat 20 2.0 10
+list all
+mean_displacement ./md_lim.dat
+list all
+"""),
+    "siblings_lin": dict(
+        n=120, box=6.0, sigma=0.1, seed=55, fractions=(1.0,), time_scaled=False,
+        scheme=synth.TimeScheme.linear(16, 1.0),
+        commands="""create_list all
+all
+msd_2d ./msd2d_xz.dat xz
+list all
+mean_displacement ./md.dat
+list all
+u2dist ./u2.dat 25 0.5 4
+list all
+displacement_dist ./dd.dat 4 20 1.0 14
+list all
+"""),
 }
 
 

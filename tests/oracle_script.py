@@ -5,8 +5,12 @@ Formats follow the reference writers: Mean_Square_Displacement::write
 (mean_square_displacement.cpp:186), Non_Gaussian_Parameter::write,
 Correlation_2D::write (correlation_2d.cpp:475-504),
 Space_Time_Correlation_Function::write (space_time_correlation_function.cpp:240),
-Structure_Factor::write (structure_factor.cpp:323-344) and
-Radial_Distribution_Function::write (radial_distribution_function.cpp:326).
+Structure_Factor::write (structure_factor.cpp:323-344),
+Radial_Distribution_Function::write (radial_distribution_function.cpp:326),
+Mean_Square_Displacement_2D::write (mean_square_displacement_2d.cpp:183),
+Mean_Displacement::write (mean_displacement.cpp:185), DebyeWaller_Dist::write
+(debyewaller_dist.cpp:101) and Displacement_Distribution::write
+(displacement_distribution.cpp:103).
 """
 from __future__ import annotations
 
@@ -170,4 +174,42 @@ class OracleRun:
         txt = f"Radial distribution function data created by AMDAT v.{VERSION}\n"
         txt += "".join(fmt(f32(f32(f32(b) * bs) + f32(bs / f32(2)))) + "\t" for b in range(nb)) + "\n"
         txt += "".join(fmt(f32(v)) + "\t" for v in mean) + "\n"
+        self.files[self.name(a[1])] = txt
+
+    def cmd_msd_2d(self, a, lst):
+        plane = {"xy": 0, "xz": 1, "yz": 2}[a[2]]
+        s = self.scheme()
+        m = orc.msd2d(s, self.unwrapped, lst, plane, self.mode)
+        t = self.times(s)
+        txt = f"2-D mean square displacement data for {a[2]} plane created by AMDAT v.{VERSION}\n"
+        txt += "".join(f"{fmt(t[g])}\t{fmt(f32(m[g]))}\n" for g in range(len(t)))
+        self.files[self.name(a[1])] = txt
+
+    def cmd_mean_displacement(self, a, lst):
+        s = self.scheme()
+        md = orc.mean_disp(s, self.unwrapped, lst, self.mode)
+        t = self.times(s)
+        txt = f"Mean displacement data created by AMDAT v.{VERSION}\n"
+        txt += "".join(f"{fmt(t[g])}\t" + "\t".join(fmt(f32(v)) for v in md[g]) + "\n"
+                       for g in range(len(t)))
+        self.files[self.name(a[1])] = txt
+
+    def _u2(self, lst, bins, maxvalue, gap):
+        s = self.scheme()
+        mean, var, dist = orc.u2dist(s, self.unwrapped, lst, gap, bins, maxvalue, self.mode)
+        bs = f32(f32(maxvalue) / f32(bins))
+        rows = "".join(f"{fmt((float(f32(b)) + 0.5) * float(bs))}\t{fmt(f32(d))}\n" for b, d in enumerate(dist))
+        return fmt(self.times(s)[gap]), fmt(f32(mean)), fmt(f32(var)), rows
+
+    def cmd_u2dist(self, a, lst):
+        t, mean, var, rows = self._u2(lst, int(a[2]), float(a[3]), int(a[4]))
+        txt = (f"MSD distribution created by AMDAT v.{VERSION}\nMSD time = {t}\n"
+               f"Mean_stiffness\t{mean}\nVariance\t{var}\n\n" + rows + "Last bin includes overflow.")
+        self.files[self.name(a[1])] = txt
+
+    def cmd_displacement_dist(self, a, lst):
+        t, mean, var, rows = self._u2(lst, int(a[3]), float(a[4]), int(a[5]))
+        txt = (f"Particle displacement distribution to the {fmt(f32(float(a[2])))} power created by "
+               f"AMDAT v.{VERSION}\nLast bin includes overflow.time = {t}\nMean\t{mean}\n"
+               f"Variance\t{var}\n\n" + rows)
         self.files[self.name(a[1])] = txt

