@@ -77,6 +77,7 @@ struct TcSmem {
   uint64_t mma_done;
   uint32_t tmem;
   volatile int bad;        // any role gave up
+  int build_stop[2];       // chunk parity: written by builder 0 before a builder barrier
   int z_issued, z_landed;  // bulk copies issued / seen complete
 };
 static_assert(sizeof(float) * TC_M * (TC_NMAX + 1) <= sizeof(((TcSmem*)0)->z), "D staging must fit the Z ring");
@@ -192,6 +193,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     umma::mbar_init(&S.mma_done, 1);
     umma::fence_mbarrier_init();
     S.bad = 0;
+    S.build_stop[0] = S.build_stop[1] = 0;
     S.z_issued = 0;
     S.z_landed = 0;
   }
@@ -324,16 +326,23 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
     if (!ok) S.bad = 1;
   } else {
-    // ---- builders: A(c) = W products of the streamed X/Y tables into stage c % TC_SA.
-    // Each warp waits for itself (lane 0 polls, the warp shares the outcome), so
-    // warps run ahead or behind one another within the ring's slack.
+    // ---- builders: A(c) = W products of the streamed X/Y tables into stage c % TC_SA
     const int btid = tid - 32 * TC_BUILD_WARP0;
     const int bw = btid >> 5;
     for (int c = 0; c < n_chunks; ++c) {
       const int sa = c % TC_SA, sz = c % TC_SZ;
-      if (!warp_wait(&S.empty_a[sa], ((c / TC_SA) & 1) ^ 1, &S.bad) ||
-          !warp_wait(&S.full_z[sz], (c / TC_SZ) & 1, &S.bad)) {
-        if (lane == 0) S.bad = 1;
+      // builder 0 decides for all builders (A stage free, X/Y of chunk c landed);
+      // the flag alternates with the chunk parity so a slow reader of chunk c
+      // never sees chunk c+1's decision
+      if (btid == 0) {
+        const bool go = !S.bad && umma::mbar_wait(&S.empty_a[sa], ((c / TC_SA) & 1) ^ 1, TC_WAIT) &&
+                        umma::mbar_wait(&S.full_z[sz], (c / TC_SZ) & 1, TC_WAIT);
+        S.build_stop[c & 1] = go ? 0 : 1;
+      }
+      __syncwarp();
+      umma::named_barrier(1, TC_BUILDERS);
+      if (*(volatile int*)&S.build_stop[c & 1]) {
+        if (btid == 0) S.bad = 1;
         break;
       }
       const float2* X = reinterpret_cast<const float2*>(S.z[sz] + 2 * TC_ZHALF);

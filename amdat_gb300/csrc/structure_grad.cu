@@ -82,17 +82,53 @@ __device__ __forceinline__ void stage_atoms(const SGParams& p, const float* P, i
   }
 }
 
-// forward: unordered pairs j > i.  Each Gaussian term is rounded once to a
-// fixed-point integer (scale 2^q chosen by the host so that a block's sum
-// cannot overflow 63 bits) and added with 64-bit shared-memory integer
-// atomics: the block histogram is exact and independent of the order of the
-// additions, so the forward is deterministic and finite differences of it
-// see only the terms that change.
+// Gaussian terms of one pair over its bins b0..b1, x_b = (b + 1/2) bin - r:
+// G_b = exp(-x_b^2 / 2 sigma^2) by the exact recurrence G_{b+1} = G_b R_b,
+// R_{b+1} = R_b Q (two exponentials per pair instead of one per bin) when
+// the bin is at most 2 sigma wide (the factors then stay within FP32 range),
+// else one exponential per bin.  f(b, x, G) receives each term.
+template <class F>
+__device__ __forceinline__ void gauss_bins(const SGParams& p, float r, float inv2s2, bool recur, F f) {
+  const int bc = (int)(r * (1.0f / p.bin));
+  const int b0 = max(0, bc - p.span), b1 = min(p.n_bins - 1, bc + p.span);
+  if (b0 > b1) return;
+  float x = fmaf((float)b0 + 0.5f, p.bin, -r);
+  if (recur) {
+    float G = __expf(-x * x * inv2s2);
+    float R = __expf(-(2.0f * x * p.bin + p.bin * p.bin) * inv2s2);
+    const float Q = __expf(-2.0f * p.bin * p.bin * inv2s2);
+    for (int b = b0; b <= b1; ++b) {
+      f(b, x, G);
+      G *= R;
+      R *= Q;
+      x += p.bin;
+    }
+  } else {
+    for (int b = b0; b <= b1; ++b) {
+      f(b, x, __expf(-x * x * inv2s2));
+      x += p.bin;
+    }
+  }
+}
+
+constexpr int SG_WARPS = SG_THREADS / 32;
+constexpr int SG_Q = 64;  // per-warp queue of in-range pairs
+
+// forward: unordered pairs j > i.  In-range pairs (about 2 % of all pairs at
+// the usual cutoffs) are compacted into a per-warp queue with ballots and
+// their bins are processed 32 at a time, so the bin loop runs with every lane
+// busy.  Each Gaussian term is rounded once to a fixed-point integer (scale
+// 2^q chosen by the host so that a block's sum cannot overflow 63 bits) and
+// added with 64-bit shared-memory integer atomics: the block histogram is
+// exact and independent of the order of the additions, so the forward is
+// deterministic and finite differences of it see only the terms that change.
 __global__ void __launch_bounds__(SG_THREADS) gsmooth_kernel(SGParams p, float qscale) {
   extern __shared__ double sh_d[];  // [n_bins] as unsigned 64-bit fixed point
   unsigned long long* sh_q = reinterpret_cast<unsigned long long*>(sh_d);
   __shared__ float sx[SG_JT], sy[SG_JT], sz[SG_JT];
+  __shared__ float q_r[SG_WARPS][SG_Q];
   const int f = blockIdx.y;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const float* P = p.w + (int64_t)p.frames[f] * 3 * p.n_pad;
   for (int b = threadIdx.x; b < p.n_bins; b += blockDim.x) sh_q[b] = 0ull;
   const int i0 = blockIdx.x * SG_THREADS, i = i0 + threadIdx.x;
@@ -106,40 +142,60 @@ __global__ void __launch_bounds__(SG_THREADS) gsmooth_kernel(SGParams p, float q
   }
   const float inv2s2 = 0.5f / (p.sigma * p.sigma);
   const float qnorm = qscale * INV_SQRT_2PI / p.sigma;
-  const float inv_bin = 1.0f / p.bin;
+  const bool recur = p.bin <= 2.0f * p.sigma;
+  const unsigned below = (1u << lane) - 1u;
+  auto flush = [&](int count) {  // lanes < count take one queued pair each
+    if (lane < count)
+      gauss_bins(p, q_r[warp][lane], inv2s2, recur, [&](int b, float, float G) {
+        atomicAdd(sh_q + b, (unsigned long long)__float2ll_rn(qnorm * G));
+      });
+  };
+  int qn = 0;  // warp-uniform queue length
   for (int j0 = i0; j0 < p.lst.n; j0 += SG_JT) {
     const int nj = min(SG_JT, p.lst.n - j0);
     __syncthreads();
     stage_atoms(p, P, j0, nj, sx, sy, sz);
     __syncthreads();
-    if (!live) continue;
-    for (int t = max(0, i + 1 - j0); t < nj; ++t) {
+    for (int t = 0; t < nj; ++t) {
       const float dx = min_image(sx[t] - xi, p.box.x, p.inv_box.x);
       const float dy = min_image(sy[t] - yi, p.box.y, p.inv_box.y);
       const float dz = min_image(sz[t] - zi, p.box.z, p.inv_box.z);
       const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-      if (r2 >= p.cut2) continue;
-      const float r = sqrtf(r2);
-      const int bc = (int)(r * inv_bin);
-      const int b1 = min(p.n_bins - 1, bc + p.span);
-      for (int b = max(0, bc - p.span); b <= b1; ++b) {
-        const float x = fmaf((float)b + 0.5f, p.bin, -r);
-        atomicAdd(sh_q + b, (unsigned long long)__float2ll_rn(qnorm * __expf(-x * x * inv2s2)));
+      const bool in = live && j0 + t > i && r2 < p.cut2;
+      const unsigned m = __ballot_sync(0xffffffffu, in);
+      if (in) q_r[warp][qn + __popc(m & below)] = sqrtf(r2);
+      qn += __popc(m);
+      if (qn >= 32) {
+        __syncwarp();
+        flush(32);
+        __syncwarp();
+        if (lane < qn - 32) q_r[warp][lane] = q_r[warp][32 + lane];
+        __syncwarp();
+        qn -= 32;
       }
     }
   }
+  __syncwarp();
+  flush(qn);
   __syncthreads();
   const double inv_q = 1.0 / (double)qscale;
   for (int b = threadIdx.x; b < p.n_bins; b += blockDim.x)
     if (sh_q[b]) atomicAdd(p.h + b, (double)sh_q[b] * inv_q);
 }
 
-// adjoint: thread per atom i, every j != i, single writer per gradient element
+// adjoint: each atom i gathers psi(r_ij) (r_i - r_j) / r_ij over every j != i.
+// In-range pairs are compacted into a per-warp queue (the pair's minimum-image
+// vector, r and its owner lane); the warp evaluates psi for 32 queued pairs
+// at a time, then every owner adds its own entries in queue order, so every
+// gradient element still has a single writer and a fixed summation order.
 __global__ void __launch_bounds__(SG_THREADS) gsmooth_adjoint_kernel(SGParams p) {
   extern __shared__ double sh_d[];  // [n_bins] weights as FP32
   float* sh_w = (float*)sh_d;
   __shared__ float sx[SG_JT], sy[SG_JT], sz[SG_JT];
+  __shared__ float4 q_v[SG_WARPS][SG_Q];  // (dx, dy, dz, r); after a flush: (s dx, s dy, s dz, -)
+  __shared__ unsigned char q_o[SG_WARPS][SG_Q];
   const int f = blockIdx.y;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const float* P = p.w + (int64_t)p.frames[f] * 3 * p.n_pad;
   for (int b = threadIdx.x; b < p.n_bins; b += blockDim.x) sh_w[b] = (float)p.wgt[b];
   const int i = blockIdx.x * SG_THREADS + threadIdx.x;
@@ -153,43 +209,71 @@ __global__ void __launch_bounds__(SG_THREADS) gsmooth_adjoint_kernel(SGParams p)
   }
   const float inv_s2 = 1.0f / (p.sigma * p.sigma);
   const float inv2s2 = 0.5f * inv_s2;
-  const float norm = INV_SQRT_2PI / p.sigma;
-  const float inv_bin = 1.0f / p.bin;
+  const float scale = INV_SQRT_2PI / p.sigma * inv_s2;
+  const bool recur = p.bin <= 2.0f * p.sigma;
+  const unsigned below = (1u << lane) - 1u;
   float g[3] = {0.f, 0.f, 0.f}, c[3] = {0.f, 0.f, 0.f};
+  auto flush = [&](int count) {
+    if (lane < count) {
+      float4 v = q_v[warp][lane];
+      float psi = 0.f;
+      gauss_bins(p, v.w, inv2s2, recur, [&](int b, float x, float G) { psi = fmaf(sh_w[b] * x, G, psi); });
+      const float s = psi * scale / v.w;
+      q_v[warp][lane] = make_float4(s * v.x, s * v.y, s * v.z, 0.f);
+    }
+    __syncwarp();
+    // owners add their entries in queue order (compensated)
+    float part[3] = {0.f, 0.f, 0.f};
+    for (int e = 0; e < count; ++e)
+      if (q_o[warp][e] == lane) {
+        const float4 v = q_v[warp][e];
+        part[0] += v.x;
+        part[1] += v.y;
+        part[2] += v.z;
+      }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const float y = __fsub_rn(part[d], c[d]), t = __fadd_rn(g[d], y);
+      c[d] = __fsub_rn(__fsub_rn(t, g[d]), y);
+      g[d] = t;
+    }
+  };
+  int qn = 0;
+  __syncthreads();
   for (int j0 = 0; j0 < p.lst.n; j0 += SG_JT) {
     const int nj = min(SG_JT, p.lst.n - j0);
     __syncthreads();
     stage_atoms(p, P, j0, nj, sx, sy, sz);
     __syncthreads();
-    if (!live) continue;
-    float tg[3] = {0.f, 0.f, 0.f};
     for (int t = 0; t < nj; ++t) {
       // d = r_i - r_j (minimum image)
       const float dx = min_image(xi - sx[t], p.box.x, p.inv_box.x);
       const float dy = min_image(yi - sy[t], p.box.y, p.inv_box.y);
       const float dz = min_image(zi - sz[t], p.box.z, p.inv_box.z);
       const float r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-      if (r2 >= p.cut2 || j0 + t == i || r2 == 0.f) continue;
-      const float r = sqrtf(r2);
-      const int bc = (int)(r * inv_bin);
-      const int b1 = min(p.n_bins - 1, bc + p.span);
-      float psi = 0.f;
-      for (int b = max(0, bc - p.span); b <= b1; ++b) {
-        const float x = fmaf((float)b + 0.5f, p.bin, -r);
-        psi = fmaf(sh_w[b] * x, __expf(-x * x * inv2s2), psi);
+      const bool in = live && j0 + t != i && r2 < p.cut2 && r2 > 0.f;
+      const unsigned m = __ballot_sync(0xffffffffu, in);
+      if (in) {
+        const int pos = qn + __popc(m & below);
+        q_v[warp][pos] = make_float4(dx, dy, dz, sqrtf(r2));
+        q_o[warp][pos] = (unsigned char)lane;
       }
-      const float s = psi * (norm * inv_s2) / r;
-      tg[0] = fmaf(s, dx, tg[0]);
-      tg[1] = fmaf(s, dy, tg[1]);
-      tg[2] = fmaf(s, dz, tg[2]);
-    }
-#pragma unroll
-    for (int d = 0; d < 3; ++d) {
-      const float y = __fsub_rn(tg[d], c[d]), s = __fadd_rn(g[d], y);
-      c[d] = __fsub_rn(__fsub_rn(s, g[d]), y);
-      g[d] = s;
+      qn += __popc(m);
+      if (qn >= 32) {
+        __syncwarp();
+        flush(32);
+        __syncwarp();
+        if (lane < qn - 32) {
+          q_v[warp][lane] = q_v[warp][32 + lane];
+          q_o[warp][lane] = q_o[warp][32 + lane];
+        }
+        __syncwarp();
+        qn -= 32;
+      }
     }
   }
+  __syncwarp();
+  flush(qn);
   if (live) {
     float* out = p.grad + ((int64_t)f * p.lst.n + i) * 3;
 #pragma unroll
