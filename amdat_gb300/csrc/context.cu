@@ -177,6 +177,7 @@ amdat_ctx::~amdat_ctx() {
   }
   for (auto* b : rho_pool) delete b;
   amdat::lattice_plans_free(this);
+  amdat::sk_adjoint_plans_free(this);
   for (auto& r : prof_pending) {
     cudaEventDestroy(r.a);
     cudaEventDestroy(r.b);

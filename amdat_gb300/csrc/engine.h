@@ -107,6 +107,7 @@ struct PairTable {
 };
 
 struct LatticePlanDev;
+struct SkAdjointPlan;
 
 struct Density {
   int32_t list = 0;
@@ -115,6 +116,7 @@ struct Density {
   int32_t n_shells = 0;
   float period = 0.f;              // k = 2 pi n / period
   int32_t n_list = 0;              // list size when the density was computed
+  std::string lattice_key;         // lattice densities: the plan key (kmax, dk, period)
   std::vector<int32_t> frames;     // system frame of each row
   std::vector<int32_t> kvec;       // [3*n_k] (lattice mode: shell-sorted)
   std::vector<int32_t> shell_off;  // lattice mode
@@ -158,6 +160,7 @@ struct amdat_ctx {
   amdat::DevBuf<unsigned char> staging;
   std::vector<amdat::DevBuf<float2>*> rho_pool;        // released density tables
   std::map<std::string, amdat::LatticePlanDev*> lattice_plans;
+  std::map<std::string, amdat::SkAdjointPlan*> sk_adjoint_plans;  // by lattice key
 
   bool profiling = false;
   std::vector<amdat::ProfRec> prof_pending;
@@ -178,6 +181,7 @@ void check_launch(const char* what);
 DevBuf<float2>* rho_acquire(amdat_ctx* ctx, size_t count);
 void rho_release(amdat_ctx* ctx, DevBuf<float2>* b);
 void lattice_plans_free(amdat_ctx* ctx);
+void sk_adjoint_plans_free(amdat_ctx* ctx);
 void fixed_turns_launch(amdat_ctx* ctx, const int32_t* d_frames, int32_t n_frames, const ListEntry& e,
                         float period, int4* out);
 

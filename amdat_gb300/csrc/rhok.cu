@@ -539,6 +539,7 @@ amdat_status amdat_wave_density_lattice(amdat_ctx* ctx, int32_t list, float kmax
     d->n_frames = n_frames;
     d->n_shells = (int32_t)P.shell_off.size() - 1;
     d->period = period;
+    d->lattice_key = key;
     d->n_list = e.n;
     d->frames.assign(frames, frames + n_frames);
     d->kvec = P.kvec;

@@ -34,6 +34,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <vector>
 
 #include "engine.h"
@@ -282,6 +283,259 @@ __global__ void __launch_bounds__(SG_THREADS) gsmooth_adjoint_kernel(SGParams p)
 }
 
 // ---------------------------------------------------------------------------
+// cell lists: boxes at least three cutoffs wide on every axis are cut into
+// cells no smaller than the cutoff; an atom's partners within the cutoff lie
+// in its own or the 26 neighbouring cells (periodic).  Per frame the list's
+// atoms are counted into cells, scattered, and each cell's atoms are put in
+// ascending list order, so every loop below runs in a fixed order.
+// ---------------------------------------------------------------------------
+struct SGCells {
+  int3 nc;
+  float3 lo, inv_cell;
+  const int32_t* start;  // [n_cells + 1]
+  const int32_t* order;  // sorted slot -> list index
+  const float4* pos;     // sorted slot -> wrapped position
+};
+
+__device__ __forceinline__ int cell_axis(float x, float lo, float inv_cell, int n) {
+  const int c = (int)((x - lo) * inv_cell);
+  return min(max(c, 0), n - 1);
+}
+
+__global__ void cell_assign_kernel(const float* __restrict__ P, int64_t n_pad, SGList lst, float3 lo,
+                                   float3 inv_cell, int3 nc, int32_t* __restrict__ cell_of,
+                                   int32_t* __restrict__ count) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= lst.n) return;
+  const int a = sg_member(lst, i);
+  const int cx = cell_axis(P[a], lo.x, inv_cell.x, nc.x);
+  const int cy = cell_axis(P[n_pad + a], lo.y, inv_cell.y, nc.y);
+  const int cz = cell_axis(P[2 * n_pad + a], lo.z, inv_cell.z, nc.z);
+  const int c = (cz * nc.y + cy) * nc.x + cx;
+  cell_of[i] = c;
+  atomicAdd(count + c, 1);
+}
+
+// exclusive scan of count[0..n) into start[0..n] (one block)
+__global__ void cell_scan_kernel(const int32_t* __restrict__ count, int32_t n, int32_t* __restrict__ start,
+                                 int32_t* __restrict__ cursor) {
+  __shared__ int32_t s_part[1024];
+  __shared__ int32_t s_carry;
+  if (threadIdx.x == 0) s_carry = 0;
+  __syncthreads();
+  for (int base = 0; base < n; base += 1024) {
+    const int i = base + threadIdx.x;
+    s_part[threadIdx.x] = i < n ? count[i] : 0;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+      const int v = threadIdx.x >= off ? s_part[threadIdx.x - off] : 0;
+      __syncthreads();
+      s_part[threadIdx.x] += v;
+      __syncthreads();
+    }
+    if (i < n) {
+      const int excl = s_carry + s_part[threadIdx.x] - count[i];
+      start[i] = excl;
+      cursor[i] = excl;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) s_carry += s_part[1023];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) start[n] = s_carry;
+}
+
+__global__ void cell_scatter_kernel(const int32_t* __restrict__ cell_of, int32_t n, int32_t* __restrict__ cursor,
+                                    int32_t* __restrict__ order) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) order[atomicAdd(cursor + cell_of[i], 1)] = i;
+}
+
+// ascending list order inside each cell, then the sorted positions
+__global__ void cell_sort_kernel(const int32_t* __restrict__ start, int32_t n_cells, int32_t* __restrict__ order,
+                                 const float* __restrict__ P, int64_t n_pad, SGList lst, float4* __restrict__ pos) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n_cells) return;
+  const int b = start[c], e = start[c + 1];
+  for (int k = b + 1; k < e; ++k) {
+    const int v = order[k];
+    int m = k - 1;
+    while (m >= b && order[m] > v) {
+      order[m + 1] = order[m];
+      --m;
+    }
+    order[m + 1] = v;
+  }
+  for (int k = b; k < e; ++k) {
+    const int a = sg_member(lst, order[k]);
+    pos[k] = make_float4(P[a], P[n_pad + a], P[2 * n_pad + a], 0.f);
+  }
+}
+
+// neighbour cell `off` (0..26) of the cell holding p, periodic
+__device__ __forceinline__ int neighbour_cell(const SGCells& C, float4 p, int off) {
+  const int dx = off % 3 - 1, dy = (off / 3) % 3 - 1, dz = off / 9 - 1;
+  int cx = cell_axis(p.x, C.lo.x, C.inv_cell.x, C.nc.x) + dx;
+  int cy = cell_axis(p.y, C.lo.y, C.inv_cell.y, C.nc.y) + dy;
+  int cz = cell_axis(p.z, C.lo.z, C.inv_cell.z, C.nc.z) + dz;
+  cx += cx < 0 ? C.nc.x : (cx >= C.nc.x ? -C.nc.x : 0);
+  cy += cy < 0 ? C.nc.y : (cy >= C.nc.y ? -C.nc.y : 0);
+  cz += cz < 0 ? C.nc.z : (cz >= C.nc.z ? -C.nc.z : 0);
+  return (cz * C.nc.y + cy) * C.nc.x + cx;
+}
+
+// forward over cells: thread per sorted slot, partners j > i (list order) in
+// the 27 cells; queue and bins as in gsmooth_kernel
+__global__ void __launch_bounds__(SG_THREADS) gsmooth_cells_kernel(SGParams p, SGCells C, float qscale) {
+  extern __shared__ double sh_d[];
+  unsigned long long* sh_q = reinterpret_cast<unsigned long long*>(sh_d);
+  __shared__ float q_r[SG_WARPS][SG_Q];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int b = threadIdx.x; b < p.n_bins; b += blockDim.x) sh_q[b] = 0ull;
+  __syncthreads();
+  const int slot = blockIdx.x * SG_THREADS + threadIdx.x;
+  const bool live = slot < p.lst.n;
+  const int i = live ? C.order[slot] : -1;
+  const float4 pi = live ? C.pos[slot] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float inv2s2 = 0.5f / (p.sigma * p.sigma);
+  const float qnorm = qscale * INV_SQRT_2PI / p.sigma;
+  const bool recur = p.bin <= 2.0f * p.sigma;
+  const unsigned below = (1u << lane) - 1u;
+  auto flush = [&](int count) {
+    if (lane < count)
+      gauss_bins(p, q_r[warp][lane], inv2s2, recur, [&](int b, float, float G) {
+        atomicAdd(sh_q + b, (unsigned long long)__float2ll_rn(qnorm * G));
+      });
+  };
+  int qn = 0;
+  for (int off = 0; off < 27; ++off) {
+    const int nb = live ? neighbour_cell(C, pi, off) : 0;
+    const int cs = live ? C.start[nb] : 0, len = live ? C.start[nb + 1] - cs : 0;
+    const int maxlen = __reduce_max_sync(0xffffffffu, len);
+    for (int k = 0; k < maxlen; ++k) {
+      bool in = false;
+      float r2 = 0.f;
+      if (k < len) {
+        const int j = C.order[cs + k];
+        const float4 pj = C.pos[cs + k];
+        const float dx = min_image(pj.x - pi.x, p.box.x, p.inv_box.x);
+        const float dy = min_image(pj.y - pi.y, p.box.y, p.inv_box.y);
+        const float dz = min_image(pj.z - pi.z, p.box.z, p.inv_box.z);
+        r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        in = j > i && r2 < p.cut2;
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, in);
+      if (in) q_r[warp][qn + __popc(m & below)] = sqrtf(r2);
+      qn += __popc(m);
+      if (qn >= 32) {
+        __syncwarp();
+        flush(32);
+        __syncwarp();
+        if (lane < qn - 32) q_r[warp][lane] = q_r[warp][32 + lane];
+        __syncwarp();
+        qn -= 32;
+      }
+    }
+  }
+  __syncwarp();
+  flush(qn);
+  __syncthreads();
+  const double inv_q = 1.0 / (double)qscale;
+  for (int b = threadIdx.x; b < p.n_bins; b += blockDim.x)
+    if (sh_q[b]) atomicAdd(p.h + b, (double)sh_q[b] * inv_q);
+}
+
+// adjoint over cells: thread per sorted slot, every partner j != i in the 27
+// cells, owner-ordered sums as in gsmooth_adjoint_kernel
+__global__ void __launch_bounds__(SG_THREADS) gsmooth_cells_adjoint_kernel(SGParams p, SGCells C, int32_t frame) {
+  extern __shared__ double sh_d[];
+  float* sh_w = (float*)sh_d;
+  __shared__ float4 q_v[SG_WARPS][SG_Q];
+  __shared__ unsigned char q_o[SG_WARPS][SG_Q];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int b = threadIdx.x; b < p.n_bins; b += blockDim.x) sh_w[b] = (float)p.wgt[b];
+  __syncthreads();
+  const int slot = blockIdx.x * SG_THREADS + threadIdx.x;
+  const bool live = slot < p.lst.n;
+  const int i = live ? C.order[slot] : -1;
+  const float4 pi = live ? C.pos[slot] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float inv_s2 = 1.0f / (p.sigma * p.sigma);
+  const float inv2s2 = 0.5f * inv_s2;
+  const float scale = INV_SQRT_2PI / p.sigma * inv_s2;
+  const bool recur = p.bin <= 2.0f * p.sigma;
+  const unsigned below = (1u << lane) - 1u;
+  float g[3] = {0.f, 0.f, 0.f}, c[3] = {0.f, 0.f, 0.f};
+  auto flush = [&](int count) {
+    if (lane < count) {
+      const float4 v = q_v[warp][lane];
+      float psi = 0.f;
+      gauss_bins(p, v.w, inv2s2, recur, [&](int b, float x, float G) { psi = fmaf(sh_w[b] * x, G, psi); });
+      const float sc = psi * scale / v.w;
+      q_v[warp][lane] = make_float4(sc * v.x, sc * v.y, sc * v.z, 0.f);
+    }
+    __syncwarp();
+    float part[3] = {0.f, 0.f, 0.f};
+    for (int e = 0; e < count; ++e)
+      if (q_o[warp][e] == lane) {
+        const float4 v = q_v[warp][e];
+        part[0] += v.x;
+        part[1] += v.y;
+        part[2] += v.z;
+      }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const float y = __fsub_rn(part[d], c[d]), t = __fadd_rn(g[d], y);
+      c[d] = __fsub_rn(__fsub_rn(t, g[d]), y);
+      g[d] = t;
+    }
+  };
+  int qn = 0;
+  for (int off = 0; off < 27; ++off) {
+    const int nb = live ? neighbour_cell(C, pi, off) : 0;
+    const int cs = live ? C.start[nb] : 0, len = live ? C.start[nb + 1] - cs : 0;
+    const int maxlen = __reduce_max_sync(0xffffffffu, len);
+    for (int k = 0; k < maxlen; ++k) {
+      bool in = false;
+      float dx = 0.f, dy = 0.f, dz = 0.f, r2 = 0.f;
+      if (k < len) {
+        const int j = C.order[cs + k];
+        const float4 pj = C.pos[cs + k];
+        dx = min_image(pi.x - pj.x, p.box.x, p.inv_box.x);
+        dy = min_image(pi.y - pj.y, p.box.y, p.inv_box.y);
+        dz = min_image(pi.z - pj.z, p.box.z, p.inv_box.z);
+        r2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        in = j != i && r2 < p.cut2 && r2 > 0.f;
+      }
+      const unsigned m = __ballot_sync(0xffffffffu, in);
+      if (in) {
+        const int pos = qn + __popc(m & below);
+        q_v[warp][pos] = make_float4(dx, dy, dz, sqrtf(r2));
+        q_o[warp][pos] = (unsigned char)lane;
+      }
+      qn += __popc(m);
+      if (qn >= 32) {
+        __syncwarp();
+        flush(32);
+        __syncwarp();
+        if (lane < qn - 32) {
+          q_v[warp][lane] = q_v[warp][32 + lane];
+          q_o[warp][lane] = q_o[warp][32 + lane];
+        }
+        __syncwarp();
+        qn -= 32;
+      }
+    }
+  }
+  __syncwarp();
+  flush(qn);
+  if (live) {
+    float* out = p.grad + ((int64_t)frame * p.lst.n + i) * 3;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) out[d] = __fsub_rn(g[d], c[d]);
+  }
+}
+
+// ---------------------------------------------------------------------------
 // structure-factor adjoint
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void phase_sc(int32_t ph, float* s, float* c) {
@@ -523,6 +777,58 @@ static SkColumnsPlan build_columns(const std::vector<int32_t>& kvec) {
   return P;
 }
 
+// device tables of the S(k) adjoint for one vector list: the column plan
+// (when the columns average >= 8 vectors and holes are few) or the vectors
+// themselves; lattice densities keep theirs per lattice
+struct SkAdjointPlan {
+  bool columns = false;
+  int64_t n_slots = 0;
+  int32_t n_chunks = 0;
+  DevBuf<SkColumn> cols;
+  DevBuf<SkChunk> chunks;
+  DevBuf<int32_t> slot;
+  DevBuf<int4> kv;
+};
+
+void sk_adjoint_plans_free(amdat_ctx* ctx) {
+  for (auto& kv : ctx->sk_adjoint_plans) delete kv.second;
+  ctx->sk_adjoint_plans.clear();
+}
+
+static SkAdjointPlan* sk_adjoint_plan_build(const std::vector<int32_t>& kvec) {
+  const int nk = (int)(kvec.size() / 3);
+  auto* A = new SkAdjointPlan();
+  try {
+    SkColumnsPlan plan = build_columns(kvec);
+    A->columns = !plan.duplicates && plan.n_slots <= 2 * (int64_t)nk && (double)nk >= 8.0 * (double)plan.cols.size();
+    A->slot.reserve(std::max(nk, 1));
+    if (A->columns) {
+      A->n_slots = plan.n_slots;
+      A->n_chunks = (int32_t)plan.chunks.size();
+      A->cols.reserve(std::max<size_t>(plan.cols.size(), 1));
+      A->chunks.reserve(std::max<size_t>(plan.chunks.size(), 1));
+      AMDAT_CUDA(cudaMemcpy(A->cols.ptr, plan.cols.data(), plan.cols.size() * sizeof(SkColumn), cudaMemcpyHostToDevice));
+      AMDAT_CUDA(cudaMemcpy(A->chunks.ptr, plan.chunks.data(), plan.chunks.size() * sizeof(SkChunk), cudaMemcpyHostToDevice));
+      AMDAT_CUDA(cudaMemcpy(A->slot.ptr, plan.slot.data(), (size_t)nk * 4, cudaMemcpyHostToDevice));
+    } else {
+      A->n_slots = nk;
+      std::vector<int32_t> slot(nk);
+      std::vector<int4> hk(nk);
+      for (int k = 0; k < nk; ++k) {
+        slot[k] = k;
+        hk[k] = make_int4(kvec[3 * (size_t)k], kvec[3 * (size_t)k + 1], kvec[3 * (size_t)k + 2], 0);
+      }
+      A->kv.reserve(std::max(nk, 1));
+      AMDAT_CUDA(cudaMemcpy(A->kv.ptr, hk.data(), (size_t)nk * sizeof(int4), cudaMemcpyHostToDevice));
+      AMDAT_CUDA(cudaMemcpy(A->slot.ptr, slot.data(), (size_t)nk * 4, cudaMemcpyHostToDevice));
+    }
+  } catch (...) {
+    delete A;
+    throw;
+  }
+  return A;
+}
+
 static void sg_check(amdat_ctx* ctx, const int32_t* frames, int32_t n_frames, float sigma, float r_max,
                      int32_t n_bins) {
   if (!ctx->have_traj) throw Error(AMDAT_ERR_STATE, "no trajectory uploaded");
@@ -556,6 +862,50 @@ static SGParams sg_params(amdat_ctx* ctx, const ListEntry& e, const int32_t* d_f
 }
 
 static size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// cell grid for a cutoff: used when every axis holds at least three cells
+// (cell edge >= cutoff) and the list is large enough to gain from it
+static bool cell_grid(amdat_ctx* ctx, const ListEntry& e, float cut, int3& nc) {
+  nc = make_int3((int)std::floor(ctx->box[0] / cut), (int)std::floor(ctx->box[1] / cut),
+                 (int)std::floor(ctx->box[2] / cut));
+  const int64_t cells = (int64_t)nc.x * nc.y * nc.z;
+  return e.n >= 1024 && nc.x >= 3 && nc.y >= 3 && nc.z >= 3 && cells <= (1 << 22);
+}
+
+// builds one frame's cell lists in ctx->scratch2 and returns their view
+static SGCells build_cells(amdat_ctx* ctx, const ListEntry& e, int32_t frame, int3 nc) {
+  const int n = e.n, n_cells = nc.x * nc.y * nc.z;
+  size_t o = 0;
+  const size_t o_cell = o; o = align256(o + (size_t)n * 4);
+  const size_t o_cnt = o; o = align256(o + (size_t)n_cells * 4);
+  const size_t o_start = o; o = align256(o + (size_t)(n_cells + 1) * 4);
+  const size_t o_cur = o; o = align256(o + (size_t)n_cells * 4);
+  const size_t o_ord = o; o = align256(o + (size_t)n * 4);
+  const size_t o_pos = o; o = align256(o + (size_t)n * sizeof(float4));
+  unsigned char* b = ctx->scratch2.reserve(o);
+  const float* P = ctx->w.ptr + (int64_t)frame * 3 * ctx->n_pad;
+  SGCells C;
+  C.nc = nc;
+  C.lo = make_float3(ctx->box_lo[0], ctx->box_lo[1], ctx->box_lo[2]);
+  C.inv_cell = make_float3((float)nc.x / ctx->box[0], (float)nc.y / ctx->box[1], (float)nc.z / ctx->box[2]);
+  C.start = (const int32_t*)(b + o_start);
+  C.order = (const int32_t*)(b + o_ord);
+  C.pos = (const float4*)(b + o_pos);
+  cudaStream_t st = ctx->stream;
+  AMDAT_CUDA(cudaMemsetAsync(b + o_cnt, 0, (size_t)n_cells * 4, st));
+  const unsigned gn = (unsigned)ceil_div(n, 256), gc = (unsigned)ceil_div(n_cells, 256);
+  cell_assign_kernel<<<gn, 256, 0, st>>>(P, ctx->n_pad, sglist(e), C.lo, C.inv_cell, nc, (int32_t*)(b + o_cell),
+                                         (int32_t*)(b + o_cnt));
+  cell_scan_kernel<<<1, 1024, 0, st>>>((const int32_t*)(b + o_cnt), n_cells, (int32_t*)(b + o_start),
+                                       (int32_t*)(b + o_cur));
+  cell_scatter_kernel<<<gn, 256, 0, st>>>((const int32_t*)(b + o_cell), n, (int32_t*)(b + o_cur),
+                                          (int32_t*)(b + o_ord));
+  cell_sort_kernel<<<gc, 256, 0, st>>>((const int32_t*)(b + o_start), n_cells, (int32_t*)(b + o_ord), P,
+                                       ctx->n_pad, sglist(e), (float4*)(b + o_pos));
+  check_launch("cell lists");
+  count_launch(ctx, 4);
+  return C;
+}
 
 // dynamic shared memory beyond what fits beside the static arrays under the
 // default 48 KB needs the opt-in attribute
@@ -593,12 +943,24 @@ amdat_status amdat_gsmooth_run(amdat_ctx* ctx, int32_t list, const int32_t* fram
       const double bound = (double)SG_THREADS * (double)e.n * (double)INV_SQRT_2PI / (double)sigma;
       const float qscale = (float)std::ldexp(1.0, (int)std::floor(std::log2(std::ldexp(1.0, 62) / bound)));
       const size_t shm = (size_t)n_bins * 8;
-      set_smem((const void*)gsmooth_kernel, shm);
-      dim3 grid((unsigned)ceil_div(e.n, SG_THREADS), (unsigned)n_frames);
-      KernelTimer kt(ctx, "gsmooth_kernel");
-      gsmooth_kernel<<<grid, SG_THREADS, shm, ctx->stream>>>(p, qscale);
-      check_launch("gsmooth_kernel");
-      count_launch(ctx);
+      int3 nc;
+      if (cell_grid(ctx, e, std::sqrt(p.cut2), nc)) {
+        set_smem((const void*)gsmooth_cells_kernel, shm);
+        for (int f = 0; f < n_frames; ++f) {
+          const SGCells C = build_cells(ctx, e, frames[f], nc);
+          KernelTimer kt(ctx, "gsmooth_kernel");
+          gsmooth_cells_kernel<<<(unsigned)ceil_div(e.n, SG_THREADS), SG_THREADS, shm, ctx->stream>>>(p, C, qscale);
+          check_launch("gsmooth_cells_kernel");
+          count_launch(ctx);
+        }
+      } else {
+        set_smem((const void*)gsmooth_kernel, shm);
+        dim3 grid((unsigned)ceil_div(e.n, SG_THREADS), (unsigned)n_frames);
+        KernelTimer kt(ctx, "gsmooth_kernel");
+        gsmooth_kernel<<<grid, SG_THREADS, shm, ctx->stream>>>(p, qscale);
+        check_launch("gsmooth_kernel");
+        count_launch(ctx);
+      }
     }
     if (!dev) AMDAT_CUDA(cudaMemcpyAsync(h, d_h, (size_t)n_bins * 8, cudaMemcpyDeviceToHost, ctx->stream));
     AMDAT_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -628,12 +990,25 @@ amdat_status amdat_gsmooth_adjoint(amdat_ctx* ctx, int32_t list, const int32_t* 
       p.wgt = d_w;
       p.grad = d_g;
       const size_t shm = (size_t)n_bins * 4;
-      set_smem((const void*)gsmooth_adjoint_kernel, shm);
-      dim3 grid((unsigned)ceil_div(e.n, SG_THREADS), (unsigned)n_frames);
-      KernelTimer kt(ctx, "gsmooth_adjoint_kernel");
-      gsmooth_adjoint_kernel<<<grid, SG_THREADS, shm, ctx->stream>>>(p);
-      check_launch("gsmooth_adjoint_kernel");
-      count_launch(ctx);
+      int3 nc;
+      if (cell_grid(ctx, e, std::sqrt(p.cut2), nc)) {
+        set_smem((const void*)gsmooth_cells_adjoint_kernel, shm);
+        for (int f = 0; f < n_frames; ++f) {
+          const SGCells C = build_cells(ctx, e, frames[f], nc);
+          KernelTimer kt(ctx, "gsmooth_adjoint_kernel");
+          gsmooth_cells_adjoint_kernel<<<(unsigned)ceil_div(e.n, SG_THREADS), SG_THREADS, shm, ctx->stream>>>(
+              p, C, f);
+          check_launch("gsmooth_cells_adjoint_kernel");
+          count_launch(ctx);
+        }
+      } else {
+        set_smem((const void*)gsmooth_adjoint_kernel, shm);
+        dim3 grid((unsigned)ceil_div(e.n, SG_THREADS), (unsigned)n_frames);
+        KernelTimer kt(ctx, "gsmooth_adjoint_kernel");
+        gsmooth_adjoint_kernel<<<grid, SG_THREADS, shm, ctx->stream>>>(p);
+        check_launch("gsmooth_adjoint_kernel");
+        count_launch(ctx);
+      }
     }
     if (!dev && gbytes) AMDAT_CUDA(cudaMemcpyAsync(grad, d_g, gbytes, cudaMemcpyDeviceToHost, ctx->stream));
     AMDAT_CUDA(cudaStreamSynchronize(ctx->stream));
@@ -679,30 +1054,22 @@ amdat_status amdat_structure_factor_adjoint(amdat_ctx* ctx, int32_t density_hand
       AMDAT_CUDA(cudaStreamSynchronize(ctx->stream));
       return;
     }
-    // the column kernel when columns average >= 8 vectors and holes are few
-    SkColumnsPlan plan = build_columns(d.kvec);
-    const bool columns = !plan.duplicates && plan.n_slots <= 2 * (int64_t)nk &&
-                         (double)nk >= 8.0 * (double)plan.cols.size();
-    const int64_t n_slots = columns ? plan.n_slots : nk;
-    std::vector<int32_t> slot;
-    std::vector<int4> hk;
-    if (columns) {
-      slot = std::move(plan.slot);
+    // the adjoint plan: kept per lattice, built per call for explicit lists
+    std::unique_ptr<SkAdjointPlan> own;
+    SkAdjointPlan* A = nullptr;
+    if (!d.lattice_key.empty()) {
+      auto it = ctx->sk_adjoint_plans.find(d.lattice_key);
+      if (it == ctx->sk_adjoint_plans.end())
+        it = ctx->sk_adjoint_plans.emplace(d.lattice_key, sk_adjoint_plan_build(d.kvec)).first;
+      A = it->second;
     } else {
-      slot.resize(nk);
-      hk.resize(nk);
-      for (int k = 0; k < nk; ++k) {
-        slot[k] = k;
-        hk[k] = make_int4(d.kvec[3 * (size_t)k], d.kvec[3 * (size_t)k + 1], d.kvec[3 * (size_t)k + 2], 0);
-      }
+      own.reset(sk_adjoint_plan_build(d.kvec));
+      A = own.get();
     }
+    const int64_t n_slots = A->n_slots;
     size_t o = 0;
     const size_t o_fr = o; o = align256(o + (size_t)F * 4);
     const size_t o_u = o; o = align256(o + (size_t)nk * 4);
-    const size_t o_sl = o; o = align256(o + (size_t)nk * 4);
-    const size_t o_k = o; o = align256(o + hk.size() * sizeof(int4));
-    const size_t o_col = o; o = align256(o + (columns ? plan.cols.size() * sizeof(SkColumn) : 0));
-    const size_t o_ch = o; o = align256(o + (columns ? plan.chunks.size() * sizeof(SkChunk) : 0));
     const size_t o_fx = o; o = align256(o + (size_t)F * n * sizeof(int4));
     const size_t o_c = o; o = align256(o + (size_t)F * n_slots * sizeof(float2));
     const size_t o_g = o; o = align256(o + (dev ? 0 : gbytes));
@@ -710,37 +1077,28 @@ amdat_status amdat_structure_factor_adjoint(amdat_ctx* ctx, int32_t density_hand
     cudaStream_t st = ctx->stream;
     AMDAT_CUDA(cudaMemcpyAsync(base + o_fr, d.frames.data(), (size_t)F * 4, cudaMemcpyHostToDevice, st));
     AMDAT_CUDA(cudaMemcpyAsync(base + o_u, u.data(), (size_t)nk * 4, cudaMemcpyHostToDevice, st));
-    AMDAT_CUDA(cudaMemcpyAsync(base + o_sl, slot.data(), (size_t)nk * 4, cudaMemcpyHostToDevice, st));
-    if (columns) {
-      AMDAT_CUDA(cudaMemcpyAsync(base + o_col, plan.cols.data(), plan.cols.size() * sizeof(SkColumn),
-                                 cudaMemcpyHostToDevice, st));
-      AMDAT_CUDA(cudaMemcpyAsync(base + o_ch, plan.chunks.data(), plan.chunks.size() * sizeof(SkChunk),
-                                 cudaMemcpyHostToDevice, st));
-    } else {
-      AMDAT_CUDA(cudaMemcpyAsync(base + o_k, hk.data(), hk.size() * sizeof(int4), cudaMemcpyHostToDevice, st));
-    }
     float2* coef = (float2*)(base + o_c);
-    if (columns) AMDAT_CUDA(cudaMemsetAsync(coef, 0, (size_t)F * n_slots * sizeof(float2), st));
+    if (A->columns) AMDAT_CUDA(cudaMemsetAsync(coef, 0, (size_t)F * n_slots * sizeof(float2), st));
     const int64_t tot = (int64_t)F * nk;
     sk_coef_kernel<<<(unsigned)std::min<int64_t>(ceil_div(tot, 256), (int64_t)ctx->n_sm * 16), 256, 0, st>>>(
-        d.rho->ptr, nk, F, (const int32_t*)(base + o_sl), (const float*)(base + o_u), n_slots, coef);
+        d.rho->ptr, nk, F, A->slot.ptr, (const float*)(base + o_u), n_slots, coef);
     check_launch("sk_coef_kernel");
     count_launch(ctx);
     fixed_turns_launch(ctx, (const int32_t*)(base + o_fr), F, e, d.period, (int4*)(base + o_fx));
     float* d_g = dev ? grad : (float*)(base + o_g);
     const float scale = (float)(6.283185307179586476925286766559 / (double)d.period);
-    if (columns) {
+    if (A->columns) {
       dim3 grid((unsigned)ceil_div(n, SKC_ATOMS), (unsigned)F);
       KernelTimer kt(ctx, "sk_adjoint_columns_kernel");
-      sk_adjoint_columns_kernel<<<grid, SKC_THREADS, 0, st>>>(
-          (const int4*)(base + o_fx), n, (const SkColumn*)(base + o_col), (const SkChunk*)(base + o_ch),
-          (int32_t)plan.chunks.size(), coef, n_slots, scale, d_g);
+      sk_adjoint_columns_kernel<<<grid, SKC_THREADS, 0, st>>>((const int4*)(base + o_fx), n, A->cols.ptr,
+                                                              A->chunks.ptr, A->n_chunks, coef, n_slots,
+                                                              scale, d_g);
       check_launch("sk_adjoint_columns_kernel");
     } else {
       dim3 grid((unsigned)ceil_div(n, SKD_THREADS), (unsigned)F);
       KernelTimer kt(ctx, "sk_adjoint_direct_kernel");
-      sk_adjoint_direct_kernel<<<grid, SKD_THREADS, 0, st>>>((const int4*)(base + o_fx), n,
-                                                             (const int4*)(base + o_k), nk, coef, scale, d_g);
+      sk_adjoint_direct_kernel<<<grid, SKD_THREADS, 0, st>>>((const int4*)(base + o_fx), n, A->kv.ptr, nk,
+                                                             coef, scale, d_g);
       check_launch("sk_adjoint_direct_kernel");
     }
     count_launch(ctx);

@@ -34,8 +34,13 @@ def _rel(a, b):
     return np.abs(a - b).max() / np.abs(b).max()
 
 
-def test_gsmooth_forward_matches_oracle(eng):
-    L, F, n = 12.0, 2, 1500
+# (box, atoms): all partners (box under three cutoffs wide), and cell lists
+GS_CASES = [(12.0, 1500), (16.0, 3000)]
+
+
+@pytest.mark.parametrize("L,n", GS_CASES)
+def test_gsmooth_forward_matches_oracle(eng, L, n):
+    F = 2
     pos = _pos(F, n, L, 11)
     _upload(eng, pos, L)
     h = eng.gsmooth(0, [0, 1], SIGMA, R_MAX, N_BINS)
@@ -49,8 +54,9 @@ def test_gsmooth_forward_matches_oracle(eng):
     assert _rel(h2, ref2) <= 1e-4
 
 
-def test_gsmooth_adjoint_matches_oracle(eng):
-    L, F, n = 12.0, 2, 1500
+@pytest.mark.parametrize("L,n", GS_CASES)
+def test_gsmooth_adjoint_matches_oracle(eng, L, n):
+    F = 2
     pos = _pos(F, n, L, 12)
     _upload(eng, pos, L)
     w = np.random.default_rng(13).standard_normal(N_BINS)
@@ -59,14 +65,14 @@ def test_gsmooth_adjoint_matches_oracle(eng):
     assert _rel(g, ref) <= 5e-4
 
 
-def test_gsmooth_adjoint_matches_fd(eng):
-    L, n = 12.0, 600
+@pytest.mark.parametrize("L,n", [(12.0, 600), (14.0, 1200)])
+def test_gsmooth_adjoint_matches_fd(eng, L, n):
     pos = _pos(1, n, L, 14)
     _upload(eng, pos, L)
     w = np.random.default_rng(15).standard_normal(N_BINS)
     g = eng.gsmooth_adjoint(0, [0], SIGMA, R_MAX, N_BINS, w, n)
     scale = np.abs(g).max()
-    for (i, c) in [(0, 0), (101, 1), (377, 2), (599, 0)]:
+    for (i, c) in [(0, 0), (101, 1), (377, 2), (n - 1, 0)]:
         vals = []
         for sgn in (1, -1):
             p = pos.copy()
