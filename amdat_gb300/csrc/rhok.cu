@@ -35,6 +35,7 @@
 #include <numeric>
 
 #include "engine.h"
+#include "tc_tiles.h"
 
 namespace amdat {
 
@@ -383,9 +384,6 @@ struct LatticePlan {
 
 }  // namespace amdat
 namespace amdat {
-struct TcPlan;
-TcPlan* tc_plan_build(const std::vector<int32_t>& kvec);
-void tc_plan_free(TcPlan* p);
 void rhok_tc_run(amdat_ctx* ctx, const TcPlan& P, const int4* fx, int32_t n_list, int32_t n_frames,
                  int32_t n_k, float2* rho);
 
@@ -403,6 +401,13 @@ void lattice_plans_free(amdat_ctx* ctx) {
   ctx->lattice_plans.clear();
 }
 
+TcPlan* lattice_tc_plan(amdat_ctx* ctx, const std::string& lattice_key) {
+  auto it = ctx->lattice_plans.find(lattice_key);
+  AMDAT_REQUIRE(it != ctx->lattice_plans.end(), "lattice plan not found");
+  if (!it->second->tc) it->second->tc = tc_plan_build(it->second->kvec);
+  return it->second->tc;
+}
+
 // tcgen05 kernel on compute capability 10.x unless AMDAT_RHOK_KERNEL=fp32
 static bool use_tensor_cores(amdat_ctx* ctx) {
   const char* e = std::getenv("AMDAT_RHOK_KERNEL");
@@ -411,6 +416,8 @@ static bool use_tensor_cores(amdat_ctx* ctx) {
   AMDAT_CUDA(cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, ctx->device));
   return major == 10;
 }
+
+bool tc_enabled(amdat_ctx* ctx) { return use_tensor_cores(ctx); }
 
 static LatticePlan plan_lattice(float kmax, float dk, float period) {
   const double two_pi = 6.283185307179586476925286766559;

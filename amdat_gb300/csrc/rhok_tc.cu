@@ -36,6 +36,7 @@
 #include <vector>
 
 #include "engine.h"
+#include "tc_tiles.h"
 #include "umma.cuh"
 
 namespace amdat {
@@ -63,10 +64,6 @@ constexpr uint32_t TC_WAIT = 1u << 19;                // try_wait calls of <= 1 
 constexpr uint32_t TC_COL_ACC = 0, TC_COL_S = 2 * TC_NMAX, TC_COL_C = 3 * TC_NMAX;
 constexpr uint32_t TC_TMEM_COLS = 4 * TC_NMAX;        // 512
 
-struct TcTile {
-  int32_t nx0, ny0, zblk, entry0;  // entry map: TC_ROWS * n ints from entry0
-  int32_t n, pad0, pad1, pad2;     // MMA N of this tile (multiple of 16, <= TC_NMAX)
-};
 
 struct TcSmem {
   unsigned char z[TC_SZ][TC_STAGE];     // [stage] Z hi, Z lo, X, Y; the epilogue stages D here
@@ -406,12 +403,6 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 // ---------------------------------------------------------------------------
 // host: tile plan over the shell-sorted vector list, launches per frame batch
 // ---------------------------------------------------------------------------
-struct TcPlan {
-  DevBuf<TcTile> tiles;
-  DevBuf<int32_t> entry_k;
-  int32_t n_tiles = 0, n_zblk = 0, nzw = 0, nmax = 0;
-  int64_t entries = 0;  // rows x columns computed per frame and atom, padding included
-};
 
 static bool tc_half_space(int nx, int ny, int nz) {
   return nz > 0 || (nz == 0 && (ny > 0 || (ny == 0 && nx > 0)));
@@ -466,6 +457,7 @@ TcPlan* tc_plan_build(const std::vector<int32_t>& kvec) {
   p->nzw = nzw;
   p->nmax = nmax;
   p->entries = computed;
+  p->host_tiles = tiles;
   p->tiles.reserve(std::max<size_t>(tiles.size(), 1));
   p->entry_k.reserve(std::max<size_t>(entries.size(), 1));
   if (!tiles.empty()) {

@@ -32,14 +32,20 @@
 // Kahan-compensated FP32 accumulators.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <map>
 #include <memory>
 #include <vector>
 
 #include "engine.h"
+#include "tc_tiles.h"
 
 namespace amdat {
+
+void sk_adjoint_tc_run(amdat_ctx* ctx, const TcPlan& P, const int4* fx, int32_t n, int32_t F,
+                       const float2* rho, int32_t n_k, const float* d_u, float max_u, float period,
+                       float* grad);
 
 struct SGList {
   int32_t n;
@@ -1052,6 +1058,27 @@ amdat_status amdat_structure_factor_adjoint(amdat_ctx* ctx, int32_t density_hand
         else std::memset(grad, 0, gbytes);
       }
       AMDAT_CUDA(cudaStreamSynchronize(ctx->stream));
+      return;
+    }
+    // lattice densities on compute capability 10.x: the tensor-core adjoint
+    // (AMDAT_SK_ADJOINT=columns selects the FP32 column kernel instead)
+    const char* sel = std::getenv("AMDAT_SK_ADJOINT");
+    if (!d.lattice_key.empty() && tc_enabled(ctx) && !(sel && std::strcmp(sel, "columns") == 0)) {
+      TcPlan* tp = lattice_tc_plan(ctx, d.lattice_key);
+      float max_u = 0.f;
+      for (int k = 0; k < nk; ++k) max_u = std::max(max_u, std::fabs(u[k]));
+      const size_t o_fr = 0, o_u = align256((size_t)F * 4), o_fx = align256(o_u + (size_t)nk * 4);
+      const size_t o_g = align256(o_fx + (size_t)F * n * sizeof(int4));
+      unsigned char* base = ctx->scratch.reserve(o_g + (dev ? 0 : gbytes));
+      cudaStream_t st = ctx->stream;
+      AMDAT_CUDA(cudaMemcpyAsync(base + o_fr, d.frames.data(), (size_t)F * 4, cudaMemcpyHostToDevice, st));
+      AMDAT_CUDA(cudaMemcpyAsync(base + o_u, u.data(), (size_t)nk * 4, cudaMemcpyHostToDevice, st));
+      fixed_turns_launch(ctx, (const int32_t*)(base + o_fr), F, e, d.period, (int4*)(base + o_fx));
+      float* d_g = dev ? grad : (float*)(base + o_g);
+      sk_adjoint_tc_run(ctx, *tp, (const int4*)(base + o_fx), n, F, d.rho->ptr, nk, (const float*)(base + o_u),
+                        max_u, d.period, d_g);
+      if (!dev) AMDAT_CUDA(cudaMemcpyAsync(grad, d_g, gbytes, cudaMemcpyDeviceToHost, st));
+      AMDAT_CUDA(cudaStreamSynchronize(st));
       return;
     }
     // the adjoint plan: kept per lattice, built per call for explicit lists

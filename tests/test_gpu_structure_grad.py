@@ -173,3 +173,21 @@ def test_torch_autograd_structure_loss():
     # forward values against the oracle as well
     h_ref = orc.gsmooth(pos_np, box, lst, list(range(F)), SIGMA, R_MAX, N_BINS)
     assert _rel(g.detach().cpu().numpy() * ideal, h_ref) <= 1e-4
+
+
+@pytest.mark.parametrize("L,kmax,n", [(12.0, 12.0, 1200), (25.0, 35.5, 300)])
+def test_sk_adjoint_tensor_cores_match_column_kernel(eng, monkeypatch, L, kmax, n):
+    """The tensor-core adjoint (default for lattice densities) against the FP32
+    column kernel on the same density, including a lattice with two nz windows."""
+    F = 2
+    pos = _pos(F, n, L, 27)
+    _upload(eng, pos, L)
+    d, nk, ns = eng.wave_density_lattice(0, kmax, 0.1, L, [0, 1])
+    kv, off = eng.wave_density_vectors(d, nk, ns)
+    w = np.random.default_rng(28).standard_normal(ns)
+    g_tc = eng.structure_factor_adjoint(d, off, w, F, n)
+    monkeypatch.setenv("AMDAT_SK_ADJOINT", "columns")
+    g_col = eng.structure_factor_adjoint(d, off, w, F, n)
+    monkeypatch.delenv("AMDAT_SK_ADJOINT")
+    eng.wave_density_free(d)
+    assert _rel(g_tc, g_col) <= 5e-4
