@@ -314,7 +314,7 @@ def structure_bench(torch, stream, device, args, n_atoms=100000, box=48.9, frame
     launches = (ext.launch_count(device) - n0) // args.steps
     kern = {}
     for name in ("gsmooth_kernel", "gsmooth_adjoint_kernel", "rhok_tc_kernel", "rhok_lattice_kernel",
-                 "sk_frames_kernel", "sk_adjoint_columns_kernel"):
+                 "sk_frames_kernel", "sk_adjoint_columns_kernel", "sk_adjoint_tc_kernel"):
         n, t = ext.profile_kernel(name, device)
         if n:
             kern[name] = t / args.steps
@@ -349,6 +349,16 @@ def structure_bench(torch, stream, device, args, n_atoms=100000, box=48.9, frame
         out["gsmooth_pairs_per_s"] = pairs / (kern["gsmooth_kernel"] / 1e3)
     if "gsmooth_adjoint_kernel" in kern:
         out["gsmooth_adjoint_ordered_pairs_per_s"] = 2 * pairs / (kern["gsmooth_adjoint_kernel"] / 1e3)
+    if "sk_adjoint_tc_kernel" in kern:
+        r = frames * n_atoms * nk / (kern["sk_adjoint_tc_kernel"] / 1e3)
+        peak = measured_peaks().get("bf16_tflops_sustained", 1700.0)
+        out["sk_adjoint_atom_k_per_s"] = r
+        out["sk_adjoint_roofline"] = {
+            "bound": "tensor", "achieved": 16 * r / 1e12, "peak": peak, "unit": "TFLOP/s",
+            "frac": 16 * r / 1e12 / peak,
+            "rule": "16 flops per atom x vector (one complex MAC for T and one for the nz-weighted T'); "
+                    "the kernel issues 3 FP16 split passes over whole tiles; peak = measured sustained "
+                    "bf16/fp16 dense rate"}
     if "sk_adjoint_columns_kernel" in kern:
         r = frames * n_atoms * nk / (kern["sk_adjoint_columns_kernel"] / 1e3)
         out["sk_adjoint_atom_k_per_s"] = r
