@@ -118,10 +118,12 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// X/Y table slot of (atom j, entry m) inside a 32-atom block: rotating each
-// atom's 8 entries by 2*(j%4) makes a warp's reads (8 entries x 4 atoms,
-// 8-byte words) free of bank conflicts
-__device__ __forceinline__ int xy_slot(int j, int m) { return j * 8 + ((m + 2 * (j & 3)) & 7); }
+// X/Y table of a 32-atom block: 8 rows (lattice index offset m) of 16 chunks
+// of 16 bytes, chunk = two atoms' (cos, sin).  Atom pair p = j / 2 of row m
+// sits in chunk 16 m + ((m + p) & 15): a builder warp's 128-bit loads (8
+// rows x 4 atom quads, or one row broadcast) are then free of bank conflicts.
+// Returns the float2 index of (atom j, row m).
+__device__ __forceinline__ int xy_slot(int j, int m) { return 2 * (16 * m + ((m + (j >> 1)) & 15)) + (j & 1); }
 
 // X and Y phase tables of one frame batch: for axis a (0 = x, 1 = y), block b
 // of 8 lattice indices (n = -nmax + 8 b + m) and chunk c of 32 atoms, a 2 KB
@@ -342,30 +344,41 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         if (btid == 0) S.bad = 1;
         break;
       }
-      const float2* X = reinterpret_cast<const float2*>(S.z[sz] + 2 * TC_ZHALF);
-      const float2* Y = X + TC_J * 8;
-      // A operand: lane = (row % 8) * 4 + (atom % 4), conflict-free 4-byte stores
+      // A operand: thread = complex row r (nx = r % 8 = lane % 8, ny = r / 8) and
+      // the atom quad q (atoms 4q..4q+3): two 128-bit loads each of X and Y,
+      // four 128-bit stores (hi and lo of the real row [Wr, -Wi] and of the
+      // imaginary row [Wi, Wr]), all free of bank conflicts
+      const float4* X4 = reinterpret_cast<const float4*>(S.z[sz] + 2 * TC_ZHALF);
+      const float4* Y4 = X4 + TC_J * 8 / 2;
+      {
+        const int m = lane & 7, rg = bw >> 1, q = (bw & 1) * 4 + (lane >> 3);
+        const int r = rg * 8 + m;
+        const float4 xa = X4[16 * m + ((m + 2 * q) & 15)], xb = X4[16 * m + ((m + 2 * q + 1) & 15)];
+        const float4 ya = Y4[16 * rg + ((rg + 2 * q) & 15)], yb = Y4[16 * rg + ((rg + 2 * q + 1) & 15)];
+        const float xr[4] = {xa.x, xa.z, xb.x, xb.z}, xi[4] = {xa.y, xa.w, xb.y, xb.w};
+        const float yr[4] = {ya.x, ya.z, yb.x, yb.z}, yi[4] = {ya.y, ya.w, yb.y, yb.w};
+        uint32_t hre[4], lre[4], him[4], lim[4];
 #pragma unroll
-      for (int it = 0; it < 4; ++it) {
-        const int combo = bw * 4 + it;  // 0..63
-        const int rg = combo >> 3, jg = combo & 7;
-        const int r = rg * 8 + (lane >> 2);   // complex row: nx = r % 8, ny = r / 8
-        const int j = jg * 4 + (lane & 3);
-        const float2 x = X[xy_slot(j, r & 7)], y = Y[xy_slot(j, r >> 3)];
-        const float wr = fmaf(x.x, y.x, -x.y * y.y), wi = fmaf(x.x, y.y, x.y * y.x);
-        // hi = fp16(w), lo = fp16(w - hi), both as (re, im) half2 pairs
-        const __half2 hi = __floats2half2_rn(wr, wi);
-        const float2 hb = __half22float2(hi);
-        const __half2 lo = __floats2half2_rn(__fsub_rn(wr, hb.x), __fsub_rn(wi, hb.y));
-        const uint32_t h = *reinterpret_cast<const uint32_t*>(&hi);
-        const uint32_t l = *reinterpret_cast<const uint32_t*>(&lo);
-        const uint32_t o_re = umma::kmajor_offset(r, 2 * j, TC_K);
-        const uint32_t o_im = o_re + (uint32_t)(TC_ROWS / 8) * (TC_K / 8) * 128;  // row r + 64
-        // real rows (Wr, -Wi): flip the sign of the high half; imaginary rows (Wi, Wr): swap halves
-        *reinterpret_cast<uint32_t*>(S.a[sa][0] + o_re) = h ^ 0x80000000u;
-        *reinterpret_cast<uint32_t*>(S.a[sa][1] + o_re) = l ^ 0x80000000u;
-        *reinterpret_cast<uint32_t*>(S.a[sa][0] + o_im) = __byte_perm(h, 0, 0x1032);
-        *reinterpret_cast<uint32_t*>(S.a[sa][1] + o_im) = __byte_perm(l, 0, 0x1032);
+        for (int a = 0; a < 4; ++a) {
+          const float wr = fmaf(xr[a], yr[a], -xi[a] * yi[a]);
+          const float nwi = fmaf(-xr[a], yi[a], -xi[a] * yr[a]);  // -Im W
+          // hi = fp16(w), lo = fp16(w - hi) of the real row (Wr, -Wi); the
+          // imaginary row (Wi, Wr) is the same pair swapped with the first
+          // element negated (round to nearest is symmetric)
+          const __half2 hi = __floats2half2_rn(wr, nwi);
+          const float2 hb = __half22float2(hi);
+          const __half2 lo = __floats2half2_rn(__fsub_rn(wr, hb.x), __fsub_rn(nwi, hb.y));
+          hre[a] = *reinterpret_cast<const uint32_t*>(&hi);
+          lre[a] = *reinterpret_cast<const uint32_t*>(&lo);
+          him[a] = __byte_perm(hre[a], 0, 0x1032) ^ 0x00008000u;
+          lim[a] = __byte_perm(lre[a], 0, 0x1032) ^ 0x00008000u;
+        }
+        const uint32_t o_re = (uint32_t)(((r >> 3) * 8 + q) * 128 + (r & 7) * 16);  // K = 8q..8q+7
+        const uint32_t o_im = o_re + (uint32_t)(TC_ROWS / 8) * (TC_K / 8) * 128;   // row r + 64
+        *reinterpret_cast<uint4*>(S.a[sa][0] + o_re) = make_uint4(hre[0], hre[1], hre[2], hre[3]);
+        *reinterpret_cast<uint4*>(S.a[sa][1] + o_re) = make_uint4(lre[0], lre[1], lre[2], lre[3]);
+        *reinterpret_cast<uint4*>(S.a[sa][0] + o_im) = make_uint4(him[0], him[1], him[2], him[3]);
+        *reinterpret_cast<uint4*>(S.a[sa][1] + o_im) = make_uint4(lim[0], lim[1], lim[2], lim[3]);
       }
       umma::fence_proxy_async_smem();
       umma::mbar_arrive(&S.full_a[sa]);
