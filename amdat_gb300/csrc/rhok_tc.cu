@@ -47,8 +47,7 @@ constexpr int TC_ROWS = 64;                   // complex rows (8 nx x 8 ny)
 constexpr int TC_NMAX = 128;                  // widest nz window (MMA N)
 constexpr int TC_M = 2 * TC_ROWS;             // MMA M = 128
 constexpr int TC_GROUP = 2;                   // chunks per tensor-memory accumulation
-constexpr int TC_SZ = 3;                      // Z ring stages
-constexpr int TC_SA = 2;                      // A ring stages
+constexpr int TC_S = 3;                       // ring stages (Z, X, Y and the A operand of one chunk)
 constexpr int TC_PRODUCER_WARP = 4;
 constexpr int TC_MMA_WARP = 5;
 constexpr int TC_BUILD_WARP0 = 6;
@@ -66,10 +65,10 @@ constexpr uint32_t TC_TMEM_COLS = 4 * TC_NMAX;        // 512
 
 
 struct TcSmem {
-  unsigned char z[TC_SZ][TC_STAGE];     // [stage] Z hi, Z lo, X, Y; the epilogue stages D here
-  unsigned char a[TC_SA][2][TC_A_BYTES]; // [stage][hi|lo]
-  uint64_t full_z[TC_SZ], empty_z[TC_SZ];
-  uint64_t full_a[TC_SA], empty_a[TC_SA];
+  unsigned char z[TC_S][TC_STAGE];      // [stage] Z hi, Z lo, X, Y; the epilogue stages D here
+  unsigned char a[TC_S][2][TC_A_BYTES];  // [stage][hi|lo]
+  uint64_t full_z[TC_S], full_a[TC_S];  // bulk copies landed / A built
+  uint64_t empty[TC_S];                 // the stage's MMAs finished (one commit per chunk)
   uint64_t full_acc[2], empty_acc[2];
   uint64_t mma_done;
   uint32_t tmem;
@@ -177,13 +176,10 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const int n_groups = (n_chunks + TC_GROUP - 1) / TC_GROUP;
 
   if (tid == 0) {
-    for (int s = 0; s < TC_SZ; ++s) {
+    for (int s = 0; s < TC_S; ++s) {
       umma::mbar_init(&S.full_z[s], 1);
-      umma::mbar_init(&S.empty_z[s], 1);
-    }
-    for (int s = 0; s < TC_SA; ++s) {
       umma::mbar_init(&S.full_a[s], TC_BUILDERS);
-      umma::mbar_init(&S.empty_a[s], 1);
+      umma::mbar_init(&S.empty[s], 1);
     }
     for (int b = 0; b < 2; ++b) {
       umma::mbar_init(&S.full_acc[b], 1);
@@ -206,12 +202,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   const uint32_t tmem = S.tmem;
 
   if (warp == TC_PRODUCER_WARP) {
-    // ---- producer: Z(c) into ring stage c % TC_SZ once the MMAs of c - TC_SZ are done
+    // ---- producer: Z(c), X(c), Y(c) into ring stage c % TC_S once the MMAs of c - TC_S are done
     if (lane == 0) {
       int c = 0;
       for (; c < n_chunks; ++c) {
-        const int s = c % TC_SZ;
-        if (S.bad || !umma::mbar_wait(&S.empty_z[s], ((c / TC_SZ) & 1) ^ 1, TC_WAIT)) {
+        const int s = c % TC_S;
+        if (S.bad || !umma::mbar_wait(&S.empty[s], ((c / TC_S) & 1) ^ 1, TC_WAIT)) {
           S.bad = 1;
           break;
         }
@@ -229,35 +225,39 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     if (lane == 0) {
       const uint32_t idesc = umma::idesc_f16_f32(TC_M, n);
       constexpr uint32_t LBO = 128, SBO = (TC_K / 8) * 128;
+      // descriptors are built once: a descriptor's address field is the byte
+      // address >> 4 (14 bits, all of shared memory), so moving to another
+      // stage, the lo half or the next k-step adds a constant
+      const uint64_t a_desc0 = umma::smem_desc(umma::smem_addr(S.a[0][0]), LBO, SBO);
+      const uint64_t b_desc0 = umma::smem_desc(umma::smem_addr(S.z[0]), LBO, SBO);
+      constexpr uint32_t A_STAGE16 = (2 * TC_A_BYTES) >> 4, A_LO16 = TC_A_BYTES >> 4;
+      constexpr uint32_t B_STAGE16 = TC_STAGE >> 4, B_LO16 = TC_ZHALF >> 4;
       bool ok = true;
       for (int c = 0; c < n_chunks; ++c) {
-        const int sz = c % TC_SZ, sa = c % TC_SA, g = c / TC_GROUP, buf = g & 1;
-        if (S.bad || !umma::mbar_wait(&S.full_z[sz], (c / TC_SZ) & 1, TC_WAIT)) {
+        const int sz = c % TC_S, sa = sz, g = c / TC_GROUP, buf = g & 1;
+        if (S.bad || !umma::mbar_wait(&S.full_z[sz], (c / TC_S) & 1, TC_WAIT)) {
           ok = false;
           break;
         }
         S.z_landed = c + 1;
-        if (!umma::mbar_wait(&S.full_a[sa], (c / TC_SA) & 1, TC_WAIT) ||
+        if (!umma::mbar_wait(&S.full_a[sa], (c / TC_S) & 1, TC_WAIT) ||
             (c % TC_GROUP == 0 && !umma::mbar_wait(&S.empty_acc[buf], ((g >> 1) & 1) ^ 1, TC_WAIT))) {
           ok = false;
           break;
         }
         umma::fence_after_sync();
         const uint32_t d = tmem + TC_COL_ACC + (uint32_t)(buf * TC_NMAX);
-        const uint32_t a_hi = umma::smem_addr(S.a[sa][0]), a_lo = umma::smem_addr(S.a[sa][1]);
-        const uint32_t b_hi = umma::smem_addr(S.z[sz]), b_lo = b_hi + TC_ZHALF;
+        const uint64_t ad = a_desc0 + (uint64_t)(sa * A_STAGE16), bd = b_desc0 + (uint64_t)(sz * B_STAGE16);
         // small cross terms first, then hi*hi, so the accumulator is still small
         // while the 2^-11-sized terms are added
-        const uint32_t pa[3] = {a_hi, a_lo, a_hi}, pb[3] = {b_lo, b_hi, b_hi};
+        const uint64_t pa[3] = {ad, ad + A_LO16, ad}, pb[3] = {bd + B_LO16, bd, bd};
 #pragma unroll
         for (int pass = 0; pass < 3; ++pass)
 #pragma unroll
           for (int ks = 0; ks < TC_K / 16; ++ks)
-            umma::mma_f16(d, umma::smem_desc(pa[pass] + ks * 256, LBO, SBO),
-                          umma::smem_desc(pb[pass] + ks * 256, LBO, SBO), idesc,
+            umma::mma_f16(d, pa[pass] + (uint64_t)(ks * 16), pb[pass] + (uint64_t)(ks * 16), idesc,
                           (c % TC_GROUP == 0 && pass == 0 && ks == 0) ? 0u : 1u);
-        umma::mma_commit(&S.empty_z[sz]);
-        umma::mma_commit(&S.empty_a[sa]);
+        umma::mma_commit(&S.empty[sz]);
         if (c % TC_GROUP == TC_GROUP - 1 || c == n_chunks - 1) umma::mma_commit(&S.full_acc[buf]);
       }
       if (!ok) S.bad = 1;
@@ -325,17 +325,18 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
     if (!ok) S.bad = 1;
   } else {
-    // ---- builders: A(c) = W products of the streamed X/Y tables into stage c % TC_SA
+    // ---- builders: A(c) = W products of the streamed X/Y tables into stage c % TC_S
     const int btid = tid - 32 * TC_BUILD_WARP0;
     const int bw = btid >> 5;
     for (int c = 0; c < n_chunks; ++c) {
-      const int sa = c % TC_SA, sz = c % TC_SZ;
+      const int sa = c % TC_S, sz = sa;
       // builder 0 decides for all builders (A stage free, X/Y of chunk c landed);
       // the flag alternates with the chunk parity so a slow reader of chunk c
       // never sees chunk c+1's decision
       if (btid == 0) {
-        const bool go = !S.bad && umma::mbar_wait(&S.empty_a[sa], ((c / TC_SA) & 1) ^ 1, TC_WAIT) &&
-                        umma::mbar_wait(&S.full_z[sz], (c / TC_SZ) & 1, TC_WAIT);
+        // the stage's copies landing implies its previous MMAs finished (the
+        // producer waited for them), so the A half of the stage is free too
+        const bool go = !S.bad && umma::mbar_wait(&S.full_z[sz], (c / TC_S) & 1, TC_WAIT);
         S.build_stop[c & 1] = go ? 0 : 1;
       }
       __syncwarp();
@@ -390,7 +391,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     // copies still in flight land before the block exits
     if (tid == 32 * TC_PRODUCER_WARP)
       for (int c = S.z_landed; c < S.z_issued; ++c)
-        umma::mbar_wait(&S.full_z[c % TC_SZ], (c / TC_SZ) & 1, TC_WAIT);
+        umma::mbar_wait(&S.full_z[c % TC_S], (c / TC_S) & 1, TC_WAIT);
     if (tid == 0) atomicExch(err, 1);
   } else if (n_groups > 0) {
     constexpr int DP = TC_NMAX + 1;

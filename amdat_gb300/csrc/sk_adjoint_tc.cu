@@ -191,7 +191,11 @@ __global__ void __launch_bounds__(SA_THREADS, 1)
     if (lane == 0) {
       const uint32_t idesc = umma::idesc_f16_f32(SA_M, SA_N);
       const uint32_t a_sbo = (uint32_t)(KA / 8) * 128, b_sbo = (SA_KC / 8) * 128;
-      const uint32_t a_hi = umma::smem_addr(A_hi), a_lo = umma::smem_addr(A_lo);
+      // descriptors built once; other stages, parts and k-steps add constants
+      // to the address field (byte address >> 4)
+      const uint64_t a_hi = umma::smem_desc(umma::smem_addr(A_hi), 128, a_sbo);
+      const uint64_t a_lo = umma::smem_desc(umma::smem_addr(A_lo), 128, a_sbo);
+      const uint64_t b_desc0 = umma::smem_desc(umma::smem_addr(B), 128, b_sbo);
       int g = 0;
       bool ok = true;
       for (int ti = 0; ti < n_list_tiles && ok; ++ti) {
@@ -209,19 +213,19 @@ __global__ void __launch_bounds__(SA_THREADS, 1)
           }
           S.landed = g + 1;
           umma::fence_after_sync();
-          const uint32_t b0 = umma::smem_addr(B + (size_t)s * SA_BSTAGE);
-          const uint32_t pb[4] = {b0, b0 + SA_BPART, b0 + 2 * SA_BPART, b0 + 3 * SA_BPART};
+          const uint64_t b0 = b_desc0 + (uint64_t)(s * (SA_BSTAGE >> 4));
+          const uint64_t aq = (uint64_t)(4 * q * 8);  // K offset of chunk q: 4q core matrices of 128 B
 #pragma unroll
           for (int which = 0; which < 2; ++which) {  // T, T'
             const uint32_t d = tmem + (uint32_t)(buf * 256 + which * 128);
-            const uint32_t bh = pb[2 * which], bl = pb[2 * which + 1];
-            const uint32_t ap[3] = {a_hi, a_lo, a_hi}, bp[3] = {bl, bh, bh};
+            const uint64_t bh = b0 + (uint64_t)(2 * which * (SA_BPART >> 4));
+            const uint64_t bl = bh + (uint64_t)(SA_BPART >> 4);
+            const uint64_t ap[3] = {a_hi + aq, a_lo + aq, a_hi + aq}, bp[3] = {bl, bh, bh};
 #pragma unroll
             for (int pass = 0; pass < 3; ++pass)
 #pragma unroll
               for (int ks = 0; ks < 2; ++ks)
-                umma::mma_f16(d, umma::smem_desc(ap[pass] + (uint32_t)(4 * q + 2 * ks) * 128, 128, a_sbo),
-                              umma::smem_desc(bp[pass] + ks * 256, 128, b_sbo), idesc,
+                umma::mma_f16(d, ap[pass] + (uint64_t)(ks * 16), bp[pass] + (uint64_t)(ks * 16), idesc,
                               (q == 0 && pass == 0 && ks == 0) ? 0u : 1u);
           }
           umma::mma_commit(&S.empty_b[s]);
