@@ -304,11 +304,16 @@ class Radial_Distribution_Function : public Analysis {
   void analyze(Trajectory_List* list) override;
   void analyze(Trajectory_List* a, Trajectory_List* b) override;
   void write(const std::string& file) const override;
+  // Radial_Distribution_Function::structure_factor (radial_distribution_function.cpp:379-434):
+  // S(k) = 1 + 4 pi rho sum_r (g(r) - 1) r sin(k r) / k dr at k = (i+1) 2 pi / max_distance
+  void structure_factor(const std::string& file, int n_ks) const;
 
  private:
   int n_bins_, timescheme_;
   float max_distance_, bin_size_;
   std::vector<float> mean_rdf_;
+  std::vector<int> n_atoms_j_;  // per analysed frame
+  float boxvolume_ = 0.f;
 };
 
 // frames visited by Analysis_Onetime::analyze (src/analysis_onetime.cpp:22-50)

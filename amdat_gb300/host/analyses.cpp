@@ -500,6 +500,8 @@ void Radial_Distribution_Function::analyze(Trajectory_List* a, Trajectory_List* 
   const float boxvolume = box.x * box.y * box.z;
   const int ni = a->show_n_trajectories(), nj = b->show_n_trajectories();
   mean_rdf_.assign(n_bins_, 0.f);
+  n_atoms_j_.assign(F, nj);
+  boxvolume_ = boxvolume;
   int n_i_total = 0;
   for (int f = 0; f < F; ++f) {
     const float rhoj = float(nj) / boxvolume;
@@ -514,6 +516,31 @@ void Radial_Distribution_Function::analyze(Trajectory_List* a, Trajectory_List* 
     }
   }
   for (int bi = 0; bi < n_bins_; ++bi) mean_rdf_[bi] /= float(n_i_total);
+}
+
+void Radial_Distribution_Function::structure_factor(const std::string& file, int n_ks) const {
+  // FP32 as the reference: mean density over the analysed frames, then the
+  // sine transform of g(r) - 1 at bin centres
+  const int n_times = (int)n_atoms_j_.size();
+  float mean_rho = 0.f;
+  for (int t = 0; t < n_times; ++t) mean_rho += float(n_atoms_j_[t]) / boxvolume_ / float(n_times);
+  const float min_k = (float)(2. * PI_RDF / max_distance_);
+  std::vector<float> klist(std::max(n_ks, 0)), sk(std::max(n_ks, 0));
+  for (int k = 0; k < n_ks; ++k) {
+    klist[k] = min_k * float(k + 1);
+    float acc = 0.f;
+    for (int b = 0; b < n_bins_; ++b) {
+      const float rshell = (float)((float(b) + 0.5) * bin_size_);
+      acc += (mean_rdf_[b] - 1) * rshell * std::sin(klist[k] * rshell) / klist[k] * bin_size_;
+    }
+    sk[k] = (float)(1. + 4. * PI_RDF * mean_rho * acc);
+  }
+  std::ofstream out = open_out(file);
+  out << "Structure factor data calculated from g(r) created by AMDAT v." << SEMVER << "\n";
+  for (int k = 0; k < n_ks; ++k) out << klist[k] << "\t";
+  out << "\n";
+  for (int k = 0; k < n_ks; ++k) out << Num{sk[k]} << "\t";
+  out << "\n";
 }
 
 void Radial_Distribution_Function::write(const std::string& file) const {

@@ -29,7 +29,18 @@ class Control {
       if (t.empty() || t[0].find('#') != std::string::npos) continue;
       lines_.push_back(line);
     }
-    while (pos_ < lines_.size()) execute(tokenize(lines_[pos_++]));
+    while (pos_ < lines_.size()) {
+      // tokens led by the flag marker '\\' are flags (Control::Control sets the
+      // marker, src/control.cpp:161; Tokenize::parse_token): '\\sname' stores
+      // the analysis under 'name'
+      flags_.clear();
+      std::vector<std::string> args;
+      for (auto& tok : tokenize(lines_[pos_++])) {
+        if (tok.size() >= 2 && tok[0] == '\\') flags_[tok[1]] = tok.substr(2);
+        else args.push_back(tok);
+      }
+      if (!args.empty()) execute(args);
+    }
   }
 
  private:
@@ -208,19 +219,38 @@ class Control {
     } else if (cmd == "rdf") {
       argcheck(a, 6, 6);
       pathcheck(a[1]);
-      Radial_Distribution_Function r(&sys(), std::atoi(a[3].c_str()), std::atoi(a[4].c_str()),
-                                     (float)std::atof(a[5].c_str()));
+      auto r = std::make_unique<Radial_Distribution_Function>(&sys(), std::atoi(a[3].c_str()),
+                                                              std::atoi(a[4].c_str()),
+                                                              (float)std::atof(a[5].c_str()));
       auto t1 = targets();
-      if (a[2] == "symmetric") r.analyze(t1[0]);
-      else if (a[2] == "asymmetric") r.analyze(t1[0], targets()[0]);
+      if (a[2] == "symmetric") r->analyze(t1[0]);
+      else if (a[2] == "asymmetric") r->analyze(t1[0], targets()[0]);
       else throw Error(AMDAT_ERR_ARGUMENT, "rdf symmetry must be symmetric or asymmetric");
-      r.write(a[1]);
+      r->write(a[1]);
+      auto fs = flags_.find('s');
+      if (fs != flags_.end()) {
+        // Control::rdf stores a copy under the flagged name (src/control.cpp:2900-2913)
+        if (stored_rdf_.count(fs->second))
+          throw Error(AMDAT_ERR_ARGUMENT, "an analysis is already stored with name " + fs->second);
+        stored_rdf_[fs->second] = std::move(r);
+      }
+    } else if (cmd == "structure_factor_from_rdf") {
+      // Control::structure_factor_from_rdf (src/control.cpp:3073-3099)
+      argcheck(a, 4, 4);
+      auto it = stored_rdf_.find(a[3]);
+      if (it == stored_rdf_.end())
+        std::cerr << "\nWarning: no analysis stored with name " << a[3]
+                  << ". Structure factor not calculated.\n";
+      else
+        it->second->structure_factor(a[1], std::atoi(a[2].c_str()));
     } else {
       throw Error(AMDAT_ERR_ARGUMENT, "command '" + cmd + "' is not part of this engine's hot path");
     }
   }
 
   int device_;
+  std::map<char, std::string> flags_;
+  std::map<std::string, std::unique_ptr<Radial_Distribution_Function>> stored_rdf_;
   std::vector<std::string> lines_;
   size_t pos_ = 0;
   std::unique_ptr<System> sys_;

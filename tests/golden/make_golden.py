@@ -130,6 +130,19 @@ list all
 mean_displacement ./md_lim.dat
 list all
 """),
+    # S(k) from a stored g(r) (rdf with the \\s flag, then structure_factor_from_rdf)
+    "sk_from_rdf": dict(
+        n=400, box=8.0, sigma=0.2, seed=66, fractions=(1.0,), time_scaled=False,
+        scheme=synth.TimeScheme.linear(6, 1.0),
+        commands="""create_list all
+all
+rdf ./rdf.dat symmetric 80 -1 0 \\sg1
+list all
+structure_factor_from_rdf ./sk_rdf.dat 40 g1
+rdf ./rdf2.dat symmetric 50 0 3.0 \\sg2
+list all
+structure_factor_from_rdf ./sk_rdf2.dat 25 g2
+"""),
     "siblings_lin": dict(
         n=120, box=6.0, sigma=0.1, seed=55, fractions=(1.0,), time_scaled=False,
         scheme=synth.TimeScheme.linear(16, 1.0),

@@ -34,6 +34,8 @@ class OracleRun:
         self.limit = 0
         self.lists = {}
         self.files = {}
+        self.flags = {}
+        self.stored = {}
 
     def scheme(self):
         return orc.scheme(self.traj.scheme, self.limit)
@@ -50,9 +52,15 @@ class OracleRun:
         lines = [ln.strip() for ln in script.splitlines() if ln.strip()]
         i = 0
         while i < len(lines):
-            a = lines[i].split()
+            toks = lines[i].split()
             i += 1
+            # '\\x...' tokens are flags (Tokenize::parse_token with the '\\' marker)
+            self.flags = {t[1]: t[2:] for t in toks if len(t) >= 2 and t[0] == "\\"}
+            a = [t for t in toks if not (len(t) >= 2 and t[0] == "\\")]
             cmd = a[0]
+            if cmd == "structure_factor_from_rdf":
+                self.cmd_structure_factor_from_rdf(a)
+                continue
             if cmd == "create_list":
                 sel = lines[i].split()
                 i += 1
@@ -171,6 +179,12 @@ class OracleRun:
         s = self.scheme()
         counts, mean = orc.rdf(s, ts, self.wrapped, self.traj.box, lst, nb, float(maxd))
         bs = f32(maxd / f32(nb))
+        if "s" in self.flags:
+            frames = len(onetime := orc_frames(s, ts))
+            self.stored[self.flags["s"]] = dict(mean=np.asarray(mean, np.float32), nb=nb, bs=bs, maxd=maxd,
+                                                nj=len(lst), n_times=frames,
+                                                vol=f32(f32(self.traj.box[0]) * f32(self.traj.box[1])
+                                                        * f32(self.traj.box[2])))
         txt = f"Radial distribution function data created by AMDAT v.{VERSION}\n"
         txt += "".join(fmt(f32(f32(f32(b) * bs) + f32(bs / f32(2)))) + "\t" for b in range(nb)) + "\n"
         txt += "".join(fmt(f32(v)) + "\t" for v in mean) + "\n"
@@ -213,3 +227,42 @@ class OracleRun:
                f"AMDAT v.{VERSION}\nLast bin includes overflow.time = {t}\nMean\t{mean}\n"
                f"Variance\t{var}\n\n" + rows)
         self.files[self.name(a[1])] = txt
+
+
+def orc_frames(s, timescheme):
+    """frames of Analysis_Onetime::analyze (as oracle.onetime_frames)"""
+    return orc.onetime_frames(s, timescheme)
+
+
+def _sk_from_rdf(st, n_ks):
+    """Radial_Distribution_Function::structure_factor (radial_distribution_function.cpp:379-434), FP32"""
+    PI = 3.1459265
+    mean_rho = f32(0)
+    for _ in range(st["n_times"]):
+        mean_rho = f32(mean_rho + f32(f32(f32(st["nj"]) / st["vol"]) / f32(st["n_times"])))
+    min_k = f32(2.0 * PI / float(st["maxd"]))
+    ks, sk = [], []
+    for k in range(n_ks):
+        kk = f32(min_k * f32(k + 1))
+        acc = f32(0)
+        for b in range(st["nb"]):
+            r = f32((float(f32(b)) + 0.5) * float(st["bs"]))
+            term = f32(f32(f32(f32(st["mean"][b] - f32(1)) * r) * f32(np.sin(f32(kk * r)))) / kk)
+            acc = f32(acc + f32(term * st["bs"]))
+        ks.append(kk)
+        sk.append(f32(1.0 + 4.0 * PI * float(mean_rho) * float(acc)))
+    return ks, sk
+
+
+def _cmd_sk_from_rdf(self, a):
+    name, n_ks = a[3], int(a[2])
+    if name not in self.stored:
+        return
+    ks, sk = _sk_from_rdf(self.stored[name], n_ks)
+    txt = f"Structure factor data calculated from g(r) created by AMDAT v.{VERSION}\n"
+    txt += "".join(fmt(k) + "\t" for k in ks) + "\n"
+    txt += "".join(fmt(v) + "\t" for v in sk) + "\n"
+    self.files[self.name(a[1])] = txt
+
+
+OracleRun.cmd_structure_factor_from_rdf = _cmd_sk_from_rdf
