@@ -131,9 +131,32 @@ def dist_setup():
     pg = None
     if world > 1:
         import torch.distributed as dist
-        dist.init_process_group("gloo")
+        if not dist.is_initialized():
+            dist.init_process_group("gloo")
         pg = dist
     return world, rank, local, pg
+
+
+def barrier(pg):
+    """Host barrier over the ranks (no-op at one rank)."""
+    if pg is not None:
+        pg.barrier()
+
+
+def max_over_ranks(pg, x):
+    """The largest of each rank's x (a step time): the job ends with its slowest rank."""
+    if pg is None:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(units_per_rank, world, ms):
+    """Whole-job throughput: every rank processes units_per_rank in a step whose
+    time is the maximum over ranks (ms)."""
+    return units_per_rank * world / (ms / 1e3)
 
 
 class ClockSampler:
@@ -401,17 +424,6 @@ def main():
     eng = E.Engine(local)
     eng.set_stream(stream.cuda_stream)
 
-    def barrier():
-        if pg is not None:
-            pg.barrier()
-
-    def max_over_ranks(x):
-        if pg is None:
-            return x
-        t = torch.tensor([x], dtype=torch.float64)
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        return float(t.item())
-
     result = {}
     clocks = ClockSampler(local)
     if args.only in ("", "isf"):
@@ -437,7 +449,7 @@ def main():
         for _ in range(args.warmup):
             step()
         torch.cuda.synchronize()
-        barrier()
+        barrier(pg)
         eng.profile_reset(True)
         l0 = eng.launch_count()
         clocks.start()
@@ -449,9 +461,9 @@ def main():
         e1.record(stream)
         torch.cuda.synchronize()
         clocks.stop()
-        barrier()
+        barrier(pg)
         ms = e0.elapsed_time(e1) / args.steps
-        ms = max_over_ranks(ms)
+        ms = max_over_ranks(pg, ms)
         launches = eng.launch_count() - l0
         kname = "rhok_tc_kernel"
         n_lat, ms_lat = eng.profile_kernel(kname)
@@ -461,7 +473,7 @@ def main():
         n_isf, ms_isf = eng.profile_kernel("isf_pairs_kernel")
         eng.profile_reset(False)
         units = float(N) * T * nk
-        value = units * world / (ms / 1e3)
+        value = job_rate(units, world, ms)
         # roofline of the dominant kernel: 8 algorithmic flops (one complex
         # multiply-accumulate) per atom*vector; the tensor-core kernel issues
         # 3 split-precision passes over whole tiles, reported as issued flops
@@ -499,17 +511,17 @@ def main():
 
         e2e_step()
         torch.cuda.synchronize()
-        barrier()
+        barrier(pg)
         t0 = time.perf_counter()
         for _ in range(max(1, min(args.steps, 2))):
             e2e_step()
         torch.cuda.synchronize()
-        e2e_ms = max_over_ranks(1e3 * (time.perf_counter() - t0) / max(1, min(args.steps, 2)))
+        e2e_ms = max_over_ranks(pg, 1e3 * (time.perf_counter() - t0) / max(1, min(args.steps, 2)))
         result["isf"] = dict(
             value=value, ms=ms, launches=launches, nk=nk, ns=ns, T=T, N=N, kname=kname, issued=issued,
             lat_ms=lat_ms, n_lat=n_lat, isf_ms=ms_isf / max(n_isf, 1), achieved=achieved,
             fp32_peak_max=fp32_peak_max, clocks=clk, plain_rate=plain_rate,
-            e2e=units * world / (e2e_ms / 1e3), e2e_ms=e2e_ms,
+            e2e=job_rate(units, world, e2e_ms), e2e_ms=e2e_ms,
             h2d=int(T * N * 3 * 4), d2h=int(G * ns * 8 + G * 8 + ns * 8))
         del pinned
 
@@ -540,7 +552,7 @@ def main():
             mstep()
         e1.record(stream)
         torch.cuda.synchronize()
-        mms = max_over_ranks(e0.elapsed_time(e1) / msteps)
+        mms = max_over_ranks(pg, e0.elapsed_time(e1) / msteps)
         n_d, ms_d = eng.profile_kernel("disp_mixed_kernel")
         eng.profile_reset(False)
         npairs = int(d_cnt.sum().item()) // mtraj.n_atoms
@@ -549,7 +561,7 @@ def main():
         mstep(precision=1)
         eng.synchronize()
         mplain = munits / (time.perf_counter() - t0)
-        result["msd"] = dict(value=munits * world / (mms / 1e3), ms=mms, kernel_ms=ms_d / max(n_d, 1),
+        result["msd"] = dict(value=job_rate(munits, world, mms), ms=mms, kernel_ms=ms_d / max(n_d, 1),
                              plain=mplain, npairs=npairs, nvec=len(shell))
 
     if args.only in ("", "batched"):
@@ -580,8 +592,8 @@ def main():
         p_fs = eng.plan(nested, shells=shells, period=L, flags=E.PLAN_AUTOTUNE | E.PLAN_GRAPH)
         tune_s = time.perf_counter() - t0
         l0 = eng.launch_count()
-        ms_msd = max_over_ranks(time_plan(p_msd, 20))
-        ms_fs = max_over_ranks(time_plan(p_fs, max(2, args.steps)))
+        ms_msd = max_over_ranks(pg, time_plan(p_msd, 20))
+        ms_fs = max_over_ranks(pg, time_plan(p_fs, max(2, args.steps)))
         blaunch = eng.launch_count() - l0
         info_msd, info_fs = p_msd.info(), p_fs.info()
         share = p_msd.sharing()
@@ -590,17 +602,17 @@ def main():
         # the same lists without work sharing (one unit of work per list)
         ns_flags = E.PLAN_AUTOTUNE | E.PLAN_GRAPH | E.PLAN_NO_SHARING
         p_ns = eng.plan(nested, flags=ns_flags)
-        ms_msd_ns = max_over_ranks(time_plan(p_ns, 10))
+        ms_msd_ns = max_over_ranks(pg, time_plan(p_ns, 10))
         p_ns.close()
         p_fs_ns = eng.plan(nested, shells=shells, period=L, flags=ns_flags)
-        ms_fs_ns = max_over_ranks(time_plan(p_fs_ns, 1))
+        ms_fs_ns = max_over_ranks(pg, time_plan(p_fs_ns, 1))
         p_fs_ns.close()
         # gathered layout (original atom order, index lists) for comparison
         eng.upload(btraj.unwrapped, btraj.box)
         eng.set_scheme(bscheme)
         gathered = [eng.list(np.sort(perm[:n]).astype(np.int32)) for n in sizes]
         p_g = eng.plan(gathered, flags=E.PLAN_GRAPH)
-        ms_g = max_over_ranks(time_plan(p_g, 10))
+        ms_g = max_over_ranks(pg, time_plan(p_g, 10))
         p_g.close()
         # plain FP64 path on the largest list (MSD + F_s), the mixed rate on the same list
         big = gathered[-1]
