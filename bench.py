@@ -38,6 +38,12 @@ sys.path.insert(0, HERE)
 METRIC = "atom·time-pairs/s (MSD+Fs) & atom·k/s (rho_k): mixed vs FP64 plain, 1 GB300"
 PEAKS_FILE = os.path.join(HERE, "MEASURED_PEAKS.json")
 FP32_LANES_PER_SM = 128
+# DRAM bytes (read + write) per frame of one rhok_tc_kernel launch on the headline
+# lattice (N=32000, |k|<=20, L=33.6), from one ncu capture of a 2-frame launch
+# (profiles/rhok_tc_kernel_N32000_k20_2frames.md: 812.5 MB read + 43.0 MB written).
+# Every stream of the launch is per frame (X/Y phase tables, Z operands, rho rows), so
+# a launch over f frames moves f times this.
+TC_DRAM_BYTES_PER_FRAME = (812.518e6 + 42.974e6) / 2
 
 
 # ---------------------------------------------------------------------------
@@ -519,7 +525,7 @@ def main():
         e2e_ms = max_over_ranks(pg, 1e3 * (time.perf_counter() - t0) / max(1, min(args.steps, 2)))
         result["isf"] = dict(
             value=value, ms=ms, launches=launches, nk=nk, ns=ns, T=T, N=N, kname=kname, issued=issued,
-            lat_ms=lat_ms, n_lat=n_lat, isf_ms=ms_isf / max(n_isf, 1), achieved=achieved,
+            lat_ms=lat_ms, n_lat=n_lat, steps=args.steps, isf_ms=ms_isf / max(n_isf, 1), achieved=achieved,
             fp32_peak_max=fp32_peak_max, clocks=clk, plain_rate=plain_rate,
             e2e=job_rate(units, world, e2e_ms), e2e_ms=e2e_ms,
             h2d=int(T * N * 3 * 4), d2h=int(G * ns * 8 + G * 8 + ns * 8))
@@ -707,7 +713,10 @@ def main():
                 {"bound": "tensor", "achieved": r["achieved"],
                  "peak": peaks.get("bf16_tflops_sustained", 1700.0), "unit": "TFLOP/s",
                  "frac": r["achieved"] / peaks.get("bf16_tflops_sustained", 1700.0),
-                 "traffic": None, "kernel": r["kname"], "kernel_ms_per_step": r["lat_ms"],
+                 "traffic": TC_DRAM_BYTES_PER_FRAME * r["T"] * r["steps"] / max(r["n_lat"], 1),
+                 "traffic_rule": "bytes per launch: ncu dram__bytes_read+write of a 2-frame "
+                                 "launch per frame x frames per launch",
+                 "kernel": r["kname"], "kernel_ms_per_step": r["lat_ms"],
                  "kernel_launches": r["n_lat"],
                  "flops_per_step": 8.0 * r["N"] * r["T"] * r["nk"],
                  "achieved_rule": "algorithmic: 8 flops (one complex MAC) per atom*vector",
