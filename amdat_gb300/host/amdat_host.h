@@ -43,7 +43,8 @@ struct Coord {
 class System {
  public:
   // block: the lines that follow "system" (trajectory type, file line, time
-  // scheme, species line, atom type line, one count line per species)
+  // scheme, species line, atom type line, one count line per species; for the
+  // xyz type also the box-size line and the box-bounds line, src/system.cpp:389-407)
   System(const std::vector<std::string>& block, int device);
   ~System();
   System(const System&) = delete;
@@ -66,7 +67,9 @@ class System {
   const std::vector<int>& atom_species() const { return atom_species_; }
 
  private:
-  void read_custom(const std::string& file);
+  void read_custom(const std::string& file, bool byid);
+  void read_xyz(const std::string& file);
+  void unwrap_from_wrapped();
   amdat_ctx* ctx_ = nullptr;
   amdat_scheme scheme_{};
   int n_atoms_ = 0, n_timesteps_ = 0, n_timegaps_ = 0;

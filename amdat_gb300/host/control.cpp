@@ -132,6 +132,9 @@ class Control {
       const size_t n_species = tokenize(block[3]).size() / 2;
       block.push_back(read_line());  // atom types
       for (size_t s = 0; s < n_species; ++s) block.push_back(read_line());
+      const auto ty = tokenize(block[0]);
+      if (!ty.empty() && ty[0] == "xyz")
+        for (int k = 0; k < 2; ++k) block.push_back(read_line());  // box size, box bounds
       lists_.clear();
       sys_.reset();
       sys_ = std::make_unique<System>(block, device_);

@@ -51,8 +51,10 @@ System::System(const std::vector<std::string>& block, int device) {
   // block: type / file line / time scheme / species / types / counts x species
   if (block.size() < 5) throw Error(AMDAT_ERR_ARGUMENT, "incomplete system block");
   const auto type = tokenize(block[0]);
-  if (type.empty() || type[0] != "custom")
-    throw Error(AMDAT_ERR_ARGUMENT, "only the custom trajectory type is supported by this engine");
+  if (type.empty() || (type[0] != "custom" && type[0] != "custom_byid" && type[0] != "xyz"))
+    throw Error(AMDAT_ERR_ARGUMENT,
+                "only the custom, custom_byid and xyz trajectory types are supported by this engine");
+  const bool xyz = type[0] == "xyz";
   const auto fileline = tokenize(block[1]);
   if (fileline.empty()) throw Error(AMDAT_ERR_ARGUMENT, "missing trajectory file");
   scheme_ = parse_scheme(tokenize(block[2]));
@@ -82,6 +84,18 @@ System::System(const std::vector<std::string>& block, int device) {
     for (auto& x : c) v.push_back(std::atoi(x.c_str()));
     type_counts_.push_back(v);
   }
+  if (xyz) {
+    // System::xyz_prep (src/system.cpp:389-407): "Lx Ly Lz", then
+    // "xlo xhi ylo yhi zlo zhi", constant over the trajectory
+    const size_t b = 5 + species_names_.size();
+    if (block.size() < b + 2) throw Error(AMDAT_ERR_ARGUMENT, "missing box lines for the xyz trajectory");
+    const auto L = tokenize(block[b]), lohi = tokenize(block[b + 1]);
+    if (L.size() < 3 || lohi.size() < 6) throw Error(AMDAT_ERR_ARGUMENT, "bad box lines for the xyz trajectory");
+    for (int d = 0; d < 3; ++d) {
+      box_[d] = (float)std::atof(L[d].c_str());
+      box_lo_[d] = (float)std::atof(lohi[2 * d].c_str());
+    }
+  }
   n_atoms_ = 0;
   for (size_t s = 0; s < species_names_.size(); ++s) {
     int per = 0;
@@ -93,7 +107,10 @@ System::System(const std::vector<std::string>& block, int device) {
   if (n_atoms_ <= 0) throw Error(AMDAT_ERR_ARGUMENT, "system has no atoms");
   // parse the whole trajectory before touching the GPU, so input errors are
   // reported the same way with or without a device
-  read_custom(fileline[0]);
+  if (xyz)
+    read_xyz(fileline[0]);
+  else
+    read_custom(fileline[0], type[0] == "custom_byid");
   check(amdat_create(device, &ctx_), "amdat_create");
   try {
     check(amdat_traj_upload(ctx_, n_timesteps_, n_atoms_, U_.data(), W_.empty() ? nullptr : W_.data(),
@@ -137,7 +154,7 @@ namespace {
 
 struct Cols {
   int x = -1, y = -1, z = -1, xs = -1, ys = -1, zs = -1, xu = -1, yu = -1, zu = -1;
-  int xsu = -1, ysu = -1, zsu = -1, ix = -1, iy = -1, iz = -1, type = -1;
+  int xsu = -1, ysu = -1, zsu = -1, ix = -1, iy = -1, iz = -1, type = -1, id = -1;
 };
 
 // next line [p, eol) of a buffer; returns pointer after the line end
@@ -170,7 +187,11 @@ inline double atof64(const char* s) { return std::strtod(s, nullptr); }
 
 }  // namespace
 
-void System::read_custom(const std::string& file) {
+// custom (src/system.cpp:1026-1360): atom lines in file order, grouped by species.
+// custom_byid (src/system.cpp:2438-2936): atom lines in any order; the "id"
+// column places each at index id-1 (ids must be 1..N), and an id keeps the type
+// it had in the first frame.
+void System::read_custom(const std::string& file, bool byid) {
   std::ifstream in(file, std::ios::binary);
   if (!in) throw Error(AMDAT_ERR_ARGUMENT, "Custom Trajectory file not found.");
   in.seekg(0, std::ios::end);
@@ -241,6 +262,8 @@ void System::read_custom(const std::string& file) {
       c.xsu = find("xsu"); c.ysu = find("ysu"); c.zsu = find("zsu");
       c.ix = find("ix"); c.iy = find("iy"); c.iz = find("iz");
       c.type = find("type");
+      c.id = find("id");
+      if (byid && c.id < 0) throw Error(AMDAT_ERR_ARGUMENT, "atom id data not provided.");
       if (c.type < 0) throw Error(AMDAT_ERR_ARGUMENT, "atom type data not provided.");
     }
     for (int a = 0; a < N; ++a) p = next_line(p, end, &eol);
@@ -259,25 +282,45 @@ void System::read_custom(const std::string& file) {
   W.assign(have_w ? (size_t)T * N * 3 : 0, 0.f);
   atom_type_.assign(N, 0);
   std::string bad_type;
+  std::vector<int> bad_id(T, 0);           // 1: id out of 1..N or repeated, 2: type changed
+  std::vector<unsigned char> seen(byid ? N : 0, 0);
   auto parse = [&](int t0, int t1) {
     for (int t = t0; t < t1; ++t) {
       const char* q = frame[t];
       const char* eol;
       for (int l = 0; l < 9; ++l) q = next_line(q, end, &eol);
-      for (int a = 0; a < N; ++a) {
+      for (int line = 0; line < N; ++line) {
         const char* ls = q;
         q = next_line(q, end, &eol);
+        const char* fe;
+        int a = line;
+        if (byid) {
+          const char* is = field(ls, eol, c.id, &fe);
+          a = std::atoi(std::string(is, fe).c_str()) - 1;
+          if (a < 0 || a >= N) {
+            bad_id[t] = 1;
+            continue;
+          }
+          if (t == 0) {
+            if (seen[a]) bad_id[t] = 1;
+            seen[a] = 1;
+          }
+        }
         float* u = &U[((size_t)t * N + a) * 3];
         float* w = have_w ? &W[((size_t)t * N + a) * 3] : nullptr;
-        const char* fe;
-        if (t == 0) {
+        if (t == 0 || byid) {
           const char* ts = field(ls, eol, c.type, &fe);
           const std::string tn(ts, fe);
           int ti = -1;
           for (size_t i = 0; i < type_names_.size(); ++i)
             if (type_names_[i] == tn) ti = (int)i;
-          if (ti < 0) bad_type = tn;
-          atom_type_[a] = ti < 0 ? 0 : ti;
+          if (ti < 0 && t == 0) bad_type = tn;  // frame 0 is parsed alone
+          if (t == 0)
+            atom_type_[a] = ti < 0 ? 0 : ti;
+          else if (ti < 0)
+            bad_id[t] = 2;
+          else if (ti >= 0 && ti != atom_type_[a])
+            bad_id[t] = 2;
         }
         const int wx[3] = {c.x, c.y, c.z}, sx[3] = {c.xs, c.ys, c.zs};
         const int ux[3] = {c.xu, c.yu, c.zu}, sux[3] = {c.xsu, c.ysu, c.zsu};
@@ -295,24 +338,118 @@ void System::read_custom(const std::string& file) {
       }
     }
   };
+  // frame 0 first: it fixes each atom's type (and, by id, its index)
+  parse(0, 1);
+  if (T > 1) {
+    const int nth = std::max(1, std::min<int>(T - 1, (int)std::thread::hardware_concurrency()));
+    std::vector<std::thread> th;
+    for (int i = 0; i < nth; ++i)
+      th.emplace_back(parse, 1 + (int)((int64_t)(T - 1) * i / nth), 1 + (int)((int64_t)(T - 1) * (i + 1) / nth));
+    for (auto& x : th) x.join();
+  }
+  if (!bad_type.empty()) throw Error(AMDAT_ERR_ARGUMENT, "Atom type " + bad_type + " in trajectory file out of range!");
+  for (int t = 0; t < T; ++t) {
+    if (bad_id[t] == 1)
+      throw Error(AMDAT_ERR_ARGUMENT,
+                  "Some problem with handling atom ids during file read in. Atom ids should begin with 1 "
+                  "and should not skip.");
+    if (bad_id[t] == 2)
+      throw Error(AMDAT_ERR_ARGUMENT, "Type of index in file does not match type in id map (frame " +
+                                          std::to_string(t) + ").");
+  }
+  if (!have_u) unwrap_from_wrapped();
+}
+
+// Trajectory::unwrap (src/trajectory.cpp:236-271): unwrapped(0) = wrapped(0), then
+// the step-to-step displacement corrected by L * int(d / (0.55 L)), in FP32
+void System::unwrap_from_wrapped() {
+  const int T = n_timesteps_, N = n_atoms_;
+  std::vector<float>& U = U_;
+  const std::vector<float>& W = W_;
+  for (int a = 0; a < N; ++a)
+    for (int t = 1; t < T; ++t)
+      for (int d = 0; d < 3; ++d) {
+        const float disp = W[((size_t)t * N + a) * 3 + d] - W[((size_t)(t - 1) * N + a) * 3 + d];
+        const float den = box_[d] * 0.55f;
+        const float q = (float)(int)(disp / den);
+        const float corr = box_[d] * q;
+        U[((size_t)t * N + a) * 3 + d] = U[((size_t)(t - 1) * N + a) * 3 + d] + (disp - corr);
+      }
+}
+
+// System::read_xyz (src/system.cpp:610-700): per frame a line with the atom
+// count, one comment line, then one "type x y z" line per atom in species and
+// molecule order. Coordinates are wrapped and read straight into float; the
+// type is its integer label (1-based). Unwrapped coordinates are derived.
+void System::read_xyz(const std::string& file) {
+  std::ifstream in(file, std::ios::binary);
+  if (!in) throw Error(AMDAT_ERR_ARGUMENT, "XYZ Trajectory file not found.");
+  in.seekg(0, std::ios::end);
+  const size_t size = (size_t)in.tellg();
+  in.seekg(0);
+  std::string buf(size, '\0');
+  in.read(&buf[0], (std::streamsize)size);
+  const char* p = buf.data();
+  const char* end = p + size;
+  const int T = n_timesteps_, N = n_atoms_;
+  std::vector<const char*> frame(T);
+  for (int t = 0; t < T; ++t) {
+    const char* eol;
+    while (p < end && (*p == '\n' || *p == '\r' || *p == ' ' || *p == '\t')) ++p;
+    if (p >= end) throw Error(AMDAT_ERR_ARGUMENT, "trajectory file ends before frame " + std::to_string(t));
+    const char* s = p;
+    p = next_line(p, end, &eol);
+    const int n = std::atoi(std::string(s, eol).c_str());
+    if (n != N) {
+      std::ostringstream m;
+      m << "The number of atoms listed in the xyz file is inconsistent with user input: " << n
+        << " != " << N;
+      throw Error(AMDAT_ERR_ARGUMENT, m.str());
+    }
+    p = next_line(p, end, &eol);  // comment line ("Atoms. Timestep: ...")
+    frame[t] = p;
+    for (int a = 0; a < N; ++a) {
+      if (p >= end) throw Error(AMDAT_ERR_ARGUMENT, "trajectory file ends inside frame " + std::to_string(t));
+      p = next_line(p, end, &eol);
+    }
+  }
+  U_.assign((size_t)T * N * 3, 0.f);
+  W_.assign((size_t)T * N * 3, 0.f);
+  atom_type_.assign(N, 0);
+  const int n_types = (int)type_names_.size();
+  std::vector<int> bad(T, 0);
+  auto parse = [&](int t0, int t1) {
+    for (int t = t0; t < t1; ++t) {
+      const char* q = frame[t];
+      for (int a = 0; a < N; ++a) {
+        const char* eol;
+        const char* ls = q;
+        q = next_line(q, end, &eol);
+        const char* fe;
+        const char* ts = field(ls, eol, 0, &fe);
+        const int ty = std::atoi(std::string(ts, fe).c_str());
+        if (ty < 1 || ty > n_types) bad[t] = 1;
+        if (t == 0) atom_type_[a] = ty >= 1 && ty <= n_types ? ty - 1 : 0;
+        float* w = &W_[((size_t)t * N + a) * 3];
+        for (int d = 0; d < 3; ++d) {
+          const char* xs = field(ls, eol, 1 + d, &fe);
+          if (xs == fe) bad[t] = 2;
+          w[d] = std::strtof(xs, nullptr);
+        }
+      }
+    }
+  };
   const int nth = std::max(1, std::min<int>(T, (int)std::thread::hardware_concurrency()));
   std::vector<std::thread> th;
   for (int i = 0; i < nth; ++i) th.emplace_back(parse, (int)((int64_t)T * i / nth), (int)((int64_t)T * (i + 1) / nth));
   for (auto& x : th) x.join();
-  if (!bad_type.empty()) throw Error(AMDAT_ERR_ARGUMENT, "Atom type " + bad_type + " in trajectory file out of range!");
-  if (!have_u) {
-    // Trajectory::unwrap (src/trajectory.cpp:236-271): step-to-step displacement
-    // corrected by L * int(d / (0.55 L)), FP32
-    for (int a = 0; a < N; ++a)
-      for (int t = 1; t < T; ++t)
-        for (int d = 0; d < 3; ++d) {
-          const float disp = W[((size_t)t * N + a) * 3 + d] - W[((size_t)(t - 1) * N + a) * 3 + d];
-          const float den = box_[d] * 0.55f;
-          const float q = (float)(int)(disp / den);
-          const float corr = box_[d] * q;
-          U[((size_t)t * N + a) * 3 + d] = U[((size_t)(t - 1) * N + a) * 3 + d] + (disp - corr);
-        }
+  for (int t = 0; t < T; ++t) {
+    if (bad[t] == 1) throw Error(AMDAT_ERR_ARGUMENT, "Atom type in trajectory file out of range!");
+    if (bad[t] == 2) throw Error(AMDAT_ERR_ARGUMENT, "incomplete atom line in xyz frame " + std::to_string(t));
   }
+  // unwrapped(0) = wrapped(0)
+  std::copy(W_.begin(), W_.begin() + (size_t)N * 3, U_.begin());
+  unwrap_from_wrapped();
 }
 
 // --- lists -----------------------------------------------------------------

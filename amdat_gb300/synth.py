@@ -87,6 +87,11 @@ class Trajectory:
     scheme: TimeScheme = field(default_factory=TimeScheme)
     type_names: tuple = ("1",)
     species: tuple = (("particle", None),)
+    # wrapped positions as a trajectory file gave them (xyz input); None means
+    # derived from the unwrapped ones
+    wrapped_given: np.ndarray | None = None
+    # the trajectory file type it is written as: "custom", "custom_byid" or "xyz"
+    file_format: str = "custom"
 
     @property
     def n_frames(self):
@@ -100,6 +105,8 @@ class Trajectory:
         """Wrapped coordinates derived from unwrapped ones exactly as AMDAT's
         custom reader does (src/system.cpp, ``calc_wrapped``):
         c = u - L * floor((u - lo) / L), every operation in FP32."""
+        if self.wrapped_given is not None:
+            return self.wrapped_given
         u = self.unwrapped.astype(np.float32)
         lo = self.box_lo.astype(np.float32)
         L = self.box.astype(np.float32)
@@ -134,12 +141,16 @@ def random_walk(n_atoms: int, box: float, scheme: TimeScheme, sigma: float, seed
                       types=types, scheme=scheme, type_names=names)
 
 
-def write_custom_dump(traj: Trajectory, path: str) -> None:
-    """LAMMPS ``custom`` dump with columns ``id type xu yu zu`` (FP32-exact)."""
+def write_custom_dump(traj: Trajectory, path: str, shuffle_seed: int | None = None) -> None:
+    """LAMMPS ``custom`` dump with columns ``id type xu yu zu`` (FP32-exact).
+
+    With shuffle_seed the atom lines of every frame are written in a seeded
+    random order (the layout ``custom_byid`` reads; ids stay 1..N)."""
     lo = traj.box_lo.astype(np.float64)
     hi = lo + traj.box.astype(np.float64)
     ids = np.arange(1, traj.n_atoms + 1)
     tnames = np.asarray(traj.type_names)[traj.types]
+    rng = np.random.default_rng(shuffle_seed) if shuffle_seed is not None else None
     with open(path, "w") as f:
         for t in range(traj.n_frames):
             f.write(f"ITEM: TIMESTEP\n{t}\nITEM: NUMBER OF ATOMS\n{traj.n_atoms}\n")
@@ -150,21 +161,75 @@ def write_custom_dump(traj: Trajectory, path: str) -> None:
             u = traj.unwrapped[t]
             lines = [f"{i} {n} {x:.9g} {y:.9g} {z:.9g}\n"
                      for i, n, (x, y, z) in zip(ids, tnames, u.tolist())]
+            if rng is not None:
+                lines = [lines[k] for k in rng.permutation(len(lines))]
             f.writelines(lines)
 
 
-def system_header(traj: Trajectory, dump_path: str) -> str:
+def write_trajectory(traj: Trajectory, path: str, shuffle_seed: int = 0) -> None:
+    """Write traj in its file_format (xyz, custom, or custom with shuffled lines)."""
+    if traj.file_format == "xyz":
+        write_xyz(traj, path)
+    elif traj.file_format == "custom_byid":
+        write_custom_dump(traj, path, shuffle_seed=shuffle_seed)
+    else:
+        write_custom_dump(traj, path)
+
+
+def write_xyz(traj: Trajectory, path: str) -> None:
+    """xyz trajectory (src/system.cpp:610-700): atom count, a comment line, then
+    ``type x y z`` per atom with the wrapped FP32 coordinates (``%.9g``)."""
+    w = traj.wrapped()
+    tnames = np.asarray(traj.type_names)[traj.types]
+    with open(path, "w") as f:
+        for t in range(traj.n_frames):
+            f.write(f"{traj.n_atoms}\nAtoms. Timestep: {t}\n")
+            f.writelines(f"{n} {x:.9g} {y:.9g} {z:.9g}\n" for n, (x, y, z) in zip(tnames, w[t].tolist()))
+
+
+def unwrap_from_wrapped(wrapped: np.ndarray, box: np.ndarray) -> np.ndarray:
+    """Trajectory::unwrap (src/trajectory.cpp:236-271) in FP32: u(0) = w(0), then
+    u(t) = u(t-1) + d - L * int(d / (0.55 L)) with d = w(t) - w(t-1)."""
+    w = wrapped.astype(np.float32)
+    L = box.astype(np.float32)
+    den = (L * np.float32(0.55)).astype(np.float32)
+    u = np.empty_like(w)
+    u[0] = w[0]
+    for t in range(1, w.shape[0]):
+        d = (w[t] - w[t - 1]).astype(np.float32)
+        q = np.trunc((d / den).astype(np.float32)).astype(np.float32)
+        u[t] = (u[t - 1] + (d - (L * q).astype(np.float32)).astype(np.float32)).astype(np.float32)
+    return u
+
+
+def as_xyz_input(traj: Trajectory) -> Trajectory:
+    """The trajectory an xyz file of traj reads back as: the wrapped positions
+    as written and the unwrapped ones derived from them by the reader."""
+    w = traj.wrapped()
+    return Trajectory(unwrapped=unwrap_from_wrapped(w, traj.box), box=traj.box, box_lo=traj.box_lo,
+                      types=traj.types, scheme=traj.scheme, type_names=traj.type_names,
+                      species=traj.species, wrapped_given=w, file_format="xyz")
+
+
+def system_header(traj: Trajectory, dump_path: str, fmt: str | None = None) -> str:
     """AMDAT ``system`` block for a dump written by write_custom_dump.
 
     One species per atom type, one atom per molecule, so species i is the
     contiguous run of atoms of type i (the custom reader requires atoms
     grouped by species in declaration order, src/system.cpp:1026).
     """
+    fmt = fmt or traj.file_format
     ntypes = len(traj.type_names)
     counts = np.bincount(traj.types, minlength=ntypes)
     species = " ".join(f"sp{i + 1} {counts[i]}" for i in range(ntypes))
-    lines = ["system", "custom", dump_path, traj.scheme.script_line(), species,
+    lines = ["system", fmt, dump_path, traj.scheme.script_line(), species,
              " ".join(traj.type_names)]
     for i in range(ntypes):
         lines.append(" ".join("1" if j == i else "0" for j in range(ntypes)))
+    if fmt == "xyz":
+        # System::xyz_prep (src/system.cpp:389-407): box lengths, then bounds
+        lo = traj.box_lo.astype(np.float32)
+        hi = (traj.box_lo.astype(np.float64) + traj.box.astype(np.float64)).astype(np.float32)
+        lines.append(" ".join(f"{np.float32(v):.9g}" for v in traj.box))
+        lines.append(" ".join(f"{lo[d]:.9g} {hi[d]:.9g}" for d in range(3)))
     return "\n".join(lines) + "\n"

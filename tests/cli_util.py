@@ -23,9 +23,10 @@ def write_qvectors(qvec, directory):
 
 
 def run_cli(traj, commands, directory, qvec=None, extra_env=None):
+    # written in the trajectory's own file format (custom, custom_byid or xyz)
     dump = os.path.join(directory, "traj.dump")
     if not os.path.exists(dump):
-        synth.write_custom_dump(traj, dump)
+        synth.write_trajectory(traj, dump)
     with open(os.path.join(directory, "in.amdat"), "w") as f:
         f.write(synth.system_header(traj, dump) + commands)
     env = dict(os.environ)

@@ -143,6 +143,48 @@ rdf ./rdf2.dat symmetric 50 0 3.0 \\sg2
 list all
 structure_factor_from_rdf ./sk_rdf2.dat 25 g2
 """),
+    # xyz input (wrapped coordinates only; the reader unwraps them), binary mixture
+    "xyz_binary": dict(
+        n=180, box=6.0, sigma=0.6, seed=77, fractions=(0.6, 0.4), fmt="xyz",
+        scheme=synth.TimeScheme.exponential(3, 8, 1.4, 0, 0, 0.01),
+        commands="""create_list all
+all
+create_list b
+type_system 2
+msd ./msd.dat
+list all
+ngp ./ngp_b.dat
+list b
+isfs ./isfs.dat 8 10 xyz 0
+list all
+vhs ./vhs.dat 0.5 30
+list all
+structure_factor ./sk.dat symmetric xyz 0 -1
+list all
+isf ./isf.dat auto symmetric xyz 0 0 10
+list all
+rdf ./rdf.dat symmetric 60 -1 0
+list all
+"""),
+    # custom_byid: atom lines shuffled in every frame, placed by their id column
+    "byid_binary": dict(
+        n=160, box=6.0, sigma=0.3, seed=88, fractions=(0.5, 0.5), fmt="custom_byid",
+        scheme=synth.TimeScheme.exponential(3, 6, 1.4, 0, 0, 0.01),
+        commands="""create_list all
+all
+create_list a
+type_system 1
+msd ./msd_a.dat
+list a
+ngp ./ngp.dat
+list all
+vhs ./vhs.dat 0.5 30
+list all
+rdf ./rdf.dat symmetric 40 -1 0
+list all
+isfs ./isfs.dat 8 9 xyz 0
+list a
+"""),
     "siblings_lin": dict(
         n=120, box=6.0, sigma=0.1, seed=55, fractions=(1.0,), time_scaled=False,
         scheme=synth.TimeScheme.linear(16, 1.0),
@@ -168,11 +210,16 @@ def make(case: str) -> None:
     traj = synth.random_walk(cfg["n"], cfg["box"], cfg["scheme"], cfg["sigma"], cfg["seed"],
                              type_fractions=cfg["fractions"],
                              time_scaled=cfg.get("time_scaled", True))
+    fmt = cfg.get("fmt", "custom")
+    if fmt == "xyz":
+        traj = synth.as_xyz_input(traj)
+    traj.file_format = fmt
     out_dir = os.path.join(HERE, case)
     os.makedirs(out_dir, exist_ok=True)
     s = cfg["scheme"]
+    extra = {"wrapped": traj.wrapped_given} if fmt == "xyz" else {}
     np.savez_compressed(os.path.join(out_dir, "traj.npz"), unwrapped=traj.unwrapped,
-                        box=traj.box, box_lo=traj.box_lo, types=traj.types,
+                        box=traj.box, box_lo=traj.box_lo, types=traj.types, fmt=np.asarray(fmt), **extra,
                         scheme=np.asarray([s.n_exponentials, s.n_exponential_steps, s.frt,
                                            s.first_exponent]),
                         scheme_f=np.asarray([s.exp_base, s.time_unit]),
@@ -181,7 +228,7 @@ def make(case: str) -> None:
         f.write(cfg["commands"])
     with tempfile.TemporaryDirectory() as tmp:
         dump = os.path.join(tmp, "traj.dump")
-        synth.write_custom_dump(traj, dump)
+        synth.write_trajectory(traj, dump)
         with open(os.path.join(tmp, "in.amdat"), "w") as f:
             f.write(synth.system_header(traj, dump) + cfg["commands"])
         r = subprocess.run([ref, "-i", "in.amdat"], cwd=tmp, capture_output=True, text=True)
@@ -207,7 +254,9 @@ def load(case: str):
     ntypes = int(z["types"].max()) + 1
     traj = synth.Trajectory(unwrapped=z["unwrapped"], box=z["box"], box_lo=z["box_lo"],
                             types=z["types"], scheme=s,
-                            type_names=tuple(str(i + 1) for i in range(ntypes)))
+                            type_names=tuple(str(i + 1) for i in range(ntypes)),
+                            wrapped_given=z["wrapped"] if "wrapped" in z.files else None,
+                            file_format=str(z["fmt"]) if "fmt" in z.files else "custom")
     with open(os.path.join(d, "script.in")) as f:
         script = f.read()
     outs = {fn: open(os.path.join(d, fn)).read() for fn in sorted(os.listdir(d))

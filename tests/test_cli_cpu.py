@@ -69,3 +69,77 @@ def test_valid_script_without_gpu(built, traj, tmp_path):
         pytest.skip("a GPU is present")
     r = run_cli(traj, "create_list all\nall\nmsd ./msd.dat\nlist all\n", str(tmp_path))
     assert r.returncode == 1 and "no CUDA device" in r.stderr
+
+
+def _xyz_script(traj, path, fmt="xyz", drop_box=False):
+    hdr = synth.system_header(traj, path, fmt)
+    if drop_box:
+        hdr = "\n".join(hdr.splitlines()[:-2]) + "\n"
+    return hdr
+
+
+def test_xyz_input_faults(built, traj, tmp_path):
+    import subprocess
+    xyz = str(tmp_path / "traj.xyz")
+    synth.write_xyz(traj, xyz)
+    bad = synth.Trajectory(unwrapped=traj.unwrapped[:, :19], box=traj.box, box_lo=traj.box_lo,
+                           types=traj.types[:19], scheme=traj.scheme)
+    (tmp_path / "in.amdat").write_text(_xyz_script(bad, xyz))
+    r = subprocess.run([CLI, "-i", "in.amdat"], cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode == 1 and "inconsistent with user input: 20 != 19" in r.stderr
+    # the box lines are part of the xyz system block
+    (tmp_path / "in.amdat").write_text(_xyz_script(traj, xyz, drop_box=True))
+    r = subprocess.run([CLI, "-i", "in.amdat"], cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode == 1 and "input script ended early" in r.stderr
+    (tmp_path / "in.amdat").write_text(_xyz_script(traj, xyz, drop_box=True) + "10 10\n0 10 0 10 0 10\n")
+    r = subprocess.run([CLI, "-i", "in.amdat"], cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode == 1 and "bad box lines" in r.stderr
+    # a type label beyond the declared atom types
+    txt = open(xyz).read().splitlines()
+    txt[5] = "7" + txt[5][1:]
+    open(xyz, "w").write("\n".join(txt) + "\n")
+    (tmp_path / "in.amdat").write_text(_xyz_script(traj, xyz))
+    r = subprocess.run([CLI, "-i", "in.amdat"], cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode == 1 and "out of range" in r.stderr
+    (tmp_path / "in.amdat").write_text(_xyz_script(traj, str(tmp_path / "none.xyz")))
+    r = subprocess.run([CLI, "-i", "in.amdat"], cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode == 1 and "XYZ Trajectory file not found" in r.stderr
+
+
+def test_xyz_valid_script_parses_without_gpu(built, traj, tmp_path):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    xyz = synth.as_xyz_input(traj)
+    r = run_cli(xyz, "create_list all\nall\nmsd ./msd.dat\nlist all\n", str(tmp_path))
+    assert r.returncode == 1 and "no CUDA device" in r.stderr
+
+
+def test_xyz_unwrap_rule():
+    # Trajectory::unwrap: a crossing of the periodic boundary is undone, a
+    # displacement below 0.55 L is kept as it is
+    box = np.array([10.0, 10.0, 10.0], np.float32)
+    w = np.array([[[9.5, 0.2, 5.0]], [[0.3, 9.9, 5.0]], [[5.6, 4.0, 5.0]]], np.float32)
+    u = synth.unwrap_from_wrapped(w, box)
+    assert np.allclose(u[1, 0], [10.3, -0.1, 5.0], atol=1e-5)
+    # a step of 5.3 (< 0.55 L) is kept; a step of -5.9 is folded by one box length
+    assert np.allclose(u[2, 0], [15.6, 4.0, 5.0], atol=1e-5)
+
+
+def test_custom_byid_faults(built, traj, tmp_path):
+    import subprocess
+    dump = str(tmp_path / "traj.dump")
+    synth.write_custom_dump(traj, dump, shuffle_seed=5)
+    lines = open(dump).read().splitlines()
+    # frame 0's first atom line takes the id of its second: one id repeats
+    a, b = lines[9].split(), lines[10].split()
+    lines[9] = " ".join([b[0]] + a[1:])
+    open(dump, "w").write("\n".join(lines) + "\n")
+    (tmp_path / "in.amdat").write_text(synth.system_header(traj, dump, "custom_byid"))
+    r = subprocess.run([CLI, "-i", "in.amdat"], cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode == 1 and "Atom ids should begin with 1" in r.stderr
+    # the same file without an id column
+    lines = [ln.replace("ITEM: ATOMS id type", "ITEM: ATOMS ix type") for ln in lines]
+    open(dump, "w").write("\n".join(lines) + "\n")
+    r = subprocess.run([CLI, "-i", "in.amdat"], cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode == 1 and "atom id data not provided" in r.stderr
