@@ -1,0 +1,440 @@
+// Spatially binned displacement analyses:
+//   System::boxify                      (src/system.cpp:4799-4870)
+//   Trajectory_List_Bins::assign_bins   (src/trajectory_list_bins.cpp:949-1096),
+//     with the region rules of its constructors (:207-394)
+//   Bin_Static_Analysis::analyze        (src/bin_static_analysis.h:69-111): one
+//     analysis per bin over the list members in that bin at the start frame t0
+//   Bin_Dynamics_Analysis::list_displacementkernel (src/bin_dynamics_analysis.h):
+//     the members in the bin at both t0 and t1 (persistence), with the pairs of
+//     displacement_list(this), i.e. fullblock 0
+// for the MSD (Mean_Square_Displacement::listkernel) and F_s
+// (Incoherent_Scattering_Function::listkernel) of every bin at once.
+//
+// The reference builds one time-dependent list per bin and runs the analysis
+// B times.  Here a bin map (flat bin per atom per frame, int32, -1 outside)
+// is built once on the device, and one pass over (time pair, list member)
+// keys each term by the member's bin: every atom's trajectory is read once per
+// pair for all bins together.  Terms of one warp that share a bin are summed
+// by the warp's lowest such lane (FP64, lane order) and added with one atomic to
+// a per-block shared-memory accumulator [bin][1 + shells], flushed to the
+// global [bin][gap][1 + shells] sums at the end of each item.  Counts are
+// exact integers; the FP64 sums are order-independent to rounding (atomics).
+#include <algorithm>
+#include <cfloat>
+#include <cstring>
+#include <vector>
+
+#include "disp_common.cuh"
+#include "engine.h"
+
+namespace amdat {
+
+constexpr int BN_THREADS = 256;
+constexpr int BN_CHUNK = 2048;
+constexpr int BN_MAX_FS = 8;
+constexpr size_t BN_STAGE_LIMIT = 48 * 1024;  // shared accumulators per block
+
+// --- boxify and bin assignment -------------------------------------------------
+__global__ void boxify_kernel(float* __restrict__ w, int64_t n_pad, int32_t n_atoms, int64_t n_terms,
+                              float3 lo, float3 hi) {
+  const float L[3] = {__fsub_rn(hi.x, lo.x), __fsub_rn(hi.y, lo.y), __fsub_rn(hi.z, lo.z)};
+  const float l[3] = {lo.x, lo.y, lo.z}, h[3] = {hi.x, hi.y, hi.z};
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_terms;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t t = i / n_atoms, a = i - t * n_atoms;
+    float* c = w + t * 3 * n_pad + a;
+    const float x[3] = {c[0], c[n_pad], c[2 * n_pad]};
+    bool out = false;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) out |= (x[d] < l[d]) | (x[d] > h[d]);
+    if (!out) continue;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const float sh = x[d] > h[d] ? -1.f : (x[d] < l[d] ? 1.f : 0.f);
+      c[d * n_pad] = __fadd_rn(x[d], __fmul_rn(L[d], sh));
+    }
+  }
+}
+
+// int((x - lo + 10 FLT_EPSILON) / (hi - lo + 20 FLT_EPSILON) * n): the two
+// differences in FP32, everything after them in FP64
+__device__ __forceinline__ int bin_axis(float x, float lo, float hi, int n) {
+  const double num = __dadd_rn((double)__fsub_rn(x, lo), (double)FLT_EPSILON * 10.0);
+  const double den = __dadd_rn((double)__fsub_rn(hi, lo), (double)FLT_EPSILON * 20.0);
+  return (int)__dmul_rn(__ddiv_rn(num, den), (double)(float)n);
+}
+
+__global__ void bins_assign_kernel(const float* __restrict__ w, int64_t n_pad, int32_t n_atoms,
+                                   int64_t n_terms, int3 nb, float3 lo, float3 hi,
+                                   int32_t* __restrict__ bins) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_terms;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t t = i / n_atoms, a = i - t * n_atoms;
+    const float* c = w + t * 3 * n_pad + a;
+    const float x = c[0], y = c[n_pad], z = c[2 * n_pad];
+    int32_t b = -1;
+    if (x < hi.x && x > lo.x && y < hi.y && y > lo.y && z < hi.z && z > lo.z)
+      b = (bin_axis(x, lo.x, hi.x, nb.x) * nb.y + bin_axis(y, lo.y, hi.y, nb.y)) * nb.z +
+          bin_axis(z, lo.z, hi.z, nb.z);
+    bins[t * n_pad + a] = b;
+  }
+}
+
+__global__ void bins_count_kernel(const int32_t* __restrict__ bins, int64_t n_pad, int32_t n_atoms,
+                                  int64_t n_terms, int32_t n_bins, unsigned long long* __restrict__ counts) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_terms;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t t = i / n_atoms, a = i - t * n_atoms;
+    const int32_t b = bins[t * n_pad + a];
+    if (b >= 0 && b < n_bins) atomicAdd(counts + t * n_bins + b, 1ull);
+  }
+}
+
+// --- the binned displacement pass ----------------------------------------------
+struct BnItem {
+  int32_t pair, a0, a1, gap;
+};
+
+struct BnParams {
+  const float* u;
+  int64_t n_pad;
+  int32_t list_first;
+  const int32_t* list_idx;  // nullptr: members are list_first + i
+  const int32_t* t0;
+  const int32_t* t1;
+  const BnItem* items;
+  int32_t n_items;
+  int32_t* counter;
+  const int32_t* bins;  // [frames][n_pad]
+  int32_t n_bins;
+  int32_t persistent;
+  int32_t n_fs;
+  const int4* kv;
+  const int32_t* kv_off;
+  const float* inv_count;
+  float period;
+  int32_t n_gaps;
+  int32_t stride;  // 1 + n_fs
+  double* acc;     // [bin][gap][stride]
+  unsigned long long* cnt;  // [bin][gap]
+  int32_t staged;  // per-block shared accumulators
+};
+
+template <bool FS>
+__global__ void __launch_bounds__(BN_THREADS) disp_bins_kernel(BnParams p) {
+  extern __shared__ double bn_smem[];  // staged: [n_bins][stride] sums, then [n_bins] counts
+  __shared__ int s_item;
+  __shared__ float s_val[BN_THREADS / 32][32][1 + BN_MAX_FS];
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int stride = p.stride;
+  double* sacc = bn_smem;
+  unsigned int* scnt = reinterpret_cast<unsigned int*>(bn_smem + (size_t)p.n_bins * stride);
+
+  for (;;) {
+    if (tid == 0) s_item = atomicAdd(p.counter, 1);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= p.n_items) break;
+    const BnItem it = p.items[item];
+    const int t0 = __ldg(p.t0 + it.pair), t1 = __ldg(p.t1 + it.pair);
+    const float* X0 = p.u + (int64_t)t0 * 3 * p.n_pad;
+    const float* X1 = p.u + (int64_t)t1 * 3 * p.n_pad;
+    const int32_t* B0 = p.bins + (int64_t)t0 * p.n_pad;
+    const int32_t* B1 = p.bins + (int64_t)t1 * p.n_pad;
+    if (p.staged) {
+      for (int i = tid; i < p.n_bins * stride; i += BN_THREADS) sacc[i] = 0.0;
+      for (int i = tid; i < p.n_bins; i += BN_THREADS) scnt[i] = 0u;
+      __syncthreads();
+    }
+    for (int base = it.a0; base < it.a1; base += BN_THREADS) {
+      const int a = base + tid;
+      int b = -1;
+      float v[1 + BN_MAX_FS];
+#pragma unroll
+      for (int k = 0; k < 1 + BN_MAX_FS; ++k) v[k] = 0.f;
+      if (a < it.a1) {
+        const int atom = p.list_idx ? __ldg(p.list_idx + a) : p.list_first + a;
+        b = __ldg(B0 + atom);
+        if (b >= 0 && p.persistent && __ldg(B1 + atom) != b) b = -1;
+        if (b >= 0) {
+          const float dx = __fsub_rn(__ldg(X1 + atom), __ldg(X0 + atom));
+          const float dy = __fsub_rn(__ldg(X1 + p.n_pad + atom), __ldg(X0 + p.n_pad + atom));
+          const float dz = __fsub_rn(__ldg(X1 + 2 * p.n_pad + atom), __ldg(X0 + 2 * p.n_pad + atom));
+          v[0] = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+          if (FS) {
+            const int32_t fx = turns_fixed(dx, p.period);
+            const int32_t fy = turns_fixed(dy, p.period);
+            const int32_t fz = turns_fixed(dz, p.period);
+#pragma unroll
+            for (int s = 0; s < BN_MAX_FS; ++s) {
+              if (s >= p.n_fs) break;
+              KSum acc = {0.f, 0.f};
+              float blk = 0.f;
+              int cnt = 0;
+              for (int q = p.kv_off[s]; q < p.kv_off[s + 1]; ++q) {
+                const int4 n = __ldg(p.kv + q);
+                const int32_t ph = (int32_t)((uint32_t)n.x * (uint32_t)fx + (uint32_t)n.y * (uint32_t)fy +
+                                             (uint32_t)n.z * (uint32_t)fz);
+                blk += cos_fixed(ph);
+                if (++cnt == 32) {
+                  kadd(acc, blk);
+                  blk = 0.f;
+                  cnt = 0;
+                }
+              }
+              kadd(acc, blk);
+              v[1 + s] = __fmul_rn(__fsub_rn(acc.s, acc.c), p.inv_count[s]);
+            }
+          }
+        }
+      }
+      // lanes of one bin: the lowest adds their terms (lane order, FP64)
+#pragma unroll
+      for (int k = 0; k < 1 + BN_MAX_FS; ++k)
+        if (k < stride) s_val[warp][lane][k] = v[k];
+      __syncwarp();
+      const unsigned peers = __match_any_sync(0xffffffffu, b);
+      if (b >= 0 && lane == __ffs(peers) - 1) {
+        const unsigned n_peers = (unsigned)__popc(peers);
+        for (int k = 0; k < stride; ++k) {
+          double sum = 0.0;
+          for (unsigned m = peers; m; m &= m - 1) sum += (double)s_val[warp][__ffs(m) - 1][k];
+          if (p.staged)
+            atomicAdd(sacc + b * stride + k, sum);
+          else
+            atomicAdd(p.acc + ((int64_t)b * p.n_gaps + it.gap) * stride + k, sum);
+        }
+        if (p.staged)
+          atomicAdd(scnt + b, n_peers);
+        else
+          atomicAdd(p.cnt + (int64_t)b * p.n_gaps + it.gap, (unsigned long long)n_peers);
+      }
+      __syncwarp();
+    }
+    if (p.staged) {
+      __syncthreads();
+      for (int i = tid; i < p.n_bins; i += BN_THREADS) {
+        if (!scnt[i]) continue;
+        atomicAdd(p.cnt + (int64_t)i * p.n_gaps + it.gap, (unsigned long long)scnt[i]);
+        for (int k = 0; k < stride; ++k)
+          atomicAdd(p.acc + ((int64_t)i * p.n_gaps + it.gap) * stride + k, sacc[i * stride + k]);
+      }
+    }
+    __syncthreads();
+  }
+}
+
+static BinMap& bin_map(amdat_ctx* ctx, int32_t handle) {
+  auto it = ctx->bin_maps.find(handle);
+  if (it == ctx->bin_maps.end()) throw Error(AMDAT_ERR_ARGUMENT, "unknown bin map handle");
+  BinMap& m = *it->second;
+  if (m.n_frames != ctx->n_frames || m.n_pad != ctx->n_pad)
+    throw Error(AMDAT_ERR_STATE, "the bin map was made for another trajectory");
+  return m;
+}
+
+static unsigned grid_for(amdat_ctx* ctx, int64_t n) {
+  return (unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n, 256), (int64_t)ctx->n_sm * 16));
+}
+
+}  // namespace amdat
+
+using namespace amdat;
+
+extern "C" {
+
+amdat_status amdat_boxify(amdat_ctx* ctx, const float* lo, const float* hi) {
+  return guarded([&] {
+    check_ctx(ctx);
+    if (!ctx->have_traj) throw Error(AMDAT_ERR_STATE, "no trajectory uploaded");
+    AMDAT_REQUIRE(lo && hi, "null bounds");
+    for (int d = 0; d < 3; ++d) AMDAT_REQUIRE(hi[d] > lo[d], "box bounds must satisfy hi > lo");
+    const int64_t n = (int64_t)ctx->n_frames * ctx->n_atoms;
+    if (n == 0) return;
+    boxify_kernel<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(ctx->w.ptr, ctx->n_pad, ctx->n_atoms, n,
+                                                              make_float3(lo[0], lo[1], lo[2]),
+                                                              make_float3(hi[0], hi[1], hi[2]));
+    check_launch("boxify_kernel");
+    count_launch(ctx);
+    // the FP64 copies are promoted again from the boxified planes when next needed
+    ctx->u64.release();
+    ctx->w64.release();
+  });
+}
+
+amdat_status amdat_bins_create(amdat_ctx* ctx, int32_t nx, int32_t ny, int32_t nz, const float* lo,
+                               const float* hi, int32_t* handle) {
+  return guarded([&] {
+    check_ctx(ctx);
+    if (!ctx->have_traj) throw Error(AMDAT_ERR_STATE, "no trajectory uploaded");
+    AMDAT_REQUIRE(lo && hi && handle, "null argument");
+    AMDAT_REQUIRE(nx > 0 && ny > 0 && nz > 0, "bin counts must be positive");
+    AMDAT_REQUIRE((int64_t)nx * ny * nz <= (1 << 24), "at most 2^24 bins");
+    auto* m = new BinMap();
+    try {
+      m->nx = nx, m->ny = ny, m->nz = nz;
+      m->n_frames = ctx->n_frames, m->n_pad = ctx->n_pad;
+      m->bin.reserve((size_t)ctx->n_frames * ctx->n_pad);
+      AMDAT_CUDA(cudaMemsetAsync(m->bin.ptr, 0xff, (size_t)ctx->n_frames * ctx->n_pad * 4, ctx->stream));
+      const int64_t n = (int64_t)ctx->n_frames * ctx->n_atoms;
+      if (n > 0) {
+        bins_assign_kernel<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(
+            ctx->w.ptr, ctx->n_pad, ctx->n_atoms, n, make_int3(nx, ny, nz), make_float3(lo[0], lo[1], lo[2]),
+            make_float3(hi[0], hi[1], hi[2]), m->bin.ptr);
+        check_launch("bins_assign_kernel");
+        count_launch(ctx);
+      }
+    } catch (...) {
+      delete m;
+      throw;
+    }
+    const int32_t h = ctx->next_bins++;
+    ctx->bin_maps[h] = m;
+    *handle = h;
+  });
+}
+
+amdat_status amdat_bins_free(amdat_ctx* ctx, int32_t handle) {
+  return guarded([&] {
+    check_ctx(ctx);
+    auto it = ctx->bin_maps.find(handle);
+    if (it == ctx->bin_maps.end()) throw Error(AMDAT_ERR_ARGUMENT, "unknown bin map handle");
+    AMDAT_CUDA(cudaStreamSynchronize(ctx->stream));
+    delete it->second;
+    ctx->bin_maps.erase(it);
+  });
+}
+
+amdat_status amdat_bins_read(amdat_ctx* ctx, int32_t handle, int32_t out_flags, int32_t* bins,
+                             int64_t* counts) {
+  return guarded([&] {
+    check_ctx(ctx);
+    AMDAT_REQUIRE(out_flags == AMDAT_OUT_HOST || out_flags == AMDAT_OUT_DEVICE, "bad out_flags");
+    BinMap& m = bin_map(ctx, handle);
+    const int T = ctx->n_frames, N = ctx->n_atoms;
+    const int32_t B = m.nx * m.ny * m.nz;
+    const cudaMemcpyKind kind = out_flags == AMDAT_OUT_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    if (bins && N > 0)
+      AMDAT_CUDA(cudaMemcpy2DAsync(bins, (size_t)N * 4, m.bin.ptr, (size_t)ctx->n_pad * 4, (size_t)N * 4, T, kind,
+                                   ctx->stream));
+    if (counts) {
+      unsigned long long* d = reinterpret_cast<unsigned long long*>(ctx->scratch.reserve((size_t)T * B * 8));
+      AMDAT_CUDA(cudaMemsetAsync(d, 0, (size_t)T * B * 8, ctx->stream));
+      const int64_t n = (int64_t)T * N;
+      if (n > 0) {
+        bins_count_kernel<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(m.bin.ptr, ctx->n_pad, N, n, B, d);
+        check_launch("bins_count_kernel");
+        count_launch(ctx);
+      }
+      AMDAT_CUDA(cudaMemcpyAsync(counts, d, (size_t)T * B * 8, kind, ctx->stream));
+    }
+    AMDAT_CUDA(cudaStreamSynchronize(ctx->stream));
+  });
+}
+
+amdat_status amdat_disp_bins_run(amdat_ctx* ctx, int32_t list, int32_t bins, int32_t persistent,
+                                 int32_t fullblock, int32_t n_shells, const int32_t* shell_offsets,
+                                 const int32_t* kvec, float period, int32_t out_flags, double* sum_d2,
+                                 int64_t* count, double* fs_sum) {
+  return guarded([&] {
+    check_ctx(ctx);
+    if (!ctx->have_traj) throw Error(AMDAT_ERR_STATE, "no trajectory uploaded");
+    if (!ctx->have_scheme) throw Error(AMDAT_ERR_STATE, "no time scheme set");
+    AMDAT_REQUIRE(out_flags == AMDAT_OUT_HOST || out_flags == AMDAT_OUT_DEVICE, "bad out_flags");
+    AMDAT_REQUIRE(n_shells >= 0 && n_shells <= BN_MAX_FS, "n_shells must be in [0, 8]");
+    AMDAT_REQUIRE(n_shells == 0 || (shell_offsets && kvec && period > 0.f), "shells need vectors and a period");
+    BinMap& m = bin_map(ctx, bins);
+    const ListEntry& e = list_entry(ctx, list);
+    // Bin_Dynamics_Analysis enumerates displacement_list(this): fullblock 0
+    const PairTable& P = pair_table(ctx, persistent ? false : fullblock != 0, false);
+    const int G = P.n_gaps;
+    const int32_t B = m.nx * m.ny * m.nz;
+    const int stride = 1 + n_shells;
+    // shells (list mode: one cosine per vector)
+    std::vector<int4> kv;
+    std::vector<int32_t> off(1, 0);
+    std::vector<float> inv;
+    for (int s = 0; s < n_shells; ++s) {
+      AMDAT_REQUIRE(shell_offsets[s + 1] >= shell_offsets[s], "shell offsets must ascend");
+      for (int q = shell_offsets[s]; q < shell_offsets[s + 1]; ++q)
+        kv.push_back(make_int4(kvec[3 * q], kvec[3 * q + 1], kvec[3 * q + 2], 0));
+      off.push_back((int32_t)kv.size());
+      const int c = shell_offsets[s + 1] - shell_offsets[s];
+      inv.push_back(c ? 1.0f / (float)c : 0.0f);
+    }
+    // items: (pair, member chunk), gap-major
+    const int nch = (int)std::max<int64_t>(1, ceil_div(e.n, BN_CHUNK));
+    std::vector<BnItem> items;
+    if (e.n > 0)
+      for (int g = 0; g < G; ++g)
+        for (int p = P.gap_first[g]; p < P.gap_first[g + 1]; ++p)
+          for (int c = 0; c < nch; ++c)
+            items.push_back(BnItem{p, (int32_t)((int64_t)e.n * c / nch), (int32_t)((int64_t)e.n * (c + 1) / nch), g});
+    auto align = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    size_t o = 0;
+    const size_t o_items = o; o = align(o + std::max<size_t>(items.size(), 1) * sizeof(BnItem));
+    const size_t o_kv = o; o = align(o + std::max<size_t>(kv.size(), 1) * sizeof(int4));
+    const size_t o_off = o; o = align(o + off.size() * 4);
+    const size_t o_inv = o; o = align(o + std::max<size_t>(inv.size(), 1) * 4);
+    const size_t o_ctr = o; o = align(o + 4);
+    const size_t o_acc = o; o = align(o + (size_t)B * G * stride * 8);
+    const size_t o_cnt = o; o = align(o + (size_t)B * G * 8);
+    unsigned char* base = ctx->scratch.reserve(o);
+    cudaStream_t st = ctx->stream;
+    if (!items.empty())
+      AMDAT_CUDA(cudaMemcpyAsync(base + o_items, items.data(), items.size() * sizeof(BnItem), cudaMemcpyHostToDevice, st));
+    if (!kv.empty()) {
+      AMDAT_CUDA(cudaMemcpyAsync(base + o_kv, kv.data(), kv.size() * sizeof(int4), cudaMemcpyHostToDevice, st));
+      AMDAT_CUDA(cudaMemcpyAsync(base + o_inv, inv.data(), inv.size() * 4, cudaMemcpyHostToDevice, st));
+    }
+    AMDAT_CUDA(cudaMemcpyAsync(base + o_off, off.data(), off.size() * 4, cudaMemcpyHostToDevice, st));
+    AMDAT_CUDA(cudaMemsetAsync(base + o_ctr, 0, o - o_ctr, st));
+    if (!items.empty()) {
+      BnParams p{};
+      p.u = ctx->u.ptr;
+      p.n_pad = ctx->n_pad;
+      p.list_first = e.first;
+      p.list_idx = e.contiguous ? nullptr : e.idx.ptr;
+      p.t0 = P.t0.ptr;
+      p.t1 = P.t1.ptr;
+      p.items = (const BnItem*)(base + o_items);
+      p.n_items = (int32_t)items.size();
+      p.counter = (int32_t*)(base + o_ctr);
+      p.bins = m.bin.ptr;
+      p.n_bins = B;
+      p.persistent = persistent ? 1 : 0;
+      p.n_fs = n_shells;
+      p.kv = (const int4*)(base + o_kv);
+      p.kv_off = (const int32_t*)(base + o_off);
+      p.inv_count = (const float*)(base + o_inv);
+      p.period = n_shells ? period : 1.0f;
+      p.n_gaps = G;
+      p.stride = stride;
+      p.acc = (double*)(base + o_acc);
+      p.cnt = (unsigned long long*)(base + o_cnt);
+      const size_t stage = (size_t)B * stride * 8 + (size_t)B * 4;
+      p.staged = stage <= BN_STAGE_LIMIT ? 1 : 0;
+      const size_t shm = p.staged ? stage : 0;
+      auto kern = n_shells ? disp_bins_kernel<true> : disp_bins_kernel<false>;
+      if (shm > 0) AMDAT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+      int per_sm = 1;
+      AMDAT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BN_THREADS, shm));
+      const int grid = (int)std::min<int64_t>((int64_t)ctx->n_sm * std::max(per_sm, 1), (int64_t)items.size());
+      KernelTimer kt(ctx, "disp_bins_kernel");
+      kern<<<grid, BN_THREADS, shm, st>>>(p);
+      check_launch("disp_bins_kernel");
+      count_launch(ctx);
+    }
+    const cudaMemcpyKind kind = out_flags == AMDAT_OUT_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    // [bin][gap][stride] -> sum_d2[bin][gap], fs_sum[bin][gap][shell]
+    if (sum_d2)
+      AMDAT_CUDA(cudaMemcpy2DAsync(sum_d2, 8, base + o_acc, (size_t)stride * 8, 8, (size_t)B * G, kind, st));
+    if (fs_sum && n_shells)
+      AMDAT_CUDA(cudaMemcpy2DAsync(fs_sum, (size_t)n_shells * 8, base + o_acc + 8, (size_t)stride * 8,
+                                   (size_t)n_shells * 8, (size_t)B * G, kind, st));
+    if (count) AMDAT_CUDA(cudaMemcpyAsync(count, base + o_cnt, (size_t)B * G * 8, kind, st));
+    AMDAT_CUDA(cudaStreamSynchronize(st));
+  });
+}
+
+}  // extern "C"

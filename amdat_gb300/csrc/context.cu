@@ -176,6 +176,7 @@ amdat_ctx::~amdat_ctx() {
     delete kv.second;
   }
   for (auto* b : rho_pool) delete b;
+  for (auto& kv : bin_maps) delete kv.second;
   amdat::lattice_plans_free(this);
   amdat::sk_adjoint_plans_free(this);
   for (auto& r : prof_pending) {

@@ -1,0 +1,50 @@
+// Device helpers shared by the displacement kernels: compensated FP32 sums and
+// the fixed-point F_s phases (a displacement as an int32 fraction of a turn,
+// 2^-31 turns per unit, so the phase of an integer lattice vector is an exact
+// wrapping integer combination and only the final conversion rounds).
+#pragma once
+
+#include <cstdint>
+
+namespace amdat {
+
+// --- compensated FP32 helpers ------------------------------------------------
+struct KSum {
+  float s, c;
+};
+__device__ __forceinline__ void kadd(KSum& k, float v) {
+  float y = __fsub_rn(v, k.c);
+  float t = __fadd_rn(k.s, y);
+  k.c = __fsub_rn(__fsub_rn(t, k.s), y);
+  k.s = t;
+}
+// error-free sum of two compensated values (TwoSum of the leading parts)
+__device__ __forceinline__ KSum kmerge(KSum a, KSum b) {
+  float s = __fadd_rn(a.s, b.s);
+  float bb = __fsub_rn(s, a.s);
+  float err = __fadd_rn(__fsub_rn(a.s, __fsub_rn(s, bb)), __fsub_rn(b.s, bb));
+  // a KSum holds the value s - c: (a.s - a.c) + (b.s - b.c) = s + err - a.c - b.c
+  KSum r;
+  r.s = s;
+  r.c = __fsub_rn(__fadd_rn(a.c, b.c), err);
+  return r;
+}
+__device__ __forceinline__ KSum kshfl(KSum v, int off) {
+  KSum o;
+  o.s = __shfl_down_sync(0xffffffffu, v.s, off);
+  o.c = __shfl_down_sync(0xffffffffu, v.c, off);
+  return o;
+}
+
+// fraction of a turn dr/L, as int32 in units of 2^-31 turns (exact wrap)
+__device__ __forceinline__ int32_t turns_fixed(float d, float period) {
+  float t = __fdiv_rn(d, period);
+  t = __fsub_rn(t, rintf(t));  // [-0.5, 0.5]
+  return __float2int_rn(__fmul_rn(t, 2147483648.0f));
+}
+// cos(2 pi * phase * 2^-31)
+__device__ __forceinline__ float cos_fixed(int32_t phase) {
+  return cospif(__fmul_rn((float)phase, 9.313225746154785e-10f));  // 2^-30
+}
+
+}  // namespace amdat

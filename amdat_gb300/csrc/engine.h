@@ -109,6 +109,14 @@ struct PairTable {
 struct LatticePlanDev;
 struct SkAdjointPlan;
 
+// Spatial bins of the wrapped coordinates: flat bin (ix * ny + iy) * nz + iz of
+// every atom in every frame, -1 outside the binned region
+struct BinMap {
+  int32_t nx = 0, ny = 0, nz = 0;
+  int32_t n_frames = 0, n_pad = 0;  // trajectory shape the map was made for
+  DevBuf<int32_t> bin;              // [frames][n_pad]
+};
+
 struct Density {
   int32_t list = 0;
   int32_t n_k = 0;
@@ -153,6 +161,8 @@ struct amdat_ctx {
   std::map<int, amdat::PairTable*> pair_cache;  // key: fullblock*2 + loop_order
   std::map<int32_t, amdat::Density*> densities;
   int32_t next_density = 1;
+  std::map<int32_t, amdat::BinMap*> bin_maps;
+  int32_t next_bins = 1;
 
   // scratch reused across calls
   amdat::DevBuf<unsigned char> scratch;

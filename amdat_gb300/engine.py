@@ -55,6 +55,8 @@ EXPORTED = [
     "amdat_disp_plan_destroy", "amdat_disp_plan_sharing", "amdat_disp_moments_noalloc",
     "amdat_gsmooth_run", "amdat_disp_axes_run",
     "amdat_gsmooth_adjoint", "amdat_structure_factor_adjoint",
+    "amdat_boxify", "amdat_bins_create", "amdat_bins_read", "amdat_bins_free",
+    "amdat_disp_bins_run",
 ]
 
 PLAN_AUTOTUNE, PLAN_GRAPH, PLAN_NO_SHARING = 1, 2, 4
@@ -91,6 +93,10 @@ def _p(a):
 
 def _i32(x):
     return np.ascontiguousarray(x, dtype=np.int32)
+
+
+def _f32(x):
+    return np.ascontiguousarray(x, dtype=np.float32)
 
 
 def make_scheme(ts, limit: int = 0) -> Scheme:
@@ -308,6 +314,46 @@ class Engine:
                                          C.c_float(bin_size), OUT_HOST, _p(ax), _p(d4), _p(cnt),
                                          _p(h) if n_bins else None))
         return dict(axis_sums=ax, sum_d4=d4, atom_pairs=cnt, d2_counts=h[:, :n_bins])
+
+    # ---- spatial bins
+    def boxify(self, lo, hi):
+        """System::boxify of the wrapped coordinates (amdat_boxify)."""
+        lo, hi = _f32(lo), _f32(hi)
+        _check(lib().amdat_boxify(self._ctx, _p(lo), _p(hi)))
+
+    def bins_create(self, nbins, lo, hi) -> int:
+        """Bin map of the wrapped coordinates (amdat_bins_create)."""
+        lo, hi = _f32(lo), _f32(hi)
+        h = C.c_int32()
+        _check(lib().amdat_bins_create(self._ctx, int(nbins[0]), int(nbins[1]), int(nbins[2]), _p(lo), _p(hi),
+                                       C.byref(h)))
+        return h.value
+
+    def bins_read(self, handle, n_frames, n_atoms, n_bins):
+        """(map [frames][atoms], members per frame and bin [frames][bins])."""
+        m = np.empty((n_frames, n_atoms), np.int32)
+        c = np.zeros((n_frames, n_bins), np.int64)
+        _check(lib().amdat_bins_read(self._ctx, int(handle), OUT_HOST, _p(m), _p(c)))
+        return m, c
+
+    def bins_free(self, handle):
+        _check(lib().amdat_bins_free(self._ctx, int(handle)))
+
+    def disp_bins(self, list_h, bins_h, n_bins, persistent=0, fullblock=0, shells=None, period=1.0):
+        """Per-bin sums (amdat_disp_bins_run): sum_d2 [B][G], count [B][G], fs_sum [B][G][S]."""
+        G = self.n_timegaps
+        d2 = np.zeros((n_bins, G))
+        cnt = np.zeros((n_bins, G), np.int64)
+        kv = off = None
+        S = 0
+        if shells is not None:
+            kv, off = _i32(shells[0]).reshape(-1), _i32(shells[1])
+            S = len(off) - 1
+        fs = np.zeros((n_bins, G, max(S, 1)))
+        _check(lib().amdat_disp_bins_run(self._ctx, int(list_h), int(bins_h), int(persistent), int(fullblock), S,
+                                         _p(off), _p(kv), C.c_float(period), OUT_HOST, _p(d2), _p(cnt),
+                                         _p(fs) if S else None))
+        return dict(sum_d2=d2, count=cnt, fs_sum=fs[:, :, :S])
 
     def plan(self, lists, fullblock=0, shells=None, period=1.0, n_bins=0, bin_max=0.0, flags=0):
         """Prepared many-list displacement run (amdat_disp_plan_*)."""

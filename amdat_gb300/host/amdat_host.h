@@ -63,6 +63,9 @@ class System {
   float min_box() const;  // min_box_dimensions().min()
   int atomtype_index(const std::string& name) const;
   int species_index(const std::string& name) const;
+  // box_boundary (src/system.cpp): the bounds as read, constant over time
+  const float* bounds_lo() const { return box_lo_; }
+  const float* bounds_hi() const { return box_hi_; }
   const std::vector<int>& atom_types() const { return atom_type_; }
   const std::vector<int>& atom_species() const { return atom_species_; }
 
@@ -73,7 +76,7 @@ class System {
   amdat_ctx* ctx_ = nullptr;
   amdat_scheme scheme_{};
   int n_atoms_ = 0, n_timesteps_ = 0, n_timegaps_ = 0;
-  float box_[3] = {0, 0, 0}, box_lo_[3] = {0, 0, 0};
+  float box_[3] = {0, 0, 0}, box_lo_[3] = {0, 0, 0}, box_hi_[3] = {0, 0, 0};
   std::vector<float> timelist_, gap_times_;
   std::vector<std::string> species_names_, type_names_;
   std::vector<int> molecules_per_species_;
@@ -122,12 +125,42 @@ class Wave_Vectors {
   std::vector<int32_t> offsets_; // [99 + 1]
 };
 
+// Trajectory_List_Bins (src/trajectory_list_bins.cpp:207-394, 949-1096): a
+// rectangular grid of bins over the box, or over a region of it (a bound of 0,
+// or one beyond the box, is the box's own); membership per frame from the
+// wrapped coordinates, which are boxified first (Control::create_bin_list).
+class Trajectory_List_Bins {
+ public:
+  Trajectory_List_Bins(System* sys, int nx, int ny, int nz);
+  Trajectory_List_Bins(System* sys, int nx, int ny, int nz, float xlo, float xhi, float ylo, float yhi,
+                       float zlo, float zhi);
+  ~Trajectory_List_Bins();
+  Trajectory_List_Bins(const Trajectory_List_Bins&) = delete;
+  Trajectory_List_Bins& operator=(const Trajectory_List_Bins&) = delete;
+  int handle() const { return handle_; }
+  int show_n_xbins() const { return n_[0]; }
+  int show_n_ybins() const { return n_[1]; }
+  int show_n_zbins() const { return n_[2]; }
+  int n_bins() const { return n_[0] * n_[1] * n_[2]; }
+
+ private:
+  void assign(const float lo[3], const float hi[3]);
+  System* sys_;
+  int n_[3];
+  int handle_ = 0;
+};
+
 class Analysis {
  public:
   virtual ~Analysis() = default;
   virtual void analyze(Trajectory_List* list) = 0;
   virtual void analyze(Trajectory_List* a, Trajectory_List* b);
   virtual void write(const std::string& file) const = 0;
+  // Bin_Static_Analysis (persistent = false) / Bin_Dynamics_Analysis
+  // (persistent = true, src/bin_static_analysis.h, src/bin_dynamics_analysis.h):
+  // one result per bin, all from one pass; select_bin(b) makes write() write bin b
+  virtual void analyze_bins(Trajectory_List* list, Trajectory_List_Bins* bins, bool persistent);
+  virtual void select_bin(int) {}
 
  protected:
   System* system = nullptr;
@@ -139,12 +172,15 @@ class Mean_Square_Displacement : public Analysis {
   explicit Mean_Square_Displacement(System* sys);
   void analyze(Trajectory_List* list) override;
   void write(const std::string& file) const override;
+  void analyze_bins(Trajectory_List* list, Trajectory_List_Bins* bins, bool persistent) override;
+  void select_bin(int b) override { msd_ = bin_msd_[b]; }
   float show(int g) const { return msd_[g]; }
   std::vector<double> sum_d4;  // kept for the NGP of the same pass
 
  private:
   std::vector<float> msd_;
   std::vector<double> weighting_;
+  std::vector<std::vector<float>> bin_msd_;
 };
 
 // Non_Gaussian_Parameter (src/non_gaussian_parameter.cpp:96-174); the
@@ -168,12 +204,15 @@ class Incoherent_Scattering_Function : public Analysis {
                                  bool fullblock);
   void analyze(Trajectory_List* list) override;
   void write(const std::string& file) const override;
+  void analyze_bins(Trajectory_List* list, Trajectory_List_Bins* bins, bool persistent) override;
+  void select_bin(int b) override { corr_ = bin_corr_[b]; }
 
  private:
   const Wave_Vectors* wv_;
   int first_, last_;
   bool fullblock_;
   std::vector<float> corr_;  // [gap][shell]
+  std::vector<std::vector<float>> bin_corr_;
 };
 
 // Mean_Square_Displacement_2D (src/mean_square_displacement_2d.cpp:79-199):

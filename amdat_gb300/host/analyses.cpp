@@ -86,6 +86,84 @@ void Mean_Square_Displacement::analyze(Trajectory_List* list) {
   }
 }
 
+// --- spatial bins ------------------------------------------------------------
+void Analysis::analyze_bins(Trajectory_List*, Trajectory_List_Bins*, bool) {
+  throw Error(AMDAT_ERR_ARGUMENT, "bin_list targets are supported for msd and isfs by this engine");
+}
+
+namespace {
+struct BinOut {
+  std::vector<double> d2, fs;  // [bin][gap], [bin][gap][shell]
+  std::vector<int64_t> cnt;    // [bin][gap]
+};
+BinOut disp_bins(System* sys, const Trajectory_List* list, const Trajectory_List_Bins* bins, bool persistent,
+                 bool fullblock, const std::vector<int32_t>* kvec, const std::vector<int32_t>* off, float period) {
+  const int G = sys->n_timegaps(), B = bins->n_bins();
+  const int S = off ? (int)off->size() - 1 : 0;
+  BinOut o;
+  o.d2.assign((size_t)B * G, 0.0);
+  o.cnt.assign((size_t)B * G, 0);
+  o.fs.assign((size_t)B * G * std::max(S, 1), 0.0);
+  // the engine takes up to 8 shells per pass
+  for (int s0 = 0; s0 < std::max(S, 1); s0 += 8) {
+    const int ns = std::min(8, S - s0);
+    std::vector<int32_t> sub_off, sub_kv;
+    std::vector<double> fs;
+    if (ns > 0) {
+      for (int s = s0; s <= s0 + ns; ++s) sub_off.push_back((*off)[s] - (*off)[s0]);
+      sub_kv.assign(kvec->begin() + 3 * (*off)[s0], kvec->begin() + 3 * (*off)[s0 + ns]);
+      fs.assign((size_t)B * G * ns, 0.0);
+    }
+    check(amdat_disp_bins_run(sys->ctx(), list->handle(), bins->handle(), persistent ? 1 : 0, fullblock ? 1 : 0,
+                              std::max(ns, 0), ns > 0 ? sub_off.data() : nullptr, ns > 0 ? sub_kv.data() : nullptr,
+                              period, AMDAT_OUT_HOST, s0 == 0 ? o.d2.data() : nullptr,
+                              s0 == 0 ? o.cnt.data() : nullptr, ns > 0 ? fs.data() : nullptr),
+          "binned displacement run");
+    for (int bg = 0; bg < B * G; ++bg)
+      for (int s = 0; s < ns; ++s) o.fs[(size_t)bg * S + s0 + s] = fs[(size_t)bg * ns + s];
+  }
+  return o;
+}
+}  // namespace
+
+Trajectory_List_Bins::Trajectory_List_Bins(System* sys, int nx, int ny, int nz) : sys_(sys), n_{nx, ny, nz} {
+  assign(sys->bounds_lo(), sys->bounds_hi());
+}
+
+Trajectory_List_Bins::Trajectory_List_Bins(System* sys, int nx, int ny, int nz, float xlo, float xhi, float ylo,
+                                           float yhi, float zlo, float zhi)
+    : sys_(sys), n_{nx, ny, nz} {
+  // src/trajectory_list_bins.cpp:308-357: a bound of 0, or one beyond the box, is the box's
+  const float* blo = sys->bounds_lo();
+  const float* bhi = sys->bounds_hi();
+  const float ulo[3] = {xlo, ylo, zlo}, uhi[3] = {xhi, yhi, zhi};
+  float lo[3], hi[3];
+  for (int d = 0; d < 3; ++d) {
+    lo[d] = (ulo[d] == 0 || ulo[d] < blo[d]) ? blo[d] : ulo[d];
+    hi[d] = (uhi[d] == 0 || uhi[d] > bhi[d]) ? bhi[d] : uhi[d];
+  }
+  assign(lo, hi);
+}
+
+void Trajectory_List_Bins::assign(const float lo[3], const float hi[3]) {
+  if (n_[0] < 1 || n_[1] < 1 || n_[2] < 1) throw Error(AMDAT_ERR_ARGUMENT, "bin counts must be positive");
+  check(amdat_boxify(sys_->ctx(), sys_->bounds_lo(), sys_->bounds_hi()), "boxify");
+  check(amdat_bins_create(sys_->ctx(), n_[0], n_[1], n_[2], lo, hi, &handle_), "bin list");
+}
+
+Trajectory_List_Bins::~Trajectory_List_Bins() {
+  if (handle_) amdat_bins_free(sys_->ctx(), handle_);
+}
+
+void Mean_Square_Displacement::analyze_bins(Trajectory_List* list, Trajectory_List_Bins* bins, bool persistent) {
+  const BinOut o = disp_bins(system, list, bins, persistent, false, nullptr, nullptr, 1.f);
+  const int G = system->n_timegaps(), B = bins->n_bins();
+  bin_msd_.assign(B, std::vector<float>(G, 0.f));
+  for (int b = 0; b < B; ++b)
+    for (int g = 0; g < G; ++g)  // msd /= weighting; an empty bin gives 0/0
+      bin_msd_[b][g] = (float)(o.d2[(size_t)b * G + g] / (double)o.cnt[(size_t)b * G + g]);
+}
+
 void Mean_Square_Displacement::write(const std::string& file) const {
   std::ofstream out = open_out(file);
   out << "Mean square displacement data created by AMDAT v." << SEMVER << "\n";
@@ -267,6 +345,20 @@ void Incoherent_Scattering_Function::analyze(Trajectory_List* list) {
   for (int g = 0; g < G; ++g)
     for (int s = 0; s < S; ++s)
       corr_[(size_t)g * S + s] = (float)(o.fs[(size_t)g * S + s] / (double)o.pairs[g]);
+}
+
+void Incoherent_Scattering_Function::analyze_bins(Trajectory_List* list, Trajectory_List_Bins* bins,
+                                                  bool persistent) {
+  std::vector<int32_t> kv, off;
+  wv_->shells(first_, last_, kv, off);
+  const BinOut o = disp_bins(system, list, bins, persistent, fullblock_, &kv, &off, wv_->period());
+  const int G = system->n_timegaps(), S = last_ - first_ + 1, B = bins->n_bins();
+  bin_corr_.assign(B, std::vector<float>((size_t)G * S, 0.f));
+  for (int b = 0; b < B; ++b)
+    for (int g = 0; g < G; ++g)
+      for (int s = 0; s < S; ++s)  // Correlation_2D::postprocess_list: corr / n_atoms
+        bin_corr_[b][(size_t)g * S + s] =
+            (float)(o.fs[((size_t)b * G + g) * S + s] / (double)o.cnt[(size_t)b * G + g]);
 }
 
 static void write_corr2d(const std::string& file, const System* sys, const Wave_Vectors* wv, int first,

@@ -81,11 +81,81 @@ class Control {
     return out;
   }
 
+  // Bin_Static_Analysis::write / Bin_Dynamics_Analysis::write file names: each
+  // index goes through `ss << i; ss.seekp(0)` on one stringstream per axis, so
+  // a shorter number overwrites only the front of a longer one written before
+  static std::vector<std::string> bin_file_names(const std::string& stem, const Trajectory_List_Bins& b,
+                                                 const char* sep) {
+    auto put = [](std::string& buf, int v) {
+      const std::string t = std::to_string(v);
+      if (t.size() >= buf.size()) buf = t;
+      else buf.replace(0, t.size(), t);
+    };
+    std::vector<std::string> out;
+    std::string sx, sy, sz;
+    for (int x = 0; x < b.show_n_xbins(); ++x)
+      for (int y = 0; y < b.show_n_ybins(); ++y)
+        for (int z = 0; z < b.show_n_zbins(); ++z) {
+          put(sx, x), put(sy, y), put(sz, z);
+          out.push_back(stem + "_bin_" + sx + sep + sy + sep + sz + ".bindata");
+        }
+    return out;
+  }
+
+  // target line "list <name> [<name2>]" or "bin_list <bins> <list> [persistence]"
+  // (Control::run_analysis, src/control.h:268-380)
   void analyze_write(Analysis& an, const std::string& file) {
-    auto t = targets();
+    const auto a = tokenize(read_line());
+    if (!a.empty() && a[0] == "bin_list") {
+      if (a.size() < 3) throw Error(AMDAT_ERR_ARGUMENT, "Insufficient number of arguments in bin_list target line.");
+      auto it = bins_.find(a[1]);
+      if (it == bins_.end()) throw Error(AMDAT_ERR_ARGUMENT, "Binned Trajectory list '" + a[1] + "' not found.");
+      Trajectory_List* l = list(a[2]);
+      // persistence takes the Bin_Dynamics_Analysis path (the binned analyses here are all dynamic)
+      const bool persistent = a.size() >= 4 && std::atoi(a[3].c_str()) != 0;
+      an.analyze_bins(l, it->second.get(), persistent);
+      const auto names = bin_file_names(file, *it->second, persistent ? "." : "_");
+      for (size_t b = 0; b < names.size(); ++b) {
+        an.select_bin((int)b);
+        an.write(names[b]);
+      }
+      return;
+    }
+    if (a.size() < 2 || a[0] != "list")
+      throw Error(AMDAT_ERR_ARGUMENT, "Command " + (a.empty() ? std::string() : a[0]) +
+                                          " not understood. Acceptable options are list or bin_list.");
+    std::vector<Trajectory_List*> t;
+    for (size_t i = 1; i < a.size(); ++i) t.push_back(list(a[i]));
     if (t.size() == 1) an.analyze(t[0]);
     else an.analyze(t[0], t[1]);
     an.write(file);
+  }
+
+  // Control::create_bin_list (src/control.cpp:3841-4000): "all nx ny nz" or
+  // "region nx ny nz xlo xhi ylo yhi zlo zhi"
+  void create_bin_list(const std::vector<std::string>& a) {
+    argcheck(a, 2, 2);
+    const auto s = tokenize(read_line());
+    if (s.empty()) throw Error(AMDAT_ERR_ARGUMENT, "No set type found.");
+    auto need = [&](size_t n) {
+      if (s.size() != n)
+        throw Error(AMDAT_ERR_ARGUMENT, "Incorrect number of arguments for command create_bin_list.");
+    };
+    auto i = [&](size_t k) { return std::atoi(s[k].c_str()); };
+    auto f = [&](size_t k) { return (float)std::atof(s[k].c_str()); };
+    std::unique_ptr<Trajectory_List_Bins> b;
+    if (s[0] == "all") {
+      need(4);
+      b = std::make_unique<Trajectory_List_Bins>(&sys(), i(1), i(2), i(3));
+    } else if (s[0] == "region") {
+      need(10);
+      b = std::make_unique<Trajectory_List_Bins>(&sys(), i(1), i(2), i(3), f(4), f(5), f(6), f(7), f(8), f(9));
+    } else if (s[0] == "distance") {
+      throw Error(AMDAT_ERR_ARGUMENT, "distance bin lists are not part of this engine");
+    } else {
+      throw Error(AMDAT_ERR_ARGUMENT, "bin_list of type " + s[0] + " invalid");
+    }
+    bins_[a[1]] = std::move(b);
   }
 
   // selection commands of Analysis::analyze(string) (src/analysis.cpp:130-209)
@@ -136,6 +206,7 @@ class Control {
       if (!ty.empty() && ty[0] == "xyz")
         for (int k = 0; k < 2; ++k) block.push_back(read_line());  // box size, box bounds
       lists_.clear();
+      bins_.clear();
       sys_.reset();
       sys_ = std::make_unique<System>(block, device_);
     } else if (cmd == "limit") {
@@ -145,6 +216,8 @@ class Control {
       argcheck(a, 2, 2);
       auto sel = select(tokenize(read_line()));
       lists_[a[1]] = std::make_unique<Trajectory_List>(&sys(), std::move(sel));
+    } else if (cmd == "create_bin_list") {
+      create_bin_list(a);
     } else if (cmd == "msd") {
       argcheck(a, 2, 2);
       pathcheck(a[1]);
@@ -258,6 +331,7 @@ class Control {
   size_t pos_ = 0;
   std::unique_ptr<System> sys_;
   std::map<std::string, std::unique_ptr<Trajectory_List>> lists_;
+  std::map<std::string, std::unique_ptr<Trajectory_List_Bins>> bins_;
 };
 
 }  // namespace

@@ -94,6 +94,7 @@ System::System(const std::vector<std::string>& block, int device) {
     for (int d = 0; d < 3; ++d) {
       box_[d] = (float)std::atof(L[d].c_str());
       box_lo_[d] = (float)std::atof(lohi[2 * d].c_str());
+      box_hi_[d] = (float)std::atof(lohi[2 * d + 1].c_str());
     }
   }
   n_atoms_ = 0;
@@ -232,6 +233,7 @@ void System::read_custom(const std::string& file, bool byid) {
     if (t == 0) {
       for (int d = 0; d < 3; ++d) {
         box_lo_[d] = lo[d];
+        box_hi_[d] = hi[d];
         box_[d] = hi[d] - lo[d];
       }
     } else {

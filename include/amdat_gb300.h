@@ -116,7 +116,7 @@ amdat_status amdat_launch_count(amdat_ctx* ctx, int64_t* count);
  * names: disp_mixed_kernel, disp_plain_kernel, rhok_list_kernel,
  * rhok_lattice_kernel, rhok_tc_kernel, rhok_plain_kernel, isf_pairs_kernel,
  * sk_frames_kernel, pair_hist_kernel, gsmooth_kernel, gsmooth_adjoint_kernel,
- * sk_adjoint_columns_kernel, sk_adjoint_direct_kernel, disp_axes_kernel.  (No counterpart in the reference, which times commands
+ * sk_adjoint_columns_kernel, sk_adjoint_direct_kernel, disp_axes_kernel, disp_bins_kernel.  (No counterpart in the reference, which times commands
  * with time(NULL), e.g. src/control.cpp:2190-2196.) */
 amdat_status amdat_profile_reset(amdat_ctx* ctx, int32_t enable);
 amdat_status amdat_profile_kernel(amdat_ctx* ctx, const char* kernel, int64_t* launches,
@@ -201,6 +201,40 @@ amdat_status amdat_disp_axes_run(amdat_ctx* ctx, int32_t list, int32_t fullblock
                                  int32_t n_bins, float bin_size, int32_t out_flags,
                                  double* axis_sums, double* sum_d4, int64_t* atom_pairs,
                                  int64_t* d2_counts);
+
+/* Spatial bins (Control::create_bin_list, src/control.cpp:3841-4000).
+ * amdat_boxify: System::boxify (src/system.cpp:4799-4870) on the wrapped
+ * coordinates: one outside [lo, hi] on an axis moves by hi - lo on that axis.
+ * amdat_bins_create: Trajectory_List_Bins (src/trajectory_list_bins.cpp:207-394,
+ * 949-1096): per frame, an atom strictly inside the region [lo, hi] gets bin
+ * (ix * ny + iy) * nz + iz with ix = int((x - lo + 10 FLT_EPSILON) /
+ * (hi - lo + 20 FLT_EPSILON) * nx) (the differences in FP32, the rest in
+ * FP64); others none.  The caller applies the region rules (a bound of 0, or
+ * one beyond the box, is the box's) and boxifies first, as create_bin_list does.
+ * amdat_bins_read: the map [frames][atoms] (-1 = no bin) and/or the members per
+ * frame and bin [frames][bins]; either may be NULL. */
+amdat_status amdat_boxify(amdat_ctx* ctx, const float lo[3], const float hi[3]);
+amdat_status amdat_bins_create(amdat_ctx* ctx, int32_t nx, int32_t ny, int32_t nz, const float lo[3],
+                               const float hi[3], int32_t* handle);
+amdat_status amdat_bins_read(amdat_ctx* ctx, int32_t handle, int32_t out_flags, int32_t* bins,
+                             int64_t* counts);
+amdat_status amdat_bins_free(amdat_ctx* ctx, int32_t handle);
+
+/* MSD and F_s of every bin in one pass: the target line "bin_list <bins>
+ * <list> [persistence]" of Control::run_analysis (src/control.h:268-380).
+ * persistent = 0: Bin_Static_Analysis (src/bin_static_analysis.h:69-111), the
+ * list members in the bin at the start frame t0, pairs of the given fullblock;
+ * persistent = 1: Bin_Dynamics_Analysis (src/bin_dynamics_analysis.h), members
+ * in the bin at t0 and at t1, pairs of fullblock 0.  Per bin b and gap g:
+ *   sum_d2[b][g]     sum of |dr|^2
+ *   count[b][g]      number of (member, time pair) terms
+ *   fs_sum[b][g][s]  sum of the shell mean of cos(k.dr), k = 2 pi n / period,
+ *                    for up to 8 shells (list mode: every vector of the shell)
+ * Any output may be NULL. */
+amdat_status amdat_disp_bins_run(amdat_ctx* ctx, int32_t list, int32_t bins, int32_t persistent,
+                                 int32_t fullblock, int32_t n_shells, const int32_t* shell_offsets,
+                                 const int32_t* kvec, float period, int32_t out_flags, double* sum_d2,
+                                 int64_t* count, double* fs_sum);
 
 /* Prepared displacement runs (many lists, one persistent launch).  A plan
  * builds its item tables on the device once; amdat_disp_plan_run is then pure

@@ -4,6 +4,7 @@
  * host (aarch64 gcc contracts a*b+c by default). */
 #include "amdat_oracle.h"
 
+#include <float.h>
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
@@ -212,8 +213,28 @@ static double dist2_64(const float* u, int n_atoms, int a, int ta, int tb) {
 /* displacement family                                                       */
 /* ------------------------------------------------------------------------- */
 
-void orc_msd(const orc_scheme* s, const float* u, int32_t n_atoms, const int32_t* list,
-             int32_t n_list, int32_t mode, double* msd, double* weighting) {
+/* Membership of a time-dependent list (a bin of Trajectory_List_Bins intersected
+ * with a static list): the atoms in bin `bin` at the start frame t0
+ * (Bin_Static_Analysis, src/bin_static_analysis.h:69-111), or at both t0 and t1
+ * (Bin_Dynamics_Analysis with persistence, src/bin_dynamics_analysis.h:
+ * list_displacementkernel; Trajectory_List::time_intersection,
+ * src/trajectory_list.cpp:252-278).  NULL: every list member. */
+typedef struct {
+  const int32_t* bins; /* [frames][atoms] flat bin or -1 */
+  int32_t bin;
+  int32_t persistent;
+} member_t;
+
+static int is_member(const member_t* f, int n_atoms, int a, int ta, int tb) {
+  if (!f) return 1;
+  if (f->bins[(size_t)ta * n_atoms + a] != f->bin) return 0;
+  return !f->persistent || f->bins[(size_t)tb * n_atoms + a] == f->bin;
+}
+
+/* Mean_Square_Displacement::list_displacementkernel / listkernel
+ * (src/mean_square_displacement.cpp:147-168): weighting += members at t0 */
+static void msd_core(const orc_scheme* s, const float* u, int32_t n_atoms, const int32_t* list,
+                     int32_t n_list, int32_t mode, const member_t* f, double* msd, double* weighting) {
   int G = orc_n_timegaps(s);
   pairs_t p = make_pairs(s, 0, 0); /* analyze(): displacement_list(this,false) */
   if (mode == ORC_REF32) {
@@ -221,11 +242,14 @@ void orc_msd(const orc_scheme* s, const float* u, int32_t n_atoms, const int32_t
     float* w = (float*)calloc(G, sizeof(float));
     for (int64_t i = 0; i < p.n; ++i) {
       int g = p.gap[i];
-      w[g] += (float)n_list;
+      int cnt = 0;
       for (int j = 0; j < n_list; ++j) {
+        if (!is_member(f, n_atoms, list[j], p.t0[i], p.t1[i])) continue;
+        ++cnt;
         float d = dist32(u, n_atoms, list[j], p.t0[i], p.t1[i]);
         m[g] += d * d;
       }
+      w[g] += (float)cnt;
     }
     for (int g = 0; g < G; ++g) {
       m[g] /= (float)w[g];
@@ -238,8 +262,11 @@ void orc_msd(const orc_scheme* s, const float* u, int32_t n_atoms, const int32_t
     double* w = (double*)calloc(G, sizeof(double));
     for (int64_t i = 0; i < p.n; ++i) {
       int g = p.gap[i];
-      w[g] += n_list;
-      for (int j = 0; j < n_list; ++j) m[g] += dist2_64(u, n_atoms, list[j], p.t0[i], p.t1[i]);
+      for (int j = 0; j < n_list; ++j) {
+        if (!is_member(f, n_atoms, list[j], p.t0[i], p.t1[i])) continue;
+        w[g] += 1.0;
+        m[g] += dist2_64(u, n_atoms, list[j], p.t0[i], p.t1[i]);
+      }
     }
     for (int g = 0; g < G; ++g) {
       msd[g] = m[g] / w[g];
@@ -248,6 +275,11 @@ void orc_msd(const orc_scheme* s, const float* u, int32_t n_atoms, const int32_t
     free(m); free(w);
   }
   free_pairs(&p);
+}
+
+void orc_msd(const orc_scheme* s, const float* u, int32_t n_atoms, const int32_t* list,
+             int32_t n_list, int32_t mode, double* msd, double* weighting) {
+  msd_core(s, u, n_atoms, list, n_list, mode, NULL, msd, weighting);
 }
 
 void orc_ngp(const orc_scheme* s, const float* u, int32_t n_atoms, const int32_t* list,
@@ -311,9 +343,10 @@ void orc_disp_moments(const orc_scheme* s, int32_t fullblock, const float* u, in
   free_pairs(&p);
 }
 
-void orc_isfs(const orc_scheme* s, int32_t fullblock, const float* u, int32_t n_atoms,
-              const int32_t* list, int32_t n_list, const int32_t* kvec_n, const int32_t* off,
-              int32_t n_shells, float spacing, double box_len, int32_t mode, double* corr) {
+static void isfs_core(const orc_scheme* s, int32_t fullblock, const float* u, int32_t n_atoms,
+                      const int32_t* list, int32_t n_list, const int32_t* kvec_n, const int32_t* off,
+                      int32_t n_shells, float spacing, double box_len, int32_t mode, const member_t* f,
+                      double* corr) {
   int G = orc_n_timegaps(s);
   pairs_t p = make_pairs(s, fullblock, 0);
   int nk = off[n_shells];
@@ -327,6 +360,7 @@ void orc_isfs(const orc_scheme* s, int32_t fullblock, const float* u, int32_t n_
       int g = p.gap[i], ta = p.t0[i], tb = p.t1[i];
       for (int j = 0; j < n_list; ++j) {
         int a = list[j];
+        if (!is_member(f, n_atoms, a, ta, tb)) continue;
         na[g] += 1.0f;
         float dx = POS(u, tb, a, 0) - POS(u, ta, a, 0);
         float dy = POS(u, tb, a, 1) - POS(u, ta, a, 1);
@@ -356,6 +390,7 @@ void orc_isfs(const orc_scheme* s, int32_t fullblock, const float* u, int32_t n_
       int g = p.gap[i], ta = p.t0[i], tb = p.t1[i];
       for (int j = 0; j < n_list; ++j) {
         int a = list[j];
+        if (!is_member(f, n_atoms, a, ta, tb)) continue;
         na[g] += 1.0;
         double dx = (double)POS(u, tb, a, 0) - (double)POS(u, ta, a, 0);
         double dy = (double)POS(u, tb, a, 1) - (double)POS(u, ta, a, 1);
@@ -375,6 +410,80 @@ void orc_isfs(const orc_scheme* s, int32_t fullblock, const float* u, int32_t n_
     free(c); free(na);
   }
   free_pairs(&p);
+}
+
+void orc_isfs(const orc_scheme* s, int32_t fullblock, const float* u, int32_t n_atoms,
+              const int32_t* list, int32_t n_list, const int32_t* kvec_n, const int32_t* off,
+              int32_t n_shells, float spacing, double box_len, int32_t mode, double* corr) {
+  isfs_core(s, fullblock, u, n_atoms, list, n_list, kvec_n, off, n_shells, spacing, box_len, mode, NULL,
+            corr);
+}
+
+/* System::boxify (src/system.cpp:4799-4870): a wrapped coordinate outside
+ * [lo, hi] on some axis moves by one box length (hi - lo, FP32) on that axis. */
+void orc_boxify(float* w, int32_t n_frames, int32_t n_atoms, const float* lo, const float* hi) {
+  for (int t = 0; t < n_frames; ++t)
+    for (int a = 0; a < n_atoms; ++a) {
+      float* c = &w[((size_t)t * n_atoms + a) * 3];
+      if (c[0] < lo[0] || c[0] > hi[0] || c[1] < lo[1] || c[1] > hi[1] || c[2] < lo[2] || c[2] > hi[2])
+        for (int d = 0; d < 3; ++d) {
+          int sh = c[d] > hi[d] ? -1 : (c[d] < lo[d] ? 1 : 0);
+          c[d] = c[d] + (hi[d] - lo[d]) * (float)sh;
+        }
+    }
+}
+
+/* Trajectory_List_Bins::assign_bins (src/trajectory_list_bins.cpp:949-1009): an
+ * atom strictly inside the region is in bin
+ * int((x - lo + 10 FLT_EPSILON) / (hi - lo + 20 FLT_EPSILON) * n) per axis, the
+ * differences in FP32 and the rest in FP64; flat bin (ix * ny + iy) * nz + iz,
+ * -1 outside. */
+void orc_assign_bins(const float* w, int32_t n_frames, int32_t n_atoms, int32_t nx, int32_t ny,
+                     int32_t nz, const float* lo, const float* hi, int32_t* bins) {
+  const int32_t n[3] = {nx, ny, nz};
+  for (int t = 0; t < n_frames; ++t)
+    for (int a = 0; a < n_atoms; ++a) {
+      const float* c = &w[((size_t)t * n_atoms + a) * 3];
+      int32_t* out = &bins[(size_t)t * n_atoms + a];
+      int in = 1;
+      for (int d = 0; d < 3; ++d) in &= (c[d] < hi[d] && c[d] > lo[d]);
+      if (!in) { *out = -1; continue; }
+      int ix[3];
+      for (int d = 0; d < 3; ++d) {
+        float num = c[d] - lo[d], den = hi[d] - lo[d];
+        ix[d] = (int)(((double)num + (double)FLT_EPSILON * 10.0) / ((double)den + (double)FLT_EPSILON * 20.0) *
+                      (double)(float)n[d]);
+      }
+      *out = (ix[0] * ny + ix[1]) * nz + ix[2];
+    }
+}
+
+/* Per bin, the MSD of the list members in that bin (membership at t0, or at t0
+ * and t1 with persistence): msd[bin][gap], weighting[bin][gap] */
+void orc_msd_bins(const orc_scheme* s, const float* u, int32_t n_atoms, const int32_t* list,
+                  int32_t n_list, const int32_t* bins, int32_t n_bins, int32_t persistent, int32_t mode,
+                  double* msd, double* weighting) {
+  int G = orc_n_timegaps(s);
+  for (int b = 0; b < n_bins; ++b) {
+    member_t f = {bins, b, persistent};
+    msd_core(s, u, n_atoms, list, n_list, mode, &f, msd + (size_t)b * G,
+             weighting ? weighting + (size_t)b * G : NULL);
+  }
+}
+
+/* Per bin, the self-intermediate scattering function: corr[bin][gap][shell].
+ * With persistence the pairs are those of displacement_list(this) (fullblock 0),
+ * as Bin_Dynamics_Analysis::analyze enumerates them. */
+void orc_isfs_bins(const orc_scheme* s, int32_t fullblock, const float* u, int32_t n_atoms,
+                   const int32_t* list, int32_t n_list, const int32_t* kvec_n, const int32_t* off,
+                   int32_t n_shells, float spacing, double box_len, const int32_t* bins, int32_t n_bins,
+                   int32_t persistent, int32_t mode, double* corr) {
+  int G = orc_n_timegaps(s);
+  for (int b = 0; b < n_bins; ++b) {
+    member_t f = {bins, b, persistent};
+    isfs_core(s, persistent ? 0 : fullblock, u, n_atoms, list, n_list, kvec_n, off, n_shells, spacing,
+              box_len, mode, &f, corr + (size_t)b * G * n_shells);
+  }
 }
 
 /* Space_Time_Correlation_Function PI (space_time_correlation_function.cpp:20) */

@@ -64,6 +64,19 @@ void orc_disp_moments(const orc_scheme* s, int32_t fullblock, const float* unwra
 void orc_isfs(const orc_scheme* s, int32_t fullblock, const float* unwrapped, int32_t n_atoms,
               const int32_t* list, int32_t n_list, const int32_t* kvec_n, const int32_t* shell_off,
               int32_t n_shells, float spacing, double box_len, int32_t mode, double* corr);
+
+/* Spatial bins of the wrapped coordinates (Trajectory_List_Bins) and the
+ * per-bin displacement analyses (Bin_Static_Analysis / Bin_Dynamics_Analysis) */
+void orc_boxify(float* wrapped, int32_t n_frames, int32_t n_atoms, const float* lo, const float* hi);
+void orc_assign_bins(const float* wrapped, int32_t n_frames, int32_t n_atoms, int32_t nx, int32_t ny,
+                     int32_t nz, const float* lo, const float* hi, int32_t* bins);
+void orc_msd_bins(const orc_scheme* s, const float* unwrapped, int32_t n_atoms, const int32_t* list,
+                  int32_t n_list, const int32_t* bins, int32_t n_bins, int32_t persistent, int32_t mode,
+                  double* msd, double* weighting);
+void orc_isfs_bins(const orc_scheme* s, int32_t fullblock, const float* unwrapped, int32_t n_atoms,
+                   const int32_t* list, int32_t n_list, const int32_t* kvec_n, const int32_t* off,
+                   int32_t n_shells, float spacing, double box_len, const int32_t* bins, int32_t n_bins,
+                   int32_t persistent, int32_t mode, double* corr);
 /* Van_Hove_Self (van_hove_self.cpp:82-103, space_time_correlation_function.cpp:216,345):
  * counts[g][b] raw, weighting[g], and the normalised correlation (REF32). */
 void orc_vhs(const orc_scheme* s, const float* unwrapped, int32_t n_atoms, const int32_t* list,

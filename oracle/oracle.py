@@ -140,6 +140,53 @@ def isfs(s, unwrapped, lst, kvec_n, shell_off, spacing, box_len, fullblock=0, mo
     return out
 
 
+def boxify(wrapped, lo, hi):
+    """System::boxify on a copy of the wrapped coordinates [frames][atoms][3]."""
+    w = np.array(wrapped, dtype=np.float32, order="C", copy=True)
+    lo, hi = _f32(np.asarray(lo)), _f32(np.asarray(hi))
+    lib().orc_boxify(_p(w), w.shape[0], w.shape[1], _p(lo), _p(hi))
+    return w
+
+
+def assign_bins(wrapped, nbins, lo, hi):
+    """Trajectory_List_Bins::assign_bins: flat bin [frames][atoms] or -1."""
+    w = _f32(wrapped)
+    lo, hi = _f32(np.asarray(lo)), _f32(np.asarray(hi))
+    out = np.empty(w.shape[:2], np.int32)
+    lib().orc_assign_bins(_p(w), w.shape[0], w.shape[1], int(nbins[0]), int(nbins[1]), int(nbins[2]),
+                          _p(lo), _p(hi), _p(out))
+    return out
+
+
+def msd_bins(s, unwrapped, lst, bins, n_bins, persistent=0, mode=F64):
+    """Per-bin MSD: (msd [bins][gaps], weighting [bins][gaps])."""
+    u = _f32(unwrapped)
+    lst = _i32(lst)
+    b = _i32(bins)
+    G = n_timegaps(s)
+    out = np.zeros((n_bins, G))
+    w = np.zeros((n_bins, G))
+    lib().orc_msd_bins(C.byref(s), _p(u), u.shape[1], _p(lst), len(lst), _p(b), int(n_bins),
+                       int(persistent), mode, _p(out), _p(w))
+    return out, w
+
+
+def isfs_bins(s, unwrapped, lst, kvec_n, shell_off, spacing, box_len, bins, n_bins, fullblock=0,
+              persistent=0, mode=F64):
+    """Per-bin self-intermediate scattering function [bins][gaps][shells]."""
+    u = _f32(unwrapped)
+    lst = _i32(lst)
+    kv = _i32(kvec_n).reshape(-1)
+    off = _i32(shell_off)
+    b = _i32(bins)
+    ns = len(off) - 1
+    out = np.zeros((n_bins, n_timegaps(s), ns))
+    lib().orc_isfs_bins(C.byref(s), int(fullblock), _p(u), u.shape[1], _p(lst), len(lst), _p(kv), _p(off), ns,
+                        C.c_float(spacing), C.c_double(box_len), _p(b), int(n_bins), int(persistent), mode,
+                        _p(out))
+    return out
+
+
 def vhs(s, unwrapped, lst, max_value, n_bins):
     u = _f32(unwrapped)
     lst = _i32(lst)

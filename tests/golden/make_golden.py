@@ -185,6 +185,32 @@ list all
 isfs ./isfs.dat 8 9 xyz 0
 list a
 """),
+    # spatial bins (create_bin_list): per-bin MSD and F_s, membership at the start
+    # frame (bin_list <bins> <list>) or at both frames (persistence flag 1)
+    "bins": dict(
+        n=300, box=6.0, sigma=0.25, seed=99, fractions=(0.7, 0.3),
+        scheme=synth.TimeScheme.exponential(3, 6, 1.4, 0, 0, 0.01),
+        commands="""create_list all
+all
+create_list b
+type_system 2
+create_bin_list slabs
+all 1 1 3
+msd ./msd_slabs.dat
+bin_list slabs all
+isfs ./isfs_slabs.dat 8 9 xyz 0
+bin_list slabs all
+msd ./msd_persist.dat
+bin_list slabs all 1
+isfs ./isfs_persist.dat 8 8 xyz 0 1
+bin_list slabs b 1
+create_bin_list cells
+region 2 1 2 1.0 5.0 0 0 0 4.0
+msd ./msd_cells.dat
+bin_list cells b
+isfs ./isfs_cells.dat 7 7 xyz 0 1
+bin_list cells all
+"""),
     "siblings_lin": dict(
         n=120, box=6.0, sigma=0.1, seed=55, fractions=(1.0,), time_scaled=False,
         scheme=synth.TimeScheme.linear(16, 1.0),
@@ -235,7 +261,7 @@ def make(case: str) -> None:
         if r.returncode != 0:
             raise SystemExit(f"reference failed on {case}:\n{r.stdout[-2000:]}\n{r.stderr[-2000:]}")
         for fn in sorted(os.listdir(tmp)):
-            if fn.endswith(".dat"):
+            if fn.endswith((".dat", ".bindata")):
                 shutil.copy(os.path.join(tmp, fn), os.path.join(out_dir, fn))
     print(case, "->", out_dir)
 
@@ -260,7 +286,7 @@ def load(case: str):
     with open(os.path.join(d, "script.in")) as f:
         script = f.read()
     outs = {fn: open(os.path.join(d, fn)).read() for fn in sorted(os.listdir(d))
-            if fn.endswith(".dat")}
+            if fn.endswith((".dat", ".bindata"))}
     return traj, script, outs
 
 

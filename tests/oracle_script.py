@@ -36,6 +36,7 @@ class OracleRun:
         self.files = {}
         self.flags = {}
         self.stored = {}
+        self.bins = {}
 
     def scheme(self):
         return orc.scheme(self.traj.scheme, self.limit)
@@ -69,11 +70,88 @@ class OracleRun:
             if cmd == "limit":
                 self.limit = int(a[1])
                 continue
+            if cmd == "create_bin_list":
+                self.bins[a[1]] = self.make_bins(lines[i].split())
+                i += 1
+                continue
             target = lines[i].split()
             i += 1
+            if target[0] == "bin_list":
+                self.run_bins(cmd, a, target)
+                continue
             lst = self.lists[target[1]]
             getattr(self, "cmd_" + cmd)(a, lst)
         return self.files
+
+    # --- spatial bins (Control::create_bin_list, src/control.cpp:3841-4000) ---
+    def box_bounds(self):
+        lo = self.traj.box_lo.astype(np.float32)
+        hi = (self.traj.box_lo.astype(np.float64) + self.traj.box.astype(np.float64)).astype(np.float32)
+        return lo, hi
+
+    def make_bins(self, spec):
+        lo, hi = self.box_bounds()
+        n = [int(spec[1]), int(spec[2]), int(spec[3])]
+        if spec[0] == "all":
+            rlo, rhi = lo.copy(), hi.copy()
+        elif spec[0] == "region":
+            # Trajectory_List_Bins region constructor (src/trajectory_list_bins.cpp:308-357):
+            # a bound of 0, or one outside the box, is the box's own
+            v = [f32(float(x)) for x in spec[4:10]]
+            rlo = np.array([lo[d] if (v[2 * d] == 0 or v[2 * d] < lo[d]) else v[2 * d] for d in range(3)], np.float32)
+            rhi = np.array([hi[d] if (v[2 * d + 1] == 0 or v[2 * d + 1] > hi[d]) else v[2 * d + 1] for d in range(3)],
+                           np.float32)
+        else:
+            raise ValueError(spec)
+        self.wrapped = orc.boxify(self.wrapped, lo, hi)  # System::boxify, kept for later commands
+        return dict(n=n, bins=orc.assign_bins(self.wrapped, n, rlo, rhi))
+
+    @staticmethod
+    def bin_names(stem, n, sep):
+        """Bin_Static_Analysis::write / Bin_Dynamics_Analysis::write file names.  Each
+        index is written with `ss << i; ss.seekp(0)` into one stringstream per axis,
+        so a shorter number overwrites only the front of a longer one."""
+        def put(buf, v):
+            t = str(v)
+            return t if len(t) >= len(buf) else t + buf[len(t):]
+        out = []
+        sx = sy = sz = ""
+        for x in range(n[0]):
+            for y in range(n[1]):
+                for z in range(n[2]):
+                    sx, sy, sz = put(sx, x), put(sy, y), put(sz, z)
+                    out.append(((x * n[1] + y) * n[2] + z, f"{stem}_bin_{sx}{sep}{sy}{sep}{sz}.bindata"))
+        return out
+
+    def run_bins(self, cmd, a, target):
+        spec = self.bins[target[1]]
+        lst = self.lists[target[2]]
+        persist = len(target) >= 4 and int(target[3]) != 0  # msd and isfs are dynamic analyses
+        n = spec["n"]
+        B = n[0] * n[1] * n[2]
+        s = self.scheme()
+        if cmd == "msd":
+            m, _ = orc.msd_bins(s, self.unwrapped, lst, spec["bins"], B, int(persist), self.mode)
+            texts = [self.msd_text(m[b], s) for b in range(B)]
+        elif cmd == "isfs":
+            m0, m1 = int(a[2]), int(a[3])
+            maxlen = float(a[5])
+            fb = int(a[6]) if len(a) > 6 else 0
+            L = maxlen if maxlen > 0 else self.min_box()
+            sp = wv.spacing(L)
+            kv, off = self.shells(m0, m1)
+            corr = orc.isfs_bins(s, self.unwrapped, lst, kv, off, float(sp), L, spec["bins"], B, fb,
+                                 int(persist), self.mode)
+            texts = [self.correlation_2d(sp, m0, m1, corr[b], s) for b in range(B)]
+        else:
+            raise ValueError(cmd)
+        for b, name in self.bin_names(self.name(a[1]), n, "." if persist else "_"):
+            self.files[name] = texts[b]
+
+    def msd_text(self, m, s):
+        t = self.times(s)
+        txt = f"Mean square displacement data created by AMDAT v.{VERSION}\n"
+        return txt + "".join(f"{fmt(t[g])}\t{fmt(f32(m[g]))}\n" for g in range(len(t)))
 
     def select(self, sel):
         if sel[0] == "all":
@@ -92,10 +170,7 @@ class OracleRun:
     def cmd_msd(self, a, lst):
         s = self.scheme()
         m = orc.msd(s, self.unwrapped, lst, self.mode)
-        t = self.times(s)
-        txt = f"Mean square displacement data created by AMDAT v.{VERSION}\n"
-        txt += "".join(f"{fmt(t[g])}\t{fmt(f32(m[g]))}\n" for g in range(len(t)))
-        self.files[self.name(a[1])] = txt
+        self.files[self.name(a[1])] = self.msd_text(m, s)
 
     def cmd_ngp(self, a, lst):
         s = self.scheme()

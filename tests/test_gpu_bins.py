@@ -1,0 +1,154 @@
+"""GPU parity of the spatial bins (amdat_boxify, amdat_bins_create) and the
+binned displacement pass (amdat_disp_bins_run) against the oracle, through the
+C ABI.  Bin maps and member counts are bit-exact; per-bin MSD <= 1e-6 relative
+and F_s (normalised, F_s(q,0) = 1) <= 1e-6 absolute to the FP64 oracle.  The
+reference's own per-bin output files are checked through the command-line
+driver (tests/golden/bins, test_gpu_cli.py)."""
+import numpy as np
+import pytest
+
+from golden.make_golden import load
+from oracle import oracle as orc
+from oracle import wavevectors as wv
+
+pytestmark = pytest.mark.gpu
+f32 = np.float32
+
+
+def _bounds(traj):
+    lo = traj.box_lo.astype(f32)
+    hi = (traj.box_lo.astype(np.float64) + traj.box.astype(np.float64)).astype(f32)
+    return lo, hi
+
+
+def _region(lo, hi, user_lo, user_hi):
+    # a bound of 0, or one beyond the box, is the box's own
+    rlo = np.array([lo[d] if (user_lo[d] == 0 or user_lo[d] < lo[d]) else user_lo[d] for d in range(3)], f32)
+    rhi = np.array([hi[d] if (user_hi[d] == 0 or user_hi[d] > hi[d]) else user_hi[d] for d in range(3)], f32)
+    return rlo, rhi
+
+
+def _wrapped_with_strays(traj, seed=5):
+    """Wrapped coordinates with some atoms moved one box length out (boxify
+    brings them back) and some exactly on a region bound (never in a bin)."""
+    w = traj.wrapped().copy()
+    rng = np.random.default_rng(seed)
+    T, N, _ = w.shape
+    L = traj.box.astype(f32)
+    for _ in range(40):
+        t, a, d = rng.integers(T), rng.integers(N), rng.integers(3)
+        w[t, a, d] = f32(w[t, a, d] + (L[d] if rng.random() < 0.5 else -L[d]))
+    w[0, 0, 0] = f32(traj.box_lo[0])
+    w[1, 1, 1] = f32(2.0)
+    return w
+
+
+CASES = [((1, 1, 3), None), ((2, 1, 2), ([1.0, 0.0, 0.0], [5.0, 0.0, 4.0])), ((4, 3, 5), None),
+         ((3, 3, 3), ([2.0, 2.0, -9.0], [0.0, 9.0, 4.5]))]
+
+
+@pytest.mark.parametrize("nb,region", CASES)
+def test_bin_map_matches_oracle(eng, nb, region):
+    traj, _, _ = load("bins")
+    w = _wrapped_with_strays(traj)
+    eng.upload(traj.unwrapped, traj.box, traj.box_lo, wrapped=w)
+    lo, hi = _bounds(traj)
+    rlo, rhi = (lo, hi) if region is None else _region(lo, hi, np.asarray(region[0], f32),
+                                                       np.asarray(region[1], f32))
+    eng.boxify(lo, hi)
+    B = nb[0] * nb[1] * nb[2]
+    h = eng.bins_create(nb, rlo, rhi)
+    got, counts = eng.bins_read(h, traj.n_frames, traj.n_atoms, B)
+    ref = orc.assign_bins(orc.boxify(w, lo, hi), nb, rlo, rhi)
+    np.testing.assert_array_equal(got, ref)
+    ref_counts = np.stack([np.bincount(r[r >= 0], minlength=B) for r in ref])
+    np.testing.assert_array_equal(counts, ref_counts)
+    assert got[0, 0] == -1  # on the lower bound: outside
+    eng.bins_free(h)
+
+
+def _check_bins(eng, traj, lst, lst_h, nb, persistent, fullblock, qvectors, m0=8, m1=9):
+    lo, hi = _bounds(traj)
+    eng.boxify(lo, hi)
+    B = nb[0] * nb[1] * nb[2]
+    h = eng.bins_create(nb, lo, hi)
+    bins = orc.assign_bins(orc.boxify(traj.wrapped(), lo, hi), nb, lo, hi)
+    n, off_all = qvectors
+    kv, off = n[off_all[m0]:off_all[m1 + 1]], off_all[m0:m1 + 2] - off_all[m0]
+    L = float(f32(traj.box.min()))
+    out = eng.disp_bins(lst_h, h, B, persistent=persistent, fullblock=fullblock, shells=(kv, off), period=L)
+    s = orc.scheme(traj.scheme)
+    msd, w = orc.msd_bins(s, traj.unwrapped, lst, bins, B, persistent, orc.F64)
+    corr = orc.isfs_bins(s, traj.unwrapped, lst, kv, off, float(wv.spacing(L)), L, bins, B, fullblock,
+                         persistent, orc.F64)
+    cnt = out["count"]
+    if fullblock == 0 or persistent:
+        # the MSD's own pairs (fullblock 0): counts are its weighting
+        np.testing.assert_array_equal(cnt, w.astype(np.int64))
+        m = cnt > 0
+        np.testing.assert_allclose(out["sum_d2"][m] / cnt[m], msd[m], rtol=1e-6, atol=1e-12)
+        assert np.isnan(msd[~m]).all()
+    m = cnt > 0
+    fs = out["fs_sum"][m] / cnt[m][:, None]
+    assert np.abs(fs - corr[m]).max() <= 1e-6
+    eng.bins_free(h)
+    return cnt
+
+
+@pytest.mark.parametrize("persistent", [0, 1])
+@pytest.mark.parametrize("fullblock", [0, 1])
+def test_disp_bins_match_oracle(eng, qvectors, persistent, fullblock):
+    traj, _, _ = load("bins")
+    eng.upload(traj.unwrapped, traj.box, traj.box_lo, wrapped=traj.wrapped())
+    eng.set_scheme(traj.scheme)
+    lst = np.arange(traj.n_atoms, dtype=np.int32)
+    _check_bins(eng, traj, lst, 0, (2, 2, 3), persistent, fullblock, qvectors)
+    # a gathered sub-list
+    sub = np.nonzero(traj.types == 1)[0].astype(np.int32)
+    _check_bins(eng, traj, sub, eng.list(sub), (1, 3, 2), persistent, fullblock, qvectors)
+
+
+def test_disp_bins_many_bins_global_path(eng):
+    """More bins than the per-block shared accumulators hold (global atomics):
+    the per-bin sums against a numpy scatter of the FP64 terms."""
+    traj, _, _ = load("bins")
+    eng.upload(traj.unwrapped, traj.box, traj.box_lo, wrapped=traj.wrapped())
+    eng.set_scheme(traj.scheme)
+    lo, hi = _bounds(traj)
+    nb = (24, 24, 24)
+    B = nb[0] * nb[1] * nb[2]
+    eng.boxify(lo, hi)
+    h = eng.bins_create(nb, lo, hi)
+    out = eng.disp_bins(0, h, B)
+    bins = orc.assign_bins(orc.boxify(traj.wrapped(), lo, hi), nb, lo, hi)
+    s = orc.scheme(traj.scheme)
+    g, t0, t1 = orc.pairs(s, 0)
+    G = eng.n_timegaps
+    u = traj.unwrapped.astype(np.float64)
+    d2 = ((u[t1] - u[t0]) ** 2).sum(-1)  # [pairs][atoms]
+    b0 = bins[t0]
+    keep = b0 >= 0
+    key = (b0 * G + g[:, None])[keep]
+    ref = np.zeros(B * G)
+    np.add.at(ref, key, d2[keep])
+    rc = np.bincount(key, minlength=B * G)
+    np.testing.assert_array_equal(out["count"].reshape(-1), rc)
+    np.testing.assert_allclose(out["sum_d2"].reshape(-1), ref, rtol=1e-6, atol=1e-9)
+    eng.bins_free(h)
+
+
+def test_bins_errors(eng, engine_mod):
+    traj, _, _ = load("bins")
+    eng.upload(traj.unwrapped, traj.box, traj.box_lo)
+    eng.set_scheme(traj.scheme)
+    lo, hi = _bounds(traj)
+    with pytest.raises(engine_mod.AmdatError):
+        eng.bins_create((0, 1, 1), lo, hi)
+    with pytest.raises(engine_mod.AmdatError):
+        eng.disp_bins(0, 12345, 1)
+    h = eng.bins_create((1, 1, 1), lo, hi)
+    # a map is tied to the trajectory it was made for
+    eng.upload(traj.unwrapped[:-1], traj.box, traj.box_lo)
+    with pytest.raises(engine_mod.AmdatError):
+        eng.disp_bins(0, h, 1)
+    eng.bins_free(h)

@@ -74,3 +74,33 @@ def test_cli_errors(tmp_path, engine_mod, qvectors):
     r = run_cli(traj, "create_list all\nall\nisfs ./f.dat 3 4 xyz 0\nlist all\n", str(tmp_path),
                 extra_env={"AMDAT_QVECTORS": str(tmp_path / "missing" / "qvector")})
     assert r.returncode == 1 and "vector file" in r.stderr
+
+
+def test_cli_bin_list_errors(tmp_path, engine_mod, qvectors):
+    traj, _, _ = load("bins")
+    base = "create_list all\nall\n"
+    r = run_cli(traj, base + "create_bin_list x\nfoo 1 1 1\n", str(tmp_path))
+    assert r.returncode == 1 and "bin_list of type foo invalid" in r.stderr
+    r = run_cli(traj, base + "create_bin_list x\nall 1 1\n", str(tmp_path))
+    assert r.returncode == 1 and "Incorrect number of arguments" in r.stderr
+    r = run_cli(traj, base + "msd ./m.dat\nbin_list nothere all\n", str(tmp_path))
+    assert r.returncode == 1 and "Binned Trajectory list 'nothere' not found." in r.stderr
+    r = run_cli(traj, base + "create_bin_list x\nall 1 1 2\nngp ./n.dat\nbin_list x all\n", str(tmp_path))
+    assert r.returncode == 1 and "bin_list targets are supported for msd and isfs" in r.stderr
+    r = run_cli(traj, base + "create_bin_list x\nall 1 1 2\nmsd ./m.dat\nbin_list x all 1\n", str(tmp_path))
+    assert r.returncode == 0, r.stderr
+    assert sorted(p.name for p in tmp_path.glob("m.dat_bin_*")) == ["m.dat_bin_0.0.0.bindata",
+                                                                    "m.dat_bin_0.0.1.bindata"]
+
+
+def test_cli_bin_file_names_past_ten_bins(tmp_path, engine_mod):
+    """Bin file names as the reference's reused stringstreams make them: with 11
+    z bins the second x row's names collide, and the last writer wins."""
+    from oracle_script import OracleRun
+    traj, _, _ = load("bins")
+    r = run_cli(traj, "create_list all\nall\ncreate_bin_list x\nall 2 1 11\nmsd ./m.dat\nbin_list x all\n",
+                str(tmp_path))
+    assert r.returncode == 0, r.stderr
+    want = {name for _, name in OracleRun.bin_names("m.dat", [2, 1, 11], "_")}
+    assert len(want) == 21
+    assert {p.name for p in tmp_path.glob("m.dat_bin_*")} == want
