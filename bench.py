@@ -620,6 +620,29 @@ def main():
         p_g = eng.plan(gathered, flags=E.PLAN_GRAPH)
         ms_g = max_over_ranks(pg, time_plan(p_g, 10))
         p_g.close()
+        # spatial bins over the same walk (create_bin_list all 4 4 4): the MSD, and
+        # MSD + F_s, of all 64 bins in one keyed pass over the 200000 atoms, with
+        # membership at t0 and with persistence (t0 and t1)
+        blo = btraj.box_lo.astype(np.float32)
+        bhi = (btraj.box_lo.astype(np.float64) + btraj.box.astype(np.float64)).astype(np.float32)
+        eng.boxify(blo, bhi)
+        bh = eng.bins_create((4, 4, 4), blo, bhi)
+        bin_ms = {}
+        for tag, kw in (("msd", {}), ("msd_persistent", {"persistent": 1}),
+                        ("msd_fs", {"shells": shells, "period": L})):
+            eng.disp_bins(0, bh, 64, **kw)  # warm-up
+            torch.cuda.synchronize()
+            eng.profile_reset(True)
+            t0 = time.perf_counter()
+            reps = 5
+            for _ in range(reps):
+                out_b = eng.disp_bins(0, bh, 64, **kw)
+            wall = (time.perf_counter() - t0) / reps
+            nk, kms = eng.profile_kernel("disp_bins_kernel")
+            eng.profile_reset(False)
+            bin_ms[tag] = dict(kernel_ms=max_over_ranks(pg, kms / max(nk, 1)), call_ms=1e3 * wall,
+                               terms=int(out_b["count"].sum()))
+        eng.bins_free(bh)
         # plain FP64 path on the largest list (MSD + F_s), the mixed rate on the same list
         big = gathered[-1]
         t1 = time.perf_counter()
@@ -631,7 +654,8 @@ def main():
             ms_msd=ms_msd, ms_fs=ms_fs, ms_gathered=ms_g, units=units, tune_s=tune_s,
             info_msd=info_msd, info_fs=info_fs, launches=blaunch, plain_rate=plain_rate,
             alg_bytes=alg_bytes, unit_bytes=unit_bytes, share=share, ms_msd_ns=ms_msd_ns,
-            ms_fs_ns=ms_fs_ns, nvec=int(shells[1][-1]), sum_n=int(sizes.sum()), npairs=npairs)
+            ms_fs_ns=ms_fs_ns, nvec=int(shells[1][-1]), sum_n=int(sizes.sum()), npairs=npairs,
+            bins=bin_ms, n_atoms=int(btraj.n_atoms), frames=int(frames_used))
 
     if args.only in ("", "pairs"):
         # RDF + van Hove self/distinct: N=64000, L=42.3, 50 linear frames, sigma=0.1
@@ -799,6 +823,21 @@ def main():
                            "fp64_plain_largest_list": b["plain_rate"],
                            "mixed_over_plain": (b["units"] / (b["ms_fs"] / 1e3)) / b["plain_rate"]},
             "autotune_s": b["tune_s"], "gpu_launches": b["launches"]}
+        # binned pass: every atom in every time pair, keyed by its bin
+        bunits = float(b["n_atoms"]) * b["npairs"]
+        bbytes = float(b["n_atoms"]) * b["frames"] * 16.0
+        bins_line = {"workload": "create_bin_list all 4 4 4 (64 bins) over the same 200000-atom walk, all "
+                                 f"{b['npairs']} time pairs, one keyed pass for every bin",
+                     "unit": "atom·time-pairs/s",
+                     "bytes_rule": f"atoms x {b['frames']} frames x 16 B (FP32 xyz + int32 bin, each frame once)"}
+        for tag, v in b["bins"].items():
+            gb = bbytes / (v["kernel_ms"] / 1e3) / 1e9
+            bins_line[tag] = {"value": bunits / (v["kernel_ms"] / 1e3), "kernel_ms": v["kernel_ms"],
+                              "call_ms": v["call_ms"], "member_terms": v["terms"],
+                              "roofline": {"bound": "hbm", "achieved": gb, "peak": hbm, "unit": "GB/s",
+                                           "frac": gb / hbm}}
+        bins_line["msd_fs"]["roofline"]["bound"] = "fp32 (one cospif per vector)"
+        line["batched"]["bins"] = bins_line
         if "value" not in line:
             line.update({"value": b["units"] / (b["ms_fs"] / 1e3), "unit": "atom·time-pairs/s",
                          "ms_per_step": b["ms_fs"], "config": {"workload": line["batched"]["workload"]}})
