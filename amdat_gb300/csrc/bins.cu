@@ -7,7 +7,8 @@
 //   Bin_Dynamics_Analysis::list_displacementkernel (src/bin_dynamics_analysis.h):
 //     the members in the bin at both t0 and t1 (persistence), with the pairs of
 //     displacement_list(this), i.e. fullblock 0
-// for the MSD (Mean_Square_Displacement::listkernel) and F_s
+// for the MSD and NGP moments (Mean_Square_Displacement / Non_Gaussian_Parameter
+// listkernels) and F_s
 // (Incoherent_Scattering_Function::listkernel) of every bin at once.
 //
 // The reference builds one time-dependent list per bin and runs the analysis
@@ -16,8 +17,9 @@
 // keys each term by the member's bin: every atom's trajectory is read once per
 // pair for all bins together.  Terms of one warp that share a bin are summed
 // by the warp's lowest such lane (FP64, lane order) and added with one atomic to
-// a per-block shared-memory accumulator [bin][1 + shells], flushed to the
-// global [bin][gap][1 + shells] sums at the end of each item.  Counts are
+// a per-block shared-memory accumulator [bin][2 + shells] (|dr|^2, |dr|^4, the
+// shell means), flushed to the global [bin][gap][2 + shells] sums at the end of
+// each item.  Counts are
 // exact integers; the FP64 sums are order-independent to rounding (atomics).
 #include <algorithm>
 #include <cfloat>
@@ -114,7 +116,7 @@ struct BnParams {
   const float* inv_count;
   float period;
   int32_t n_gaps;
-  int32_t stride;  // 1 + n_fs
+  int32_t stride;  // 2 + n_fs: |dr|^2, |dr|^4, shells
   double* acc;     // [bin][gap][stride]
   unsigned long long* cnt;  // [bin][gap]
   int32_t staged;  // per-block shared accumulators
@@ -124,7 +126,7 @@ template <bool FS>
 __global__ void __launch_bounds__(BN_THREADS) disp_bins_kernel(BnParams p) {
   extern __shared__ double bn_smem[];  // staged: [n_bins][stride] sums, then [n_bins] counts
   __shared__ int s_item;
-  __shared__ float s_val[BN_THREADS / 32][32][1 + BN_MAX_FS];
+  __shared__ float s_val[BN_THREADS / 32][32][2 + BN_MAX_FS];
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int stride = p.stride;
   double* sacc = bn_smem;
@@ -149,9 +151,9 @@ __global__ void __launch_bounds__(BN_THREADS) disp_bins_kernel(BnParams p) {
     for (int base = it.a0; base < it.a1; base += BN_THREADS) {
       const int a = base + tid;
       int b = -1;
-      float v[1 + BN_MAX_FS];
+      float v[2 + BN_MAX_FS];
 #pragma unroll
-      for (int k = 0; k < 1 + BN_MAX_FS; ++k) v[k] = 0.f;
+      for (int k = 0; k < 2 + BN_MAX_FS; ++k) v[k] = 0.f;
       if (a < it.a1) {
         const int atom = p.list_idx ? __ldg(p.list_idx + a) : p.list_first + a;
         b = __ldg(B0 + atom);
@@ -161,6 +163,7 @@ __global__ void __launch_bounds__(BN_THREADS) disp_bins_kernel(BnParams p) {
           const float dy = __fsub_rn(__ldg(X1 + p.n_pad + atom), __ldg(X0 + p.n_pad + atom));
           const float dz = __fsub_rn(__ldg(X1 + 2 * p.n_pad + atom), __ldg(X0 + 2 * p.n_pad + atom));
           v[0] = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+          v[1] = v[0] * v[0];
           if (FS) {
             const int32_t fx = turns_fixed(dx, p.period);
             const int32_t fy = turns_fixed(dy, p.period);
@@ -183,14 +186,14 @@ __global__ void __launch_bounds__(BN_THREADS) disp_bins_kernel(BnParams p) {
                 }
               }
               kadd(acc, blk);
-              v[1 + s] = __fmul_rn(__fsub_rn(acc.s, acc.c), p.inv_count[s]);
+              v[2 + s] = __fmul_rn(__fsub_rn(acc.s, acc.c), p.inv_count[s]);
             }
           }
         }
       }
       // lanes of one bin: the lowest adds their terms (lane order, FP64)
 #pragma unroll
-      for (int k = 0; k < 1 + BN_MAX_FS; ++k)
+      for (int k = 0; k < 2 + BN_MAX_FS; ++k)
         if (k < stride) s_val[warp][lane][k] = v[k];
       __syncwarp();
       const unsigned peers = __match_any_sync(0xffffffffu, b);
@@ -221,6 +224,44 @@ __global__ void __launch_bounds__(BN_THREADS) disp_bins_kernel(BnParams p) {
       }
     }
     __syncthreads();
+  }
+}
+
+// --- fast particles -------------------------------------------------------------
+// Fast_Particles::listkernel (src/fast_particles.cpp): over the pairs of one gap,
+// a list member whose u2 = float(pow(|dr|, 2)) exceeds the threshold is fast in
+// the exponential block of its start frame, int(float(t0 - frt) / float(K))
+// (|dr| = sqrtf((dx*dx + dy*dy) + dz*dz), the reference's FP32 chain).
+__global__ void fast_mark_kernel(const float* __restrict__ u, int64_t n_pad, int32_t list_n, int32_t list_first,
+                                 const int32_t* __restrict__ list_idx, const int32_t* __restrict__ t0,
+                                 const int32_t* __restrict__ t1, int32_t p0, int32_t n_pairs, int32_t frt,
+                                 int32_t K, int32_t n_blocks, float min_u2, unsigned char* __restrict__ fast) {
+  const int64_t n = (int64_t)n_pairs * list_n;
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int p = p0 + (int)(i / list_n), m = (int)(i % list_n);
+    const int atom = list_idx ? list_idx[m] : list_first + m;
+    const int a = t0[p], b = t1[p];
+    const float* X0 = u + (int64_t)a * 3 * n_pad;
+    const float* X1 = u + (int64_t)b * 3 * n_pad;
+    const float dx = __fsub_rn(X1[atom], X0[atom]);
+    const float dy = __fsub_rn(X1[n_pad + atom], X0[n_pad + atom]);
+    const float dz = __fsub_rn(X1[2 * n_pad + atom], X0[2 * n_pad + atom]);
+    const float d = __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz)));
+    const float u2 = __double2float_rn((double)d * (double)d);
+    const int blk = (int)__fdiv_rn(__fsub_rn((float)a, (float)frt), (float)K);
+    if (u2 > min_u2 && blk >= 0 && blk < n_blocks) fast[(int64_t)blk * n_pad + atom] = 1;
+  }
+}
+
+// membership map of the block list: frame t belongs to block int(float(t - frt) / float(K))
+__global__ void fast_map_kernel(const unsigned char* __restrict__ fast, int64_t n_pad, int32_t n_atoms,
+                                int64_t n_terms, int32_t frt, int32_t K, int32_t n_blocks,
+                                int32_t* __restrict__ bins) {
+  for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n_terms;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t t = i / n_atoms, a = i - t * n_atoms;
+    const int blk = (int)__fdiv_rn((float)(t - frt), (float)K);
+    bins[t * n_pad + a] = (blk >= 0 && blk < n_blocks && fast[(int64_t)blk * n_pad + a]) ? 0 : -1;
   }
 }
 
@@ -294,6 +335,52 @@ amdat_status amdat_bins_create(amdat_ctx* ctx, int32_t nx, int32_t ny, int32_t n
   });
 }
 
+amdat_status amdat_fast_particles(amdat_ctx* ctx, int32_t list, int32_t gap, float min_u2, int32_t* handle) {
+  return guarded([&] {
+    check_ctx(ctx);
+    if (!ctx->have_traj) throw Error(AMDAT_ERR_STATE, "no trajectory uploaded");
+    if (!ctx->have_scheme) throw Error(AMDAT_ERR_STATE, "no time scheme set");
+    AMDAT_REQUIRE(handle != nullptr, "null handle");
+    const ListEntry& e = list_entry(ctx, list);
+    const PairTable& P = pair_table(ctx, false, false);  // displacement_list(this, gap, false)
+    AMDAT_REQUIRE(gap >= 0 && gap < P.n_gaps, "gap out of range");
+    const int32_t K = ctx->scheme.n_exponential_steps, n_blocks = ctx->scheme.n_exponentials;
+    const int32_t frt = ctx->scheme.frt;
+    AMDAT_REQUIRE(K > 0 && n_blocks > 0, "the scheme has no exponential blocks");
+    auto* m = new BinMap();
+    try {
+      m->nx = m->ny = m->nz = 1;
+      m->n_frames = ctx->n_frames, m->n_pad = ctx->n_pad;
+      m->bin.reserve((size_t)ctx->n_frames * ctx->n_pad);
+      AMDAT_CUDA(cudaMemsetAsync(m->bin.ptr, 0xff, (size_t)ctx->n_frames * ctx->n_pad * 4, ctx->stream));
+      unsigned char* fast = ctx->scratch.reserve((size_t)n_blocks * ctx->n_pad);
+      AMDAT_CUDA(cudaMemsetAsync(fast, 0, (size_t)n_blocks * ctx->n_pad, ctx->stream));
+      const int32_t p0 = P.gap_first[gap], np = P.gap_first[gap + 1] - p0;
+      if (np > 0 && e.n > 0) {
+        fast_mark_kernel<<<grid_for(ctx, (int64_t)np * e.n), 256, 0, ctx->stream>>>(
+            ctx->u.ptr, ctx->n_pad, e.n, e.first, e.contiguous ? nullptr : e.idx.ptr, P.t0.ptr, P.t1.ptr, p0, np,
+            frt, K, n_blocks, min_u2, fast);
+        check_launch("fast_mark_kernel");
+        count_launch(ctx);
+      }
+      const int64_t n = (int64_t)ctx->n_frames * ctx->n_atoms;
+      if (n > 0) {
+        fast_map_kernel<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(fast, ctx->n_pad, ctx->n_atoms, n, frt, K,
+                                                                    n_blocks, m->bin.ptr);
+        check_launch("fast_map_kernel");
+        count_launch(ctx);
+      }
+      AMDAT_CUDA(cudaStreamSynchronize(ctx->stream));
+    } catch (...) {
+      delete m;
+      throw;
+    }
+    const int32_t h = ctx->next_bins++;
+    ctx->bin_maps[h] = m;
+    *handle = h;
+  });
+}
+
 amdat_status amdat_bins_free(amdat_ctx* ctx, int32_t handle) {
   return guarded([&] {
     check_ctx(ctx);
@@ -335,7 +422,7 @@ amdat_status amdat_bins_read(amdat_ctx* ctx, int32_t handle, int32_t out_flags, 
 amdat_status amdat_disp_bins_run(amdat_ctx* ctx, int32_t list, int32_t bins, int32_t persistent,
                                  int32_t fullblock, int32_t n_shells, const int32_t* shell_offsets,
                                  const int32_t* kvec, float period, int32_t out_flags, double* sum_d2,
-                                 int64_t* count, double* fs_sum) {
+                                 double* sum_d4, int64_t* count, double* fs_sum) {
   return guarded([&] {
     check_ctx(ctx);
     if (!ctx->have_traj) throw Error(AMDAT_ERR_STATE, "no trajectory uploaded");
@@ -349,7 +436,7 @@ amdat_status amdat_disp_bins_run(amdat_ctx* ctx, int32_t list, int32_t bins, int
     const PairTable& P = pair_table(ctx, persistent ? false : fullblock != 0, false);
     const int G = P.n_gaps;
     const int32_t B = m.nx * m.ny * m.nz;
-    const int stride = 1 + n_shells;
+    const int stride = 2 + n_shells;
     // shells (list mode: one cosine per vector)
     std::vector<int4> kv;
     std::vector<int32_t> off(1, 0);
@@ -426,11 +513,13 @@ amdat_status amdat_disp_bins_run(amdat_ctx* ctx, int32_t list, int32_t bins, int
       count_launch(ctx);
     }
     const cudaMemcpyKind kind = out_flags == AMDAT_OUT_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-    // [bin][gap][stride] -> sum_d2[bin][gap], fs_sum[bin][gap][shell]
+    // [bin][gap][stride] -> sum_d2[bin][gap], sum_d4[bin][gap], fs_sum[bin][gap][shell]
     if (sum_d2)
       AMDAT_CUDA(cudaMemcpy2DAsync(sum_d2, 8, base + o_acc, (size_t)stride * 8, 8, (size_t)B * G, kind, st));
+    if (sum_d4)
+      AMDAT_CUDA(cudaMemcpy2DAsync(sum_d4, 8, base + o_acc + 8, (size_t)stride * 8, 8, (size_t)B * G, kind, st));
     if (fs_sum && n_shells)
-      AMDAT_CUDA(cudaMemcpy2DAsync(fs_sum, (size_t)n_shells * 8, base + o_acc + 8, (size_t)stride * 8,
+      AMDAT_CUDA(cudaMemcpy2DAsync(fs_sum, (size_t)n_shells * 8, base + o_acc + 16, (size_t)stride * 8,
                                    (size_t)n_shells * 8, (size_t)B * G, kind, st));
     if (count) AMDAT_CUDA(cudaMemcpyAsync(count, base + o_cnt, (size_t)B * G * 8, kind, st));
     AMDAT_CUDA(cudaStreamSynchronize(st));

@@ -56,7 +56,7 @@ EXPORTED = [
     "amdat_gsmooth_run", "amdat_disp_axes_run",
     "amdat_gsmooth_adjoint", "amdat_structure_factor_adjoint",
     "amdat_boxify", "amdat_bins_create", "amdat_bins_read", "amdat_bins_free",
-    "amdat_disp_bins_run",
+    "amdat_disp_bins_run", "amdat_fast_particles",
 ]
 
 PLAN_AUTOTUNE, PLAN_GRAPH, PLAN_NO_SHARING = 1, 2, 4
@@ -336,13 +336,20 @@ class Engine:
         _check(lib().amdat_bins_read(self._ctx, int(handle), OUT_HOST, _p(m), _p(c)))
         return m, c
 
+    def fast_particles(self, list_h, gap, min_u2) -> int:
+        """Block-wise fast-particle membership as a one-bin map (amdat_fast_particles)."""
+        h = C.c_int32()
+        _check(lib().amdat_fast_particles(self._ctx, int(list_h), int(gap), C.c_float(min_u2), C.byref(h)))
+        return h.value
+
     def bins_free(self, handle):
         _check(lib().amdat_bins_free(self._ctx, int(handle)))
 
     def disp_bins(self, list_h, bins_h, n_bins, persistent=0, fullblock=0, shells=None, period=1.0):
-        """Per-bin sums (amdat_disp_bins_run): sum_d2 [B][G], count [B][G], fs_sum [B][G][S]."""
+        """Per-bin sums (amdat_disp_bins_run): sum_d2, sum_d4, count [B][G], fs_sum [B][G][S]."""
         G = self.n_timegaps
         d2 = np.zeros((n_bins, G))
+        d4 = np.zeros((n_bins, G))
         cnt = np.zeros((n_bins, G), np.int64)
         kv = off = None
         S = 0
@@ -351,9 +358,9 @@ class Engine:
             S = len(off) - 1
         fs = np.zeros((n_bins, G, max(S, 1)))
         _check(lib().amdat_disp_bins_run(self._ctx, int(list_h), int(bins_h), int(persistent), int(fullblock), S,
-                                         _p(off), _p(kv), C.c_float(period), OUT_HOST, _p(d2), _p(cnt),
+                                         _p(off), _p(kv), C.c_float(period), OUT_HOST, _p(d2), _p(d4), _p(cnt),
                                          _p(fs) if S else None))
-        return dict(sum_d2=d2, count=cnt, fs_sum=fs[:, :, :S])
+        return dict(sum_d2=d2, sum_d4=d4, count=cnt, fs_sum=fs[:, :, :S])
 
     def plan(self, lists, fullblock=0, shells=None, period=1.0, n_bins=0, bin_max=0.0, flags=0):
         """Prepared many-list displacement run (amdat_disp_plan_*)."""

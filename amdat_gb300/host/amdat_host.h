@@ -59,6 +59,8 @@ class System {
   int n_exponentials() const { return scheme_.n_exponentials; }
   int n_exponential_steps() const { return scheme_.n_exponential_steps; }
   const std::vector<float>& timegaps() const { return gap_times_; }
+  float show_time(int frame) const { return timelist_[frame]; }
+  int show_frt() const { return scheme_.frt; }
   Coord size() const { return Coord{box_[0], box_[1], box_[2]}; }
   float min_box() const;  // min_box_dimensions().min()
   int atomtype_index(const std::string& name) const;
@@ -87,16 +89,25 @@ class System {
 
 // Static_Trajectory_List: membership fixed over time, ascending atom index
 // (src/static_trajectory_list.cpp, src/trajectory_list.cpp:315-333)
+class Trajectory_List_Bins;
+
 class Trajectory_List {
  public:
   Trajectory_List(System* sys, std::vector<int32_t> atoms);
+  // Exptime_Trajectory_List (src/exptime_trajectory_list.cpp): membership that
+  // changes with the exponential block of the frame, held as a one-bin map of
+  // the engine over all atoms (Fast_Particles makes these)
+  Trajectory_List(System* sys, std::shared_ptr<Trajectory_List_Bins> membership);
   int handle() const { return handle_; }
   int show_n_trajectories(int = 0) const { return (int)atoms_.size(); }
   const std::vector<int32_t>& atoms() const { return atoms_; }
+  bool time_dependent() const { return (bool)membership_; }
+  Trajectory_List_Bins* membership() const { return membership_.get(); }
 
  private:
   int handle_ = 0;
   std::vector<int32_t> atoms_;
+  std::shared_ptr<Trajectory_List_Bins> membership_;
 };
 
 // Wave_Vectors(System*, plane, max_length_scale) (src/wave_vectors.cpp:77-171,
@@ -134,6 +145,8 @@ class Trajectory_List_Bins {
   Trajectory_List_Bins(System* sys, int nx, int ny, int nz);
   Trajectory_List_Bins(System* sys, int nx, int ny, int nz, float xlo, float xhi, float ylo, float yhi,
                        float zlo, float zhi);
+  // takes over a one-bin map the engine made (amdat_fast_particles)
+  Trajectory_List_Bins(System* sys, int one_bin_handle);
   ~Trajectory_List_Bins();
   Trajectory_List_Bins(const Trajectory_List_Bins&) = delete;
   Trajectory_List_Bins& operator=(const Trajectory_List_Bins&) = delete;
@@ -191,10 +204,13 @@ class Non_Gaussian_Parameter : public Analysis {
   explicit Non_Gaussian_Parameter(System* sys);
   void analyze(Trajectory_List* list) override;
   void write(const std::string& file) const override;
+  void analyze_bins(Trajectory_List* list, Trajectory_List_Bins* bins, bool persistent) override;
+  void select_bin(int b) override { ngp_ = bin_ngp_[b]; }
   int max() const;
 
  private:
   std::vector<float> ngp_;
+  std::vector<std::vector<float>> bin_ngp_;
 };
 
 // Incoherent_Scattering_Function (src/incoherent_scattering_function.cpp:176-299)
@@ -274,12 +290,44 @@ class Van_Hove_Self : public Analysis {
   Van_Hove_Self(System* sys, int n_bins, float max_value);
   void analyze(Trajectory_List* list) override;
   void write(const std::string& file) const override;
+  int show_n_bins() const { return n_bins_; }
+  float show_bin_size() const { return bin_size_; }
+  float show(int gap, int bin) const { return corr_[(size_t)gap * n_bins_ + bin]; }
 
  protected:
   int n_bins_;
   float max_value_, bin_size_;
   std::vector<float> corr_;  // [gap][bin]
 };
+
+// Gaussian_Comparison (src/gaussian_comparison.cpp): the self van Hove at one
+// time gap against the Gaussian of the same MSD, both times the shell volume;
+// their crossings bound the slow and fast particles, and the fractions follow
+class Gaussian_Comparison {
+ public:
+  Gaussian_Comparison(System* sys, int time_index, const Van_Hove_Self& vhs, float msd);
+  void write(const std::string& file) const;
+  int show_time_index() const { return time_index_; }
+  float show_fastboundary() const { return fastboundary_; }
+
+ private:
+  System* sys_;
+  int time_index_, n_bins_;
+  float bin_size_;
+  std::vector<float> gaussian_, van_hove_;
+  int slow_index_ = 0, fast_index_ = 0;
+  float slowboundary_ = 0, fastboundary_ = 0;
+  float slow_ = 0, fast_ = 0, gslow_ = 0, gfast_ = 0;
+  bool error_ = false;
+};
+
+// Fast_Particles (src/fast_particles.cpp): the members of `list` whose squared
+// displacement over time gap `gap` exceeds min_u2, per exponential block, as a
+// time-dependent list; block_counts gets the members of each block
+// (Exptime_Trajectory_List::write_count writes them, see write_block_counts)
+std::unique_ptr<Trajectory_List> fast_particles(System* sys, Trajectory_List* list, int gap, float min_u2,
+                                                std::vector<int64_t>* block_counts);
+void write_block_counts(const System* sys, const std::vector<int64_t>& counts, const std::string& file);
 
 // Van_Hove_Distinct with the distance the reference intends to bin
 // (src/van_hove_distinct.cpp:159-213)

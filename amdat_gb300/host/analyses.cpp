@@ -88,12 +88,13 @@ void Mean_Square_Displacement::analyze(Trajectory_List* list) {
 
 // --- spatial bins ------------------------------------------------------------
 void Analysis::analyze_bins(Trajectory_List*, Trajectory_List_Bins*, bool) {
-  throw Error(AMDAT_ERR_ARGUMENT, "bin_list targets are supported for msd and isfs by this engine");
+  throw Error(AMDAT_ERR_ARGUMENT,
+              "bin_list targets and time-dependent lists are supported for msd, ngp and isfs by this engine");
 }
 
 namespace {
 struct BinOut {
-  std::vector<double> d2, fs;  // [bin][gap], [bin][gap][shell]
+  std::vector<double> d2, d4, fs;  // [bin][gap], [bin][gap], [bin][gap][shell]
   std::vector<int64_t> cnt;    // [bin][gap]
 };
 BinOut disp_bins(System* sys, const Trajectory_List* list, const Trajectory_List_Bins* bins, bool persistent,
@@ -102,6 +103,7 @@ BinOut disp_bins(System* sys, const Trajectory_List* list, const Trajectory_List
   const int S = off ? (int)off->size() - 1 : 0;
   BinOut o;
   o.d2.assign((size_t)B * G, 0.0);
+  o.d4.assign((size_t)B * G, 0.0);
   o.cnt.assign((size_t)B * G, 0);
   o.fs.assign((size_t)B * G * std::max(S, 1), 0.0);
   // the engine takes up to 8 shells per pass
@@ -117,7 +119,8 @@ BinOut disp_bins(System* sys, const Trajectory_List* list, const Trajectory_List
     check(amdat_disp_bins_run(sys->ctx(), list->handle(), bins->handle(), persistent ? 1 : 0, fullblock ? 1 : 0,
                               std::max(ns, 0), ns > 0 ? sub_off.data() : nullptr, ns > 0 ? sub_kv.data() : nullptr,
                               period, AMDAT_OUT_HOST, s0 == 0 ? o.d2.data() : nullptr,
-                              s0 == 0 ? o.cnt.data() : nullptr, ns > 0 ? fs.data() : nullptr),
+                              s0 == 0 ? o.d4.data() : nullptr, s0 == 0 ? o.cnt.data() : nullptr,
+                              ns > 0 ? fs.data() : nullptr),
           "binned displacement run");
     for (int bg = 0; bg < B * G; ++bg)
       for (int s = 0; s < ns; ++s) o.fs[(size_t)bg * S + s0 + s] = fs[(size_t)bg * ns + s];
@@ -150,6 +153,9 @@ void Trajectory_List_Bins::assign(const float lo[3], const float hi[3]) {
   check(amdat_boxify(sys_->ctx(), sys_->bounds_lo(), sys_->bounds_hi()), "boxify");
   check(amdat_bins_create(sys_->ctx(), n_[0], n_[1], n_[2], lo, hi, &handle_), "bin list");
 }
+
+Trajectory_List_Bins::Trajectory_List_Bins(System* sys, int one_bin_handle)
+    : sys_(sys), n_{1, 1, 1}, handle_(one_bin_handle) {}
 
 Trajectory_List_Bins::~Trajectory_List_Bins() {
   if (handle_) amdat_bins_free(sys_->ctx(), handle_);
@@ -309,6 +315,19 @@ void Non_Gaussian_Parameter::analyze(Trajectory_List* list) {
   }
 }
 
+void Non_Gaussian_Parameter::analyze_bins(Trajectory_List* list, Trajectory_List_Bins* bins, bool persistent) {
+  const BinOut o = disp_bins(system, list, bins, persistent, false, nullptr, nullptr, 1.f);
+  const int G = system->n_timegaps(), B = bins->n_bins();
+  bin_ngp_.assign(B, std::vector<float>(G, 0.f));
+  for (int b = 0; b < B; ++b)
+    for (int g = 0; g < G; ++g) {
+      const size_t i = (size_t)b * G + g;
+      const double w = (double)o.cnt[i];
+      const double msd = o.d2[i] / w;
+      bin_ngp_[b][g] = (float)(o.d4[i] * (3.0 / w) / (5.0 * msd * msd) - 1.0);
+    }
+}
+
 int Non_Gaussian_Parameter::max() const {
   int best = -1;
   float bv = 0;
@@ -427,6 +446,108 @@ void Van_Hove_Self::write(const std::string& file) const {
     for (int b = 0; b < n_bins_ - 1; ++b) out << Num{corr_[(size_t)g * n_bins_ + b]} << "\t";
     out << Num{corr_[(size_t)g * n_bins_ + n_bins_ - 1]} << "\n";
   }
+}
+
+// --- Gaussian comparison and fast particles ----------------------------------
+namespace {
+constexpr double GC_PI = 3.14159265;  // src/gaussian_comparison.cpp:15
+}
+
+Gaussian_Comparison::Gaussian_Comparison(System* sys, int time_index, const Van_Hove_Self& vhs, float msd)
+    : sys_(sys), time_index_(time_index), n_bins_(vhs.show_n_bins()), bin_size_(vhs.show_bin_size()) {
+  if (time_index < 0 || time_index >= sys->n_timegaps())
+    throw Error(AMDAT_ERR_ARGUMENT, "time index of the Gaussian comparison out of range");
+  // scale_van_hoves: both curves times the shell volume, the reference's
+  // float/double mix (float storage, double pow/exp)
+  const float alpha = (float)(3.0 / (2.0 * (double)msd));
+  gaussian_.assign(n_bins_, 0.f);
+  van_hove_.assign(n_bins_, 0.f);
+  for (int b = 0; b < n_bins_; ++b) {
+    const float inner = float(b) * bin_size_;
+    const float shell = (float)(4.0 / 3.0 * GC_PI *
+                                (std::pow(((double)float(b) + 1.0) * (double)bin_size_, 3.0) - std::pow((double)inner, 3.0)));
+    van_hove_[b] = vhs.show(time_index, b) * shell;
+    const double r = ((double)float(b) + .5) * (double)bin_size_;
+    gaussian_[b] = (float)(std::pow((double)alpha / GC_PI, 3.0 / 2.0) * std::exp(-(double)alpha * std::pow(r, 2.0)) *
+                           (double)shell);
+  }
+  // find_crossovers
+  for (int b = 1; b < n_bins_; ++b)
+    if (gaussian_[b] >= van_hove_[b]) {
+      slow_index_ = b - 1;
+      break;
+    }
+  for (int b = slow_index_ + 1; b < n_bins_; ++b)
+    if (gaussian_[b] <= van_hove_[b]) {
+      fast_index_ = b;
+      break;
+    }
+  error_ = fast_index_ == 0;
+  slowboundary_ = (float)std::pow(((double)float(slow_index_) + .5) * (double)bin_size_, 2.0);
+  fastboundary_ = (float)std::pow(((double)float(fast_index_) - .5) * (double)bin_size_, 2.0);
+  // determine_fractions
+  for (int b = 1; b <= slow_index_; ++b) {
+    slow_ += van_hove_[b];
+    gslow_ += gaussian_[b];
+  }
+  fast_ = (float)(1.0 - (double)slow_);
+  gfast_ = (float)(1.0 - (double)gslow_);
+  for (int b = slow_index_ + 1; b < fast_index_; ++b) {
+    fast_ -= van_hove_[b];
+    gfast_ -= gaussian_[b];
+  }
+}
+
+void Gaussian_Comparison::write(const std::string& file) const {
+  std::ofstream out = open_out(file);
+  if (error_)
+    out << "Warning: program cannot identify two crossing points between self Van Hove and Gaussian "
+           "approximation self Van Hove.  Fractions of slow and fast particles will be incorrect.\n";
+  out << "Gaussian comparison data created by AMDAT v." << SEMVER << "\n";
+  out << "t*\n" << sys_->timegaps()[time_index_] << "\n";
+  out << "Slow_Cutoff: " << std::pow((double)slowboundary_, 0.5) << "\n";
+  out << "Fast_Cutoff: " << std::pow((double)fastboundary_, 0.5) << "\n";
+  out << "\tSlow_Fraction\tFast_Fraction\n";
+  out << "Gaussian\t" << gslow_ << "\t" << gfast_ << "\n";
+  out << "Actual\t" << slow_ << "\t" << fast_ << "\n";
+  out << "Excess\t" << slow_ - gslow_ << "\t" << fast_ - gfast_ << "\n\n";
+  out << "Self_Van_Hove*shellvolume\n";
+  out << "radius\tgaussian\tactual\n";
+  for (int b = 0; b < n_bins_; ++b)
+    out << (b + .5) * (double)bin_size_ << "\t" << Num{gaussian_[b]} << "\t" << Num{van_hove_[b]} << "\n";
+}
+
+std::unique_ptr<Trajectory_List> fast_particles(System* sys, Trajectory_List* list, int gap, float min_u2,
+                                                std::vector<int64_t>* block_counts) {
+  if (list->time_dependent())
+    throw Error(AMDAT_ERR_ARGUMENT, "fast particles of a time-dependent list are not supported by this engine");
+  if (gap < 0 || gap >= sys->n_timegaps()) throw Error(AMDAT_ERR_ARGUMENT, "time index out of range");
+  int32_t h = 0;
+  check(amdat_fast_particles(sys->ctx(), list->handle(), gap, min_u2, &h), "fast particles");
+  auto bins = std::make_shared<Trajectory_List_Bins>(sys, h);
+  if (block_counts) {
+    std::vector<int64_t> per_frame((size_t)sys->n_timesteps(), 0);
+    check(amdat_bins_read(sys->ctx(), h, AMDAT_OUT_HOST, nullptr, per_frame.data()), "fast particle counts");
+    const int nb = sys->n_exponentials(), K = sys->n_exponential_steps();
+    block_counts->assign(nb, 0);
+    for (int b = 0; b < nb; ++b) {
+      const int t = b * K + sys->show_frt();  // the block's first frame
+      if (t >= 0 && t < sys->n_timesteps()) (*block_counts)[b] = per_frame[t];
+    }
+  }
+  return std::make_unique<Trajectory_List>(sys, std::move(bins));
+}
+
+void write_block_counts(const System* sys, const std::vector<int64_t>& counts, const std::string& file) {
+  // Exptime_Trajectory_List::write_count (src/exptime_trajectory_list.cpp)
+  const int nb = (int)counts.size();
+  double avg = 0;
+  for (int b = 0; b < nb; ++b) avg += double(counts[b]) / double(nb);
+  std::ofstream out = open_out(file);
+  out << "Average_trajectories:\t" << avg << "\n";
+  out << "Count_List\n";
+  for (int b = 0; b < nb; ++b)
+    out << sys->show_time(b * sys->n_exponential_steps() + sys->show_frt()) << "\t" << counts[b] << "\n";
 }
 
 Van_Hove_Distinct::Van_Hove_Distinct(System* sys, int n_bins, float max_value)

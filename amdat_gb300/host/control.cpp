@@ -77,7 +77,11 @@ class Control {
     if (a.size() < 2 || a[0] != "list")
       throw Error(AMDAT_ERR_ARGUMENT, "only 'list <name>' targets are supported by this engine");
     std::vector<Trajectory_List*> out;
-    for (size_t i = 1; i < a.size(); ++i) out.push_back(list(a[i]));
+    for (size_t i = 1; i < a.size(); ++i) {
+      out.push_back(list(a[i]));
+      if (out.back()->time_dependent())
+        throw Error(AMDAT_ERR_ARGUMENT, "time-dependent lists (find_fast) are supported by msd, ngp and isfs here");
+    }
     return out;
   }
 
@@ -126,6 +130,16 @@ class Control {
                                           " not understood. Acceptable options are list or bin_list.");
     std::vector<Trajectory_List*> t;
     for (size_t i = 1; i < a.size(); ++i) t.push_back(list(a[i]));
+    if (t.size() == 1 && t[0]->time_dependent()) {
+      // a time-dependent list: its members at each start frame (one-bin static pass)
+      an.analyze_bins(t[0], t[0]->membership(), false);
+      an.select_bin(0);
+      an.write(file);
+      return;
+    }
+    for (auto* l : t)
+      if (l->time_dependent())
+        throw Error(AMDAT_ERR_ARGUMENT, "time-dependent lists (find_fast) are supported by msd, ngp and isfs here");
     if (t.size() == 1) an.analyze(t[0]);
     else an.analyze(t[0], t[1]);
     an.write(file);
@@ -207,6 +221,8 @@ class Control {
         for (int k = 0; k < 2; ++k) block.push_back(read_line());  // box size, box bounds
       lists_.clear();
       bins_.clear();
+      vhs_.reset();
+      gc_.reset();
       sys_.reset();
       sys_ = std::make_unique<System>(block, device_);
     } else if (cmd == "limit") {
@@ -256,8 +272,48 @@ class Control {
     } else if (cmd == "vhs") {
       argcheck(a, 4, 4);
       pathcheck(a[1]);
-      Van_Hove_Self v(&sys(), std::atoi(a[3].c_str()), (float)std::atof(a[2].c_str()));
-      analyze_write(v, a[1]);
+      auto v = std::make_unique<Van_Hove_Self>(&sys(), std::atoi(a[3].c_str()), (float)std::atof(a[2].c_str()));
+      analyze_write(*v, a[1]);
+      vhs_ = std::move(v);  // vhs_defined: compare_gaussian reads the last one
+    } else if (cmd == "compare_gaussian") {
+      // Control::compare_gaussian (src/control.cpp:3378-3422): MSD and NGP of the
+      // target list, then the comparison at the NGP peak (or the given time index)
+      if (!vhs_)
+        throw Error(AMDAT_ERR_STATE,
+                    "self van hove not yet defined.  Self van hove must be calculated prior to compare_gaussian "
+                    "calculation.");
+      if (a.size() != 2 && a.size() != 3)
+        throw Error(AMDAT_ERR_ARGUMENT, "Incorrect number of arguments for gaussian comparison method.");
+      auto t = targets();
+      Mean_Square_Displacement m(&sys());
+      m.analyze(t[0]);
+      Non_Gaussian_Parameter n(&sys());
+      n.analyze(t[0]);
+      const int ti = a.size() == 3 ? std::atoi(a[2].c_str()) : n.max();
+      if (ti < 0) throw Error(AMDAT_ERR_ARGUMENT, "the non-Gaussian parameter has no positive maximum");
+      gc_ = std::make_unique<Gaussian_Comparison>(&sys(), ti, *vhs_, m.show(ti));
+      gc_->write(a[1]);
+    } else if (cmd == "find_fast" || cmd == "find_fast_fixedthreshold") {
+      // Control::find_fast / find_fast_fixedthreshold (src/control.cpp:3430-3500)
+      int gap;
+      float threshold;
+      if (cmd == "find_fast") {
+        argcheck(a, 3, 3);
+        if (!gc_)
+          throw Error(AMDAT_ERR_STATE,
+                      "A guassian comparison analysis myst be defined prior to calculating fast particle list.");
+        gap = gc_->show_time_index();
+        threshold = gc_->show_fastboundary();
+      } else {
+        argcheck(a, 5, 5);
+        gap = std::atoi(a[3].c_str());
+        threshold = (float)std::atof(a[4].c_str());
+      }
+      auto t = targets();
+      std::vector<int64_t> counts;
+      auto fast = fast_particles(&sys(), t[0], gap, threshold, &counts);
+      write_block_counts(&sys(), counts, a[2]);
+      lists_[a[1]] = std::move(fast);
     } else if (cmd == "vhd") {
       argcheck(a, 5, 5);
       pathcheck(a[1]);
@@ -330,6 +386,8 @@ class Control {
   std::vector<std::string> lines_;
   size_t pos_ = 0;
   std::unique_ptr<System> sys_;
+  std::unique_ptr<Van_Hove_Self> vhs_;
+  std::unique_ptr<Gaussian_Comparison> gc_;
   std::map<std::string, std::unique_ptr<Trajectory_List>> lists_;
   std::map<std::string, std::unique_ptr<Trajectory_List_Bins>> bins_;
 };

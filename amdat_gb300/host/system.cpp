@@ -464,6 +464,13 @@ Trajectory_List::Trajectory_List(System* sys, std::vector<int32_t> atoms) : atom
     check(amdat_list_create(sys->ctx(), atoms_.data(), (int32_t)atoms_.size(), &handle_), "list");
 }
 
+Trajectory_List::Trajectory_List(System* sys, std::shared_ptr<Trajectory_List_Bins> membership)
+    : handle_(0), membership_(std::move(membership)) {
+  // the binned pass runs over all atoms and keys each by the membership map
+  atoms_.resize(sys->n_atoms());
+  for (int a = 0; a < sys->n_atoms(); ++a) atoms_[a] = a;
+}
+
 // --- wave vectors ----------------------------------------------------------
 static const double PI_WV = 3.14159265358979323846;  // src/wave_vectors.cpp:16
 

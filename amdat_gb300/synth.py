@@ -115,25 +115,27 @@ class Trajectory:
 
 
 def random_walk(n_atoms: int, box: float, scheme: TimeScheme, sigma: float, seed: int,
-                type_fractions=(1.0,), type_names=None, time_scaled=True) -> Trajectory:
+                type_fractions=(1.0,), type_names=None, time_scaled=True, type_mobility=None) -> Trajectory:
     """Unwrapped FP64 random walk, rounded to FP32.
 
     sigma is the per-frame step for unit time; with time_scaled the step of a
     frame interval dt is sigma*sqrt(dt) (the convention of the exponential
-    schemes), otherwise sigma per frame.
+    schemes), otherwise sigma per frame.  type_mobility scales the step of each
+    atom type (a mixture of mobilities gives a non-Gaussian self van Hove).
     """
     rng = np.random.default_rng(seed)
     T = scheme.n_timesteps
     times = scheme.timelist().astype(np.float64)
+    counts = np.floor(np.asarray(type_fractions) * n_atoms).astype(int)
+    counts[-1] = n_atoms - counts[:-1].sum()
+    types = np.repeat(np.arange(len(counts), dtype=np.int32), counts)
+    scale = np.ones((n_atoms, 1)) if type_mobility is None else np.asarray(type_mobility, np.float64)[types][:, None]
     pos = np.empty((T, n_atoms, 3), dtype=np.float64)
     pos[0] = rng.random((n_atoms, 3)) * box
     for t in range(1, T):
         dt = times[t] - times[t - 1]
         step = sigma * math.sqrt(max(dt, 0.0)) if time_scaled else sigma
-        pos[t] = pos[t - 1] + step * rng.standard_normal((n_atoms, 3))
-    counts = np.floor(np.asarray(type_fractions) * n_atoms).astype(int)
-    counts[-1] = n_atoms - counts[:-1].sum()
-    types = np.repeat(np.arange(len(counts), dtype=np.int32), counts)
+        pos[t] = pos[t - 1] + step * scale * rng.standard_normal((n_atoms, 3))
     names = tuple(type_names or [str(i + 1) for i in range(len(counts))])
     return Trajectory(unwrapped=pos.astype(np.float32),
                       box=np.full(3, box, dtype=np.float32),

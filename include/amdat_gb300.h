@@ -220,13 +220,24 @@ amdat_status amdat_bins_read(amdat_ctx* ctx, int32_t handle, int32_t out_flags, 
                              int64_t* counts);
 amdat_status amdat_bins_free(amdat_ctx* ctx, int32_t handle);
 
-/* MSD and F_s of every bin in one pass: the target line "bin_list <bins>
+/* Fast_Particles (src/fast_particles.cpp; Control::find_fast and
+ * find_fast_fixedthreshold, src/control.cpp:3430-3500): over the time pairs of
+ * one gap (fullblock 0), the list members whose u2 = float(pow(|dr|, 2)) exceeds
+ * min_u2 are fast in the exponential block of the pair's start frame.  The
+ * result is an Exptime_Trajectory_List (src/exptime_trajectory_list.cpp): a
+ * one-bin map where frame t holds the fast set of block int(float(t - frt) / K).
+ * Use it as the bins of amdat_disp_bins_run (static) to analyse the list, and
+ * amdat_bins_read for the members per frame; free it with amdat_bins_free. */
+amdat_status amdat_fast_particles(amdat_ctx* ctx, int32_t list, int32_t gap, float min_u2, int32_t* handle);
+
+/* MSD and NGP moments and F_s of every bin in one pass: the target line "bin_list <bins>
  * <list> [persistence]" of Control::run_analysis (src/control.h:268-380).
  * persistent = 0: Bin_Static_Analysis (src/bin_static_analysis.h:69-111), the
  * list members in the bin at the start frame t0, pairs of the given fullblock;
  * persistent = 1: Bin_Dynamics_Analysis (src/bin_dynamics_analysis.h), members
  * in the bin at t0 and at t1, pairs of fullblock 0.  Per bin b and gap g:
  *   sum_d2[b][g]     sum of |dr|^2
+ *   sum_d4[b][g]     sum of |dr|^4
  *   count[b][g]      number of (member, time pair) terms
  *   fs_sum[b][g][s]  sum of the shell mean of cos(k.dr), k = 2 pi n / period,
  *                    for up to 8 shells (list mode: every vector of the shell)
@@ -234,7 +245,7 @@ amdat_status amdat_bins_free(amdat_ctx* ctx, int32_t handle);
 amdat_status amdat_disp_bins_run(amdat_ctx* ctx, int32_t list, int32_t bins, int32_t persistent,
                                  int32_t fullblock, int32_t n_shells, const int32_t* shell_offsets,
                                  const int32_t* kvec, float period, int32_t out_flags, double* sum_d2,
-                                 int64_t* count, double* fs_sum);
+                                 double* sum_d4, int64_t* count, double* fs_sum);
 
 /* Prepared displacement runs (many lists, one persistent launch).  A plan
  * builds its item tables on the device once; amdat_disp_plan_run is then pure

@@ -282,27 +282,31 @@ void orc_msd(const orc_scheme* s, const float* u, int32_t n_atoms, const int32_t
   msd_core(s, u, n_atoms, list, n_list, mode, NULL, msd, weighting);
 }
 
-void orc_ngp(const orc_scheme* s, const float* u, int32_t n_atoms, const int32_t* list,
-             int32_t n_list, int32_t mode, double* ngp) {
+/* Non_Gaussian_Parameter (src/non_gaussian_parameter.cpp:96-141) after its MSD
+ * pass (src/control.cpp:3345-3372), both over the same (possibly time-dependent)
+ * list: weighting += members at t0 */
+static void ngp_core(const orc_scheme* s, const float* u, int32_t n_atoms, const int32_t* list,
+                     int32_t n_list, int32_t mode, const member_t* f, double* ngp) {
   int G = orc_n_timegaps(s);
   double* msd = (double*)malloc(sizeof(double) * G);
-  orc_msd(s, u, n_atoms, list, n_list, mode, msd, 0); /* Control::ngp runs MSD first */
+  msd_core(s, u, n_atoms, list, n_list, mode, f, msd, 0); /* Control::ngp runs MSD first */
   pairs_t p = make_pairs(s, 0, 0);
   if (mode == ORC_REF32) {
     float* q = (float*)calloc(G, sizeof(float));
     long* w = (long*)calloc(G, sizeof(long));
     for (int64_t i = 0; i < p.n; ++i) {
       int g = p.gap[i];
-      w[g] += n_list;
       for (int j = 0; j < n_list; ++j) {
+        if (!is_member(f, n_atoms, list[j], p.t0[i], p.t1[i])) continue;
+        ++w[g];
         float d = dist32(u, n_atoms, list[j], p.t0[i], p.t1[i]);
         q[g] = (float)((double)q[g] + pow((double)d, 4.0)); /* float += double pow */
       }
     }
     for (int g = 0; g < G; ++g) {
       float m = (float)msd[g];
-      double f = (3.0 / (double)(float)w[g]) / (5 * pow((double)m, 2.0));
-      q[g] = (float)((double)q[g] * f);
+      double fct = (3.0 / (double)(float)w[g]) / (5 * pow((double)m, 2.0));
+      q[g] = (float)((double)q[g] * fct);
       q[g] = (float)((double)q[g] - 1.0);
       ngp[g] = q[g];
     }
@@ -312,8 +316,9 @@ void orc_ngp(const orc_scheme* s, const float* u, int32_t n_atoms, const int32_t
     double* w = (double*)calloc(G, sizeof(double));
     for (int64_t i = 0; i < p.n; ++i) {
       int g = p.gap[i];
-      w[g] += n_list;
       for (int j = 0; j < n_list; ++j) {
+        if (!is_member(f, n_atoms, list[j], p.t0[i], p.t1[i])) continue;
+        w[g] += 1.0;
         double d2 = dist2_64(u, n_atoms, list[j], p.t0[i], p.t1[i]);
         q[g] += d2 * d2;
       }
@@ -323,6 +328,11 @@ void orc_ngp(const orc_scheme* s, const float* u, int32_t n_atoms, const int32_t
   }
   free(msd);
   free_pairs(&p);
+}
+
+void orc_ngp(const orc_scheme* s, const float* u, int32_t n_atoms, const int32_t* list,
+             int32_t n_list, int32_t mode, double* ngp) {
+  ngp_core(s, u, n_atoms, list, n_list, mode, NULL, ngp);
 }
 
 void orc_disp_moments(const orc_scheme* s, int32_t fullblock, const float* u, int32_t n_atoms,
@@ -484,6 +494,42 @@ void orc_isfs_bins(const orc_scheme* s, int32_t fullblock, const float* u, int32
     isfs_core(s, persistent ? 0 : fullblock, u, n_atoms, list, n_list, kvec_n, off, n_shells, spacing,
               box_len, mode, &f, corr + (size_t)b * G * n_shells);
   }
+}
+
+void orc_ngp_bins(const orc_scheme* s, const float* u, int32_t n_atoms, const int32_t* list, int32_t n_list,
+                  const int32_t* bins, int32_t n_bins, int32_t persistent, int32_t mode, double* ngp) {
+  int G = orc_n_timegaps(s);
+  for (int b = 0; b < n_bins; ++b) {
+    member_t f = {bins, b, persistent};
+    ngp_core(s, u, n_atoms, list, n_list, mode, &f, ngp + (size_t)b * G);
+  }
+}
+
+/* Fast_Particles::analyze / listkernel (src/fast_particles.cpp): the pairs of one
+ * gap (displacement_list(this, gap, false)); a member with
+ * float(pow(|dr|, 2)) > min_u2 is fast in block int((float(t0) - float(frt)) / float(K)).
+ * fast[block][atom] = 1; then the membership map of the Exptime_Trajectory_List:
+ * bins[t][atom] = fast[int(float(t - frt) / float(K))][atom] ? 0 : -1. */
+void orc_fast_particles(const orc_scheme* s, const float* u, int32_t n_atoms, const int32_t* list,
+                        int32_t n_list, int32_t gap, float min_u2, int32_t* fast, int32_t* bins) {
+  int T = orc_n_timesteps(s);
+  int K = s->n_exponential_steps, nb = s->n_exponentials;
+  memset(fast, 0, sizeof(int32_t) * (size_t)nb * n_atoms);
+  pairs_t p = make_pairs(s, 0, 0);
+  for (int64_t i = 0; i < p.n; ++i) {
+    if (p.gap[i] != gap) continue;
+    int blk = (int)(((float)p.t0[i] - (float)s->frt) / (float)K);
+    for (int j = 0; j < n_list; ++j) {
+      float u2 = (float)pow(dist32(u, n_atoms, list[j], p.t0[i], p.t1[i]), 2.0);
+      if (u2 > min_u2 && blk >= 0 && blk < nb) fast[(size_t)blk * n_atoms + list[j]] = 1;
+    }
+  }
+  for (int t = 0; t < T; ++t) {
+    int blk = (int)((float)(t - s->frt) / (float)K);
+    for (int a = 0; a < n_atoms; ++a)
+      bins[(size_t)t * n_atoms + a] = (blk >= 0 && blk < nb && fast[(size_t)blk * n_atoms + a]) ? 0 : -1;
+  }
+  free_pairs(&p);
 }
 
 /* Space_Time_Correlation_Function PI (space_time_correlation_function.cpp:20) */

@@ -187,6 +187,28 @@ def isfs_bins(s, unwrapped, lst, kvec_n, shell_off, spacing, box_len, bins, n_bi
     return out
 
 
+def ngp_bins(s, unwrapped, lst, bins, n_bins, persistent=0, mode=F64):
+    """Per-bin NGP (its MSD pass over the same members) [bins][gaps]."""
+    u = _f32(unwrapped)
+    lst = _i32(lst)
+    b = _i32(bins)
+    out = np.zeros((n_bins, n_timegaps(s)))
+    lib().orc_ngp_bins(C.byref(s), _p(u), u.shape[1], _p(lst), len(lst), _p(b), int(n_bins), int(persistent),
+                       mode, _p(out))
+    return out
+
+
+def fast_particles(s, unwrapped, lst, gap, min_u2):
+    """Fast_Particles: (fast [blocks][atoms] 0/1, membership map [frames][atoms] 0/-1)."""
+    u = _f32(unwrapped)
+    lst = _i32(lst)
+    fast = np.zeros((s.n_exponentials, u.shape[1]), np.int32)
+    bins = np.zeros(u.shape[:2], np.int32)
+    lib().orc_fast_particles(C.byref(s), _p(u), u.shape[1], _p(lst), len(lst), int(gap), C.c_float(min_u2),
+                             _p(fast), _p(bins))
+    return fast, bins
+
+
 def vhs(s, unwrapped, lst, max_value, n_bins):
     u = _f32(unwrapped)
     lst = _i32(lst)

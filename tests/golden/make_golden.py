@@ -211,6 +211,35 @@ bin_list cells b
 isfs ./isfs_cells.dat 7 7 xyz 0 1
 bin_list cells all
 """),
+    # a two-mobility mixture: self van Hove vs its Gaussian (compare_gaussian), the
+    # fast particles per block (find_fast, find_fast_fixedthreshold) and analyses
+    # of those time-dependent lists
+    "fast": dict(
+        n=400, box=7.0, sigma=0.12, seed=111, fractions=(0.75, 0.25), mobility=(1.0, 4.0),
+        scheme=synth.TimeScheme.exponential(4, 8, 1.3, 0, 0, 0.01),
+        commands="""create_list all
+all
+create_list b
+type_system 2
+vhs ./vhs.dat 0.6 60
+list all
+compare_gaussian ./gc.dat
+list all
+find_fast fast ./fast_count.dat
+list all
+msd ./msd_fast.dat
+list fast
+ngp ./ngp_fast.dat
+list fast
+isfs ./isfs_fast.dat 8 9 xyz 0
+list fast
+find_fast_fixedthreshold quick ./fast_fixed.dat 6 0.05
+list b
+msd ./msd_quick.dat
+list quick
+compare_gaussian ./gc_t5.dat 5
+list b
+"""),
     "siblings_lin": dict(
         n=120, box=6.0, sigma=0.1, seed=55, fractions=(1.0,), time_scaled=False,
         scheme=synth.TimeScheme.linear(16, 1.0),
@@ -235,7 +264,8 @@ def make(case: str) -> None:
         raise SystemExit("reference source tree not found; set AMDAT_REFERENCE")
     traj = synth.random_walk(cfg["n"], cfg["box"], cfg["scheme"], cfg["sigma"], cfg["seed"],
                              type_fractions=cfg["fractions"],
-                             time_scaled=cfg.get("time_scaled", True))
+                             time_scaled=cfg.get("time_scaled", True),
+                             type_mobility=cfg.get("mobility"))
     fmt = cfg.get("fmt", "custom")
     if fmt == "xyz":
         traj = synth.as_xyz_input(traj)

@@ -37,6 +37,8 @@ class OracleRun:
         self.flags = {}
         self.stored = {}
         self.bins = {}
+        self.last_vhs = None
+        self.gc = None
 
     def scheme(self):
         return orc.scheme(self.traj.scheme, self.limit)
@@ -80,8 +82,118 @@ class OracleRun:
                 self.run_bins(cmd, a, target)
                 continue
             lst = self.lists[target[1]]
+            if isinstance(lst, dict):  # time-dependent list (find_fast)
+                self.run_timelist(cmd, a, lst)
+                continue
             getattr(self, "cmd_" + cmd)(a, lst)
         return self.files
+
+    # --- compare_gaussian / find_fast (src/control.cpp:3378-3500) ---
+    def cmd_compare_gaussian(self, a, lst):
+        """Gaussian_Comparison (gaussian_comparison.cpp), float storage and double pow/exp."""
+        import math
+        s = self.scheme()
+        msd = orc.msd(s, self.unwrapped, lst, self.mode)
+        ngp = orc.ngp(s, self.unwrapped, lst, self.mode)
+        if len(a) == 3:
+            ti = int(a[2])
+        else:
+            ti, best = -1, f32(0)
+            for g in range(1, len(ngp)):
+                if f32(ngp[g]) > best:
+                    best, ti = f32(ngp[g]), g
+        v = self.last_vhs
+        nb, bs = v["nb"], v["bs"]
+        PI = 3.14159265
+        alpha = f32(3.0 / (2.0 * float(f32(msd[ti]))))
+        gauss, vh = [], []
+        for b in range(nb):
+            shell = f32(4.0 / 3.0 * PI * (math.pow((float(f32(b)) + 1.0) * float(bs), 3.0)
+                                          - math.pow(float(f32(f32(b) * bs)), 3.0)))
+            vh.append(f32(f32(v["corr"][ti][b]) * shell))
+            r = (float(f32(b)) + .5) * float(bs)
+            gauss.append(f32(math.pow(float(alpha) / PI, 1.5) * math.exp(-float(alpha) * math.pow(r, 2.0))
+                             * float(shell)))
+        si = fi = 0
+        for b in range(1, nb):
+            if gauss[b] >= vh[b]:
+                si = b - 1
+                break
+        for b in range(si + 1, nb):
+            if gauss[b] <= vh[b]:
+                fi = b
+                break
+        slowb = f32(math.pow((float(f32(si)) + .5) * float(bs), 2.0))
+        fastb = f32(math.pow((float(f32(fi)) - .5) * float(bs), 2.0))
+        slow = gslow = f32(0)
+        for b in range(1, si + 1):
+            slow = f32(slow + vh[b])
+            gslow = f32(gslow + gauss[b])
+        fast, gfast = f32(1.0 - float(slow)), f32(1.0 - float(gslow))
+        for b in range(si + 1, fi):
+            fast = f32(fast - vh[b])
+            gfast = f32(gfast - gauss[b])
+        self.gc = dict(ti=ti, fastb=fastb)
+        t = self.times(s)
+        txt = ""
+        if fi == 0:
+            txt += ("Warning: program cannot identify two crossing points between self Van Hove and Gaussian "
+                    "approximation self Van Hove.  Fractions of slow and fast particles will be incorrect.\n")
+        txt += f"Gaussian comparison data created by AMDAT v.{VERSION}\n"
+        txt += f"t*\n{fmt(t[ti])}\n"
+        txt += f"Slow_Cutoff: {fmt(math.pow(float(slowb), 0.5))}\nFast_Cutoff: {fmt(math.pow(float(fastb), 0.5))}\n"
+        txt += "\tSlow_Fraction\tFast_Fraction\n"
+        txt += f"Gaussian\t{fmt(gslow)}\t{fmt(gfast)}\nActual\t{fmt(slow)}\t{fmt(fast)}\n"
+        txt += f"Excess\t{fmt(f32(slow - gslow))}\t{fmt(f32(fast - gfast))}\n\n"
+        txt += "Self_Van_Hove*shellvolume\nradius\tgaussian\tactual\n"
+        for b in range(nb):
+            txt += f"{fmt((b + .5) * float(bs))}\t{fmt(gauss[b])}\t{fmt(vh[b])}\n"
+        self.files[self.name(a[1])] = txt
+
+    def _fast(self, a, lst, gap, threshold):
+        s = self.scheme()
+        fast, bins = orc.fast_particles(s, self.unwrapped, lst, gap, float(threshold))
+        counts = fast.sum(axis=1)
+        nb = len(counts)
+        avg = 0.0
+        for c in counts:
+            avg += float(c) / float(nb)
+        times = self.traj.scheme.timelist()
+        K, frt = self.traj.scheme.n_exponential_steps, self.traj.scheme.frt
+        txt = f"Average_trajectories:\t{fmt(avg)}\nCount_List\n"
+        txt += "".join(f"{fmt(times[b * K + frt])}\t{int(c)}\n" for b, c in enumerate(counts))
+        self.files[self.name(a[2])] = txt
+        self.lists[a[1]] = dict(bins=bins)
+
+    def cmd_find_fast(self, a, lst):
+        self._fast(a, lst, self.gc["ti"], self.gc["fastb"])
+
+    def cmd_find_fast_fixedthreshold(self, a, lst):
+        self._fast(a, lst, int(a[3]), f32(float(a[4])))
+
+    def run_timelist(self, cmd, a, td):
+        """msd / ngp / isfs over a time-dependent list: members at each start frame."""
+        s = self.scheme()
+        allat = np.arange(self.traj.n_atoms, dtype=np.int32)
+        if cmd == "msd":
+            m, _ = orc.msd_bins(s, self.unwrapped, allat, td["bins"], 1, 0, self.mode)
+            self.files[self.name(a[1])] = self.msd_text(m[0], s)
+        elif cmd == "ngp":
+            q = orc.ngp_bins(s, self.unwrapped, allat, td["bins"], 1, 0, self.mode)[0]
+            t = self.times(s)
+            txt = f"Non-Gaussian parameter data created by AMDAT v.{VERSION}\n"
+            self.files[self.name(a[1])] = txt + "".join(f"{fmt(t[g])}\t{fmt(f32(q[g]))}\n" for g in range(len(t)))
+        elif cmd == "isfs":
+            m0, m1 = int(a[2]), int(a[3])
+            maxlen = float(a[5])
+            fb = int(a[6]) if len(a) > 6 else 0
+            L = maxlen if maxlen > 0 else self.min_box()
+            sp = wv.spacing(L)
+            kv, off = self.shells(m0, m1)
+            corr = orc.isfs_bins(s, self.unwrapped, allat, kv, off, float(sp), L, td["bins"], 1, fb, 0, self.mode)
+            self.files[self.name(a[1])] = self.correlation_2d(sp, m0, m1, corr[0], s)
+        else:
+            raise ValueError(cmd)
 
     # --- spatial bins (Control::create_bin_list, src/control.cpp:3841-4000) ---
     def box_bounds(self):
@@ -218,6 +330,7 @@ class OracleRun:
         s = self.scheme()
         counts, w, corr = orc.vhs(s, self.unwrapped, lst, float(vmax), nb)
         bs = f32(vmax / f32(nb))
+        self.last_vhs = dict(corr=np.asarray(corr, np.float32), nb=nb, bs=bs)
         t = self.times(s)
         txt = f"Correlation data created by AMDAT v.{VERSION}\n{nb} bins\n{len(t)} times\n\n\t"
         txt += "".join(fmt(f32(f32(bs / f32(2)) + f32(f32(b) * bs))) + "\t" for b in range(nb)) + "\n"

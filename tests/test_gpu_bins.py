@@ -152,3 +152,41 @@ def test_bins_errors(eng, engine_mod):
     with pytest.raises(engine_mod.AmdatError):
         eng.disp_bins(0, h, 1)
     eng.bins_free(h)
+
+
+def _referenced(u):
+    """The engine's stored coordinates: re-referenced to frame 0 in one FP32 rounding."""
+    u = np.asarray(u, np.float32)
+    return (u - u[0:1]).astype(np.float32)
+
+
+@pytest.mark.parametrize("gap,thr", [(3, 0.004), (6, 0.05), (0, 0.0)])
+def test_fast_particles_match_oracle(eng, gap, thr):
+    """Fast_Particles membership per block, bit-exact against the oracle run on the
+    same frame-0-referenced coordinates; NGP and MSD of the time-dependent list."""
+    traj, _, _ = load("fast")
+    eng.upload(traj.unwrapped, traj.box, traj.box_lo)
+    eng.set_scheme(traj.scheme)
+    sub = np.nonzero(traj.types == 1)[0].astype(np.int32)
+    s = orc.scheme(traj.scheme)
+    u = _referenced(traj.unwrapped)
+    for lst, h_list in ((np.arange(traj.n_atoms, dtype=np.int32), 0), (sub, eng.list(sub))):
+        h = eng.fast_particles(h_list, gap, thr)
+        got, counts = eng.bins_read(h, traj.n_frames, traj.n_atoms, 1)
+        fast, ref = orc.fast_particles(s, u, lst, gap, thr)
+        np.testing.assert_array_equal(got, ref)
+        K = traj.scheme.n_exponential_steps
+        np.testing.assert_array_equal(counts[::K][:fast.shape[0], 0], fast.sum(1))
+        out = eng.disp_bins(0, h, 1)
+        allat = np.arange(traj.n_atoms, dtype=np.int32)
+        msd, w = orc.msd_bins(s, u, allat, ref, 1, 0, orc.F64)
+        ngp = orc.ngp_bins(s, u, allat, ref, 1, 0, orc.F64)
+        np.testing.assert_array_equal(out["count"][0], w[0].astype(np.int64))
+        m = out["count"][0] > 0
+        gm = out["sum_d2"][0][m] / out["count"][0][m]
+        np.testing.assert_allclose(gm, msd[0][m], rtol=1e-6, atol=1e-12)
+        wq = out["count"][0][m].astype(float)
+        gq = out["sum_d4"][0][m] * 3.0 / wq / (5.0 * gm * gm) - 1.0
+        ok = np.abs(msd[0][m]) > 0
+        np.testing.assert_allclose(gq[ok], ngp[0][m][ok], rtol=1e-6, atol=1e-9)
+        eng.bins_free(h)
