@@ -17,7 +17,7 @@
 // box in units of 2^-31 turns).
 //
 // Per frame batch, zgen_kernel precomputes the B operands (Z hi/lo in the
-// K-major core-matrix layout, one blob per (frame, nz window, chunk)).  The
+// K-major 128-byte-swizzled layout, one blob per (frame, nz window, chunk)).  The
 // main kernel is warp-specialised, one CTA per SM, 512 TMEM columns:
 //   warps 0-3   drain: TMEM accumulator -> Kahan (s, c) columns, then the epilogue
 //   warp 4      producer: bulk copies (cp.async.bulk) of Z into a 3-stage ring
@@ -77,6 +77,10 @@ struct TcSmem {
   int z_issued, z_landed;  // bulk copies issued / seen complete
 };
 static_assert(sizeof(float) * TC_M * (TC_NMAX + 1) <= sizeof(((TcSmem*)0)->z), "D staging must fit the Z ring");
+// operands use the 128-byte-swizzled K-major layout: 128-byte rows, 1024-byte aligned tiles
+static_assert(TC_K * 2 == 128, "one chunk's K must fill a 128-byte swizzle row");
+static_assert(TC_STAGE % 1024 == 0 && TC_ZHALF % 1024 == 0 && TC_A_BYTES % 1024 == 0,
+              "every operand tile must start on a 1024-byte boundary");
 
 __device__ __forceinline__ void tc_split(float x, __half& hi, __half& lo) {
   hi = __float2half_rn(x);
@@ -111,7 +115,7 @@ __global__ void __launch_bounds__(256)
     __half rh, rl, ih, il;
     tc_split(co, rh, rl);
     tc_split(s, ih, il);
-    const uint32_t off = umma::kmajor_offset(col, 2 * j, TC_K);
+    const uint32_t off = umma::kmajor_sw128_offset(col, 2 * j);
     *reinterpret_cast<__half2*>(hi + off) = __halves2half2(rh, ih);
     *reinterpret_cast<__half2*>(lo + off) = __halves2half2(rl, il);
   }
@@ -224,12 +228,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     // ---- MMA issuer
     if (lane == 0) {
       const uint32_t idesc = umma::idesc_f16_f32(TC_M, n);
-      constexpr uint32_t LBO = 128, SBO = (TC_K / 8) * 128;
       // descriptors are built once: a descriptor's address field is the byte
       // address >> 4 (14 bits, all of shared memory), so moving to another
-      // stage, the lo half or the next k-step adds a constant
-      const uint64_t a_desc0 = umma::smem_desc(umma::smem_addr(S.a[0][0]), LBO, SBO);
-      const uint64_t b_desc0 = umma::smem_desc(umma::smem_addr(S.z[0]), LBO, SBO);
+      // stage, the lo half (both 1024-byte aligned) or the next k-step (32 B
+      // inside the swizzled 128-byte rows) adds a constant
+      const uint64_t a_desc0 = umma::smem_desc_sw128(umma::smem_addr(S.a[0][0]));
+      const uint64_t b_desc0 = umma::smem_desc_sw128(umma::smem_addr(S.z[0]));
       constexpr uint32_t A_STAGE16 = (2 * TC_A_BYTES) >> 4, A_LO16 = TC_A_BYTES >> 4;
       constexpr uint32_t B_STAGE16 = TC_STAGE >> 4, B_LO16 = TC_ZHALF >> 4;
       bool ok = true;
@@ -255,7 +259,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         for (int pass = 0; pass < 3; ++pass)
 #pragma unroll
           for (int ks = 0; ks < TC_K / 16; ++ks)
-            umma::mma_f16(d, pa[pass] + (uint64_t)(ks * 16), pb[pass] + (uint64_t)(ks * 16), idesc,
+            umma::mma_f16(d, pa[pass] + (uint64_t)(ks * 2), pb[pass] + (uint64_t)(ks * 2), idesc,
                           (c % TC_GROUP == 0 && pass == 0 && ks == 0) ? 0u : 1u);
         umma::mma_commit(&S.empty[sz]);
         if (c % TC_GROUP == TC_GROUP - 1 || c == n_chunks - 1) umma::mma_commit(&S.full_acc[buf]);
@@ -374,8 +378,8 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           him[a] = __byte_perm(hre[a], 0, 0x1032) ^ 0x00008000u;
           lim[a] = __byte_perm(lre[a], 0, 0x1032) ^ 0x00008000u;
         }
-        const uint32_t o_re = (uint32_t)(((r >> 3) * 8 + q) * 128 + (r & 7) * 16);  // K = 8q..8q+7
-        const uint32_t o_im = o_re + (uint32_t)(TC_ROWS / 8) * (TC_K / 8) * 128;   // row r + 64
+        const uint32_t o_re = (uint32_t)(r * 128 + ((q ^ (r & 7)) << 4));  // K = 8q..8q+7, 128-byte swizzle
+        const uint32_t o_im = o_re + (uint32_t)TC_ROWS * 128;                  // row r + 64, same swizzle
         *reinterpret_cast<uint4*>(S.a[sa][0] + o_re) = make_uint4(hre[0], hre[1], hre[2], hre[3]);
         *reinterpret_cast<uint4*>(S.a[sa][1] + o_re) = make_uint4(lre[0], lre[1], lre[2], lre[3]);
         *reinterpret_cast<uint4*>(S.a[sa][0] + o_im) = make_uint4(him[0], him[1], him[2], him[3]);

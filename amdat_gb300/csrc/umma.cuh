@@ -25,6 +25,15 @@ __host__ __device__ __forceinline__ uint32_t kmajor_offset(int row, int k, int K
   return (uint32_t)(((row >> 3) * (K >> 3) + (k >> 3)) * 128 + (row & 7) * 16 + (k & 7) * 2);
 }
 
+// byte offset of element (row, k) in a K-major tile of 64 16-bit elements (128 B)
+// per row in the 128-byte swizzled layout: rows are 128 B apart and the 16-byte
+// chunk k/8 of row r sits at chunk position (k/8) ^ (r % 8), so the 8 rows of a
+// 1024-byte atom spread every chunk column over all banks.  Tile bases are
+// 1024-byte aligned.
+__host__ __device__ __forceinline__ uint32_t kmajor_sw128_offset(int row, int k) {
+  return (uint32_t)(row * 128 + ((((k >> 3) ^ row) & 7) << 4) + (k & 7) * 2);
+}
+
 // shared-memory matrix descriptor (tcgen05): start address, leading and stride
 // byte offsets (all >> 4), descriptor version 1 (bits 46-47), no swizzle
 __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo_bytes, uint32_t sbo_bytes) {
@@ -35,6 +44,15 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo_bytes
   d |= (uint64_t)1 << 46;  // version
   // base offset 0 (bits 49-51), absolute LBO mode 0 (bit 52), layout 0 = no swizzle (bits 61-63)
   return d;
+}
+
+// descriptor of a K-major 128-byte-swizzled tile (kmajor_sw128_offset): stride
+// 1024 B between 8-row atoms, leading offset unused, layout type 2 (128-byte
+// swizzle) in bits 61-63.  A K step of 16 elements inside the 128-byte row adds
+// 32 B to the start address (2 in the >> 4 field); the hardware applies the
+// swizzle to the full address, so the atom base must stay 1024-byte aligned.
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr) {
+  return smem_desc(saddr, 16, 1024) | ((uint64_t)2 << 61);
 }
 
 // instruction descriptor for kind::f16: A = B = F16, D = F32, both K-major, dense
