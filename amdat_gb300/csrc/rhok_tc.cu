@@ -20,10 +20,12 @@
 // K-major 128-byte-swizzled layout, one blob per (frame, nz window, chunk)).  The
 // main kernel is warp-specialised, one CTA per SM, 512 TMEM columns:
 //   warps 0-3   drain: TMEM accumulator -> Kahan (s, c) columns, then the epilogue
-//   warp 4      producer: bulk copies (cp.async.bulk) of Z into a 3-stage ring
-//   warp 5      MMA issuer: 12 tcgen05.mma per chunk into one of two accumulators
-//   warps 6-13  builders: X/Y phase tables (sincospif) and the A operand (W
-//               products, FP16 split, K-major stores) into a 2-stage ring
+//   warp 4      producer: bulk copies (cp.async.bulk) of Z hi/lo and the X/Y
+//               phase tables of each chunk into a 3-stage ring
+//   warps 5-6   MMA issuers, one per accumulator (alternate 64-atom groups):
+//               12 tcgen05.mma per chunk
+//   warps 7-22  builders: the A operand of the chunk (W = X Y products, FP16
+//               split, swizzled K-major stores) into the same ring stage
 // Hand-offs are mbarriers (bulk-copy transactions, tcgen05.commit, thread
 // arrivals); every wait is bounded, and a timeout makes every role stop, wait
 // for its own copies and MMAs, free tensor memory and report through an error
@@ -49,11 +51,12 @@ constexpr int TC_M = 2 * TC_ROWS;             // MMA M = 128
 constexpr int TC_GROUP = 2;                   // chunks per tensor-memory accumulation
 constexpr int TC_S = 3;                       // ring stages (Z, X, Y and the A operand of one chunk)
 constexpr int TC_PRODUCER_WARP = 4;
-constexpr int TC_MMA_WARP = 5;
-constexpr int TC_BUILD_WARP0 = 6;
+constexpr int TC_MMA_WARP = 5;                // warps 5 and 6: one per accumulator
+constexpr int TC_MMA_WARPS = 2;
+constexpr int TC_BUILD_WARP0 = TC_MMA_WARP + TC_MMA_WARPS;
 constexpr int TC_BUILDERS = 512;              // 16 builder warps
 constexpr int TC_DRAINERS = 128;              // warps 0-3, one per TMEM lane quadrant
-constexpr int TC_THREADS = 32 * TC_BUILD_WARP0 + TC_BUILDERS;  // 704
+constexpr int TC_THREADS = 32 * TC_BUILD_WARP0 + TC_BUILDERS;  // 736
 constexpr uint32_t TC_A_BYTES = TC_M * TC_K * 2;      // 16 KB (one of hi / lo)
 constexpr uint32_t TC_ZHALF = TC_NMAX * TC_K * 2;     // 16 KB (one of hi / lo, widest window)
 constexpr uint32_t TC_XYB = TC_J * 8 * sizeof(float2);  // 2 KB: 8 phases of 32 atoms (X or Y)
@@ -189,7 +192,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       umma::mbar_init(&S.full_acc[b], 1);
       umma::mbar_init(&S.empty_acc[b], TC_DRAINERS);
     }
-    umma::mbar_init(&S.mma_done, 1);
+    umma::mbar_init(&S.mma_done, TC_MMA_WARPS);
     umma::fence_mbarrier_init();
     S.bad = 0;
     S.build_stop[0] = S.build_stop[1] = 0;
@@ -224,8 +227,11 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       }
       S.z_issued = c;
     }
-  } else if (warp == TC_MMA_WARP) {
-    // ---- MMA issuer
+  } else if (warp >= TC_MMA_WARP && warp < TC_MMA_WARP + TC_MMA_WARPS) {
+    // ---- MMA issuers: warp TC_MMA_WARP + b issues the groups of accumulator b
+    // (even / odd groups), so two threads keep the tensor pipe fed; the two
+    // accumulators are independent, and each chunk's stage is read by one issuer
+    const int mine = warp - TC_MMA_WARP;
     if (lane == 0) {
       const uint32_t idesc = umma::idesc_f16_f32(TC_M, n);
       // descriptors are built once: a descriptor's address field is the byte
@@ -239,11 +245,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       bool ok = true;
       for (int c = 0; c < n_chunks; ++c) {
         const int sz = c % TC_S, sa = sz, g = c / TC_GROUP, buf = g & 1;
+        if (buf != mine) continue;
         if (S.bad || !umma::mbar_wait(&S.full_z[sz], (c / TC_S) & 1, TC_WAIT)) {
           ok = false;
           break;
         }
-        S.z_landed = c + 1;
+        atomicMax(&S.z_landed, c + 1);
         if (!umma::mbar_wait(&S.full_a[sa], (c / TC_S) & 1, TC_WAIT) ||
             (c % TC_GROUP == 0 && !umma::mbar_wait(&S.empty_acc[buf], ((g >> 1) & 1) ^ 1, TC_WAIT))) {
           ok = false;
