@@ -17,9 +17,9 @@
 // keys each term by the member's bin: every atom's trajectory is read once per
 // pair for all bins together.  Terms of one warp that share a bin are summed
 // by the warp's lowest such lane (FP64, lane order) and added with one atomic to
-// a per-block shared-memory accumulator [bin][2 + shells] (|dr|^2, |dr|^4, the
-// shell means), flushed to the global [bin][gap][2 + shells] sums at the end of
-// each item.  Counts are
+// a per-block shared-memory accumulator [bin][stride] (|dr|^2, |dr|^4 when
+// asked for, the shell means), flushed to the global [bin][gap][stride] sums at
+// the end of each item.  Counts are
 // exact integers; the FP64 sums are order-independent to rounding (atomics).
 #include <algorithm>
 #include <cfloat>
@@ -116,7 +116,8 @@ struct BnParams {
   const float* inv_count;
   float period;
   int32_t n_gaps;
-  int32_t stride;  // 2 + n_fs: |dr|^2, |dr|^4, shells
+  int32_t want_d4;  // |dr|^4 column present
+  int32_t stride;   // 1 + want_d4 + n_fs: |dr|^2, [|dr|^4], shells
   double* acc;     // [bin][gap][stride]
   unsigned long long* cnt;  // [bin][gap]
   int32_t staged;  // per-block shared accumulators
@@ -192,9 +193,10 @@ __global__ void __launch_bounds__(BN_THREADS) disp_bins_kernel(BnParams p) {
         }
       }
       // lanes of one bin: the lowest adds their terms (lane order, FP64)
+      // staged columns: |dr|^2, then |dr|^4 only when asked for, then the shells
 #pragma unroll
       for (int k = 0; k < 2 + BN_MAX_FS; ++k)
-        if (k < stride) s_val[warp][lane][k] = v[k];
+        if (k < stride) s_val[warp][lane][k] = (k == 0 || p.want_d4) ? v[k] : v[k + 1 < 2 + BN_MAX_FS ? k + 1 : k];
       __syncwarp();
       const unsigned peers = __match_any_sync(0xffffffffu, b);
       if (b >= 0 && lane == __ffs(peers) - 1) {
@@ -436,7 +438,8 @@ amdat_status amdat_disp_bins_run(amdat_ctx* ctx, int32_t list, int32_t bins, int
     const PairTable& P = pair_table(ctx, persistent ? false : fullblock != 0, false);
     const int G = P.n_gaps;
     const int32_t B = m.nx * m.ny * m.nz;
-    const int stride = 2 + n_shells;
+    const int want_d4 = sum_d4 ? 1 : 0;
+    const int stride = 1 + want_d4 + n_shells;
     // shells (list mode: one cosine per vector)
     std::vector<int4> kv;
     std::vector<int32_t> off(1, 0);
@@ -496,6 +499,7 @@ amdat_status amdat_disp_bins_run(amdat_ctx* ctx, int32_t list, int32_t bins, int
       p.inv_count = (const float*)(base + o_inv);
       p.period = n_shells ? period : 1.0f;
       p.n_gaps = G;
+      p.want_d4 = want_d4;
       p.stride = stride;
       p.acc = (double*)(base + o_acc);
       p.cnt = (unsigned long long*)(base + o_cnt);
@@ -519,7 +523,7 @@ amdat_status amdat_disp_bins_run(amdat_ctx* ctx, int32_t list, int32_t bins, int
     if (sum_d4)
       AMDAT_CUDA(cudaMemcpy2DAsync(sum_d4, 8, base + o_acc + 8, (size_t)stride * 8, 8, (size_t)B * G, kind, st));
     if (fs_sum && n_shells)
-      AMDAT_CUDA(cudaMemcpy2DAsync(fs_sum, (size_t)n_shells * 8, base + o_acc + 16, (size_t)stride * 8,
+      AMDAT_CUDA(cudaMemcpy2DAsync(fs_sum, (size_t)n_shells * 8, base + o_acc + 8 * (1 + want_d4), (size_t)stride * 8,
                                    (size_t)n_shells * 8, (size_t)B * G, kind, st));
     if (count) AMDAT_CUDA(cudaMemcpyAsync(count, base + o_cnt, (size_t)B * G * 8, kind, st));
     AMDAT_CUDA(cudaStreamSynchronize(st));

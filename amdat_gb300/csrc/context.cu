@@ -54,6 +54,17 @@ const PairTable& pair_table(amdat_ctx* ctx, bool fullblock, bool loop_order) {
   t->n_pairs = (int64_t)p.gap.size();
   t->n_gaps = scheme_n_timegaps(ctx->scheme);
   t->gap_first = p.gap_first;
+  t->lagged = true;
+  t->lag.assign(t->n_gaps, 0);
+  for (int g = 0; g < t->n_gaps && t->lagged; ++g)
+    for (int i = p.gap_first[g]; i < p.gap_first[g + 1]; ++i) {
+      const int k = i - p.gap_first[g];
+      if (k == 0) t->lag[g] = p.t1[i] - p.t0[i];
+      if (p.t0[i] != k || p.t1[i] - p.t0[i] != t->lag[g]) {
+        t->lagged = false;
+        break;
+      }
+    }
   const size_t n = p.gap.size();
   t->t0.reserve(n);
   t->t1.reserve(n);

@@ -104,6 +104,10 @@ struct PairTable {
   int32_t n_gaps = 0;
   std::vector<int32_t> gap_first;
   DevBuf<int32_t> t0, t1, gap;
+  // lagged tables (linear schemes): every gap's pairs, in order, are
+  // (t, t + lag[g]) for t = 0 .. count - 1
+  bool lagged = false;
+  std::vector<int32_t> lag;
 };
 
 struct LatticePlanDev;

@@ -15,8 +15,10 @@
 // products, and the warp folds its 32 vectors with shuffles into one FP64
 // partial per (tile, gap).  A finalize kernel adds the partials of each
 // (shell, gap) in tile order in FP64 and divides by the shell size, so the
-// result is deterministic.
+// result is deterministic.  Linear schemes (lagged pair tables) take
+// isf_lag_kernel, which reuses each frame's density across 8 gaps.
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -73,6 +75,87 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
     for (int off = KT / 2; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off, KT);
     if (kk == 0 && g < n_gaps) part[(int64_t)blockIdx.x * n_gaps + g] = v;
+  }
+}
+
+// Lagged pair tables (the linear schemes: gap g's pairs are (t, t + lag_g) for
+// t = 0 .. cnt_g - 1): a warp owns blocks of 8 gaps with consecutive lags and a
+// lane (one k) runs once over t.  rho1(t) is read once per step, and
+// rho2(t + lag) of the 8 gaps sits in a register window that slides by one
+// frame per step (one new load), so two shared-memory loads feed 8 products.
+// Each gap keeps its Kahan sum in t order, the pair order of the table, so the
+// partials equal the pair-table kernel's.
+__global__ void __launch_bounds__(256)
+    isf_lag_kernel(const float2* __restrict__ rho1, const float2* __restrict__ rho2, int32_t n_frames,
+                   int32_t n_k, const KTile* __restrict__ tiles, const int32_t* __restrict__ lag,
+                   const int32_t* __restrict__ gap_first, int32_t n_gaps, double* __restrict__ part) {
+  constexpr int KT = 32;
+  extern __shared__ float2 sh[];
+  const bool same = rho1 == rho2;
+  float2* s1 = sh;
+  float2* s2 = same ? sh : sh + (size_t)n_frames * KT;
+  const KTile T = tiles[blockIdx.x];
+  for (int i = threadIdx.x; i < n_frames * KT; i += blockDim.x) {
+    const int f = i / KT, k = i % KT;
+    const float2 z = make_float2(0.f, 0.f);
+    s1[i] = k < T.nk ? rho1[(int64_t)f * n_k + T.k0 + k] : z;
+    if (!same) s2[i] = k < T.nk ? rho2[(int64_t)f * n_k + T.k0 + k] : z;
+  }
+  __syncthreads();
+  const int kk = threadIdx.x & 31, warp = threadIdx.x >> 5, n_warps = blockDim.x >> 5;
+  const float2 zero = make_float2(0.f, 0.f);
+  for (int g0 = 8 * warp; g0 < n_gaps; g0 += 8 * n_warps) {
+    int cnt[8], tmax = 0;
+    bool window = true;  // lags g0 .. g0+7 consecutive (gaps without pairs do not matter)
+    const int lag0 = lag[g0];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      cnt[j] = g0 + j < n_gaps ? gap_first[g0 + j + 1] - gap_first[g0 + j] : 0;
+      if (cnt[j] > 0 && lag[g0 + j] != lag0 + j) window = false;
+      tmax = max(tmax, cnt[j]);
+    }
+    KSumF acc[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) acc[j] = KSumF{0.f, 0.f};
+    if (window) {
+      // r[(u + j) & 7] holds rho2(t + lag0 + j) at step u of each 8-step round
+      float2 r[8];
+#pragma unroll
+      for (int j = 0; j < 8; ++j) r[j] = lag0 + j < n_frames ? s2[(lag0 + j) * KT + kk] : zero;
+      for (int t0 = 0; t0 < tmax; t0 += 8) {
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int t = t0 + u;
+          if (t < tmax) {
+            const float2 a = s1[t * KT + kk];
+#pragma unroll
+            for (int j = 0; j < 8; ++j) {
+              const float2 b = r[(u + j) & 7];
+              if (t < cnt[j]) ksadd(acc[j], fmaf(a.x, b.x, a.y * b.y));
+            }
+            const int tn = t + 1 + lag0 + 7;
+            r[u & 7] = tn < n_frames ? s2[tn * KT + kk] : zero;
+          }
+        }
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 8; ++j) {
+        if (cnt[j] == 0) continue;
+        const int L = lag[g0 + j];
+        for (int t = 0; t < cnt[j]; ++t) {
+          const float2 a = s1[t * KT + kk], b = s2[(t + L) * KT + kk];
+          ksadd(acc[j], fmaf(a.x, b.x, a.y * b.y));
+        }
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      double v = (double)acc[j].s - (double)acc[j].c;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+      if (kk == 0 && g0 + j < n_gaps) part[(int64_t)blockIdx.x * n_gaps + g0 + j] = v;
+    }
   }
 }
 
@@ -175,6 +258,7 @@ amdat_status amdat_isf_run(amdat_ctx* ctx, int32_t h1, int32_t h2, int32_t fullb
     size_t o = 0;
     const size_t o_t = o; o = align(o + std::max<size_t>(tiles.size(), 1) * sizeof(KTile));
     const size_t o_gf = o; o = align(o + (G + 1) * 4);
+    const size_t o_lag = o; o = align(o + std::max(G, 1) * 4);
     const size_t o_stf = o; o = align(o + stf.size() * 4);
     const size_t o_inv = o; o = align(o + invc.size() * 4);
     const size_t o_part = o; o = align(o + std::max<size_t>(tiles.size(), 1) * G * 8);
@@ -183,6 +267,7 @@ amdat_status amdat_isf_run(amdat_ctx* ctx, int32_t h1, int32_t h2, int32_t fullb
     std::vector<unsigned char> host(o_part, 0);
     std::memcpy(host.data() + o_t, tiles.data(), tiles.size() * sizeof(KTile));
     std::memcpy(host.data() + o_gf, P.gap_first.data(), (G + 1) * 4);
+    if (P.lagged) std::memcpy(host.data() + o_lag, P.lag.data(), G * 4);
     std::memcpy(host.data() + o_stf, stf.data(), stf.size() * 4);
     std::memcpy(host.data() + o_inv, invc.data(), invc.size() * 4);
     AMDAT_CUDA(cudaMemcpyAsync(base, host.data(), o_part, cudaMemcpyHostToDevice, ctx->stream));
@@ -197,7 +282,15 @@ amdat_status amdat_isf_run(amdat_ctx* ctx, int32_t h1, int32_t h2, int32_t fullb
             d1.rho->ptr, d2.rho->ptr, T, d1.n_k, (const KTile*)(base + o_t), P.t0.ptr, P.t1.ptr,
             (const int32_t*)(base + o_gf), G, part);
       };
-      switch (KT) {
+      const char* force = std::getenv("AMDAT_ISF_KERNEL");  // "pairs": the pair-table kernel always
+      if (P.lagged && KT == 32 && !(force && std::strcmp(force, "pairs") == 0)) {
+        // linear schemes: one pass over t per block of 8 gaps
+        AMDAT_CUDA(cudaFuncSetAttribute(isf_lag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+        KernelTimer kt(ctx, "isf_lag_kernel");
+        isf_lag_kernel<<<(unsigned)tiles.size(), 256, shm, ctx->stream>>>(
+            d1.rho->ptr, d2.rho->ptr, T, d1.n_k, (const KTile*)(base + o_t), (const int32_t*)(base + o_lag),
+            (const int32_t*)(base + o_gf), G, part);
+      } else switch (KT) {
         case 32: launch(isf_pairs_kernel<32>); break;
         case 16: launch(isf_pairs_kernel<16>); break;
         case 8: launch(isf_pairs_kernel<8>); break;
@@ -205,7 +298,7 @@ amdat_status amdat_isf_run(amdat_ctx* ctx, int32_t h1, int32_t h2, int32_t fullb
         case 2: launch(isf_pairs_kernel<2>); break;
         default: launch(isf_pairs_kernel<1>); break;
       }
-      check_launch("isf_pairs_kernel");
+      check_launch("isf correlator kernel");
       count_launch(ctx);
     } else {
       AMDAT_CUDA(cudaMemsetAsync(part, 0, G * 8, ctx->stream));

@@ -345,11 +345,11 @@ class Engine:
     def bins_free(self, handle):
         _check(lib().amdat_bins_free(self._ctx, int(handle)))
 
-    def disp_bins(self, list_h, bins_h, n_bins, persistent=0, fullblock=0, shells=None, period=1.0):
+    def disp_bins(self, list_h, bins_h, n_bins, persistent=0, fullblock=0, shells=None, period=1.0, d4=True):
         """Per-bin sums (amdat_disp_bins_run): sum_d2, sum_d4, count [B][G], fs_sum [B][G][S]."""
         G = self.n_timegaps
         d2 = np.zeros((n_bins, G))
-        d4 = np.zeros((n_bins, G))
+        d4s = np.zeros((n_bins, G))
         cnt = np.zeros((n_bins, G), np.int64)
         kv = off = None
         S = 0
@@ -358,9 +358,10 @@ class Engine:
             S = len(off) - 1
         fs = np.zeros((n_bins, G, max(S, 1)))
         _check(lib().amdat_disp_bins_run(self._ctx, int(list_h), int(bins_h), int(persistent), int(fullblock), S,
-                                         _p(off), _p(kv), C.c_float(period), OUT_HOST, _p(d2), _p(d4), _p(cnt),
+                                         _p(off), _p(kv), C.c_float(period), OUT_HOST, _p(d2),
+                                         _p(d4s) if d4 else None, _p(cnt),
                                          _p(fs) if S else None))
-        return dict(sum_d2=d2, sum_d4=d4, count=cnt, fs_sum=fs[:, :, :S])
+        return dict(sum_d2=d2, sum_d4=d4s if d4 else None, count=cnt, fs_sum=fs[:, :, :S])
 
     def plan(self, lists, fullblock=0, shells=None, period=1.0, n_bins=0, bin_max=0.0, flags=0):
         """Prepared many-list displacement run (amdat_disp_plan_*)."""

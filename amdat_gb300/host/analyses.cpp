@@ -98,7 +98,8 @@ struct BinOut {
   std::vector<int64_t> cnt;    // [bin][gap]
 };
 BinOut disp_bins(System* sys, const Trajectory_List* list, const Trajectory_List_Bins* bins, bool persistent,
-                 bool fullblock, const std::vector<int32_t>* kvec, const std::vector<int32_t>* off, float period) {
+                 bool fullblock, const std::vector<int32_t>* kvec, const std::vector<int32_t>* off, float period,
+                 bool want_d4 = false) {
   const int G = sys->n_timegaps(), B = bins->n_bins();
   const int S = off ? (int)off->size() - 1 : 0;
   BinOut o;
@@ -119,7 +120,7 @@ BinOut disp_bins(System* sys, const Trajectory_List* list, const Trajectory_List
     check(amdat_disp_bins_run(sys->ctx(), list->handle(), bins->handle(), persistent ? 1 : 0, fullblock ? 1 : 0,
                               std::max(ns, 0), ns > 0 ? sub_off.data() : nullptr, ns > 0 ? sub_kv.data() : nullptr,
                               period, AMDAT_OUT_HOST, s0 == 0 ? o.d2.data() : nullptr,
-                              s0 == 0 ? o.d4.data() : nullptr, s0 == 0 ? o.cnt.data() : nullptr,
+                              s0 == 0 && want_d4 ? o.d4.data() : nullptr, s0 == 0 ? o.cnt.data() : nullptr,
                               ns > 0 ? fs.data() : nullptr),
           "binned displacement run");
     for (int bg = 0; bg < B * G; ++bg)
@@ -316,7 +317,7 @@ void Non_Gaussian_Parameter::analyze(Trajectory_List* list) {
 }
 
 void Non_Gaussian_Parameter::analyze_bins(Trajectory_List* list, Trajectory_List_Bins* bins, bool persistent) {
-  const BinOut o = disp_bins(system, list, bins, persistent, false, nullptr, nullptr, 1.f);
+  const BinOut o = disp_bins(system, list, bins, persistent, false, nullptr, nullptr, 1.f, true);
   const int G = system->n_timegaps(), B = bins->n_bins();
   bin_ngp_.assign(B, std::vector<float>(G, 0.f));
   for (int b = 0; b < B; ++b)

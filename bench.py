@@ -476,7 +476,9 @@ def main():
         if n_lat == 0:
             kname = "rhok_lattice_kernel"
             n_lat, ms_lat = eng.profile_kernel(kname)
-        n_isf, ms_isf = eng.profile_kernel("isf_pairs_kernel")
+        n_isf, ms_isf = eng.profile_kernel("isf_lag_kernel")  # linear scheme: the lag kernel
+        if n_isf == 0:
+            n_isf, ms_isf = eng.profile_kernel("isf_pairs_kernel")
         eng.profile_reset(False)
         units = float(N) * T * nk
         value = job_rate(units, world, ms)
@@ -628,8 +630,8 @@ def main():
         eng.boxify(blo, bhi)
         bh = eng.bins_create((4, 4, 4), blo, bhi)
         bin_ms = {}
-        for tag, kw in (("msd", {}), ("msd_persistent", {"persistent": 1}),
-                        ("msd_fs", {"shells": shells, "period": L})):
+        for tag, kw in (("msd", {"d4": False}), ("msd_ngp", {}), ("msd_persistent", {"persistent": 1, "d4": False}),
+                        ("msd_fs", {"shells": shells, "period": L, "d4": False})):
             eng.disp_bins(0, bh, 64, **kw)  # warm-up
             torch.cuda.synchronize()
             eng.profile_reset(True)

@@ -237,7 +237,7 @@ amdat_status amdat_fast_particles(amdat_ctx* ctx, int32_t list, int32_t gap, flo
  * persistent = 1: Bin_Dynamics_Analysis (src/bin_dynamics_analysis.h), members
  * in the bin at t0 and at t1, pairs of fullblock 0.  Per bin b and gap g:
  *   sum_d2[b][g]     sum of |dr|^2
- *   sum_d4[b][g]     sum of |dr|^4
+ *   sum_d4[b][g]     sum of |dr|^4 (accumulated only when sum_d4 is given)
  *   count[b][g]      number of (member, time pair) terms
  *   fs_sum[b][g][s]  sum of the shell mean of cos(k.dr), k = 2 pi n / period,
  *                    for up to 8 shells (list mode: every vector of the shell)

@@ -77,6 +77,12 @@ def _check_bins(eng, traj, lst, lst_h, nb, persistent, fullblock, qvectors, m0=8
     kv, off = n[off_all[m0]:off_all[m1 + 1]], off_all[m0:m1 + 2] - off_all[m0]
     L = float(f32(traj.box.min()))
     out = eng.disp_bins(lst_h, h, B, persistent=persistent, fullblock=fullblock, shells=(kv, off), period=L)
+    # without the |dr|^4 column the other columns are unchanged
+    out3 = eng.disp_bins(lst_h, h, B, persistent=persistent, fullblock=fullblock, shells=(kv, off), period=L,
+                         d4=False)
+    np.testing.assert_array_equal(out3["count"], out["count"])
+    np.testing.assert_allclose(out3["sum_d2"], out["sum_d2"], rtol=1e-12, atol=1e-15)
+    np.testing.assert_allclose(out3["fs_sum"], out["fs_sum"], rtol=1e-12, atol=1e-12)
     s = orc.scheme(traj.scheme)
     msd, w = orc.msd_bins(s, traj.unwrapped, lst, bins, B, persistent, orc.F64)
     corr = orc.isfs_bins(s, traj.unwrapped, lst, kv, off, float(wv.spacing(L)), L, bins, B, fullblock,

@@ -61,6 +61,33 @@ def test_isf_and_sk_reference_shells(fb, eng, qvectors):
     np.testing.assert_allclose(sk, ref_sk, rtol=1e-5, atol=1e-7)
 
 
+@pytest.mark.parametrize("frames,n", [(40, 300), (137, 200)])
+def test_isf_linear_scheme_lag_kernel(eng, monkeypatch, qvectors, frames, n):
+    """Linear schemes take the sliding-window correlator: its per-gap sums equal
+    the pair-table kernel's to the bit (same Kahan order), and the FP64 oracle."""
+    scheme = synth.TimeScheme.linear(frames, 1.0)
+    traj = synth.random_walk(n, 7.0, scheme, 0.2, seed=31, time_scaled=False)
+    eng.upload(traj.unwrapped, traj.box)
+    eng.set_scheme(scheme)
+    L = float(np.float32(traj.box.min()))
+    kv, off = _shells(qvectors, 0, 12)
+    fr = np.arange(traj.n_frames, dtype=np.int32)
+    h = eng.wave_density(0, kv, L, fr)
+    corr, pc = eng.isf(h, h, off)
+    monkeypatch.setenv("AMDAT_ISF_KERNEL", "pairs")
+    corr_p, pc_p = eng.isf(h, h, off)
+    monkeypatch.delenv("AMDAT_ISF_KERNEL")
+    np.testing.assert_array_equal(pc, pc_p)
+    np.testing.assert_array_equal(corr, corr_p)
+    got = corr / (pc[:, None] * n)
+    s = orc.scheme(scheme)
+    rho = orc.rhok(traj.wrapped(), np.arange(n, dtype=np.int32), fr, kv, float(wv.spacing(L)), L, orc.F64)
+    ref = orc.isf(s, rho, rho, off, n, 0, orc.F64)
+    scale = np.maximum(np.abs(ref[0]), 1e-3)
+    assert (np.abs(got - ref) / scale).max() <= 1e-5
+    eng.wave_density_free(h)
+
+
 def test_rhok_lattice_mode(eng):
     """All half-space lattice vectors |k| <= kmax, shell-sorted: every element
     against the FP64 oracle on the returned vector list."""
