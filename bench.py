@@ -40,10 +40,10 @@ PEAKS_FILE = os.path.join(HERE, "MEASURED_PEAKS.json")
 FP32_LANES_PER_SM = 128
 # DRAM bytes (read + write) per frame of one rhok_tc_kernel launch on the headline
 # lattice (N=32000, |k|<=20, L=33.6), from one ncu capture of a 2-frame launch
-# (profiles/rhok_tc_kernel_N32000_k20_2frames.md: 812.5 MB read + 43.0 MB written).
-# Every stream of the launch is per frame (X/Y phase tables, Z operands, rho rows), so
-# a launch over f frames moves f times this.
-TC_DRAM_BYTES_PER_FRAME = (812.518e6 + 42.974e6) / 2
+# (profiles/rhok_tc_kernel_N32000_k20_2frames.md, design E: 815.5 MB read + 42.8 MB
+# written).  Every stream of the launch is per frame (X/Y phase tables, Z operands, rho
+# rows), so a launch over f frames moves f times this.
+TC_DRAM_BYTES_PER_FRAME = (815.539e6 + 42.798e6) / 2
 
 
 # ---------------------------------------------------------------------------
