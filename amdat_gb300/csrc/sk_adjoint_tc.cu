@@ -11,13 +11,13 @@
 // K = 2 x nz window, re/im interleaved) in shared memory, streams the
 // coefficient tiles (C and nz C, FP16 hi/lo, scaled into FP16 range) in
 // chunks of 16 nz by bulk copy through a 3-stage ring, runs 12 tcgen05.mma per
-// chunk (3 split passes x 2 k-steps x {T, T'}) into one of two TMEM
-// accumulator pairs, and four epilogue warps (one atom per thread) read T and
+// chunk (3 split passes x 2 k-steps x {T, T'}; warp 5 issues the T and warp 6
+// the T' MMAs) into one of two TMEM accumulator pairs, and four epilogue warps (one atom per thread) read T and
 // T', form W from exact fixed-point phases and add the tile's contribution to
 // the atom's Kahan-compensated sums.  Every atom's gradient is written by one
 // thread after a fixed sequence of tiles: deterministic.
 //
-// Warps 0-3: epilogue; warp 4: producer; warp 5: MMA issuer.  Waits are
+// Warps 0-3: epilogue; warp 4: producer; warps 5-6: MMA issuers (T, T').  Waits are
 // bounded; a timeout makes every role stop, wait for its copies and MMAs,
 // free tensor memory and set an error word.
 #include <cuda_fp16.h>
@@ -38,7 +38,8 @@ constexpr int SA_N = 128;                         // 64 complex rows -> Re, Im r
 constexpr int SA_STAGES = 3;
 constexpr uint32_t SA_BPART = SA_N * SA_KC * 2;   // 8 KB: one of C hi, C lo, C' hi, C' lo
 constexpr uint32_t SA_BSTAGE = 4 * SA_BPART;      // 32 KB per chunk
-constexpr int SA_THREADS = 192;
+constexpr int SA_ISSUERS = 2;                    // warp 5 issues T, warp 6 issues T'
+constexpr int SA_THREADS = 32 * (5 + SA_ISSUERS);  // 224
 constexpr uint32_t SA_WAIT = 1u << 19;             // try_wait calls of <= 1 us
 constexpr uint32_t SA_TMEM_COLS = 512;             // two (T, T') accumulator pairs
 
@@ -129,13 +130,13 @@ __global__ void __launch_bounds__(SA_THREADS, 1)
   if (tid == 0) {
     for (int s = 0; s < SA_STAGES; ++s) {
       umma::mbar_init(&S.full_b[s], 1);
-      umma::mbar_init(&S.empty_b[s], 1);
+      umma::mbar_init(&S.empty_b[s], SA_ISSUERS);
     }
     for (int b = 0; b < 2; ++b) {
-      umma::mbar_init(&S.full_acc[b], 1);
+      umma::mbar_init(&S.full_acc[b], SA_ISSUERS);
       umma::mbar_init(&S.empty_acc[b], 128);
     }
-    umma::mbar_init(&S.mma_done, 1);
+    umma::mbar_init(&S.mma_done, SA_ISSUERS);
     umma::fence_mbarrier_init();
     S.bad = 0;
     S.issued = 0;
@@ -186,8 +187,11 @@ __global__ void __launch_bounds__(SA_THREADS, 1)
       if (!ok) S.bad = 1;
       S.issued = g;
     }
-  } else if (warp == 5) {
-    // ---- MMA issuer: D[atom][row] of T and T' per tile
+  } else if (warp == 5 || warp == 6) {
+    // ---- MMA issuers: D[atom][row] per tile, warp 5 for T and warp 6 for T'
+    // (separate accumulators, the same chunk stages: each stage and each
+    // accumulator pair is released once both issuers' MMAs on it complete)
+    const int which = warp - 5;
     if (lane == 0) {
       const uint32_t idesc = umma::idesc_f16_f32(SA_M, SA_N);
       const uint32_t a_sbo = (uint32_t)(KA / 8) * 128, b_sbo = (SA_KC / 8) * 128;
@@ -211,12 +215,11 @@ __global__ void __launch_bounds__(SA_THREADS, 1)
             ok = false;
             break;
           }
-          S.landed = g + 1;
+          atomicMax(&S.landed, g + 1);
           umma::fence_after_sync();
           const uint64_t b0 = b_desc0 + (uint64_t)(s * (SA_BSTAGE >> 4));
           const uint64_t aq = (uint64_t)(4 * q * 8);  // K offset of chunk q: 4q core matrices of 128 B
-#pragma unroll
-          for (int which = 0; which < 2; ++which) {  // T, T'
+          {
             const uint32_t d = tmem + (uint32_t)(buf * 256 + which * 128);
             const uint64_t bh = b0 + (uint64_t)(2 * which * (SA_BPART >> 4));
             const uint64_t bl = bh + (uint64_t)(SA_BPART >> 4);
