@@ -196,3 +196,34 @@ def test_fast_particles_match_oracle(eng, gap, thr):
         gq = out["sum_d4"][0][m][ok] * 3.0 / wq / (5.0 * gm[ok] * gm[ok]) - 1.0
         np.testing.assert_allclose(gq, ngp[0][m][ok], rtol=1e-6, atol=1e-9)
         eng.bins_free(h)
+
+
+def test_bins_edge_cases(eng):
+    """An empty list, a region no atom is in, a single-atom list and a fast-particle
+    threshold nothing passes: zero counts (the reference's 0/0 normalisation), no faults."""
+    traj, _, _ = load("bins")
+    eng.upload(traj.unwrapped, traj.box, traj.box_lo, wrapped=traj.wrapped())
+    eng.set_scheme(traj.scheme)
+    lo, hi = _bounds(traj)
+    G = eng.n_timegaps
+    eng.boxify(lo, hi)
+    h = eng.bins_create((2, 2, 2), lo, hi)
+    empty = eng.list(np.zeros(0, np.int32))
+    out = eng.disp_bins(empty, h, 8)
+    assert out["count"].sum() == 0 and not out["sum_d2"].any()
+    one = eng.list(np.array([7], np.int32))
+    out = eng.disp_bins(one, h, 8)
+    assert out["count"].sum() == len(orc.pairs(orc.scheme(traj.scheme), 0)[0])  # one member per pair
+    eng.bins_free(h)
+    # a region thinner than any spacing between atoms and the box edge: no members
+    h = eng.bins_create((1, 1, 1), lo, np.array([lo[0], hi[1], hi[2]], np.float32) + np.float32(1e-6))
+    m, c = eng.bins_read(h, traj.n_frames, traj.n_atoms, 1)
+    assert (m == -1).all() and c.sum() == 0
+    out = eng.disp_bins(0, h, 1)
+    assert out["count"].sum() == 0
+    eng.bins_free(h)
+    h = eng.fast_particles(0, 1, 1e30)
+    m, c = eng.bins_read(h, traj.n_frames, traj.n_atoms, 1)
+    assert (m == -1).all()
+    assert eng.disp_bins(0, h, 1)["count"].shape == (1, G)
+    eng.bins_free(h)
