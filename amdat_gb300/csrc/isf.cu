@@ -283,8 +283,8 @@ amdat_status amdat_isf_run(amdat_ctx* ctx, int32_t h1, int32_t h2, int32_t fullb
             (const int32_t*)(base + o_gf), G, part);
       };
       const char* force = std::getenv("AMDAT_ISF_KERNEL");  // "pairs": the pair-table kernel always
-      if (P.lagged && KT == 32 && !(force && std::strcmp(force, "pairs") == 0)) {
-        // linear schemes: one pass over t per block of 8 gaps
+      // linear schemes with enough gaps to occupy the block's 8 warps (8 gaps each)
+      if (P.lagged && KT == 32 && G >= 64 && !(force && std::strcmp(force, "pairs") == 0)) {
         AMDAT_CUDA(cudaFuncSetAttribute(isf_lag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
         KernelTimer kt(ctx, "isf_lag_kernel");
         isf_lag_kernel<<<(unsigned)tiles.size(), 256, shm, ctx->stream>>>(

@@ -61,7 +61,7 @@ def test_isf_and_sk_reference_shells(fb, eng, qvectors):
     np.testing.assert_allclose(sk, ref_sk, rtol=1e-5, atol=1e-7)
 
 
-@pytest.mark.parametrize("frames,n", [(40, 300), (137, 200)])
+@pytest.mark.parametrize("frames,n", [(72, 300), (137, 200)])
 def test_isf_linear_scheme_lag_kernel(eng, monkeypatch, qvectors, frames, n):
     """Linear schemes take the sliding-window correlator: its per-gap sums equal
     the pair-table kernel's to the bit (same Kahan order), and the FP64 oracle."""
