@@ -55,6 +55,7 @@ constexpr int TC_MMA_WARP = 5;                // warps 5 and 6: one per accumula
 constexpr int TC_MMA_WARPS = 2;
 constexpr int TC_BUILD_WARP0 = TC_MMA_WARP + TC_MMA_WARPS;
 constexpr int TC_BUILDERS = 512;              // 16 builder warps
+constexpr int TC_BUILD_GROUP = TC_BUILDERS / 2;  // two groups of 8 warps, alternate chunks
 constexpr int TC_DRAINERS = 128;              // warps 0-3, one per TMEM lane quadrant
 constexpr int TC_THREADS = 32 * TC_BUILD_WARP0 + TC_BUILDERS;  // 736
 constexpr uint32_t TC_A_BYTES = TC_M * TC_K * 2;      // 16 KB (one of hi / lo)
@@ -76,7 +77,7 @@ struct TcSmem {
   uint64_t mma_done;
   uint32_t tmem;
   volatile int bad;        // any role gave up
-  int build_stop[2];       // chunk parity: written by builder 0 before a builder barrier
+  int build_stop[2][2];    // [group][chunk parity]: written by the group's first thread before its barrier
   int z_issued, z_landed;  // bulk copies issued / seen complete
 };
 static_assert(sizeof(float) * TC_M * (TC_NMAX + 1) <= sizeof(((TcSmem*)0)->z), "D staging must fit the Z ring");
@@ -185,7 +186,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   if (tid == 0) {
     for (int s = 0; s < TC_S; ++s) {
       umma::mbar_init(&S.full_z[s], 1);
-      umma::mbar_init(&S.full_a[s], TC_BUILDERS);
+      umma::mbar_init(&S.full_a[s], TC_BUILD_GROUP);  // one group builds each chunk
       umma::mbar_init(&S.empty[s], 1);
     }
     for (int b = 0; b < 2; ++b) {
@@ -195,7 +196,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     umma::mbar_init(&S.mma_done, TC_MMA_WARPS);
     umma::fence_mbarrier_init();
     S.bad = 0;
-    S.build_stop[0] = S.build_stop[1] = 0;
+    S.build_stop[0][0] = S.build_stop[0][1] = S.build_stop[1][0] = S.build_stop[1][1] = 0;
     S.z_issued = 0;
     S.z_landed = 0;
   }
@@ -336,35 +337,42 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
     }
     if (!ok) S.bad = 1;
   } else {
-    // ---- builders: A(c) = W products of the streamed X/Y tables into stage c % TC_S
+    // ---- builders: A(c) = W products of the streamed X/Y tables into stage c % TC_S.
+    // Two groups of 8 warps build alternate chunks (group g: chunks c with c % 2 == g),
+    // so the wait / build / fence chain of one chunk overlaps the next one's.
     const int btid = tid - 32 * TC_BUILD_WARP0;
-    const int bw = btid >> 5;
-    for (int c = 0; c < n_chunks; ++c) {
-      const int sa = c % TC_S, sz = sa;
-      // builder 0 decides for all builders (A stage free, X/Y of chunk c landed);
-      // the flag alternates with the chunk parity so a slow reader of chunk c
-      // never sees chunk c+1's decision
-      if (btid == 0) {
-        // the stage's copies landing implies its previous MMAs finished (the
-        // producer waited for them), so the A half of the stage is free too
+    const int grp = btid / TC_BUILD_GROUP, gtid = btid % TC_BUILD_GROUP, gw = gtid >> 5;
+    for (int c = grp; c < n_chunks; c += 2) {
+      const int sa = c % TC_S, sz = sa, par = (c >> 1) & 1;
+      // the group's first thread decides for the group (X/Y of chunk c landed;
+      // the stage's copies landing implies its previous MMAs finished, since the
+      // producer waited for them, so the A half of the stage is free too); the
+      // flag alternates with the group's chunk parity so a slow reader of one
+      // chunk never sees the next one's decision
+      if (gtid == 0) {
         const bool go = !S.bad && umma::mbar_wait(&S.full_z[sz], (c / TC_S) & 1, TC_WAIT);
-        S.build_stop[c & 1] = go ? 0 : 1;
+        S.build_stop[grp][par] = go ? 0 : 1;
       }
       __syncwarp();
-      umma::named_barrier(1, TC_BUILDERS);
-      if (*(volatile int*)&S.build_stop[c & 1]) {
-        if (btid == 0) S.bad = 1;
+      if (grp == 0)
+        umma::named_barrier(1, TC_BUILD_GROUP);
+      else
+        umma::named_barrier(2, TC_BUILD_GROUP);
+      if (*(volatile int*)&S.build_stop[grp][par]) {
+        if (gtid == 0) S.bad = 1;
         break;
       }
-      // A operand: thread = complex row r (nx = r % 8 = lane % 8, ny = r / 8) and
-      // the atom quad q (atoms 4q..4q+3): two 128-bit loads each of X and Y,
-      // four 128-bit stores (hi and lo of the real row [Wr, -Wi] and of the
-      // imaginary row [Wi, Wr]), all free of bank conflicts
+      // A operand: thread = complex row r (nx = lane % 8, ny = warp of the group)
+      // and the atom octet o (atom quads 2o, 2o+1): four 128-bit loads each of X
+      // and Y, eight 128-bit stores (hi and lo of the real row [Wr, -Wi] and of
+      // the imaginary row [Wi, Wr] for both quads), all free of bank conflicts
       const float4* X4 = reinterpret_cast<const float4*>(S.z[sz] + 2 * TC_ZHALF);
       const float4* Y4 = X4 + TC_J * 8 / 2;
-      {
-        const int m = lane & 7, rg = bw >> 1, q = (bw & 1) * 4 + (lane >> 3);
-        const int r = rg * 8 + m;
+      const int m = lane & 7, rg = gw, o = lane >> 3;
+      const int r = rg * 8 + m;
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int q = 2 * o + h;
         const float4 xa = X4[16 * m + ((m + 2 * q) & 15)], xb = X4[16 * m + ((m + 2 * q + 1) & 15)];
         const float4 ya = Y4[16 * rg + ((rg + 2 * q) & 15)], yb = Y4[16 * rg + ((rg + 2 * q + 1) & 15)];
         const float xr[4] = {xa.x, xa.z, xb.x, xb.z}, xi[4] = {xa.y, xa.w, xb.y, xb.w};
