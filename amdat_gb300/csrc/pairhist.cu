@@ -11,7 +11,9 @@
 // bin = int(length / bin_size) - with correctly rounded, uncontracted
 // operations, so the integer counts equal the reference's bit for bit.
 // Pairs whose squared length is safely beyond the last bin skip the square
-// root and the division.
+// root and the division; the others estimate the bin from rsqrtf and take
+// the correctly rounded chain only when the estimate lies within its error
+// bound of a bin edge.
 //
 // A block owns 256 members i of list 1 (positions in registers) and streams
 // list 2 through shared memory in tiles of 1024.  Counts go to per-warp
@@ -61,6 +63,7 @@ struct PHParams {
   int32_t symmetric;       // l1 == l2 and frame_a == frame_b: visit j > i, count 2
   float3 box;
   float bin_size;
+  float inv_bin;  // 1 / bin_size (the fast bin estimate)
   float s2_cut;
   int32_t n_bins;
   unsigned long long* counts;  // [rows][n_bins]
@@ -106,13 +109,24 @@ __global__ void __launch_bounds__(PH_THREADS)
     int t_begin = 0;
     if (p.symmetric) t_begin = max(0, i + 1 - j0);  // j > i
     for (int t = t_begin; t < nj; ++t) {
-      if (sid[t] == ai) continue;  // i != j (same atom in both lists)
+      // i != j: implied by j > i for the symmetric pass, checked otherwise
+      if (!p.symmetric && sid[t] == ai) continue;
       const float mx = min_image(__fsub_rn(sx[t], xi), p.box.x);
       const float my = min_image(__fsub_rn(sy[t], yi), p.box.y);
       const float mz = min_image(__fsub_rn(sz[t], zi), p.box.z);
       const float s2 = __fadd_rn(__fadd_rn(__fmul_rn(mx, mx), __fmul_rn(my, my)), __fmul_rn(mz, mz));
       if (s2 < p.s2_cut) {
-        const int b = (int)__fdiv_rn(__fsqrt_rn(s2), p.bin_size);
+        // bin = int(sqrt_rn(s2) / bin_size), the reference's chain.  First from
+        // rsqrtf (<= 2 ulp) and the reciprocal bin size: within 1e-6 relative of
+        // the exact quotient, so its integer part is the exact one unless the
+        // quotient lies within that margin of an integer; those pairs (and
+        // s2 = 0) take the correctly rounded chain.
+        const float x = __fmul_rn(__fmul_rn(s2, rsqrtf(s2)), p.inv_bin);
+        int b = (int)x;
+        const float frac = __fsub_rn(x, (float)b);
+        const float margin = fmaf(x, 1e-6f, 1e-6f);
+        if (!(s2 > 0.f) || frac <= margin || frac >= 1.f - margin)
+          b = (int)__fdiv_rn(__fsqrt_rn(s2), p.bin_size);
         if (b >= 0 && b < p.n_bins) atomicAdd(hist + b, inc);
       }
     }
@@ -161,6 +175,7 @@ static void run_pair_hist(amdat_ctx* ctx, const ListEntry& l1, const ListEntry& 
   p.symmetric = symmetric ? 1 : 0;
   p.box = make_float3(ctx->box[0], ctx->box[1], ctx->box[2]);
   p.bin_size = max_distance / (float)n_bins;
+  p.inv_bin = 1.0f / p.bin_size;
   // squared lengths at or above this are past the last bin for sure
   const double cut = (double)max_distance * (1.0 + 1e-5);
   p.s2_cut = (float)(cut * cut);

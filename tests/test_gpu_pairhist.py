@@ -77,3 +77,28 @@ def test_rdf_large_symmetric_matches_ordered(eng):
     ordered = eng.rdf(0, allh, fr, 7.5, 300)
     np.testing.assert_array_equal(sym, ordered)
     assert sym[0].sum() > 0
+
+
+@pytest.mark.parametrize("nb,maxd", [(40, 4.0), (80, 4.0), (64, 3.2)])
+def test_rdf_lattice_distances_on_bin_edges(eng, nb, maxd):
+    """Atoms on a cubic lattice whose spacing is a whole number of bins: many pair
+    distances (a, 2a, 3a, ...) fall exactly on bin edges, where the bin must come
+    from the correctly rounded chain; counts equal the oracle's."""
+    a = 0.5
+    g = np.arange(12, dtype=np.float64) * a
+    pos = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    rng = np.random.default_rng(8)
+    pos = pos[rng.permutation(len(pos))[:900]]
+    jitter = np.zeros_like(pos)
+    jitter[::7] = rng.normal(0, 1e-6, (len(pos[::7]), 3))  # a few just off the edges
+    frame = (pos + jitter).astype(np.float32)
+    L = np.float32(12 * a)
+    traj = synth.Trajectory(unwrapped=np.stack([frame, frame]), box=np.full(3, L, np.float32),
+                            box_lo=np.zeros(3, np.float32), types=np.zeros(len(pos), np.int32),
+                            scheme=synth.TimeScheme.linear(2, 1.0))
+    eng.upload(traj.unwrapped, traj.box, traj.box_lo, wrapped=traj.unwrapped)
+    s = orc.scheme(traj.scheme)
+    lst = np.arange(len(pos), dtype=np.int32)
+    counts = eng.rdf(0, 0, np.array([0, 1], np.int32), maxd, nb)
+    ref, _ = orc.rdf(s, -1, traj.unwrapped, traj.box, lst, nb, maxd)
+    np.testing.assert_array_equal(counts, ref)
