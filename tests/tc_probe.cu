@@ -72,3 +72,23 @@ extern "C" int tc_probe_run(const void* A, const void* B, void* D, int lbo, int 
   if (e == cudaSuccess) e = cudaDeviceSynchronize();
   return (int)e;
 }
+
+// A bounded wait that runs out: an mbarrier nothing arrives on, polled with the
+// engine's bounded try_wait (max_iter polls of <= 1 us).  The kernel records
+// the outcome (1 = gave up) and returns normally, so the context stays usable.
+extern "C" __global__ void wait_timeout_kernel(int* status, unsigned max_iter) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_mbarrier_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) *status = mbar_wait(&bar, 0, max_iter) ? 0 : 1;
+}
+
+extern "C" int wait_timeout_run(void* status, unsigned max_iter) {
+  wait_timeout_kernel<<<1, 32>>>((int*)status, max_iter);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  return (int)e;
+}

@@ -35,3 +35,15 @@ def test_umma_layout(probe):
     assert st == 0 and int(err.item()) == 0
     got = D.cpu().numpy()
     assert np.abs(got - ref).max() < 1e-4 * max(1.0, np.abs(ref).max()), np.abs(got - ref).max()
+
+
+def test_bounded_wait_times_out_and_context_stays_usable(probe):
+    """A wait on an mbarrier that nothing completes gives up after its bounded
+    number of polls and reports it; the context then still runs kernels."""
+    import torch
+    status = torch.full((1,), -1, dtype=torch.int32, device="cuda")
+    rc = probe.wait_timeout_run(C.c_void_p(status.data_ptr()), C.c_uint(1000))
+    assert rc == 0
+    assert int(status.item()) == 1
+    # the context is intact: the layout probe still runs and is correct
+    test_umma_layout(probe)
