@@ -69,6 +69,8 @@ struct PHParams {
   unsigned long long* counts;  // [rows][n_bins]
 };
 
+// SYM: the symmetric pass (list1 == list2, one frame): j > i, each pair counted twice
+template <bool SYM>
 __global__ void __launch_bounds__(PH_THREADS)
     pair_hist_kernel(PHParams p) {
   extern __shared__ unsigned int sh_hist[];  // [8 warps][n_bins]
@@ -91,8 +93,8 @@ __global__ void __launch_bounds__(PH_THREADS)
     yi = A[p.n_pad + ai];
     zi = A[2 * p.n_pad + ai];
   }
-  const unsigned int inc = p.symmetric ? 2u : 1u;
-  const int j_begin = p.symmetric ? i0 : 0;
+  const unsigned int inc = SYM ? 2u : 1u;
+  const int j_begin = SYM ? i0 : 0;
   __syncthreads();
   for (int j0 = j_begin; j0 < p.l2.n; j0 += PH_JT) {
     const int nj = min(PH_JT, p.l2.n - j0);
@@ -107,10 +109,10 @@ __global__ void __launch_bounds__(PH_THREADS)
     __syncthreads();
     if (!live) continue;
     int t_begin = 0;
-    if (p.symmetric) t_begin = max(0, i + 1 - j0);  // j > i
+    if (SYM) t_begin = max(0, i + 1 - j0);  // j > i
     for (int t = t_begin; t < nj; ++t) {
       // i != j: implied by j > i for the symmetric pass, checked otherwise
-      if (!p.symmetric && sid[t] == ai) continue;
+      if (!SYM && sid[t] == ai) continue;
       const float mx = min_image(__fsub_rn(sx[t], xi), p.box.x);
       const float my = min_image(__fsub_rn(sy[t], yi), p.box.y);
       const float mz = min_image(__fsub_rn(sz[t], zi), p.box.z);
@@ -183,12 +185,13 @@ static void run_pair_hist(amdat_ctx* ctx, const ListEntry& l1, const ListEntry& 
   p.counts = (unsigned long long*)(base + o_cnt);
   if (n_q && l1.n > 0 && l2.n > 0) {
     const size_t shm = (size_t)8 * n_bins * 4;
+    auto kern = symmetric ? pair_hist_kernel<true> : pair_hist_kernel<false>;
     if (shm > 48 * 1024)
-      AMDAT_CUDA(cudaFuncSetAttribute(pair_hist_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
+      AMDAT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
     AMDAT_REQUIRE(n_q <= 65535, "at most 65535 frames or time pairs per call");
     dim3 grid((unsigned)ceil_div(l1.n, PH_THREADS), (unsigned)n_q);
     KernelTimer kt(ctx, "pair_hist_kernel");
-    pair_hist_kernel<<<grid, PH_THREADS, shm, ctx->stream>>>(p);
+    kern<<<grid, PH_THREADS, shm, ctx->stream>>>(p);
     check_launch("pair_hist_kernel");
     count_launch(ctx);
   }
