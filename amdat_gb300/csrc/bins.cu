@@ -123,7 +123,9 @@ struct BnParams {
   int32_t staged;  // per-block shared accumulators
 };
 
-template <bool FS>
+// FS: F_s shells in the columns after |dr|^2 (and |dr|^4); AXES: the columns are
+// instead dx, dy, dz, dx^2, dy^2, dz^2 (msd_2d and mean_displacement per bin)
+template <bool FS, bool AXES = false>
 __global__ void __launch_bounds__(BN_THREADS) disp_bins_kernel(BnParams p) {
   extern __shared__ double bn_smem[];  // staged: [n_bins][stride] sums, then [n_bins] counts
   __shared__ int s_item;
@@ -163,8 +165,13 @@ __global__ void __launch_bounds__(BN_THREADS) disp_bins_kernel(BnParams p) {
           const float dx = __fsub_rn(__ldg(X1 + atom), __ldg(X0 + atom));
           const float dy = __fsub_rn(__ldg(X1 + p.n_pad + atom), __ldg(X0 + p.n_pad + atom));
           const float dz = __fsub_rn(__ldg(X1 + 2 * p.n_pad + atom), __ldg(X0 + 2 * p.n_pad + atom));
-          v[0] = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-          v[1] = v[0] * v[0];
+          if (AXES) {
+            v[0] = dx, v[1] = dy, v[2] = dz;
+            v[3] = __fmul_rn(dx, dx), v[4] = __fmul_rn(dy, dy), v[5] = __fmul_rn(dz, dz);
+          } else {
+            v[0] = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+            v[1] = v[0] * v[0];
+          }
           if (FS) {
             const int32_t fx = turns_fixed(dx, p.period);
             const int32_t fy = turns_fixed(dy, p.period);
@@ -196,7 +203,8 @@ __global__ void __launch_bounds__(BN_THREADS) disp_bins_kernel(BnParams p) {
       // staged columns: |dr|^2, then |dr|^4 only when asked for, then the shells
 #pragma unroll
       for (int k = 0; k < 2 + BN_MAX_FS; ++k)
-        if (k < stride) s_val[warp][lane][k] = (k == 0 || p.want_d4) ? v[k] : v[k + 1 < 2 + BN_MAX_FS ? k + 1 : k];
+        if (k < stride)
+          s_val[warp][lane][k] = (AXES || k == 0 || p.want_d4) ? v[k] : v[k + 1 < 2 + BN_MAX_FS ? k + 1 : k];
       __syncwarp();
       const unsigned peers = __match_any_sync(0xffffffffu, b);
       if (b >= 0 && lane == __ffs(peers) - 1) {
@@ -421,10 +429,11 @@ amdat_status amdat_bins_read(amdat_ctx* ctx, int32_t handle, int32_t out_flags, 
   });
 }
 
-amdat_status amdat_disp_bins_run(amdat_ctx* ctx, int32_t list, int32_t bins, int32_t persistent,
-                                 int32_t fullblock, int32_t n_shells, const int32_t* shell_offsets,
-                                 const int32_t* kvec, float period, int32_t out_flags, double* sum_d2,
-                                 double* sum_d4, int64_t* count, double* fs_sum) {
+static amdat_status disp_bins_impl(amdat_ctx* ctx, int32_t list, int32_t bins, int32_t persistent,
+                                   int32_t fullblock, int32_t n_shells, const int32_t* shell_offsets,
+                                   const int32_t* kvec, float period, int32_t out_flags, double* sum_d2,
+                                   double* sum_d4, int64_t* count, double* fs_sum, bool axes_mode,
+                                   double* axis_sums) {
   return guarded([&] {
     check_ctx(ctx);
     if (!ctx->have_traj) throw Error(AMDAT_ERR_STATE, "no trajectory uploaded");
@@ -438,8 +447,11 @@ amdat_status amdat_disp_bins_run(amdat_ctx* ctx, int32_t list, int32_t bins, int
     const PairTable& P = pair_table(ctx, persistent ? false : fullblock != 0, false);
     const int G = P.n_gaps;
     const int32_t B = m.nx * m.ny * m.nz;
-    const int want_d4 = sum_d4 ? 1 : 0;
-    const int stride = 1 + want_d4 + n_shells;
+    const bool axes = axes_mode;
+    AMDAT_REQUIRE(!axes || axis_sums != nullptr, "null axis_sums");
+    AMDAT_REQUIRE(!axes || n_shells == 0, "per-axis sums take no shells");
+    const int want_d4 = sum_d4 && !axes ? 1 : 0;
+    const int stride = axes ? 6 : 1 + want_d4 + n_shells;
     // shells (list mode: one cosine per vector)
     std::vector<int4> kv;
     std::vector<int32_t> off(1, 0);
@@ -506,7 +518,7 @@ amdat_status amdat_disp_bins_run(amdat_ctx* ctx, int32_t list, int32_t bins, int
       const size_t stage = (size_t)B * stride * 8 + (size_t)B * 4;
       p.staged = stage <= BN_STAGE_LIMIT ? 1 : 0;
       const size_t shm = p.staged ? stage : 0;
-      auto kern = n_shells ? disp_bins_kernel<true> : disp_bins_kernel<false>;
+      auto kern = axes ? disp_bins_kernel<false, true> : (n_shells ? disp_bins_kernel<true> : disp_bins_kernel<false>);
       if (shm > 0) AMDAT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
       int per_sm = 1;
       AMDAT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BN_THREADS, shm));
@@ -517,10 +529,12 @@ amdat_status amdat_disp_bins_run(amdat_ctx* ctx, int32_t list, int32_t bins, int
       count_launch(ctx);
     }
     const cudaMemcpyKind kind = out_flags == AMDAT_OUT_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
-    // [bin][gap][stride] -> sum_d2[bin][gap], sum_d4[bin][gap], fs_sum[bin][gap][shell]
-    if (sum_d2)
+    // [bin][gap][stride] -> sum_d2[bin][gap], sum_d4[bin][gap], fs_sum[bin][gap][shell],
+    // or axis_sums[bin][gap][6]
+    if (axes) AMDAT_CUDA(cudaMemcpyAsync(axis_sums, base + o_acc, (size_t)B * G * 6 * 8, kind, st));
+    if (sum_d2 && !axes)
       AMDAT_CUDA(cudaMemcpy2DAsync(sum_d2, 8, base + o_acc, (size_t)stride * 8, 8, (size_t)B * G, kind, st));
-    if (sum_d4)
+    if (want_d4)
       AMDAT_CUDA(cudaMemcpy2DAsync(sum_d4, 8, base + o_acc + 8, (size_t)stride * 8, 8, (size_t)B * G, kind, st));
     if (fs_sum && n_shells)
       AMDAT_CUDA(cudaMemcpy2DAsync(fs_sum, (size_t)n_shells * 8, base + o_acc + 8 * (1 + want_d4), (size_t)stride * 8,
@@ -528,6 +542,20 @@ amdat_status amdat_disp_bins_run(amdat_ctx* ctx, int32_t list, int32_t bins, int
     if (count) AMDAT_CUDA(cudaMemcpyAsync(count, base + o_cnt, (size_t)B * G * 8, kind, st));
     AMDAT_CUDA(cudaStreamSynchronize(st));
   });
+}
+
+amdat_status amdat_disp_bins_run(amdat_ctx* ctx, int32_t list, int32_t bins, int32_t persistent,
+                                 int32_t fullblock, int32_t n_shells, const int32_t* shell_offsets,
+                                 const int32_t* kvec, float period, int32_t out_flags, double* sum_d2,
+                                 double* sum_d4, int64_t* count, double* fs_sum) {
+  return disp_bins_impl(ctx, list, bins, persistent, fullblock, n_shells, shell_offsets, kvec, period,
+                        out_flags, sum_d2, sum_d4, count, fs_sum, false, nullptr);
+}
+
+amdat_status amdat_disp_bins_axes_run(amdat_ctx* ctx, int32_t list, int32_t bins, int32_t persistent,
+                                      int32_t out_flags, double* axis_sums, int64_t* count) {
+  return disp_bins_impl(ctx, list, bins, persistent, 0, 0, nullptr, nullptr, 1.0f, out_flags, nullptr, nullptr,
+                        count, nullptr, true, axis_sums);
 }
 
 }  // extern "C"

@@ -123,12 +123,19 @@ __global__ void __launch_bounds__(PH_THREADS)
         // the exact quotient, so its integer part is the exact one unless the
         // quotient lies within that margin of an integer; those pairs (and
         // s2 = 0) take the correctly rounded chain.
-        const float x = __fmul_rn(__fmul_rn(s2, rsqrtf(s2)), p.inv_bin);
-        int b = (int)x;
-        const float frac = __fsub_rn(x, (float)b);
-        const float margin = fmaf(x, 1e-6f, 1e-6f);
-        if (!(s2 > 0.f) || frac <= margin || frac >= 1.f - margin)
+        // (the symmetric RDF pass, where most pairs are in range; the sparse
+        // distinct van Hove pass keeps the short exact branch)
+        int b;
+        if (SYM) {
+          const float x = __fmul_rn(__fmul_rn(s2, rsqrtf(s2)), p.inv_bin);
+          b = (int)x;
+          const float frac = __fsub_rn(x, (float)b);
+          const float margin = fmaf(x, 1e-6f, 1e-6f);
+          if (!(s2 > 0.f) || frac <= margin || frac >= 1.f - margin)
+            b = (int)__fdiv_rn(__fsqrt_rn(s2), p.bin_size);
+        } else {
           b = (int)__fdiv_rn(__fsqrt_rn(s2), p.bin_size);
+        }
         if (b >= 0 && b < p.n_bins) atomicAdd(hist + b, inc);
       }
     }

@@ -56,7 +56,7 @@ EXPORTED = [
     "amdat_gsmooth_run", "amdat_disp_axes_run",
     "amdat_gsmooth_adjoint", "amdat_structure_factor_adjoint",
     "amdat_boxify", "amdat_bins_create", "amdat_bins_read", "amdat_bins_free",
-    "amdat_disp_bins_run", "amdat_fast_particles",
+    "amdat_disp_bins_run", "amdat_disp_bins_axes_run", "amdat_fast_particles",
 ]
 
 PLAN_AUTOTUNE, PLAN_GRAPH, PLAN_NO_SHARING = 1, 2, 4
@@ -335,6 +335,15 @@ class Engine:
         c = np.zeros((n_frames, n_bins), np.int64)
         _check(lib().amdat_bins_read(self._ctx, int(handle), OUT_HOST, _p(m), _p(c)))
         return m, c
+
+    def disp_bins_axes(self, list_h, bins_h, n_bins, persistent=0):
+        """Per-bin axis sums [B][G][6] (dx, dy, dz, dx^2, dy^2, dz^2) and counts [B][G]."""
+        G = self.n_timegaps
+        ax = np.zeros((n_bins, G, 6))
+        cnt = np.zeros((n_bins, G), np.int64)
+        _check(lib().amdat_disp_bins_axes_run(self._ctx, int(list_h), int(bins_h), int(persistent), OUT_HOST,
+                                              _p(ax), _p(cnt)))
+        return dict(axis_sums=ax, count=cnt)
 
     def fast_particles(self, list_h, gap, min_u2) -> int:
         """Block-wise fast-particle membership as a one-bin map (amdat_fast_particles)."""

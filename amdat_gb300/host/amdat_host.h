@@ -238,11 +238,14 @@ class Mean_Square_Displacement_2D : public Analysis {
   Mean_Square_Displacement_2D(System* sys, const std::string& plane);
   void analyze(Trajectory_List* list) override;
   void write(const std::string& file) const override;
+  void analyze_bins(Trajectory_List* list, Trajectory_List_Bins* bins, bool persistent) override;
+  void select_bin(int b) override { msd_ = bin_msd_[b]; }
 
  private:
   std::string plane_;
   int a_ = 0, b_ = 1;  // axes of the plane
   std::vector<float> msd_;
+  std::vector<std::vector<float>> bin_msd_;
 };
 
 // Mean_Displacement (src/mean_displacement.cpp:149-199): mean vector displacement
@@ -251,9 +254,12 @@ class Mean_Displacement : public Analysis {
   explicit Mean_Displacement(System* sys);
   void analyze(Trajectory_List* list) override;
   void write(const std::string& file) const override;
+  void analyze_bins(Trajectory_List* list, Trajectory_List_Bins* bins, bool persistent) override;
+  void select_bin(int b) override { md_ = bin_md_[b]; }
 
  private:
   std::vector<float> md_;  // [gap][3]
+  std::vector<std::vector<float>> bin_md_;
 };
 
 // DebyeWaller_Dist (src/debyewaller_dist.cpp:14-99, command u2dist): the

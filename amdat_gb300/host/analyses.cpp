@@ -89,7 +89,8 @@ void Mean_Square_Displacement::analyze(Trajectory_List* list) {
 // --- spatial bins ------------------------------------------------------------
 void Analysis::analyze_bins(Trajectory_List*, Trajectory_List_Bins*, bool) {
   throw Error(AMDAT_ERR_ARGUMENT,
-              "bin_list targets and time-dependent lists are supported for msd, ngp and isfs by this engine");
+              "bin_list targets and time-dependent lists are supported for msd, msd_2d, mean_displacement, "
+              "ngp and isfs by this engine");
 }
 
 namespace {
@@ -216,6 +217,39 @@ void Mean_Square_Displacement_2D::analyze(Trajectory_List* list) {
     msd_[g] = (float)((o.ax[(size_t)g * 6 + 3 + a_] + o.ax[(size_t)g * 6 + 3 + b_]) / (double)o.pairs[g]);
 }
 
+namespace {
+struct BinAxes {
+  std::vector<double> ax;  // [bin][gap][6]
+  std::vector<int64_t> cnt;
+};
+BinAxes bin_axes(System* sys, const Trajectory_List* list, const Trajectory_List_Bins* bins, bool persistent) {
+  BinAxes o;
+  const size_t n = (size_t)bins->n_bins() * sys->n_timegaps();
+  o.ax.assign(n * 6, 0.0);
+  o.cnt.assign(n, 0);
+  check(amdat_disp_bins_axes_run(sys->ctx(), list->handle(), bins->handle(), persistent ? 1 : 0, AMDAT_OUT_HOST,
+                                 o.ax.data(), o.cnt.data()),
+        "binned displacement axes run");
+  return o;
+}
+}  // namespace
+
+void Mean_Square_Displacement_2D::analyze_bins(Trajectory_List* list, Trajectory_List_Bins* bins, bool persistent) {
+  const BinAxes o = bin_axes(system, list, bins, persistent);
+  const int G = system->n_timegaps(), B = bins->n_bins();
+  // with persistence the reference never calls analyze(), which would zero the
+  // weighting: it starts from initialize()'s timegap_weighting() (fullblock 1,
+  // src/mean_square_displacement_2d.cpp:116) and the member counts add to that
+  std::vector<int32_t> w0(G, 0);
+  if (persistent) check(amdat_scheme_weighting(&system->scheme(), 1, w0.data()), "timegap weighting");
+  bin_msd_.assign(B, std::vector<float>(G, 0.f));
+  for (int b = 0; b < B; ++b)
+    for (int g = 0; g < G; ++g) {
+      const size_t i = (size_t)b * G + g;
+      bin_msd_[b][g] = (float)((o.ax[i * 6 + 3 + a_] + o.ax[i * 6 + 3 + b_]) / (double)(o.cnt[i] + w0[g]));
+    }
+}
+
 void Mean_Square_Displacement_2D::write(const std::string& file) const {
   std::ofstream out = open_out(file);
   out << "2-D mean square displacement data for " << plane_ << " plane created by AMDAT v." << SEMVER
@@ -232,6 +266,17 @@ void Mean_Displacement::analyze(Trajectory_List* list) {
   md_.assign((size_t)G * 3, 0.f);
   for (int g = 0; g < G; ++g)
     for (int c = 0; c < 3; ++c) md_[(size_t)g * 3 + c] = (float)(o.ax[(size_t)g * 6 + c] / (double)o.pairs[g]);
+}
+
+void Mean_Displacement::analyze_bins(Trajectory_List* list, Trajectory_List_Bins* bins, bool persistent) {
+  const BinAxes o = bin_axes(system, list, bins, persistent);
+  const int G = system->n_timegaps(), B = bins->n_bins();
+  bin_md_.assign(B, std::vector<float>((size_t)G * 3, 0.f));
+  for (int b = 0; b < B; ++b)
+    for (int g = 0; g < G; ++g) {
+      const size_t i = (size_t)b * G + g;
+      for (int c = 0; c < 3; ++c) bin_md_[b][(size_t)g * 3 + c] = (float)(o.ax[i * 6 + c] / (double)o.cnt[i]);
+    }
 }
 
 void Mean_Displacement::write(const std::string& file) const {

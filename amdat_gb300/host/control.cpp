@@ -80,7 +80,7 @@ class Control {
     for (size_t i = 1; i < a.size(); ++i) {
       out.push_back(list(a[i]));
       if (out.back()->time_dependent())
-        throw Error(AMDAT_ERR_ARGUMENT, "time-dependent lists (find_fast) are supported by msd, ngp and isfs here");
+        throw Error(AMDAT_ERR_ARGUMENT, "time-dependent lists (find_fast) are supported by msd, msd_2d, mean_displacement, ngp and isfs here");
     }
     return out;
   }
@@ -139,7 +139,7 @@ class Control {
     }
     for (auto* l : t)
       if (l->time_dependent())
-        throw Error(AMDAT_ERR_ARGUMENT, "time-dependent lists (find_fast) are supported by msd, ngp and isfs here");
+        throw Error(AMDAT_ERR_ARGUMENT, "time-dependent lists (find_fast) are supported by msd, msd_2d, mean_displacement, ngp and isfs here");
     if (t.size() == 1) an.analyze(t[0]);
     else an.analyze(t[0], t[1]);
     an.write(file);

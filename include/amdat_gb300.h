@@ -246,6 +246,13 @@ amdat_status amdat_disp_bins_run(amdat_ctx* ctx, int32_t list, int32_t bins, int
                                  int32_t fullblock, int32_t n_shells, const int32_t* shell_offsets,
                                  const int32_t* kvec, float period, int32_t out_flags, double* sum_d2,
                                  double* sum_d4, int64_t* count, double* fs_sum);
+/* Per-axis sums of every bin in one pass (Bin_Static_Analysis /
+ * Bin_Dynamics_Analysis of Mean_Square_Displacement_2D, src/mean_square_displacement_2d.cpp,
+ * and Mean_Displacement, src/mean_displacement.cpp; fullblock 0):
+ *   axis_sums[b][g][6]  sums of dx, dy, dz, dx^2, dy^2, dz^2
+ *   count[b][g]         number of (member, time pair) terms */
+amdat_status amdat_disp_bins_axes_run(amdat_ctx* ctx, int32_t list, int32_t bins, int32_t persistent,
+                                      int32_t out_flags, double* axis_sums, int64_t* count);
 
 /* Prepared displacement runs (many lists, one persistent launch).  A plan
  * builds its item tables on the device once; amdat_disp_plan_run is then pure

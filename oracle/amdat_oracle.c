@@ -1003,18 +1003,31 @@ void orc_sk_grad(const float* r, int32_t n_atoms, const int32_t* list, int32_t n
 /* sibling displacement analyses                                             */
 /* ------------------------------------------------------------------------- */
 
-void orc_msd2d(const orc_scheme* s, const float* u, int32_t n_atoms, const int32_t* list,
-               int32_t n_list, int32_t plane, int32_t mode, double* msd) {
+/* Mean_Square_Displacement_2D (src/mean_square_displacement_2d.cpp:79-199) and
+ * Mean_Displacement (src/mean_displacement.cpp:149-199) over a (possibly
+ * time-dependent) list: weighting += members at t0 */
+static void msd2d_core(const orc_scheme* s, const float* u, int32_t n_atoms, const int32_t* list,
+                       int32_t n_list, int32_t plane, int32_t mode, const member_t* f, double* msd) {
   const int G = orc_n_timegaps(s);
   const int ca = plane == 2 ? 1 : 0, cb = plane == 0 ? 1 : 2;
   pairs_t p = make_pairs(s, 0, 0); /* analyze(): displacement_list(this) with fullblock false */
   int64_t* w = (int64_t*)calloc(G, sizeof(int64_t));
+  if (f && f->persistent) {
+    /* Bin_Dynamics_Analysis never calls analyze(), which would zero the weighting:
+     * it starts from initialize()'s system->timegap_weighting() (fullblock default 1,
+     * src/mean_square_displacement_2d.cpp:116) and the member counts add to that */
+    int32_t* tw = (int32_t*)malloc(sizeof(int32_t) * G);
+    orc_timegap_weighting(s, 1, tw);
+    for (int g = 0; g < G; ++g) w[g] = tw[g];
+    free(tw);
+  }
   if (mode == ORC_REF32) {
     float* m = (float*)calloc(G, sizeof(float));
     for (int64_t i = 0; i < p.n; ++i) {
       int g = p.gap[i];
-      w[g] += n_list;
       for (int j = 0; j < n_list; ++j) {
+        if (!is_member(f, n_atoms, list[j], p.t0[i], p.t1[i])) continue;
+        ++w[g];
         float a = POS(u, p.t1[i], list[j], ca) - POS(u, p.t0[i], list[j], ca);
         float b = POS(u, p.t1[i], list[j], cb) - POS(u, p.t0[i], list[j], cb);
         float d = sqrtf(a * a + b * b);
@@ -1027,8 +1040,9 @@ void orc_msd2d(const orc_scheme* s, const float* u, int32_t n_atoms, const int32
     double* m = (double*)calloc(G, sizeof(double));
     for (int64_t i = 0; i < p.n; ++i) {
       int g = p.gap[i];
-      w[g] += n_list;
       for (int j = 0; j < n_list; ++j) {
+        if (!is_member(f, n_atoms, list[j], p.t0[i], p.t1[i])) continue;
+        ++w[g];
         double a = (double)POS(u, p.t1[i], list[j], ca) - (double)POS(u, p.t0[i], list[j], ca);
         double b = (double)POS(u, p.t1[i], list[j], cb) - (double)POS(u, p.t0[i], list[j], cb);
         m[g] += a * a + b * b;
@@ -1041,8 +1055,13 @@ void orc_msd2d(const orc_scheme* s, const float* u, int32_t n_atoms, const int32
   free_pairs(&p);
 }
 
-void orc_mean_disp(const orc_scheme* s, const float* u, int32_t n_atoms, const int32_t* list,
-                   int32_t n_list, int32_t mode, double* md) {
+void orc_msd2d(const orc_scheme* s, const float* u, int32_t n_atoms, const int32_t* list,
+               int32_t n_list, int32_t plane, int32_t mode, double* msd) {
+  msd2d_core(s, u, n_atoms, list, n_list, plane, mode, NULL, msd);
+}
+
+static void mean_disp_core(const orc_scheme* s, const float* u, int32_t n_atoms, const int32_t* list,
+                           int32_t n_list, int32_t mode, const member_t* f, double* md) {
   const int G = orc_n_timegaps(s);
   pairs_t p = make_pairs(s, 0, 0);
   int64_t* w = (int64_t*)calloc(G, sizeof(int64_t));
@@ -1050,9 +1069,11 @@ void orc_mean_disp(const orc_scheme* s, const float* u, int32_t n_atoms, const i
     float* m = (float*)calloc((size_t)G * 3, sizeof(float));
     for (int64_t i = 0; i < p.n; ++i) {
       int g = p.gap[i];
-      w[g] += n_list;
-      for (int j = 0; j < n_list; ++j)
+      for (int j = 0; j < n_list; ++j) {
+        if (!is_member(f, n_atoms, list[j], p.t0[i], p.t1[i])) continue;
+        ++w[g];
         for (int c = 0; c < 3; ++c) m[3 * g + c] += POS(u, p.t1[i], list[j], c) - POS(u, p.t0[i], list[j], c);
+      }
     }
     for (int g = 0; g < G; ++g)
       for (int c = 0; c < 3; ++c) md[3 * g + c] = m[3 * g + c] / (float)w[g];
@@ -1061,10 +1082,12 @@ void orc_mean_disp(const orc_scheme* s, const float* u, int32_t n_atoms, const i
     double* m = (double*)calloc((size_t)G * 3, sizeof(double));
     for (int64_t i = 0; i < p.n; ++i) {
       int g = p.gap[i];
-      w[g] += n_list;
-      for (int j = 0; j < n_list; ++j)
+      for (int j = 0; j < n_list; ++j) {
+        if (!is_member(f, n_atoms, list[j], p.t0[i], p.t1[i])) continue;
+        ++w[g];
         for (int c = 0; c < 3; ++c)
           m[3 * g + c] += (double)POS(u, p.t1[i], list[j], c) - (double)POS(u, p.t0[i], list[j], c);
+      }
     }
     for (int g = 0; g < G; ++g)
       for (int c = 0; c < 3; ++c) md[3 * g + c] = m[3 * g + c] / (double)w[g];
@@ -1072,6 +1095,31 @@ void orc_mean_disp(const orc_scheme* s, const float* u, int32_t n_atoms, const i
   }
   free(w);
   free_pairs(&p);
+}
+
+void orc_mean_disp(const orc_scheme* s, const float* u, int32_t n_atoms, const int32_t* list,
+                   int32_t n_list, int32_t mode, double* md) {
+  mean_disp_core(s, u, n_atoms, list, n_list, mode, NULL, md);
+}
+
+void orc_msd2d_bins(const orc_scheme* s, const float* u, int32_t n_atoms, const int32_t* list, int32_t n_list,
+                    int32_t plane, const int32_t* bins, int32_t n_bins, int32_t persistent, int32_t mode,
+                    double* msd) {
+  int G = orc_n_timegaps(s);
+  for (int b = 0; b < n_bins; ++b) {
+    member_t f = {bins, b, persistent};
+    msd2d_core(s, u, n_atoms, list, n_list, plane, mode, &f, msd + (size_t)b * G);
+  }
+}
+
+void orc_mean_disp_bins(const orc_scheme* s, const float* u, int32_t n_atoms, const int32_t* list,
+                        int32_t n_list, const int32_t* bins, int32_t n_bins, int32_t persistent, int32_t mode,
+                        double* md) {
+  int G = orc_n_timegaps(s);
+  for (int b = 0; b < n_bins; ++b) {
+    member_t f = {bins, b, persistent};
+    mean_disp_core(s, u, n_atoms, list, n_list, mode, &f, md + (size_t)b * G * 3);
+  }
 }
 
 void orc_u2dist(const orc_scheme* s, const float* u, int32_t n_atoms, const int32_t* list,

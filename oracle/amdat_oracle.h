@@ -80,6 +80,12 @@ void orc_isfs_bins(const orc_scheme* s, int32_t fullblock, const float* unwrappe
 void orc_ngp_bins(const orc_scheme* s, const float* unwrapped, int32_t n_atoms, const int32_t* list,
                   int32_t n_list, const int32_t* bins, int32_t n_bins, int32_t persistent, int32_t mode,
                   double* ngp);
+void orc_msd2d_bins(const orc_scheme* s, const float* unwrapped, int32_t n_atoms, const int32_t* list,
+                    int32_t n_list, int32_t plane, const int32_t* bins, int32_t n_bins, int32_t persistent,
+                    int32_t mode, double* msd);
+void orc_mean_disp_bins(const orc_scheme* s, const float* unwrapped, int32_t n_atoms, const int32_t* list,
+                        int32_t n_list, const int32_t* bins, int32_t n_bins, int32_t persistent, int32_t mode,
+                        double* md);
 void orc_fast_particles(const orc_scheme* s, const float* unwrapped, int32_t n_atoms, const int32_t* list,
                         int32_t n_list, int32_t gap, float min_u2, int32_t* fast, int32_t* bins);
 /* Van_Hove_Self (van_hove_self.cpp:82-103, space_time_correlation_function.cpp:216,345):

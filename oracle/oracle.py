@@ -198,6 +198,28 @@ def ngp_bins(s, unwrapped, lst, bins, n_bins, persistent=0, mode=F64):
     return out
 
 
+def msd2d_bins(s, unwrapped, lst, plane, bins, n_bins, persistent=0, mode=F64):
+    """Per-bin Mean_Square_Displacement_2D [bins][gaps] (plane 0 = xy, 1 = xz, 2 = yz)."""
+    u = _f32(unwrapped)
+    lst = _i32(lst)
+    b = _i32(bins)
+    out = np.zeros((n_bins, n_timegaps(s)))
+    lib().orc_msd2d_bins(C.byref(s), _p(u), u.shape[1], _p(lst), len(lst), int(plane), _p(b), int(n_bins),
+                         int(persistent), mode, _p(out))
+    return out
+
+
+def mean_disp_bins(s, unwrapped, lst, bins, n_bins, persistent=0, mode=F64):
+    """Per-bin Mean_Displacement [bins][gaps][3]."""
+    u = _f32(unwrapped)
+    lst = _i32(lst)
+    b = _i32(bins)
+    out = np.zeros((n_bins, n_timegaps(s), 3))
+    lib().orc_mean_disp_bins(C.byref(s), _p(u), u.shape[1], _p(lst), len(lst), _p(b), int(n_bins),
+                             int(persistent), mode, _p(out))
+    return out
+
+
 def fast_particles(s, unwrapped, lst, gap, min_u2):
     """Fast_Particles: (fast [blocks][atoms] 0/1, membership map [frames][atoms] 0/-1)."""
     u = _f32(unwrapped)

@@ -211,6 +211,30 @@ bin_list cells b
 isfs ./isfs_cells.dat 7 7 xyz 0 1
 bin_list cells all
 """),
+    # msd_2d and mean_displacement per bin (static and persistent) and of a
+    # fast-particle list
+    "bins_axes": dict(
+        n=260, box=6.0, sigma=0.25, seed=121, fractions=(0.6, 0.4), mobility=(1.0, 3.0),
+        scheme=synth.TimeScheme.exponential(3, 6, 1.4, 0, 0, 0.01),
+        commands="""create_list all
+all
+create_list b
+type_system 2
+create_bin_list slabs
+all 1 2 2
+msd_2d ./msd2d_slabs.dat xy
+bin_list slabs all
+mean_displacement ./md_slabs.dat
+bin_list slabs b 1
+msd_2d ./msd2d_p.dat yz
+bin_list slabs all 1
+find_fast_fixedthreshold quick ./quick.dat 5 0.02
+list all
+mean_displacement ./md_quick.dat
+list quick
+msd_2d ./msd2d_quick.dat xz
+list quick
+"""),
     # a two-mobility mixture: self van Hove vs its Gaussian (compare_gaussian), the
     # fast particles per block (find_fast, find_fast_fixedthreshold) and analyses
     # of those time-dependent lists

@@ -192,6 +192,13 @@ class OracleRun:
             kv, off = self.shells(m0, m1)
             corr = orc.isfs_bins(s, self.unwrapped, allat, kv, off, float(sp), L, td["bins"], 1, fb, 0, self.mode)
             self.files[self.name(a[1])] = self.correlation_2d(sp, m0, m1, corr[0], s)
+        elif cmd == "msd_2d":
+            plane = {"xy": 0, "xz": 1, "yz": 2}[a[2]]
+            m = orc.msd2d_bins(s, self.unwrapped, allat, plane, td["bins"], 1, 0, self.mode)
+            self.files[self.name(a[1])] = self.msd2d_text(a[2], m[0], s)
+        elif cmd == "mean_displacement":
+            md = orc.mean_disp_bins(s, self.unwrapped, allat, td["bins"], 1, 0, self.mode)
+            self.files[self.name(a[1])] = self.md_text(md[0], s)
         else:
             raise ValueError(cmd)
 
@@ -255,10 +262,28 @@ class OracleRun:
             corr = orc.isfs_bins(s, self.unwrapped, lst, kv, off, float(sp), L, spec["bins"], B, fb,
                                  int(persist), self.mode)
             texts = [self.correlation_2d(sp, m0, m1, corr[b], s) for b in range(B)]
+        elif cmd == "msd_2d":
+            plane = {"xy": 0, "xz": 1, "yz": 2}[a[2]]
+            m = orc.msd2d_bins(s, self.unwrapped, lst, plane, spec["bins"], B, int(persist), self.mode)
+            texts = [self.msd2d_text(a[2], m[b], s) for b in range(B)]
+        elif cmd == "mean_displacement":
+            md = orc.mean_disp_bins(s, self.unwrapped, lst, spec["bins"], B, int(persist), self.mode)
+            texts = [self.md_text(md[b], s) for b in range(B)]
         else:
             raise ValueError(cmd)
         for b, name in self.bin_names(self.name(a[1]), n, "." if persist else "_"):
             self.files[name] = texts[b]
+
+    def msd2d_text(self, plane, m, s):
+        t = self.times(s)
+        txt = f"2-D mean square displacement data for {plane} plane created by AMDAT v.{VERSION}\n"
+        return txt + "".join(f"{fmt(t[g])}\t{fmt(f32(m[g]))}\n" for g in range(len(t)))
+
+    def md_text(self, md, s):
+        t = self.times(s)
+        txt = f"Mean displacement data created by AMDAT v.{VERSION}\n"
+        return txt + "".join(f"{fmt(t[g])}\t" + "\t".join(fmt(f32(v)) for v in md[g]) + "\n"
+                             for g in range(len(t)))
 
     def msd_text(self, m, s):
         t = self.times(s)
@@ -382,19 +407,12 @@ class OracleRun:
         plane = {"xy": 0, "xz": 1, "yz": 2}[a[2]]
         s = self.scheme()
         m = orc.msd2d(s, self.unwrapped, lst, plane, self.mode)
-        t = self.times(s)
-        txt = f"2-D mean square displacement data for {a[2]} plane created by AMDAT v.{VERSION}\n"
-        txt += "".join(f"{fmt(t[g])}\t{fmt(f32(m[g]))}\n" for g in range(len(t)))
-        self.files[self.name(a[1])] = txt
+        self.files[self.name(a[1])] = self.msd2d_text(a[2], m, s)
 
     def cmd_mean_displacement(self, a, lst):
         s = self.scheme()
         md = orc.mean_disp(s, self.unwrapped, lst, self.mode)
-        t = self.times(s)
-        txt = f"Mean displacement data created by AMDAT v.{VERSION}\n"
-        txt += "".join(f"{fmt(t[g])}\t" + "\t".join(fmt(f32(v)) for v in md[g]) + "\n"
-                       for g in range(len(t)))
-        self.files[self.name(a[1])] = txt
+        self.files[self.name(a[1])] = self.md_text(md, s)
 
     def _u2(self, lst, bins, maxvalue, gap):
         s = self.scheme()

@@ -227,3 +227,31 @@ def test_bins_edge_cases(eng):
     assert (m == -1).all()
     assert eng.disp_bins(0, h, 1)["count"].shape == (1, G)
     eng.bins_free(h)
+
+
+@pytest.mark.parametrize("persistent", [0, 1])
+def test_disp_bins_axes_match_oracle(eng, persistent):
+    """Per-bin axis sums (msd_2d, mean_displacement) against the FP64 oracle."""
+    traj, _, _ = load("bins_axes")
+    eng.upload(traj.unwrapped, traj.box, traj.box_lo, wrapped=traj.wrapped())
+    eng.set_scheme(traj.scheme)
+    lo, hi = _bounds(traj)
+    nb = (1, 2, 2)
+    B = 4
+    eng.boxify(lo, hi)
+    h = eng.bins_create(nb, lo, hi)
+    bins = orc.assign_bins(orc.boxify(traj.wrapped(), lo, hi), nb, lo, hi)
+    s = orc.scheme(traj.scheme)
+    lst = np.arange(traj.n_atoms, dtype=np.int32)
+    out = eng.disp_bins_axes(0, h, B, persistent)
+    cnt = out["count"]
+    m = cnt > 0
+    md = orc.mean_disp_bins(s, traj.unwrapped, lst, bins, B, persistent, orc.F64)
+    got_md = out["axis_sums"][..., :3][m] / cnt[m][:, None]
+    scale = np.abs(md[m]).max()
+    assert np.abs(got_md - md[m]).max() <= 1e-6 * scale + 1e-12
+    if not persistent:  # the oracle's persistent msd_2d carries the reference's weighting offset
+        m2 = orc.msd2d_bins(s, traj.unwrapped, lst, 0, bins, B, 0, orc.F64)
+        got2 = (out["axis_sums"][..., 3] + out["axis_sums"][..., 4])[m] / cnt[m]
+        np.testing.assert_allclose(got2, m2[m], rtol=1e-6, atol=1e-12)
+    eng.bins_free(h)

@@ -86,7 +86,7 @@ def test_cli_bin_list_errors(tmp_path, engine_mod, qvectors):
     r = run_cli(traj, base + "msd ./m.dat\nbin_list nothere all\n", str(tmp_path))
     assert r.returncode == 1 and "Binned Trajectory list 'nothere' not found." in r.stderr
     r = run_cli(traj, base + "create_bin_list x\nall 1 1 2\nvhs ./v.dat 1.0 10\nbin_list x all\n", str(tmp_path))
-    assert r.returncode == 1 and "supported for msd, ngp and isfs" in r.stderr
+    assert r.returncode == 1 and "are supported for msd" in r.stderr
     r = run_cli(traj, base + "create_bin_list x\nall 1 1 2\nmsd ./m.dat\nbin_list x all 1\n", str(tmp_path))
     assert r.returncode == 0, r.stderr
     assert sorted(p.name for p in tmp_path.glob("m.dat_bin_*")) == ["m.dat_bin_0.0.0.bindata",
