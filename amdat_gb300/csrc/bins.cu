@@ -275,6 +275,16 @@ __global__ void fast_map_kernel(const unsigned char* __restrict__ fast, int64_t 
   }
 }
 
+// members of each frame (CSR) -> one-bin map: bins[t][atom] = 0 for members
+__global__ void timelist_map_kernel(const int32_t* __restrict__ offsets, const int32_t* __restrict__ idx,
+                                    int32_t n_frames, int64_t n_pad, int32_t* __restrict__ bins) {
+  const int t = blockIdx.y;
+  if (t >= n_frames) return;
+  for (int32_t e = offsets[t] + blockIdx.x * blockDim.x + threadIdx.x; e < offsets[t + 1];
+       e += gridDim.x * blockDim.x)
+    bins[(int64_t)t * n_pad + idx[e]] = 0;
+}
+
 static BinMap& bin_map(amdat_ctx* ctx, int32_t handle) {
   auto it = ctx->bin_maps.find(handle);
   if (it == ctx->bin_maps.end()) throw Error(AMDAT_ERR_ARGUMENT, "unknown bin map handle");
@@ -378,6 +388,45 @@ amdat_status amdat_fast_particles(amdat_ctx* ctx, int32_t list, int32_t gap, flo
         fast_map_kernel<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(fast, ctx->n_pad, ctx->n_atoms, n, frt, K,
                                                                     n_blocks, m->bin.ptr);
         check_launch("fast_map_kernel");
+        count_launch(ctx);
+      }
+      AMDAT_CUDA(cudaStreamSynchronize(ctx->stream));
+    } catch (...) {
+      delete m;
+      throw;
+    }
+    const int32_t h = ctx->next_bins++;
+    ctx->bin_maps[h] = m;
+    *handle = h;
+  });
+}
+
+amdat_status amdat_timelist_create(amdat_ctx* ctx, const int32_t* frame_offsets, const int32_t* atom_idx,
+                                   int32_t* handle) {
+  return guarded([&] {
+    check_ctx(ctx);
+    if (!ctx->have_traj) throw Error(AMDAT_ERR_STATE, "no trajectory uploaded");
+    AMDAT_REQUIRE(frame_offsets && handle, "null argument");
+    const int T = ctx->n_frames;
+    AMDAT_REQUIRE(T <= 65535, "at most 65535 frames");
+    AMDAT_REQUIRE(frame_offsets[0] == 0, "frame_offsets[0] must be 0");
+    for (int t = 0; t < T; ++t) AMDAT_REQUIRE(frame_offsets[t + 1] >= frame_offsets[t], "frame offsets must ascend");
+    const int64_t n = frame_offsets[T];
+    AMDAT_REQUIRE(n == 0 || atom_idx, "null atom indices");
+    for (int64_t e = 0; e < n; ++e)
+      AMDAT_REQUIRE(atom_idx[e] >= 0 && atom_idx[e] < ctx->n_atoms, "atom index out of range");
+    auto* m = new BinMap();
+    try {
+      m->nx = m->ny = m->nz = 1;
+      m->n_frames = T, m->n_pad = ctx->n_pad;
+      m->bin.reserve((size_t)T * ctx->n_pad);
+      AMDAT_CUDA(cudaMemsetAsync(m->bin.ptr, 0xff, (size_t)T * ctx->n_pad * 4, ctx->stream));
+      if (n > 0) {
+        int32_t* d = reinterpret_cast<int32_t*>(ctx->scratch.reserve((size_t)(T + 1 + n) * 4));
+        AMDAT_CUDA(cudaMemcpyAsync(d, frame_offsets, (size_t)(T + 1) * 4, cudaMemcpyHostToDevice, ctx->stream));
+        AMDAT_CUDA(cudaMemcpyAsync(d + T + 1, atom_idx, (size_t)n * 4, cudaMemcpyHostToDevice, ctx->stream));
+        timelist_map_kernel<<<dim3(8, (unsigned)T), 256, 0, ctx->stream>>>(d, d + T + 1, T, ctx->n_pad, m->bin.ptr);
+        check_launch("timelist_map_kernel");
         count_launch(ctx);
       }
       AMDAT_CUDA(cudaStreamSynchronize(ctx->stream));

@@ -56,7 +56,7 @@ EXPORTED = [
     "amdat_gsmooth_run", "amdat_disp_axes_run",
     "amdat_gsmooth_adjoint", "amdat_structure_factor_adjoint",
     "amdat_boxify", "amdat_bins_create", "amdat_bins_read", "amdat_bins_free",
-    "amdat_disp_bins_run", "amdat_disp_bins_axes_run", "amdat_fast_particles",
+    "amdat_disp_bins_run", "amdat_disp_bins_axes_run", "amdat_fast_particles", "amdat_timelist_create",
 ]
 
 PLAN_AUTOTUNE, PLAN_GRAPH, PLAN_NO_SHARING = 1, 2, 4
@@ -349,6 +349,15 @@ class Engine:
         """Block-wise fast-particle membership as a one-bin map (amdat_fast_particles)."""
         h = C.c_int32()
         _check(lib().amdat_fast_particles(self._ctx, int(list_h), int(gap), C.c_float(min_u2), C.byref(h)))
+        return h.value
+
+    def timelist(self, members_per_frame) -> int:
+        """Time-dependent list from the members of each frame (amdat_timelist_create)."""
+        off = np.concatenate([[0], np.cumsum([len(m) for m in members_per_frame])]).astype(np.int32)
+        idx = (np.concatenate([np.asarray(m, np.int32) for m in members_per_frame])
+               if off[-1] else np.zeros(1, np.int32)).astype(np.int32)
+        h = C.c_int32()
+        _check(lib().amdat_timelist_create(self._ctx, _p(off), _p(idx), C.byref(h)))
         return h.value
 
     def bins_free(self, handle):

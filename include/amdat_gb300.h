@@ -230,6 +230,17 @@ amdat_status amdat_bins_free(amdat_ctx* ctx, int32_t handle);
  * amdat_bins_read for the members per frame; free it with amdat_bins_free. */
 amdat_status amdat_fast_particles(amdat_ctx* ctx, int32_t list, int32_t gap, float min_u2, int32_t* handle);
 
+/* A time-dependent list (Trajectory_List with membership per internal time,
+ * src/trajectory_list.h:25,58; the analyses iterate the members of the start
+ * frame t0, src/trajectory_list.cpp:191-222): the members of frame t are
+ * atom_idx[frame_offsets[t] .. frame_offsets[t + 1]) (CSR over the trajectory's
+ * frames; order and repeats do not matter).  Returns a one-bin map handle: bin 0
+ * holds each frame's members, for amdat_disp_bins_run / amdat_disp_bins_axes_run
+ * (persistent 0: members at t0; 1: members at t0 and t1), amdat_bins_read and
+ * amdat_bins_free. */
+amdat_status amdat_timelist_create(amdat_ctx* ctx, const int32_t* frame_offsets, const int32_t* atom_idx,
+                                   int32_t* handle);
+
 /* MSD and NGP moments and F_s of every bin in one pass: the target line "bin_list <bins>
  * <list> [persistence]" of Control::run_analysis (src/control.h:268-380).
  * persistent = 0: Bin_Static_Analysis (src/bin_static_analysis.h:69-111), the

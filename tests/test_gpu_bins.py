@@ -255,3 +255,31 @@ def test_disp_bins_axes_match_oracle(eng, persistent):
         got2 = (out["axis_sums"][..., 3] + out["axis_sums"][..., 4])[m] / cnt[m]
         np.testing.assert_allclose(got2, m2[m], rtol=1e-6, atol=1e-12)
     eng.bins_free(h)
+
+
+def test_timelist_matches_oracle(eng):
+    """A time-dependent list given as per-frame members (CSR): msd and the member
+    counts against the oracle on the same membership, static and persistent."""
+    traj, _, _ = load("bins")
+    eng.upload(traj.unwrapped, traj.box, traj.box_lo)
+    eng.set_scheme(traj.scheme)
+    rng = np.random.default_rng(3)
+    T, N = traj.n_frames, traj.n_atoms
+    members = [np.sort(rng.choice(N, size=rng.integers(0, N // 2), replace=False)) for _ in range(T)]
+    members[2] = np.zeros(0, np.int64)  # a frame without members
+    h = eng.timelist(members)
+    got, counts = eng.bins_read(h, T, N, 1)
+    ref = -np.ones((T, N), np.int32)
+    for t, m in enumerate(members):
+        ref[t, m] = 0
+    np.testing.assert_array_equal(got, ref)
+    np.testing.assert_array_equal(counts[:, 0], [len(m) for m in members])
+    s = orc.scheme(traj.scheme)
+    allat = np.arange(N, dtype=np.int32)
+    for persistent in (0, 1):
+        out = eng.disp_bins(0, h, 1, persistent=persistent)
+        msd, w = orc.msd_bins(s, traj.unwrapped, allat, ref, 1, persistent, orc.F64)
+        np.testing.assert_array_equal(out["count"][0], w[0].astype(np.int64))
+        m = out["count"][0] > 0
+        np.testing.assert_allclose(out["sum_d2"][0][m] / out["count"][0][m], msd[0][m], rtol=1e-6, atol=1e-12)
+    eng.bins_free(h)
