@@ -456,7 +456,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--frames", type=int, default=400, help="frames of the headline workload")
-    ap.add_argument("--only", default="", choices=["", "isf", "msd", "batched", "pairs", "structure", "cli"],
+    ap.add_argument("--only", default="", choices=["", "isf", "msd", "batched", "pairs", "structure", "cli",
+                                                   "perlist"],
                     help="run one workload only (profiling)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     args = ap.parse_args()
@@ -634,6 +635,23 @@ def main():
         result["msd"] = dict(value=job_rate(munits, world, mms), ms=mms, kernel_ms=ms_d / max(n_d, 1),
                              plain=mplain, npairs=npairs, nvec=len(shell),
                              plan_value=job_rate(munits, world, pms), plan_ms=pms)
+
+    if args.only == "perlist":
+        # profiling aid: the batched workload's per-list MSD + NGP plan alone
+        btraj, bscheme, sizes, perm = batched_workload()
+        eng.upload(btraj.unwrapped[:, perm], btraj.box)
+        eng.set_scheme(bscheme)
+        nested = [eng.list(np.arange(n, dtype=np.int32)) for n in sizes]
+        plan = eng.plan(nested, flags=E.PLAN_AUTOTUNE | E.PLAN_NO_SHARING)
+        for _ in range(args.warmup):
+            plan.run()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            plan.run()
+        torch.cuda.synchronize()
+        result["perlist"] = dict(ms=1e3 * (time.perf_counter() - t0) / max(args.steps, 1), info=plan.info())
+        plan.close()
 
     if args.only in ("", "batched"):
         btraj, bscheme, sizes, perm = batched_workload()
@@ -930,6 +948,8 @@ def main():
                     "counted_pairs_in_range": q["rdf_total"]},
             "vhs": {"value": q["gs_rate"], "unit": "atom·time-pairs/s", "ms_per_step": q["gs_ms"]},
             "vhd": {"value": q["gd_rate"], "unit": "ordered pairs/s", "ms_per_step": q["gd_ms"]}}
+    if "perlist" in result:
+        line["perlist"] = result["perlist"]
     if "structure" in result:
         line["structure"] = result["structure"]
         if "value" not in line:
