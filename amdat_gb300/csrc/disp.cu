@@ -121,7 +121,34 @@ __global__ void __launch_bounds__(MODE == 0 ? DISP_THREADS : FS_THREADS)
 #pragma unroll
     for (int s = 0; s < MAX_FS; ++s) fs[s] = KSum{0.f, 0.f};
 
-    for (int a = it.a0 + tid; a < it.a1; a += nthr) {
+    int a_start = it.a0 + tid;
+    if (MODE == 0 && !GS) {
+      // MSD-only passes are load-latency bound: MSD_BATCH atoms' six loads each
+      // are issued before any of them is used
+      constexpr int MSD_BATCH = 4;  // 8 costs occupancy (registers) and is slower
+      for (; a_start + (MSD_BATCH - 1) * nthr < it.a1; a_start += MSD_BATCH * nthr) {
+        int at[MSD_BATCH];
+#pragma unroll
+        for (int k = 0; k < MSD_BATCH; ++k)
+          at[k] = L.idx ? __ldg(L.idx + a_start + k * nthr) : L.first + a_start + k * nthr;
+        float d[MSD_BATCH][3];
+#pragma unroll
+        for (int k = 0; k < MSD_BATCH; ++k) {
+          d[k][0] = __fsub_rn(__ldg(X1 + at[k]), __ldg(X0 + at[k]));
+          d[k][1] = __fsub_rn(__ldg(X1 + p.n_pad + at[k]), __ldg(X0 + p.n_pad + at[k]));
+          d[k][2] = __fsub_rn(__ldg(X1 + 2 * p.n_pad + at[k]), __ldg(X0 + 2 * p.n_pad + at[k]));
+        }
+        if (p.want_moments) {
+#pragma unroll
+          for (int k = 0; k < MSD_BATCH; ++k) {
+            const float d2 = fmaf(d[k][2], d[k][2], fmaf(d[k][1], d[k][1], d[k][0] * d[k][0]));
+            kadd(m2, d2);
+            kadd(m4, d2 * d2);
+          }
+        }
+      }
+    }
+    for (int a = a_start; a < it.a1; a += nthr) {
       const int atom = L.idx ? __ldg(L.idx + a) : L.first + a;
       const float dx = __fsub_rn(__ldg(X1 + atom), __ldg(X0 + atom));
       const float dy = __fsub_rn(__ldg(X1 + p.n_pad + atom), __ldg(X0 + p.n_pad + atom));
