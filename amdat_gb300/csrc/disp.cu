@@ -93,7 +93,7 @@ template <int MODE, bool GS>
 __global__ void __launch_bounds__(MODE == 0 ? DISP_THREADS : FS_THREADS)
     disp_mixed_kernel(DispParams p) {
   extern __shared__ float smem[];
-  __shared__ int s_item;
+  __shared__ int s_item[2];  // the item being processed and the next one (fetched ahead)
   __shared__ KSum s_red[(MODE == 0 ? DISP_THREADS : FS_THREADS) / 32][2 + MAX_FS];
   unsigned int* hist = reinterpret_cast<unsigned int*>(smem);  // [n_bins] when GS
   float* tab = smem + (GS ? ((p.n_bins + 3) & ~3) : 0);         // octant tables
@@ -101,11 +101,15 @@ __global__ void __launch_bounds__(MODE == 0 ? DISP_THREADS : FS_THREADS)
   const int lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
   const int n_fs = MODE ? p.n_fs : 0;
 
-  for (;;) {
-    if (tid == 0) s_item = atomicAdd(p.counter, 1);
-    __syncthreads();
-    const int slot = s_item;
+  // the next item's index is fetched from the work counter while the current
+  // one is processed (two slots: slot i & 1 is read after the barrier that ends
+  // item i - 1, and written again only after the barriers inside item i + 1)
+  if (tid == 0) s_item[0] = atomicAdd(p.counter, 1);
+  __syncthreads();
+  for (int iter = 0;; ++iter) {
+    const int slot = s_item[iter & 1];
     if (slot >= p.n_items) break;
+    if (tid == 0) s_item[(iter + 1) & 1] = atomicAdd(p.counter, 1);
     const int item = p.schedule ? __ldg(p.schedule + slot) : slot;
     const DispItem it = p.items[item];
     const ListDev L = p.lists[it.list];
