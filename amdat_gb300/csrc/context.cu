@@ -437,6 +437,7 @@ amdat_status amdat_set_scheme(amdat_ctx* ctx, const amdat_scheme* s) {
     scheme_check(*s);
     ctx->scheme = *s;
     ctx->have_scheme = true;
+    ++ctx->scheme_serial;
     for (auto& kv : ctx->pair_cache) delete kv.second;
     ctx->pair_cache.clear();
   });

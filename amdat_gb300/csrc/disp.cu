@@ -60,17 +60,26 @@ struct ListDev {
   const int32_t* idx;  // nullptr: members are atoms first..first+n-1
 };
 
+// One item as the kernel reads it, stored in processing order: everything a
+// block needs to start streaming in one 48-byte record, so a single read (not
+// a chain of dependent table reads) precedes an item's loads.
+struct alignas(16) DispDesc {
+  int32_t item;    // row of the item's partials
+  int32_t unit;    // work-unit slot (G_s output row)
+  int32_t a0, a1;  // member range [a0, a1)
+  int32_t t0, t1, gap;
+  int32_t first;        // members are first + a when idx is null
+  const int32_t* idx;   // member atom indexes, or null
+  int64_t reserved;
+};
+static_assert(sizeof(DispDesc) == 48, "descriptor layout");
+
 struct DispParams {
   const float* u;
   int64_t n_pad;
-  const int32_t* t0;
-  const int32_t* t1;
-  const int32_t* gap;
-  const DispItem* items;
+  const DispDesc* desc;  // [n_items], processing order
   int32_t n_items;
-  const ListDev* lists;
   int32_t* counter;
-  const int32_t* schedule;  // processing order of items (locality), nullptr = table order
   double* part;  // [n_items][n_out]
   int32_t n_out;
   int32_t want_moments;
@@ -93,7 +102,7 @@ template <int MODE, bool GS>
 __global__ void __launch_bounds__(MODE == 0 ? DISP_THREADS : FS_THREADS)
     disp_mixed_kernel(DispParams p) {
   extern __shared__ float smem[];
-  __shared__ int s_item[2];  // the item being processed and the next one (fetched ahead)
+  __shared__ int s_item[2];  // counter slots of the item being processed and the next one
   __shared__ KSum s_red[(MODE == 0 ? DISP_THREADS : FS_THREADS) / 32][2 + MAX_FS];
   unsigned int* hist = reinterpret_cast<unsigned int*>(smem);  // [n_bins] when GS
   float* tab = smem + (GS ? ((p.n_bins + 3) & ~3) : 0);         // octant tables
@@ -101,21 +110,21 @@ __global__ void __launch_bounds__(MODE == 0 ? DISP_THREADS : FS_THREADS)
   const int lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
   const int n_fs = MODE ? p.n_fs : 0;
 
-  // the next item's index is fetched from the work counter while the current
-  // one is processed (two slots: slot i & 1 is read after the barrier that ends
-  // item i - 1, and written again only after the barriers inside item i + 1)
+  // the next item's counter slot is fetched while the current item is
+  // processed (two slots: slot i & 1 is read after the barrier that ends item
+  // i - 1 and written again only after the barriers inside item i + 1); the
+  // item itself is one descriptor read
   if (tid == 0) s_item[0] = atomicAdd(p.counter, 1);
   __syncthreads();
   for (int iter = 0;; ++iter) {
     const int slot = s_item[iter & 1];
     if (slot >= p.n_items) break;
     if (tid == 0) s_item[(iter + 1) & 1] = atomicAdd(p.counter, 1);
-    const int item = p.schedule ? __ldg(p.schedule + slot) : slot;
-    const DispItem it = p.items[item];
-    const ListDev L = p.lists[it.list];
-    const int t0 = p.t0[it.pair], t1 = p.t1[it.pair], g = p.gap[it.pair];
-    const float* X0 = p.u + (int64_t)t0 * 3 * p.n_pad;
-    const float* X1 = p.u + (int64_t)t1 * 3 * p.n_pad;
+    const DispDesc it = p.desc[slot];
+    const int item = it.item, g = it.gap;
+    const ListDev L{0, it.first, it.idx};
+    const float* X0 = p.u + (int64_t)it.t0 * 3 * p.n_pad;
+    const float* X1 = p.u + (int64_t)it.t1 * 3 * p.n_pad;
     if (GS)
       for (int b = tid; b < p.n_bins; b += nthr) hist[b] = 0u;
     if (GS) __syncthreads();
@@ -244,7 +253,7 @@ __global__ void __launch_bounds__(MODE == 0 ? DISP_THREADS : FS_THREADS)
     }
     if (GS) {
       __syncthreads();
-      unsigned long long* dst = p.gs + ((int64_t)it.list * p.n_gaps + g) * p.n_bins;
+      unsigned long long* dst = p.gs + ((int64_t)it.unit * p.n_gaps + g) * p.n_bins;
       for (int b = tid; b < p.n_bins; b += nthr)
         if (hist[b]) atomicAdd(dst + b, (unsigned long long)hist[b]);
     }
@@ -556,6 +565,7 @@ static void disp_plain(amdat_ctx* ctx, const amdat_disp_request* req, int32_t ou
 struct amdat_disp_plan {
   int n_lists = 0, G = 0, S = 0, NB = 0, n_passes = 1, n_out = 2;
   bool fullblock = false;
+  uint64_t scheme_serial = 0;  // time scheme the descriptors were made for
   float bin_max = 0.f, period = 1.f;
   amdat::ShellSet sh;
   std::vector<int32_t> lsize;
@@ -569,10 +579,10 @@ struct amdat_disp_plan {
   amdat::DevBuf<int32_t> class_idx;       // atoms of gathered classes
   int chunk = 0, blocks_per_sm = 0, n_items = 0;
   double tuned_ms = 0.0;
-  // device: [items | item_first | schedule | units | counters | kv | off | inv | lu_off | lu_units |
+  // device: [descriptors | item_first | counters | kv | off | inv | lu_off | lu_units |
   //          part | unit d2 | d4 | fs | gs | list d2 | d4 | fs | gs]
   amdat::DevBuf<unsigned char> dev;
-  size_t o_items = 0, o_first = 0, o_sched = 0, o_lists = 0, o_counter = 0, o_kv = 0, o_off = 0,
+  size_t o_desc = 0, o_first = 0, o_counter = 0, o_kv = 0, o_off = 0,
          o_inv = 0, o_luo = 0, o_luu = 0, o_part = 0, o_ud2 = 0, o_ud4 = 0, o_ufs = 0, o_ugs = 0,
          o_d2 = 0, o_d4 = 0, o_fs = 0, o_gs = 0, bytes = 0;
   cudaGraph_t graph = nullptr;
@@ -612,16 +622,28 @@ static void plan_tables(amdat_ctx* ctx, amdat_disp_plan& pl, const PairTable& P,
   std::vector<int32_t> sched(items.size());
   for (size_t i = 0; i < sched.size(); ++i) sched[i] = (int32_t)i;
   std::stable_sort(sched.begin(), sched.end(), [&](int32_t a, int32_t b) { return key[a] < key[b]; });
+  // descriptors in processing order (the pair table's frames resolved here)
+  std::vector<int32_t> ht0(P.n_pairs), ht1(P.n_pairs), hgap(P.n_pairs);
+  if (P.n_pairs) {
+    AMDAT_CUDA(cudaMemcpy(ht0.data(), P.t0.ptr, P.n_pairs * 4, cudaMemcpyDeviceToHost));
+    AMDAT_CUDA(cudaMemcpy(ht1.data(), P.t1.ptr, P.n_pairs * 4, cudaMemcpyDeviceToHost));
+    AMDAT_CUDA(cudaMemcpy(hgap.data(), P.gap.ptr, P.n_pairs * 4, cudaMemcpyDeviceToHost));
+  }
+  std::vector<DispDesc> desc(items.size());
+  for (size_t k = 0; k < sched.size(); ++k) {
+    const DispItem& it = items[sched[k]];
+    const ListDev& L = pl.udev[it.list];
+    desc[k] = DispDesc{sched[k], it.list, it.a0, it.a1, ht0[it.pair], ht1[it.pair],
+                       hgap[it.pair], L.first, L.idx, 0};
+  }
   pl.n_items = (int)items.size();
   pl.chunk = chunk;
   pl.blocks_per_sm = blocks_per_sm;
   auto align = [](size_t x) { return (x + 255) & ~(size_t)255; };
   const size_t S1 = (size_t)std::max(pl.S, 1), NB1 = (size_t)std::max(pl.NB, 1);
   size_t o = 0;
-  pl.o_items = o; o = align(o + std::max<size_t>(items.size(), 1) * sizeof(DispItem));
+  pl.o_desc = o; o = align(o + std::max<size_t>(desc.size(), 1) * sizeof(DispDesc));
   pl.o_first = o; o = align(o + item_first.size() * 4);
-  pl.o_sched = o; o = align(o + std::max<size_t>(sched.size(), 1) * 4);
-  pl.o_lists = o; o = align(o + pl.udev.size() * sizeof(ListDev));
   pl.o_counter = o; o = align(o + 4 * (size_t)pl.n_passes);
   pl.o_kv = o; o = align(o + std::max<size_t>(pl.sh.kv.size(), 1) * sizeof(int4));
   pl.o_off = o; o = align(o + std::max<size_t>(pl.sh.off.size(), 1) * 4);
@@ -647,10 +669,8 @@ static void plan_tables(amdat_ctx* ctx, amdat_disp_plan& pl, const PairTable& P,
   pl.bytes = o;
   unsigned char* base = pl.dev.reserve(o);
   std::vector<unsigned char> host(pl.o_part, 0);
-  std::memcpy(host.data() + pl.o_items, items.data(), items.size() * sizeof(DispItem));
+  std::memcpy(host.data() + pl.o_desc, desc.data(), desc.size() * sizeof(DispDesc));
   std::memcpy(host.data() + pl.o_first, item_first.data(), item_first.size() * 4);
-  std::memcpy(host.data() + pl.o_sched, sched.data(), sched.size() * 4);
-  std::memcpy(host.data() + pl.o_lists, pl.udev.data(), pl.udev.size() * sizeof(ListDev));
   if (pl.S) {
     std::memcpy(host.data() + pl.o_kv, pl.sh.kv.data(), pl.sh.kv.size() * sizeof(int4));
     std::memcpy(host.data() + pl.o_off, pl.sh.off.data(), pl.sh.off.size() * 4);
@@ -681,14 +701,9 @@ static void plan_launch(amdat_ctx* ctx, amdat_disp_plan& pl, const PairTable& P)
     DispParams p{};
     p.u = ctx->u.ptr;
     p.n_pad = ctx->n_pad;
-    p.t0 = P.t0.ptr;
-    p.t1 = P.t1.ptr;
-    p.gap = P.gap.ptr;
-    p.items = (const DispItem*)(base + pl.o_items);
+    p.desc = (const DispDesc*)(base + pl.o_desc);
     p.n_items = pl.n_items;
-    p.lists = (const ListDev*)(base + pl.o_lists);
     p.counter = (int32_t*)(base + pl.o_counter) + pass;
-    p.schedule = (const int32_t*)(base + pl.o_sched);
     p.part = (double*)(base + pl.o_part);
     p.n_out = pl.n_out;
     p.want_moments = pass == 0;
@@ -874,6 +889,7 @@ static amdat_disp_plan* plan_create(amdat_ctx* ctx, const amdat_disp_request* re
     pl->S = req->n_shells;
     pl->NB = req->n_bins;
     pl->fullblock = req->fullblock != 0;
+    pl->scheme_serial = ctx->scheme_serial;
     pl->bin_max = req->bin_max;
     pl->period = req->kvec_period;
     if (pl->S) {
@@ -978,6 +994,8 @@ static amdat_disp_plan* plan_create(amdat_ctx* ctx, const amdat_disp_request* re
 
 static void plan_run(amdat_ctx* ctx, amdat_disp_plan* pl) {
   AMDAT_REQUIRE(pl != nullptr, "null plan");
+  if (pl->scheme_serial != ctx->scheme_serial)
+    throw Error(AMDAT_ERR_STATE, "the time scheme changed after the plan was made; make a new plan");
   const PairTable& P = pair_table(ctx, pl->fullblock, false);
   if (pl->exec) {
     KernelTimer kt(ctx, "disp_plan_graph");

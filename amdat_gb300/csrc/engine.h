@@ -162,6 +162,7 @@ struct amdat_ctx {
   std::vector<amdat::ListEntry*> lists;
   amdat_scheme scheme{};
   bool have_scheme = false;
+  uint64_t scheme_serial = 0;  // bumped by every amdat_set_scheme (plans bake pair frames)
   std::map<int, amdat::PairTable*> pair_cache;  // key: fullblock*2 + loop_order
   std::map<int32_t, amdat::Density*> densities;
   int32_t next_density = 1;
