@@ -47,11 +47,13 @@ constexpr int DISP_CHUNK = 4096;  // list members per item
 constexpr int MAX_FS = 8;         // shells per pass
 constexpr int DISP_THREADS = 256;
 constexpr int FS_THREADS = 128;
+constexpr int MAX_PAIRS_PER_ITEM = 64;
 
 struct DispItem {
   int32_t list;  // slot in the launch's list table
-  int32_t pair;
+  int32_t pair;  // first pair; n_pairs consecutive pairs of one gap
   int32_t a0, a1;  // member range [a0, a1) of the list
+  int32_t n_pairs;
 };
 
 struct ListDev {
@@ -70,7 +72,8 @@ struct alignas(16) DispDesc {
   int32_t t0, t1, gap;
   int32_t first;        // members are first + a when idx is null
   const int32_t* idx;   // member atom indexes, or null
-  int64_t reserved;
+  int32_t n_pairs;      // > 1: pairs (frames[pf + i].x, .y), i < n_pairs, all of this gap
+  int32_t pf;
 };
 static_assert(sizeof(DispDesc) == 48, "descriptor layout");
 
@@ -78,6 +81,7 @@ struct DispParams {
   const float* u;
   int64_t n_pad;
   const DispDesc* desc;  // [n_items], processing order
+  const int2* frames;    // (t0, t1) of the pairs of multi-pair items
   int32_t n_items;
   int32_t* counter;
   double* part;  // [n_items][n_out]
@@ -135,7 +139,57 @@ __global__ void __launch_bounds__(MODE == 0 ? DISP_THREADS : FS_THREADS)
     for (int s = 0; s < MAX_FS; ++s) fs[s] = KSum{0.f, 0.f};
 
     int a_start = it.a0 + tid;
-    if (MODE == 0 && !GS) {
+    if (MODE == 0 && !GS && it.n_pairs > 1) {
+      // a small member range over several pairs of one gap: the block walks
+      // the flat (pair, member) range, element e = pair * nm + member, so
+      // every thread has loads in flight even when nm is below the block size
+      const int nm = it.a1 - it.a0, total = it.n_pairs * nm;
+      const int q = nthr / nm, r = nthr - q * nm;  // a stride of nthr elements
+      int pr = tid / nm, a = tid - pr * nm;
+      const int2* F = p.frames + it.pf;
+      auto offsets = [&](int64_t& o0, int64_t& o1) {
+        const int2 tt = __ldg(F + pr);
+        const int atom = L.idx ? __ldg(L.idx + it.a0 + a) : L.first + it.a0 + a;
+        o0 = (int64_t)tt.x * 3 * p.n_pad + atom;
+        o1 = (int64_t)tt.y * 3 * p.n_pad + atom;
+        pr += q;
+        a += r;
+        if (a >= nm) {
+          a -= nm;
+          ++pr;
+        }
+      };
+      int e = tid;
+      constexpr int MP_BATCH = 4;
+      for (; e + (MP_BATCH - 1) * nthr < total; e += MP_BATCH * nthr) {
+        int64_t o0[MP_BATCH], o1[MP_BATCH];
+#pragma unroll
+        for (int k = 0; k < MP_BATCH; ++k) offsets(o0[k], o1[k]);
+        float d[MP_BATCH][3];
+#pragma unroll
+        for (int k = 0; k < MP_BATCH; ++k)
+#pragma unroll
+          for (int ax = 0; ax < 3; ++ax)
+            d[k][ax] = __fsub_rn(__ldg(p.u + o1[k] + ax * p.n_pad), __ldg(p.u + o0[k] + ax * p.n_pad));
+#pragma unroll
+        for (int k = 0; k < MP_BATCH; ++k) {
+          const float d2 = fmaf(d[k][2], d[k][2], fmaf(d[k][1], d[k][1], d[k][0] * d[k][0]));
+          kadd(m2, d2);
+          kadd(m4, d2 * d2);
+        }
+      }
+      for (; e < total; e += nthr) {
+        int64_t o0, o1;
+        offsets(o0, o1);
+        const float dx = __fsub_rn(__ldg(p.u + o1), __ldg(p.u + o0));
+        const float dy = __fsub_rn(__ldg(p.u + o1 + p.n_pad), __ldg(p.u + o0 + p.n_pad));
+        const float dz = __fsub_rn(__ldg(p.u + o1 + 2 * p.n_pad), __ldg(p.u + o0 + 2 * p.n_pad));
+        const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        kadd(m2, d2);
+        kadd(m4, d2 * d2);
+      }
+      a_start = it.a1;  // nothing left for the single-pair loops
+    } else if (MODE == 0 && !GS) {
       // MSD-only passes are load-latency bound: MSD_BATCH atoms' six loads each
       // are issued before any of them is used
       constexpr int MSD_BATCH = 4;  // 8 costs occupancy (registers) and is slower
@@ -579,10 +633,10 @@ struct amdat_disp_plan {
   amdat::DevBuf<int32_t> class_idx;       // atoms of gathered classes
   int chunk = 0, blocks_per_sm = 0, n_items = 0;
   double tuned_ms = 0.0;
-  // device: [descriptors | item_first | counters | kv | off | inv | lu_off | lu_units |
+  // device: [descriptors | pair frames | item_first | counters | kv | off | inv | lu_off | lu_units |
   //          part | unit d2 | d4 | fs | gs | list d2 | d4 | fs | gs]
   amdat::DevBuf<unsigned char> dev;
-  size_t o_desc = 0, o_first = 0, o_counter = 0, o_kv = 0, o_off = 0,
+  size_t o_desc = 0, o_frames = 0, o_first = 0, o_counter = 0, o_kv = 0, o_off = 0,
          o_inv = 0, o_luo = 0, o_luu = 0, o_part = 0, o_ud2 = 0, o_ud4 = 0, o_ufs = 0, o_ugs = 0,
          o_d2 = 0, o_d4 = 0, o_fs = 0, o_gs = 0, bytes = 0;
   cudaGraph_t graph = nullptr;
@@ -602,18 +656,27 @@ static void plan_tables(amdat_ctx* ctx, amdat_disp_plan& pl, const PairTable& P,
   std::vector<DispItem> items;
   std::vector<int32_t> item_first(n_ug + 1, 0);
   std::vector<int64_t> key;  // schedule key per item: (unit, chunk, pair)
+  // moments-only passes give a unit smaller than half a chunk several pairs
+  // of one gap per item (the finalize sums a (unit, gap)'s items anyway), so
+  // small lists do not pay one item's fixed cost per pair
+  const bool multi_pair = pl.S == 0 && pl.NB == 0;
   for (int u = 0; u < pl.n_units; ++u) {
     const int nch = (int)std::max<int64_t>(1, ceil_div(pl.usize[u], chunk));
+    const int ppi = (multi_pair && pl.usize[u] > 0 && 2 * pl.usize[u] <= chunk)
+                        ? std::min(MAX_PAIRS_PER_ITEM, chunk / pl.usize[u])
+                        : 1;
     for (int g = 0; g < G; ++g) {
       item_first[(size_t)u * G + g] = (int32_t)items.size();
       if (pl.usize[u] == 0) continue;
-      for (int pr = P.gap_first[g]; pr < P.gap_first[g + 1]; ++pr)
+      for (int pr = P.gap_first[g]; pr < P.gap_first[g + 1]; pr += ppi) {
+        const int np = std::min(ppi, P.gap_first[g + 1] - pr);
         for (int c = 0; c < nch; ++c) {
           const int a0 = (int)((int64_t)pl.usize[u] * c / nch);
           const int a1 = (int)((int64_t)pl.usize[u] * (c + 1) / nch);
-          items.push_back(DispItem{u, pr, a0, a1});
+          items.push_back(DispItem{u, pr, a0, a1, np});
           key.push_back(((int64_t)u << 40) | ((int64_t)c << 20) | (int64_t)pr);
         }
+      }
     }
   }
   item_first[n_ug] = (int32_t)items.size();
@@ -630,11 +693,14 @@ static void plan_tables(amdat_ctx* ctx, amdat_disp_plan& pl, const PairTable& P,
     AMDAT_CUDA(cudaMemcpy(hgap.data(), P.gap.ptr, P.n_pairs * 4, cudaMemcpyDeviceToHost));
   }
   std::vector<DispDesc> desc(items.size());
+  std::vector<int2> frames;
   for (size_t k = 0; k < sched.size(); ++k) {
     const DispItem& it = items[sched[k]];
     const ListDev& L = pl.udev[it.list];
     desc[k] = DispDesc{sched[k], it.list, it.a0, it.a1, ht0[it.pair], ht1[it.pair],
-                       hgap[it.pair], L.first, L.idx, 0};
+                       hgap[it.pair], L.first, L.idx, it.n_pairs, (int32_t)frames.size()};
+    if (it.n_pairs > 1)
+      for (int i = 0; i < it.n_pairs; ++i) frames.push_back(make_int2(ht0[it.pair + i], ht1[it.pair + i]));
   }
   pl.n_items = (int)items.size();
   pl.chunk = chunk;
@@ -643,6 +709,7 @@ static void plan_tables(amdat_ctx* ctx, amdat_disp_plan& pl, const PairTable& P,
   const size_t S1 = (size_t)std::max(pl.S, 1), NB1 = (size_t)std::max(pl.NB, 1);
   size_t o = 0;
   pl.o_desc = o; o = align(o + std::max<size_t>(desc.size(), 1) * sizeof(DispDesc));
+  pl.o_frames = o; o = align(o + std::max<size_t>(frames.size(), 1) * sizeof(int2));
   pl.o_first = o; o = align(o + item_first.size() * 4);
   pl.o_counter = o; o = align(o + 4 * (size_t)pl.n_passes);
   pl.o_kv = o; o = align(o + std::max<size_t>(pl.sh.kv.size(), 1) * sizeof(int4));
@@ -670,6 +737,7 @@ static void plan_tables(amdat_ctx* ctx, amdat_disp_plan& pl, const PairTable& P,
   unsigned char* base = pl.dev.reserve(o);
   std::vector<unsigned char> host(pl.o_part, 0);
   std::memcpy(host.data() + pl.o_desc, desc.data(), desc.size() * sizeof(DispDesc));
+  std::memcpy(host.data() + pl.o_frames, frames.data(), frames.size() * sizeof(int2));
   std::memcpy(host.data() + pl.o_first, item_first.data(), item_first.size() * 4);
   if (pl.S) {
     std::memcpy(host.data() + pl.o_kv, pl.sh.kv.data(), pl.sh.kv.size() * sizeof(int4));
@@ -702,6 +770,7 @@ static void plan_launch(amdat_ctx* ctx, amdat_disp_plan& pl, const PairTable& P)
     p.u = ctx->u.ptr;
     p.n_pad = ctx->n_pad;
     p.desc = (const DispDesc*)(base + pl.o_desc);
+    p.frames = (const int2*)(base + pl.o_frames);
     p.n_items = pl.n_items;
     p.counter = (int32_t*)(base + pl.o_counter) + pass;
     p.part = (double*)(base + pl.o_part);

@@ -2,8 +2,9 @@
 scripts unchanged and writes the reference's output files.  Integer-count
 outputs (vhs, rdf) must match the reference binary's files token for token;
 floating-point outputs must agree with the FP64 oracle to the 6 printed
-digits (+-2 in the last) and with the reference's own FP32 results to its
-accuracy (2e-3 relative)."""
+digits (+-2 in the last; the cancelling non-Gaussian parameter to 1e-8 of
+1 + NGP) and with the reference's own FP32 results to its accuracy (2e-3
+relative)."""
 import math
 import os
 
@@ -21,6 +22,11 @@ EXACT = ("vhs", "rdf")
 # histograms of |dr|^2 (u2dist, displacement_dist): a count can cross a bin
 # edge where the engine's frame-0-referenced displacement rounds differently
 COUNT_DERIVED = ("u2", "dd")
+# the non-Gaussian parameter 3<r^4>/(5<r^2>^2) - 1 of a random walk is a
+# near-total cancellation (values ~1e-3 printed to 1e-9): its printed digits
+# are held to 1e-8 relative in <r^4>/<r^2>^2 (the moment sums agree with the
+# FP64 oracle to ~1e-9 relative; their summation order follows the work split)
+CANCELLING = ("ngp",)
 
 
 def _num(t):
@@ -59,6 +65,9 @@ def test_cli_matches_reference_files(case, tmp_path, engine_mod, qvectors):
                 mism += 1
                 continue
             assert abs(fg - fw) <= 2e-3 * max(abs(fw), 1e-2), (name, g, w)
+            if name.startswith(CANCELLING):
+                assert ulp_close(g, o, 2) or abs(fg - float(o)) <= 1e-8 * (1 + abs(float(o))), (name, g, o)
+                continue
             assert ulp_close(g, o, 2), (name, g, o)
         assert mism <= 2, f"{case}/{name}: {mism} count-derived tokens differ"
 

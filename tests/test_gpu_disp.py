@@ -229,6 +229,41 @@ def test_plan_sharing_matches_per_list(eng, engine_mod, layout):
     alone.close()
 
 
+@pytest.mark.parametrize("fb", [0, 1])
+def test_multi_pair_items_match_oracle(eng, engine_mod, fb):
+    """Moments-only plans give lists below half a chunk several pairs of one
+    gap per work item; sizes around every threshold (1 member, the block size,
+    half a chunk, whole chunks), contiguous and gathered, match the oracle."""
+    scheme = synth.TimeScheme.exponential(5, 9, 1.3, 0, 0, 0.005)
+    traj = synth.random_walk(9000, 20.0, scheme, 0.4, 23)
+    eng.upload(traj.unwrapped, traj.box)
+    eng.set_scheme(traj.scheme)
+    s = orc.scheme(traj.scheme)
+    rng = np.random.default_rng(29)
+    sizes = [1, 2, 3, 37, 255, 256, 257, 1000, 2047, 2048, 2049, 4096, 4100, 9000]
+    sets = [np.arange(n, dtype=np.int32) for n in sizes]
+    sets += [np.sort(rng.choice(traj.n_atoms, size=n, replace=False)).astype(np.int32)
+             for n in (1, 5, 300, 2000, 3000)]
+    handles = [eng.list(x) for x in sets]
+    plans = [eng.plan(handles, fullblock=fb, flags=engine_mod.PLAN_NO_SHARING),
+             eng.plan(handles, fullblock=fb)]
+    for pl in plans:
+        pl.run()
+        out = pl.read()
+        for i, lst in enumerate(sets):
+            d2, d4, cnt = orc.disp_moments(s, traj.unwrapped, lst, fb)
+            np.testing.assert_array_equal(out["atom_pairs"][i], cnt)
+            np.testing.assert_allclose(out["sum_d2"][i], d2, rtol=1e-6, atol=1e-12)
+            np.testing.assert_allclose(out["sum_d4"][i], d4, rtol=1e-6, atol=1e-14)
+    # the descriptors hold the scheme's frames: a plan made for another scheme
+    # is refused, not run on stale pairs
+    eng.set_scheme(synth.TimeScheme.exponential(4, 9, 1.3, 0, 0, 0.005))
+    with pytest.raises(RuntimeError, match="time scheme changed"):
+        plans[0].run()
+    for pl in plans:
+        pl.close()
+
+
 def test_errors_are_status_codes(eng, engine_mod):
     with pytest.raises(engine_mod.AmdatError) as e:
         eng.disp(0)
