@@ -43,6 +43,9 @@ __device__ __forceinline__ int32_t turns_fixed(float d, float period) {
   return __float2int_rn(__fmul_rn(t, 2147483648.0f));
 }
 // cos(2 pi * phase * 2^-31)
+// |d|^2 in the displacement kernels' fixed order: fma(z, z, fma(y, y, x * x))
+__device__ __forceinline__ float sq3(float x, float y, float z) { return fmaf(z, z, fmaf(y, y, x * x)); }
+
 __device__ __forceinline__ float cos_fixed(int32_t phase) {
   return cospif(__fmul_rn((float)phase, 9.313225746154785e-10f));  // 2^-30
 }

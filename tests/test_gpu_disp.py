@@ -232,8 +232,10 @@ def test_plan_sharing_matches_per_list(eng, engine_mod, layout):
 @pytest.mark.parametrize("fb", [0, 1])
 def test_multi_pair_items_match_oracle(eng, engine_mod, fb):
     """Moments-only plans give lists below half a chunk several pairs of one
-    gap per work item; sizes around every threshold (1 member, the block size,
-    half a chunk, whole chunks), contiguous and gathered, match the oracle."""
+    gap per work item, and contiguous ranges are read four atoms per load;
+    sizes around every threshold (1 member, the block size, half a chunk,
+    whole chunks, ranges off the 4-atom grid), contiguous and gathered, match
+    the oracle."""
     scheme = synth.TimeScheme.exponential(5, 9, 1.3, 0, 0, 0.005)
     traj = synth.random_walk(9000, 20.0, scheme, 0.4, 23)
     eng.upload(traj.unwrapped, traj.box)
@@ -242,6 +244,8 @@ def test_multi_pair_items_match_oracle(eng, engine_mod, fb):
     rng = np.random.default_rng(29)
     sizes = [1, 2, 3, 37, 255, 256, 257, 1000, 2047, 2048, 2049, 4096, 4100, 9000]
     sets = [np.arange(n, dtype=np.int32) for n in sizes]
+    # contiguous ranges off the 4-atom grid (16-byte loads with ragged ends)
+    sets += [np.arange(a, b, dtype=np.int32) for a, b in ((3, 5004), (77, 9000), (1, 6), (5, 4103))]
     sets += [np.sort(rng.choice(traj.n_atoms, size=n, replace=False)).astype(np.int32)
              for n in (1, 5, 300, 2000, 3000)]
     handles = [eng.list(x) for x in sets]
