@@ -69,6 +69,9 @@ const PairTable& pair_table(amdat_ctx* ctx, bool fullblock, bool loop_order) {
   t->t0.reserve(n);
   t->t1.reserve(n);
   t->gap.reserve(n);
+  t->h_t0 = p.t0;
+  t->h_t1 = p.t1;
+  t->h_gap = p.gap;
   AMDAT_CUDA(cudaMemcpy(t->t0.ptr, p.t0.data(), n * 4, cudaMemcpyHostToDevice));
   AMDAT_CUDA(cudaMemcpy(t->t1.ptr, p.t1.data(), n * 4, cudaMemcpyHostToDevice));
   AMDAT_CUDA(cudaMemcpy(t->gap.ptr, p.gap.data(), n * 4, cudaMemcpyHostToDevice));
@@ -161,6 +164,8 @@ static void upload_impl(amdat_ctx* ctx, int32_t T, int32_t N, const Real* unwrap
   else std::memset(ctx->box_lo, 0, sizeof(ctx->box_lo));
   for (auto& kv : ctx->pair_cache) delete kv.second;
   ctx->pair_cache.clear();
+  ctx->disp_cache.clear();
+  ++ctx->traj_serial;
   AMDAT_CUDA(cudaStreamSynchronize(ctx->stream));
   ctx->have_traj = true;
   // list 0 = all atoms (contiguous); lists of a trajectory with another atom
@@ -180,6 +185,7 @@ static void upload_impl(amdat_ctx* ctx, int32_t T, int32_t N, const Real* unwrap
 using namespace amdat;
 
 amdat_ctx::~amdat_ctx() {
+  disp_cache.clear();
   for (auto* l : lists) delete l;
   for (auto& kv : pair_cache) delete kv.second;
   for (auto& kv : densities) {
@@ -438,6 +444,7 @@ amdat_status amdat_set_scheme(amdat_ctx* ctx, const amdat_scheme* s) {
     ctx->scheme = *s;
     ctx->have_scheme = true;
     ++ctx->scheme_serial;
+    ctx->disp_cache.clear();
     for (auto& kv : ctx->pair_cache) delete kv.second;
     ctx->pair_cache.clear();
   });

@@ -48,6 +48,7 @@ constexpr int MAX_FS = 8;         // shells per pass
 constexpr int DISP_THREADS = 256;
 constexpr int FS_THREADS = 128;
 constexpr int MAX_PAIRS_PER_ITEM = 64;
+constexpr size_t DISP_CACHE_PLANS = 8;  // one-shot requests kept prepared
 
 struct DispItem {
   int32_t list;  // slot in the launch's list table
@@ -654,6 +655,8 @@ struct amdat_disp_plan {
   int n_lists = 0, G = 0, S = 0, NB = 0, n_passes = 1, n_out = 2;
   bool fullblock = false;
   uint64_t scheme_serial = 0;  // time scheme the descriptors were made for
+  const float* traj_u = nullptr;  // trajectory storage and shape the plan reads
+  int32_t traj_atoms = 0, traj_frames = 0, traj_pad = 0;
   float bin_max = 0.f, period = 1.f;
   amdat::ShellSet sh;
   std::vector<int32_t> lsize;
@@ -720,12 +723,7 @@ static void plan_tables(amdat_ctx* ctx, amdat_disp_plan& pl, const PairTable& P,
   for (size_t i = 0; i < sched.size(); ++i) sched[i] = (int32_t)i;
   std::stable_sort(sched.begin(), sched.end(), [&](int32_t a, int32_t b) { return key[a] < key[b]; });
   // descriptors in processing order (the pair table's frames resolved here)
-  std::vector<int32_t> ht0(P.n_pairs), ht1(P.n_pairs), hgap(P.n_pairs);
-  if (P.n_pairs) {
-    AMDAT_CUDA(cudaMemcpy(ht0.data(), P.t0.ptr, P.n_pairs * 4, cudaMemcpyDeviceToHost));
-    AMDAT_CUDA(cudaMemcpy(ht1.data(), P.t1.ptr, P.n_pairs * 4, cudaMemcpyDeviceToHost));
-    AMDAT_CUDA(cudaMemcpy(hgap.data(), P.gap.ptr, P.n_pairs * 4, cudaMemcpyDeviceToHost));
-  }
+  const std::vector<int32_t>&ht0 = P.h_t0, &ht1 = P.h_t1, &hgap = P.h_gap;
   std::vector<DispDesc> desc(items.size());
   std::vector<int2> frames;
   for (size_t k = 0; k < sched.size(); ++k) {
@@ -993,6 +991,10 @@ static amdat_disp_plan* plan_create(amdat_ctx* ctx, const amdat_disp_request* re
     pl->NB = req->n_bins;
     pl->fullblock = req->fullblock != 0;
     pl->scheme_serial = ctx->scheme_serial;
+    pl->traj_u = ctx->u.ptr;
+    pl->traj_atoms = ctx->n_atoms;
+    pl->traj_frames = ctx->n_frames;
+    pl->traj_pad = ctx->n_pad;
     pl->bin_max = req->bin_max;
     pl->period = req->kvec_period;
     if (pl->S) {
@@ -1099,6 +1101,11 @@ static void plan_run(amdat_ctx* ctx, amdat_disp_plan* pl) {
   AMDAT_REQUIRE(pl != nullptr, "null plan");
   if (pl->scheme_serial != ctx->scheme_serial)
     throw Error(AMDAT_ERR_STATE, "the time scheme changed after the plan was made; make a new plan");
+  // a re-upload of the same shape keeps the storage and the lists; another
+  // shape may move the storage and drops the lists the descriptors point into
+  if (pl->traj_u != ctx->u.ptr || pl->traj_atoms != ctx->n_atoms || pl->traj_frames != ctx->n_frames ||
+      pl->traj_pad != ctx->n_pad)
+    throw Error(AMDAT_ERR_STATE, "a trajectory of another shape was uploaded after the plan was made; make a new plan");
   const PairTable& P = pair_table(ctx, pl->fullblock, false);
   if (pl->exec) {
     KernelTimer kt(ctx, "disp_plan_graph");
@@ -1139,7 +1146,34 @@ static void disp_run_impl(amdat_ctx* ctx, const amdat_disp_request* req, const i
     disp_plain(ctx, &r, out_flags, sum_d2, sum_d4, atom_pairs, fs_sum, gs_counts);
     return;
   }
-  std::unique_ptr<amdat_disp_plan> pl(plan_create(ctx, req, lists, n_lists, 0));
+  // repeated one-shot runs of one request reuse its prepared plan (tables,
+  // descriptors and buffers); a new scheme or trajectory clears the cache
+  std::string key;
+  auto put = [&key](const void* v, size_t n) { key.append(static_cast<const char*>(v), n); };
+  put(&ctx->scheme_serial, 8);
+  put(&ctx->traj_serial, 8);
+  put(&req->fullblock, 4);
+  put(&req->n_shells, 4);
+  put(&req->kvec_period, 4);
+  put(&req->n_bins, 4);
+  put(&req->bin_max, 4);
+  put(&n_lists, 4);
+  put(lists, 4 * (size_t)n_lists);
+  if (req->n_shells > 0) {
+    put(req->shell_offsets, 4 * (size_t)(req->n_shells + 1));
+    put(req->kvec_n, 12 * (size_t)std::max(req->shell_offsets[req->n_shells], 0));
+  }
+  std::shared_ptr<amdat_disp_plan> pl;
+  auto& cache = ctx->disp_cache;
+  for (size_t i = 0; i < cache.size(); ++i)
+    if (cache[i].first == key) {
+      pl = cache[i].second;
+      cache.erase(cache.begin() + (std::ptrdiff_t)i);
+      break;
+    }
+  if (!pl) pl.reset(plan_create(ctx, req, lists, n_lists, 0), [](amdat_disp_plan* p) { delete p; });
+  cache.emplace_back(std::move(key), pl);
+  if (cache.size() > DISP_CACHE_PLANS) cache.erase(cache.begin());
   plan_run(ctx, pl.get());
   plan_read(ctx, pl.get(), out_flags, sum_d2, sum_d4, atom_pairs, fs_sum, gs_counts);
   AMDAT_CUDA(cudaStreamSynchronize(ctx->stream));

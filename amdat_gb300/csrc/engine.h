@@ -5,6 +5,7 @@
 
 #include <cstdint>
 #include <map>
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -104,6 +105,7 @@ struct PairTable {
   int32_t n_gaps = 0;
   std::vector<int32_t> gap_first;
   DevBuf<int32_t> t0, t1, gap;
+  std::vector<int32_t> h_t0, h_t1, h_gap;  // host copies (plan tables resolve pairs on the host)
   // lagged tables (linear schemes): every gap's pairs, in order, are
   // (t, t + lag[g]) for t = 0 .. count - 1
   bool lagged = false;
@@ -163,6 +165,10 @@ struct amdat_ctx {
   amdat_scheme scheme{};
   bool have_scheme = false;
   uint64_t scheme_serial = 0;  // bumped by every amdat_set_scheme (plans bake pair frames)
+  uint64_t traj_serial = 0;    // bumped by every trajectory upload
+  // one-shot displacement runs keep their prepared plans, keyed by the whole
+  // request (scheme and trajectory serials included), most recent last
+  std::vector<std::pair<std::string, std::shared_ptr<amdat_disp_plan>>> disp_cache;
   std::map<int, amdat::PairTable*> pair_cache;  // key: fullblock*2 + loop_order
   std::map<int32_t, amdat::Density*> densities;
   int32_t next_density = 1;

@@ -872,6 +872,7 @@ def main():
         if "value" not in line:
             line.update({"value": m["value"], "unit": "atom·time-pairs/s",
                          "ms_per_step": m["ms"], "config": {"workload": sec["workload"]}})
+            line["msd_detail"] = {k: sec[k] for k in ("kernel_ms", "plan_graph", "fp64_plain")}
         else:
             line["secondary"] = sec
     if "batched" in result:

@@ -268,6 +268,48 @@ def test_multi_pair_items_match_oracle(eng, engine_mod, fb):
         pl.close()
 
 
+def test_one_shot_plan_cache(eng, engine_mod):
+    """Repeated one-shot runs reuse the request's prepared plan: the same
+    request gives identical numbers, and a new scheme, a new trajectory or
+    other shells are never served from the cache."""
+    traj, _, _ = load("lin_binary")
+    eng.upload(traj.unwrapped, traj.box)
+    eng.set_scheme(traj.scheme)
+    shell = lattice_shell(7.0, 2.0, 2.6)
+    off = np.array([0, len(shell)], np.int32)
+    kw = dict(shells=(shell, off), period=7.0, n_bins=25, bin_max=1.0)
+    a = eng.disp(0, **kw)
+    for _ in range(3):
+        b = eng.disp(0, **kw)
+        for k in a:
+            np.testing.assert_array_equal(a[k], b[k])
+    far = lattice_shell(7.0, 5.0, 5.4)
+    other = eng.disp(0, shells=(far, np.array([0, len(far)], np.int32)), period=7.0)
+    m = a["atom_pairs"] > 0
+    assert np.abs(other["fs_sum"][m] - a["fs_sum"][m]).max() > 1e-3 * a["atom_pairs"].max()
+    s2 = synth.TimeScheme.linear(traj.n_frames - 3)
+    eng.set_scheme(s2)
+    c = eng.disp(0)
+    d2, _, cnt = orc.disp_moments(orc.scheme(s2), traj.unwrapped, None, 0)
+    np.testing.assert_array_equal(c["atom_pairs"], cnt)
+    np.testing.assert_allclose(c["sum_d2"], d2, rtol=1e-6, atol=1e-12)
+    moved = traj.unwrapped * np.float32(1.5)
+    eng.upload(moved, traj.box)
+    eng.set_scheme(traj.scheme)
+    e = eng.disp(0)
+    d2, _, _ = orc.disp_moments(orc.scheme(traj.scheme), moved, None, 0)
+    np.testing.assert_allclose(e["sum_d2"], d2, rtol=1e-6, atol=1e-12)
+    # a prepared plan survives a re-upload of the same shape, not of another
+    plan = eng.plan([0])
+    eng.upload(traj.unwrapped, traj.box)
+    plan.run()
+    np.testing.assert_allclose(plan.read()["sum_d2"][0], a["sum_d2"], rtol=1e-7)
+    eng.upload(traj.unwrapped[:, :-5], traj.box)
+    with pytest.raises(RuntimeError, match="another shape"):
+        plan.run()
+    plan.close()
+
+
 def test_errors_are_status_codes(eng, engine_mod):
     with pytest.raises(engine_mod.AmdatError) as e:
         eng.disp(0)
