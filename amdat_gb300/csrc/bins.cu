@@ -35,6 +35,9 @@ constexpr int BN_THREADS = 256;
 constexpr int BN_CHUNK = 2048;
 constexpr int BN_MAX_FS = 8;
 constexpr size_t BN_STAGE_LIMIT = 48 * 1024;  // shared accumulators per block
+constexpr int BN_WARPS = BN_THREADS / 32;
+constexpr int BN_SUM_CHUNK = 8192;                 // members per item of the sums kernel
+constexpr size_t BN_SUM_SMEM_LIMIT = 96 * 1024;   // its per-warp accumulators
 
 // --- boxify and bin assignment -------------------------------------------------
 __global__ void boxify_kernel(float* __restrict__ w, int64_t n_pad, int32_t n_atoms, int64_t n_terms,
@@ -232,6 +235,132 @@ __global__ void __launch_bounds__(BN_THREADS) disp_bins_kernel(BnParams p) {
         for (int k = 0; k < stride; ++k)
           atomicAdd(p.acc + ((int64_t)i * p.n_gaps + it.gap) * stride + k, sacc[i * stride + k]);
       }
+    }
+    __syncthreads();
+  }
+}
+
+// Compensated FP32 shared-memory accumulation: the atomic's old value gives the
+// exact rounding error of the add (Knuth's TwoSum), which goes to a second
+// accumulator, so hi + lo keeps the terms' sum to second order.
+__device__ __forceinline__ void cadd_shared(float* hi, float* lo, float v) {
+  const float old = atomicAdd(hi, v);
+  const float s = __fadd_rn(old, v);
+  const float bv = __fsub_rn(s, old);
+  const float err = __fadd_rn(__fsub_rn(old, __fsub_rn(s, bv)), __fsub_rn(v, bv));
+  atomicAdd(lo, err);
+}
+
+// The binned pass without F_s (moments, or AXES: dx, dy, dz, dx^2, dy^2, dz^2):
+// each warp adds its atoms' terms to its own compensated FP32 accumulators in
+// shared memory ([warp][bin][column] hi and lo, [warp][bin] counts), and each
+// item ends with one FP64 sum over the warps (warp order) per (bin, column),
+// added to the (bin, gap) outputs.  Contiguous lists read four atoms per
+// 16-byte load of the positions and of the bin map (rows are 128-atom aligned).
+template <bool AXES>
+__global__ void __launch_bounds__(BN_THREADS) disp_bins_sum_kernel(BnParams p) {
+  extern __shared__ float bw_smem[];
+  __shared__ int s_item[2];
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int stride = AXES ? 6 : p.stride;
+  const int per_warp = p.n_bins * stride;
+  float* hi = bw_smem;
+  float* lo = hi + BN_WARPS * per_warp;
+  unsigned int* cnt = reinterpret_cast<unsigned int*>(lo + BN_WARPS * per_warp);
+  for (int i = tid; i < BN_WARPS * per_warp; i += BN_THREADS) hi[i] = lo[i] = 0.f;
+  for (int i = tid; i < BN_WARPS * p.n_bins; i += BN_THREADS) cnt[i] = 0u;
+  float* wh = hi + warp * per_warp;
+  float* wl = lo + warp * per_warp;
+  unsigned int* wc = cnt + warp * p.n_bins;
+  auto add = [&](int b, float dx, float dy, float dz) {
+    if (b < 0) return;
+    float* h = wh + b * stride;
+    float* l = wl + b * stride;
+    if (AXES) {
+      cadd_shared(h, l, dx);
+      cadd_shared(h + 1, l + 1, dy);
+      cadd_shared(h + 2, l + 2, dz);
+      cadd_shared(h + 3, l + 3, __fmul_rn(dx, dx));
+      cadd_shared(h + 4, l + 4, __fmul_rn(dy, dy));
+      cadd_shared(h + 5, l + 5, __fmul_rn(dz, dz));
+    } else {
+      const float d2 = sq3(dx, dy, dz);
+      cadd_shared(h, l, d2);
+      if (stride > 1) cadd_shared(h + 1, l + 1, d2 * d2);
+    }
+    atomicAdd(wc + b, 1u);
+  };
+
+  // the next item's counter slot is fetched while the current one runs
+  if (tid == 0) s_item[0] = atomicAdd(p.counter, 1);
+  __syncthreads();
+  for (int iter = 0;; ++iter) {
+    const int slot = s_item[iter & 1];
+    if (slot >= p.n_items) break;
+    if (tid == 0) s_item[(iter + 1) & 1] = atomicAdd(p.counter, 1);
+    const BnItem it = p.items[slot];
+    const int t0 = __ldg(p.t0 + it.pair), t1 = __ldg(p.t1 + it.pair);
+    const float* X0 = p.u + (int64_t)t0 * 3 * p.n_pad;
+    const float* X1 = p.u + (int64_t)t1 * 3 * p.n_pad;
+    const int32_t* B0 = p.bins + (int64_t)t0 * p.n_pad;
+    const int32_t* B1 = p.bins + (int64_t)t1 * p.n_pad;
+    auto one = [&](int atom) {
+      int b = __ldg(B0 + atom);
+      if (b >= 0 && p.persistent && __ldg(B1 + atom) != b) b = -1;
+      if (b < 0) return;
+      add(b, __fsub_rn(__ldg(X1 + atom), __ldg(X0 + atom)),
+          __fsub_rn(__ldg(X1 + p.n_pad + atom), __ldg(X0 + p.n_pad + atom)),
+          __fsub_rn(__ldg(X1 + 2 * p.n_pad + atom), __ldg(X0 + 2 * p.n_pad + atom)));
+    };
+    const int lo_a = p.list_first + it.a0, hi_a = p.list_first + it.a1;
+    if (!p.list_idx && (hi_a >> 2) > ((lo_a + 3) >> 2)) {
+      const int v0 = (lo_a + 3) >> 2, v1 = hi_a >> 2;  // whole quads [v0, v1)
+      const int64_t qp = p.n_pad >> 2;
+      const float4* A0 = reinterpret_cast<const float4*>(X0);
+      const float4* A1 = reinterpret_cast<const float4*>(X1);
+      for (int v = v0 + tid; v < v1; v += BN_THREADS) {
+        int4 b0 = __ldg(reinterpret_cast<const int4*>(B0) + v);
+        if (p.persistent) {
+          const int4 b1 = __ldg(reinterpret_cast<const int4*>(B1) + v);
+          b0.x = b1.x == b0.x ? b0.x : -1;
+          b0.y = b1.y == b0.y ? b0.y : -1;
+          b0.z = b1.z == b0.z ? b0.z : -1;
+          b0.w = b1.w == b0.w ? b0.w : -1;
+        }
+        if (b0.x < 0 && b0.y < 0 && b0.z < 0 && b0.w < 0) continue;  // no member of a bin
+        const float4 x0 = __ldg(A0 + v), x1 = __ldg(A1 + v);
+        const float4 y0 = __ldg(A0 + qp + v), y1 = __ldg(A1 + qp + v);
+        const float4 z0 = __ldg(A0 + 2 * qp + v), z1 = __ldg(A1 + 2 * qp + v);
+        add(b0.x, __fsub_rn(x1.x, x0.x), __fsub_rn(y1.x, y0.x), __fsub_rn(z1.x, z0.x));
+        add(b0.y, __fsub_rn(x1.y, x0.y), __fsub_rn(y1.y, y0.y), __fsub_rn(z1.y, z0.y));
+        add(b0.z, __fsub_rn(x1.z, x0.z), __fsub_rn(y1.z, y0.z), __fsub_rn(z1.z, z0.z));
+        add(b0.w, __fsub_rn(x1.w, x0.w), __fsub_rn(y1.w, y0.w), __fsub_rn(z1.w, z0.w));
+      }
+      const int n_head = 4 * v0 - lo_a, n_tail = hi_a - 4 * v1;
+      if (tid < n_head + n_tail) one(tid < n_head ? lo_a + tid : 4 * v1 + (tid - n_head));
+    } else {
+      for (int a = it.a0 + tid; a < it.a1; a += BN_THREADS)
+        one(p.list_idx ? __ldg(p.list_idx + a) : p.list_first + a);
+    }
+    __syncthreads();
+    // flush in FP64, warps in order; the accumulators are cleared for the next item
+    for (int e = tid; e < per_warp; e += BN_THREADS) {
+      double sum = 0.0;
+      for (int w = 0; w < BN_WARPS; ++w) {
+        sum += (double)hi[w * per_warp + e] + (double)lo[w * per_warp + e];
+        hi[w * per_warp + e] = 0.f;
+        lo[w * per_warp + e] = 0.f;
+      }
+      const int b = e / stride, k = e - b * stride;
+      if (sum != 0.0) atomicAdd(p.acc + ((int64_t)b * p.n_gaps + it.gap) * stride + k, sum);
+    }
+    for (int b = tid; b < p.n_bins; b += BN_THREADS) {
+      unsigned long long c = 0;
+      for (int w = 0; w < BN_WARPS; ++w) {
+        c += cnt[w * p.n_bins + b];
+        cnt[w * p.n_bins + b] = 0u;
+      }
+      if (c) atomicAdd(p.cnt + (int64_t)b * p.n_gaps + it.gap, c);
     }
     __syncthreads();
   }
@@ -513,8 +642,11 @@ static amdat_status disp_bins_impl(amdat_ctx* ctx, int32_t list, int32_t bins, i
       const int c = shell_offsets[s + 1] - shell_offsets[s];
       inv.push_back(c ? 1.0f / (float)c : 0.0f);
     }
+    // without F_s, a grid of per-warp shared accumulators when they fit
+    const size_t sum_smem = (size_t)BN_WARPS * B * (2 * (size_t)stride + 1) * 4;
+    const bool sum_kernel = n_shells == 0 && sum_smem <= BN_SUM_SMEM_LIMIT;
     // items: (pair, member chunk), gap-major
-    const int nch = (int)std::max<int64_t>(1, ceil_div(e.n, BN_CHUNK));
+    const int nch = (int)std::max<int64_t>(1, ceil_div(e.n, sum_kernel ? BN_SUM_CHUNK : BN_CHUNK));
     std::vector<BnItem> items;
     if (e.n > 0)
       for (int g = 0; g < G; ++g)
@@ -566,8 +698,12 @@ static amdat_status disp_bins_impl(amdat_ctx* ctx, int32_t list, int32_t bins, i
       p.cnt = (unsigned long long*)(base + o_cnt);
       const size_t stage = (size_t)B * stride * 8 + (size_t)B * 4;
       p.staged = stage <= BN_STAGE_LIMIT ? 1 : 0;
-      const size_t shm = p.staged ? stage : 0;
+      size_t shm = p.staged ? stage : 0;
       auto kern = axes ? disp_bins_kernel<false, true> : (n_shells ? disp_bins_kernel<true> : disp_bins_kernel<false>);
+      if (sum_kernel) {
+        kern = axes ? disp_bins_sum_kernel<true> : disp_bins_sum_kernel<false>;
+        shm = sum_smem;
+      }
       if (shm > 0) AMDAT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
       int per_sm = 1;
       AMDAT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, BN_THREADS, shm));
