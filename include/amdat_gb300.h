@@ -171,7 +171,10 @@ typedef struct {
  *   atom_pairs[g]  number of (atom, time pair) terms
  *   fs_sum[g][s]   sum of the shell mean of cos(k.dr)
  *   gs_counts[g][b] histogram counts (bin = int(|dr| / (bin_max/n_bins)))
- * out_flags = AMDAT_OUT_DEVICE: the five pointers are device pointers. */
+ * out_flags = AMDAT_OUT_DEVICE: the five pointers are device pointers.
+ * The context keeps the prepared plans of its last eight requests (lists,
+ * shells, bins, fullblock), so a repeated request only launches; a new scheme
+ * or trajectory upload drops them. */
 amdat_status amdat_disp_run(amdat_ctx* ctx, const amdat_disp_request* req, int32_t out_flags,
                             double* sum_d2, double* sum_d4, int64_t* atom_pairs, double* fs_sum,
                             int64_t* gs_counts);
@@ -272,9 +275,12 @@ amdat_status amdat_disp_bins_axes_run(amdat_ctx* ctx, int32_t list, int32_t bins
  * atom-chunk sizes and blocks per SM and keeps the fastest (remembered per
  * process and, when AMDAT_TUNE_CACHE names a file, across processes as JSON
  * lines).  Results stay in the plan until amdat_disp_plan_read.  The plan
- * refers to the context's trajectory, lists and scheme: rebuild it after
- * changing them.  (The reference runs one Analysis copy per list, e.g.
- * Bin_Static_Analysis, src/bin_static_analysis.h:69-111.) */
+ * refers to the context's trajectory, lists and scheme: amdat_disp_plan_run
+ * returns AMDAT_ERR_STATE after amdat_set_scheme or after the upload of a
+ * trajectory of another shape (a re-upload of the same shape keeps the plan
+ * valid and the next run reads the new coordinates).  (The reference runs one
+ * Analysis copy per list, e.g. Bin_Static_Analysis,
+ * src/bin_static_analysis.h:69-111.) */
 #define AMDAT_PLAN_AUTOTUNE 1
 #define AMDAT_PLAN_GRAPH 2
 /* Lists that overlap (nested lists, bins plus their union, ...) share work:
