@@ -457,7 +457,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--frames", type=int, default=400, help="frames of the headline workload")
     ap.add_argument("--only", default="", choices=["", "isf", "msd", "batched", "pairs", "structure", "cli",
-                                                   "perlist"],
+                                                   "perlist", "bins"],
                     help="run one workload only (profiling)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     args = ap.parse_args()
@@ -652,6 +652,24 @@ def main():
         torch.cuda.synchronize()
         result["perlist"] = dict(ms=1e3 * (time.perf_counter() - t0) / max(args.steps, 1), info=plan.info())
         plan.close()
+
+    if args.only == "bins":
+        # profiling aid: the batched workload's 64-bin MSD pass alone
+        btraj, bscheme, sizes, perm = batched_workload()
+        eng.upload(btraj.unwrapped, btraj.box)
+        eng.set_scheme(bscheme)
+        blo = btraj.box_lo.astype(np.float32)
+        bhi = (btraj.box_lo.astype(np.float64) + btraj.box.astype(np.float64)).astype(np.float32)
+        eng.boxify(blo, bhi)
+        bh = eng.bins_create((4, 4, 4), blo, bhi)
+        for _ in range(args.warmup):
+            eng.disp_bins(0, bh, 64, d4=False)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            eng.disp_bins(0, bh, 64, d4=False)
+        result["bins_only"] = dict(call_ms=1e3 * (time.perf_counter() - t0) / max(args.steps, 1))
+        eng.bins_free(bh)
 
     if args.only in ("", "batched"):
         btraj, bscheme, sizes, perm = batched_workload()
@@ -951,6 +969,8 @@ def main():
             "vhd": {"value": q["gd_rate"], "unit": "ordered pairs/s", "ms_per_step": q["gd_ms"]}}
     if "perlist" in result:
         line["perlist"] = result["perlist"]
+    if "bins_only" in result:
+        line["bins_only"] = result["bins_only"]
     if "structure" in result:
         line["structure"] = result["structure"]
         if "value" not in line:
