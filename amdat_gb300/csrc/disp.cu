@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(MODE == 0 ? DISP_THREADS : FS_THREADS)
             const int4 n = __ldg(p.kv + v);
             const int32_t ph = (int32_t)((uint32_t)n.x * (uint32_t)fx + (uint32_t)n.y * (uint32_t)fy +
                                          (uint32_t)n.z * (uint32_t)fz);
-            blk += cos_fixed(ph);
+            blk += cos_fixed_sfu(ph);
             if (++cnt == 32) {
               kadd(acc, blk);
               blk = 0.f;

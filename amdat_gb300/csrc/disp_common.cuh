@@ -42,12 +42,20 @@ __device__ __forceinline__ int32_t turns_fixed(float d, float period) {
   t = __fsub_rn(t, rintf(t));  // [-0.5, 0.5]
   return __float2int_rn(__fmul_rn(t, 2147483648.0f));
 }
-// cos(2 pi * phase * 2^-31)
 // |d|^2 in the displacement kernels' fixed order: fma(z, z, fma(y, y, x * x))
 __device__ __forceinline__ float sq3(float x, float y, float z) { return fmaf(z, z, fmaf(y, y, x * x)); }
 
+// cos(2 pi * phase * 2^-31)
 __device__ __forceinline__ float cos_fixed(int32_t phase) {
   return cospif(__fmul_rn((float)phase, 9.313225746154785e-10f));  // 2^-30
+}
+
+// cos of the same fixed-point phase through the SFU cosine: the phase is first
+// reduced to [-1/2, 1/2) turn (a wrapping doubling of the int32: units of 2^-32
+// turn), where __cosf's absolute error is below 2^-21.4
+__device__ __forceinline__ float cos_fixed_sfu(int32_t phase) {
+  const int32_t r = (int32_t)((uint32_t)phase << 1);
+  return __cosf(__fmul_rn((float)r, 1.4629180792671596e-09f));  // 2 pi / 2^32
 }
 
 }  // namespace amdat
