@@ -110,6 +110,32 @@ def test_fs_reference_shells(case, m0, m1, fb, eng, qvectors):
     assert np.abs(got - ref).max() <= 1e-6
 
 
+def test_fs_single_vector_terms_within_cosine_bound(eng):
+    """Vector-list F_s evaluates each cos(k.dr) with the SFU cosine of the
+    fixed-point phase reduced to [-pi, pi).  On a dyadic grid (coordinates in
+    multiples of 2^-10, box 8) every displacement and phase is exact, so
+    one-vector shells of single atoms (phases of many turns, both signs) show
+    the cosine's own error: within its 2^-21.4 bound of the FP64 oracle, plus
+    the FP32 accumulation."""
+    traj, _, _ = load("exp_small")
+    u = (np.round(traj.unwrapped.astype(np.float64) * 1024.0) / 1024.0).astype(np.float32)
+    box = np.full(3, 8.0, np.float32)
+    eng.upload(u, box)
+    eng.set_scheme(traj.scheme)
+    kv = np.array([[1, 0, 0], [37, -11, 5], [0, 0, -48], [-23, 29, 31]], np.int32)
+    off = np.arange(len(kv) + 1, dtype=np.int32)
+    s = orc.scheme(traj.scheme)
+    for atom in (0, 7, 100):
+        h = eng.list([atom])
+        out = eng.disp(h, shells=(kv, off), period=8.0)
+        # the engine's k is 2 pi n / L exactly (phases in fixed-point turns): the
+        # oracle gets the FP64 spacing, not the reference's FP32-rounded one
+        ref = orc.isfs(s, u, np.array([atom], np.int32), kv, off, 2.0 * np.pi / 8.0, 8.0, 0, orc.F64)
+        m = out["atom_pairs"] > 0
+        got = out["fs_sum"][m] / out["atom_pairs"][m][:, None]
+        assert np.abs(got - ref[m]).max() <= 3.6e-7 + 1e-7
+
+
 def test_fs_lattice_shell_octant_mode(eng):
     """Whole lattice shell |k| in [7.0, 7.2] (sign-symmetric: octant tables)."""
     box = 16.8
