@@ -225,8 +225,8 @@ __global__ void __launch_bounds__(MODE == 0 ? DISP_THREADS : FS_THREADS)
       }
       a_start = it.a1;  // nothing left for the loops below
     } else if (MODE == 0 && !GS) {
-      // MSD-only passes are load-latency bound: MSD_BATCH atoms' six loads each
-      // are issued before any of them is used
+      // gathered members (index lists): MSD_BATCH atoms' six loads each are
+      // issued before any of them is used (the pass is load-latency bound)
       constexpr int MSD_BATCH = 4;  // 8 costs occupancy (registers) and is slower
       for (; a_start + (MSD_BATCH - 1) * nthr < it.a1; a_start += MSD_BATCH * nthr) {
         int at[MSD_BATCH];
