@@ -190,10 +190,21 @@ __global__ void __launch_bounds__(MODE == 0 ? DISP_THREADS : FS_THREADS)
         kadd(m4, d2 * d2);
       }
       a_start = it.a1;  // nothing left for the single-pair loops
-    } else if (MODE == 0 && !GS && !L.idx && (L.first + it.a1) / 4 > (L.first + it.a0 + 3) / 4) {
+    } else if (MODE == 0 && !L.idx && (L.first + it.a1) / 4 > (L.first + it.a0 + 3) / 4) {
       // contiguous members: one 16-byte load per plane and frame brings four
       // consecutive atoms (planes start on 128-atom boundaries); the < 4 atoms
       // before the first and after the last whole quad go one per thread
+      auto term = [&](float dx, float dy, float dz) {
+        const float e = sq3(dx, dy, dz);
+        kadd(m2, e);
+        kadd(m4, e * e);
+        if (GS) {
+          // the reference's FP32 chain: sqrt((dx*dx + dy*dy) + dz*dz) / bin_size
+          const float s2 = __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+          const int b = (int)__fdiv_rn(__fsqrt_rn(s2), p.bin_size);
+          if (b >= 0 && b < p.n_bins) atomicAdd(hist + b, 1u);
+        }
+      };
       const int lo = L.first + it.a0, hi = L.first + it.a1;
       const int v0 = (lo + 3) >> 2, v1 = hi >> 2;  // whole quads [v0, v1)
       const float4* A0 = reinterpret_cast<const float4*>(X0);
@@ -203,25 +214,17 @@ __global__ void __launch_bounds__(MODE == 0 ? DISP_THREADS : FS_THREADS)
         const float4 x0 = __ldg(A0 + v), x1 = __ldg(A1 + v);
         const float4 y0 = __ldg(A0 + qp + v), y1 = __ldg(A1 + qp + v);
         const float4 z0 = __ldg(A0 + 2 * qp + v), z1 = __ldg(A1 + 2 * qp + v);
-        const float e[4] = {
-            sq3(__fsub_rn(x1.x, x0.x), __fsub_rn(y1.x, y0.x), __fsub_rn(z1.x, z0.x)),
-            sq3(__fsub_rn(x1.y, x0.y), __fsub_rn(y1.y, y0.y), __fsub_rn(z1.y, z0.y)),
-            sq3(__fsub_rn(x1.z, x0.z), __fsub_rn(y1.z, y0.z), __fsub_rn(z1.z, z0.z)),
-            sq3(__fsub_rn(x1.w, x0.w), __fsub_rn(y1.w, y0.w), __fsub_rn(z1.w, z0.w))};
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          kadd(m2, e[k]);
-          kadd(m4, e[k] * e[k]);
-        }
+        term(__fsub_rn(x1.x, x0.x), __fsub_rn(y1.x, y0.x), __fsub_rn(z1.x, z0.x));
+        term(__fsub_rn(x1.y, x0.y), __fsub_rn(y1.y, y0.y), __fsub_rn(z1.y, z0.y));
+        term(__fsub_rn(x1.z, x0.z), __fsub_rn(y1.z, y0.z), __fsub_rn(z1.z, z0.z));
+        term(__fsub_rn(x1.w, x0.w), __fsub_rn(y1.w, y0.w), __fsub_rn(z1.w, z0.w));
       }
       const int n_head = 4 * v0 - lo, n_tail = hi - 4 * v1;
       if (tid < n_head + n_tail) {
         const int atom = tid < n_head ? lo + tid : 4 * v1 + (tid - n_head);
-        const float e = sq3(__fsub_rn(__ldg(X1 + atom), __ldg(X0 + atom)),
-                            __fsub_rn(__ldg(X1 + p.n_pad + atom), __ldg(X0 + p.n_pad + atom)),
-                            __fsub_rn(__ldg(X1 + 2 * p.n_pad + atom), __ldg(X0 + 2 * p.n_pad + atom)));
-        kadd(m2, e);
-        kadd(m4, e * e);
+        term(__fsub_rn(__ldg(X1 + atom), __ldg(X0 + atom)),
+             __fsub_rn(__ldg(X1 + p.n_pad + atom), __ldg(X0 + p.n_pad + atom)),
+             __fsub_rn(__ldg(X1 + 2 * p.n_pad + atom), __ldg(X0 + 2 * p.n_pad + atom)));
       }
       a_start = it.a1;  // nothing left for the loops below
     } else if (MODE == 0 && !GS) {
