@@ -143,8 +143,16 @@ extern "C" amdat_status amdat_disp_moments_noalloc(const amdat_scheme* scheme, i
                   "time scheme too large for the 16 MiB no-allocation scratch");
     const int64_t max_items = (int64_t)((NOALLOC_SCRATCH_BYTES - fixed - 1024) /
                                         (sizeof(NoallocItem) + 2 * sizeof(double)));
+    // every time pair needs at least one item (one chunk of all atoms): a scheme
+    // with more pairs than items cannot run here, whatever the chunk size
+    if (n_pairs > max_items)
+      throw Error(AMDAT_ERR_ARGUMENT,
+                  "time scheme has " + std::to_string(n_pairs) + " time pairs; the 16 MiB "
+                  "no-allocation scratch holds at most " + std::to_string(max_items) +
+                  " for this scheme");
+    // chunks of 4096 atoms, doubled until the items fit; at most one chunk per pair
     int64_t chunk = 4096;
-    while (n_pairs * ceil_div(n_atoms, chunk) > max_items) chunk *= 2;
+    while (chunk < n_atoms && n_pairs * ceil_div(n_atoms, chunk) > max_items) chunk *= 2;
     const int nch = (int)ceil_div(n_atoms, chunk);
     std::vector<NoallocItem> items;
     items.reserve((size_t)(n_pairs * nch));

@@ -401,8 +401,9 @@ amdat_status amdat_structure_factor_adjoint(amdat_ctx* ctx, int32_t density,
  * stream (NULL = legacy default stream, the device current on the calling
  * thread).  No context is used and nothing is allocated: the temporaries live
  * in a 16 MiB __device__ array that every GPU loading this library holds until
- * exit.  The work must fit in it (about 500k time-pair x atom-chunk items):
- * larger schemes return AMDAT_ERR_ARGUMENT.  The first call on a device looks
+ * exit.  The work must fit in it: one work item per time pair and atom chunk,
+ * about 419k items at most, so a scheme of more than about 419k time pairs
+ * (a linear scheme of more than about 915 frames) returns AMDAT_ERR_ARGUMENT.  The first call on a device looks
  * up the array's address (and may load the module), so make it before any
  * stream capture.  Calls share the array: calls whose GPU work overlaps race.
  * ------------------------------------------------------------------------- */

@@ -81,3 +81,22 @@ def test_no_device_reports_status(E):
     st = E.lib().amdat_create(0, C.byref(ctx))
     assert st == 4  # AMDAT_ERR_NO_DEVICE
     assert E.lib().amdat_last_error()
+
+
+@pytest.mark.parametrize("frames", [1000, 1300])
+def test_noalloc_rejects_too_many_time_pairs_before_any_gpu_work(E, frames):
+    """Linear schemes of 1000 and 1300 frames (499,501 and 844,351 time pairs)
+    pass the fixed-table size check but need more work items than the fixed
+    scratch holds even at one atom chunk per pair.  The entry point must return
+    AMDAT_ERR_ARGUMENT from its host-side check, not loop or divide by zero.
+    The pointers are never dereferenced: the check runs before any CUDA call."""
+    st = _noalloc_call(E, frames)
+    assert st == 1, E.lib().amdat_last_error()
+    msg = E.lib().amdat_last_error()
+    assert b"time pairs" in msg and b"16 MiB" in msg
+
+
+def _noalloc_call(E, frames):
+    s = E.make_scheme(synth.TimeScheme.linear(frames, 1.0))
+    fake = C.c_void_p(256)  # never dereferenced: rejected on the host
+    return E.lib().amdat_disp_moments_noalloc(C.byref(s), 0, fake, frames, 1, None, fake, fake)
