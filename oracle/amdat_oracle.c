@@ -877,6 +877,88 @@ void orc_rhok_parallel(const float* r, int32_t n_atoms, const int32_t* frames, i
   }
 }
 
+/* rho(k) of integer-lattice vectors in FP64, factored per axis: the density
+ * of Wave_Density::listkernel (src/wave_density.cpp:339-365), sum over atoms of
+ * exp(i k.r) with r the wrapped coordinate, written as
+ *   exp(i k.r) = X_a(nx) Y_a(ny) Z_a(nz),  X_a(n) = exp(i 2 pi n x_a / L)
+ * where every table entry is a direct FP64 cos/sin of its own phase and the
+ * products and sums are FP64 (relative error ~1e-15 per term against the
+ * direct orc_rhok_parallel).  Vectors are grouped by (nx, ny) column, so each
+ * column's X Y product is formed once per atom; columns run in parallel.
+ * kvec_n entries must satisfy |n| <= nmax on every axis. */
+void orc_rhok_lattice(const float* r, int32_t n_atoms, const int32_t* frames, int32_t n_frames,
+                      const int32_t* kvec_n, int32_t n_k, double box_len, int32_t n_threads,
+                      double* rho) {
+  int nmax = 0;
+  for (int i = 0; i < 3 * n_k; ++i) nmax = abs(kvec_n[i]) > nmax ? abs(kvec_n[i]) : nmax;
+  const int W = 2 * nmax + 1;
+  const size_t tab = (size_t)W * n_atoms; /* [axis][n + nmax][atom] re and im planes */
+  double* re = (double*)malloc(sizeof(double) * 3 * (tab ? tab : 1));
+  double* im = (double*)malloc(sizeof(double) * 3 * (tab ? tab : 1));
+  /* vectors sorted by column (nx, ny): counting sort on the column index */
+  int32_t* col_start = (int32_t*)calloc((size_t)W * W + 1, sizeof(int32_t));
+  int32_t* order = (int32_t*)malloc(sizeof(int32_t) * (n_k > 0 ? n_k : 1));
+  for (int v = 0; v < n_k; ++v)
+    col_start[(kvec_n[3 * v] + nmax) * W + (kvec_n[3 * v + 1] + nmax) + 1]++;
+  for (int c = 0; c < W * W; ++c) col_start[c + 1] += col_start[c];
+  {
+    int32_t* fill = (int32_t*)malloc(sizeof(int32_t) * ((size_t)W * W + 1));
+    memcpy(fill, col_start, sizeof(int32_t) * ((size_t)W * W + 1));
+    for (int v = 0; v < n_k; ++v) order[fill[(kvec_n[3 * v] + nmax) * W + (kvec_n[3 * v + 1] + nmax)]++] = v;
+    free(fill);
+  }
+  const double tpl = TWO_PI / box_len;
+  const int nth = n_threads > 0 ? n_threads : 1;
+  for (int f = 0; f < n_frames; ++f) {
+    const int t = frames[f];
+#pragma omp parallel for num_threads(nth) schedule(static)
+    for (int64_t e = 0; e < (int64_t)3 * W * n_atoms; ++e) {
+      const int axis = (int)(e / ((int64_t)W * n_atoms));
+      const int n = (int)((e / n_atoms) % W) - nmax;
+      const int a = (int)(e % n_atoms);
+      const double ph = tpl * (double)n * (double)POS(r, t, a, axis);
+      re[e] = cos(ph);
+      im[e] = sin(ph);
+    }
+    double* out = rho + (size_t)f * n_k * 2;
+#pragma omp parallel num_threads(nth)
+    {
+      double* wr = (double*)malloc(sizeof(double) * (n_atoms > 0 ? n_atoms : 1));
+      double* wi = (double*)malloc(sizeof(double) * (n_atoms > 0 ? n_atoms : 1));
+#pragma omp for schedule(dynamic, 4)
+      for (int c = 0; c < W * W; ++c) {
+        if (col_start[c + 1] == col_start[c]) continue;
+        const double* xr = re + (size_t)(c / W) * n_atoms;
+        const double* xi = im + (size_t)(c / W) * n_atoms;
+        const double* yr = re + tab + (size_t)(c % W) * n_atoms;
+        const double* yi = im + tab + (size_t)(c % W) * n_atoms;
+        for (int a = 0; a < n_atoms; ++a) {
+          wr[a] = xr[a] * yr[a] - xi[a] * yi[a];
+          wi[a] = xr[a] * yi[a] + xi[a] * yr[a];
+        }
+        for (int i = col_start[c]; i < col_start[c + 1]; ++i) {
+          const int v = order[i];
+          const double* zr = re + 2 * tab + (size_t)(kvec_n[3 * v + 2] + nmax) * n_atoms;
+          const double* zi = im + 2 * tab + (size_t)(kvec_n[3 * v + 2] + nmax) * n_atoms;
+          double sr = 0, si = 0;
+          for (int a = 0; a < n_atoms; ++a) {
+            sr += wr[a] * zr[a] - wi[a] * zi[a];
+            si += wr[a] * zi[a] + wi[a] * zr[a];
+          }
+          out[2 * v] = sr;
+          out[2 * v + 1] = si;
+        }
+      }
+      free(wr);
+      free(wi);
+    }
+  }
+  free(re);
+  free(im);
+  free(col_start);
+  free(order);
+}
+
 /* ------------------------------------------------------------------------- */
 /* differentiable structure (FP64; no reference counterpart)                 */
 /* ------------------------------------------------------------------------- */

@@ -129,6 +129,9 @@ void orc_disp_fs_parallel(const orc_scheme* s, int32_t fullblock, const float* u
 void orc_rhok_parallel(const float* wrapped, int32_t n_atoms, const int32_t* frames,
                        int32_t n_frames, const int32_t* kvec_n, int32_t n_k, double box_len,
                        int32_t n_threads, double* rho);
+void orc_rhok_lattice(const float* wrapped, int32_t n_atoms, const int32_t* frames,
+                      int32_t n_frames, const int32_t* kvec_n, int32_t n_k, double box_len,
+                      int32_t n_threads, double* rho);
 
 /* Differentiable structure (no reference counterpart; restates the engine's
  * definitions in FP64 from the FP32 wrapped coordinates).

@@ -333,6 +333,19 @@ def rhok_parallel(wrapped, frames, kvec_n, box_len, n_threads):
     return out
 
 
+def rhok_lattice(wrapped, frames, kvec_n, box_len, n_threads):
+    """FP64 rho(k) of integer-lattice vectors from per-axis phasor tables (every
+    atom of the trajectory); agrees with rhok_parallel to FP64 rounding."""
+    r = _f32(wrapped)
+    fr = _i32(frames)
+    kv = _i32(kvec_n).reshape(-1)
+    nk = len(kv) // 3
+    out = np.zeros((len(fr), nk, 2))
+    lib().orc_rhok_lattice(_p(r), r.shape[1], _p(fr), len(fr), _p(kv), nk, C.c_double(box_len),
+                           int(n_threads), _p(out))
+    return out
+
+
 def gsmooth(wrapped, box, lst, frames, sigma, r_max, n_bins):
     """FP64 Gaussian-smoothed pair histogram (the engine's amdat_gsmooth_run)."""
     r = _f32(wrapped)
