@@ -410,7 +410,13 @@ class Engine:
         _check(lib().amdat_wave_density_vectors(self._ctx, int(handle), _p(kv), _p(off)))
         return kv, off
 
-    def wave_density_read(self, handle, n_frames, n_k):
+    def wave_density_read(self, handle, n_frames, n_k, out_device=None):
+        """rho[frame][k] as float32 (re, im) pairs; with out_device (a device
+        pointer to n_frames * n_k float2) the table is copied on the device."""
+        if out_device is not None:
+            _check(lib().amdat_wave_density_read(self._ctx, int(handle), OUT_DEVICE,
+                                                 C.c_void_p(out_device)))
+            return None
         rho = np.zeros((n_frames, n_k, 2), np.float32)
         _check(lib().amdat_wave_density_read(self._ctx, int(handle), OUT_HOST, _p(rho)))
         return rho

@@ -39,11 +39,16 @@ METRIC = "atom·time-pairs/s (MSD+Fs) & atom·k/s (rho_k): mixed vs FP64 plain, 
 PEAKS_FILE = os.path.join(HERE, "MEASURED_PEAKS.json")
 FP32_LANES_PER_SM = 128
 # DRAM bytes (read + write) per frame of one rhok_tc_kernel launch on the headline
-# lattice (N=32000, |k|<=20, L=33.6), from one ncu capture of a 2-frame launch
-# (profiles/rhok_tc_kernel_N32000_k20_2frames.md, design E: 815.5 MB read + 42.8 MB
-# written).  Every stream of the launch is per frame (X/Y phase tables, Z operands, rho
-# rows), so a launch over f frames moves f times this.
+# lattice (N=32000, |k|<=20, L=33.6), from one ncu capture of a 2-frame launch of
+# this kernel (815.5 MB read + 42.8 MB written).  Every stream of the launch is per
+# frame (X/Y phase tables, Z operands, rho rows), so a launch over f frames moves f
+# times this.
 TC_DRAM_BYTES_PER_FRAME = (815.539e6 + 42.798e6) / 2
+# DRAM bytes (read + write) of one launch of the per-list MSD + NGP plan over the 64
+# nested lists, from one ncu capture of disp_mixed_kernel on that workload
+PERLIST_DRAM_BYTES = 2.33e9
+# MUFU (special-function unit) results per clock per SM: 4 per sub-partition
+MUFU_PER_SM_CLK = 16
 
 
 # ---------------------------------------------------------------------------
@@ -232,32 +237,38 @@ def measured_peaks():
 # CPU baseline (restatement of the reference algorithm, all host threads)
 # ---------------------------------------------------------------------------
 def cpu_rhok_sample(traj, vectors, threads, target_s=12.0):
-    """rho(k) of one frame over a vector sample, FP64, OpenMP over vectors;
-    grows the sample until it takes about target_s."""
+    """rho(k) of the middle frame over a random vector sample, FP64, OpenMP over
+    vectors (the reference's Wave_Density loop restated); grows the sample until
+    it takes about target_s / 4.  Returns (rate, description, seconds, sample
+    indices into vectors, rho [1][sample][2])."""
     from oracle import oracle as orc
     wrapped = traj.wrapped()
     rng = np.random.default_rng(0)
     nk = 2000
     frames = np.array([traj.n_frames // 2], np.int32)
     while True:
-        sel = vectors[rng.choice(len(vectors), size=min(nk, len(vectors)), replace=False)]
+        idx = np.sort(rng.choice(len(vectors), size=min(nk, len(vectors)), replace=False))
         t0 = time.perf_counter()
-        orc.rhok_parallel(wrapped, frames, sel, float(traj.box[0]), threads)
+        out = orc.rhok_parallel(wrapped, frames, vectors[idx], float(traj.box[0]), threads)
         dt = time.perf_counter() - t0
-        units = traj.n_atoms * len(sel)
+        units = traj.n_atoms * len(idx)
         if dt >= target_s / 4 or nk >= len(vectors):
-            return units / dt, f"1 frame x {len(sel)} random vectors x {traj.n_atoms} atoms", dt
+            return (units / dt, f"1 frame x {len(idx)} random vectors x {traj.n_atoms} atoms", dt,
+                    idx, out)
         nk = int(min(len(vectors), nk * max(2.0, (target_s / 4) / max(dt, 1e-3))))
 
 
 def cpu_disp_sample(traj, scheme, shell, threads):
+    """MSD and F_s of every time pair and atom, FP64 (OpenMP over atoms).
+    Returns (rate, description, seconds, per-gap sum |dr|^2, per-gap F_s sums)."""
     from oracle import oracle as orc
     s = orc.scheme(scheme)
     t0 = time.perf_counter()
-    orc.disp_fs_parallel(s, traj.unwrapped, shell, float(traj.box[0]), threads)
+    d2, fs = orc.disp_fs_parallel(s, traj.unwrapped, shell, float(traj.box[0]), threads)
     dt = time.perf_counter() - t0
     npairs = len(orc.pairs(s, 0)[0])
-    return npairs * traj.n_atoms / dt, f"all {npairs} time pairs x {traj.n_atoms} atoms, {len(shell)} vectors", dt
+    return (npairs * traj.n_atoms / dt, f"all {npairs} time pairs x {traj.n_atoms} atoms, {len(shell)} vectors",
+            dt, d2, fs)
 
 
 def write_qvector_files(directory):
@@ -309,37 +320,106 @@ def cli_bench():
                 units=float(traj.n_atoms) * npairs)
 
 
+REF_SHELLS = 20  # the reference arm's q-vector shells 0..20 (2,843 vectors)
+REF_FRAMES = 2   # frames of the headline walk in the reference arm's sample
+
+
+def reference_isf_sample(binary, threads, tmp):
+    """The reference program's own coherent-ISF command on a bounded sample of the
+    headline workload: the first REF_FRAMES frames of the N=32000, L=33.6 walk
+    (custom dump), `isf ... auto symmetric xyz 0 0 REF_SHELLS` over the list of
+    all atoms, i.e. Wave_Density::listkernel over every atom, frame and vector of
+    the reference's q-vector shells 0..REF_SHELLS, then the correlator.  Returns
+    a closure timing one run (seconds of the command: the run with the command
+    minus the best of three runs of the same system block without it) and the
+    sample's atom*k units."""
+    from amdat_gb300 import synth
+    traj, _, _ = isf_workload(REF_FRAMES)
+    dump = os.path.join(tmp, "traj.dump")
+    synth.write_custom_dump(traj, dump)
+    header = synth.system_header(traj, dump)
+    z = np.load(os.path.join(HERE, "tests", "golden", "qvectors3d.npz"))
+    n_vec = int(z["offsets"][REF_SHELLS + 1])
+    scripts = {"header": header + "create_list all\nall\n",
+               "isf": header + f"create_list all\nall\nisf ./isf.dat auto symmetric xyz 0 0 {REF_SHELLS}\nlist all\n"}
+    for k, text in scripts.items():
+        with open(os.path.join(tmp, f"{k}.in"), "w") as f:
+            f.write(text)
+
+    def run(tag):
+        t0 = time.perf_counter()
+        r = subprocess.run([binary, "-n", str(threads), "-i", f"{tag}.in"], cwd=tmp,
+                           capture_output=True, text=True)
+        dt = time.perf_counter() - t0
+        if r.returncode != 0:
+            raise RuntimeError(f"reference AMDAT failed: {(r.stdout + r.stderr)[-500:]}")
+        return dt
+
+    base = min(run("header") for _ in range(3))
+    units = float(traj.n_atoms) * REF_FRAMES * n_vec
+    desc = (f"reference AMDAT binary (built here from its sources), `isf ... auto symmetric xyz 0 0 "
+            f"{REF_SHELLS}`: {REF_FRAMES} frames x {n_vec} q-vectors (shells 0..{REF_SHELLS}) x "
+            f"{traj.n_atoms} atoms; command time = run - system-block-only run ({base:.2f} s, best of 3)")
+    return (lambda: run("isf") - base), units, desc
+
+
 def run_reference(args):
+    """The reference arm: the reference AMDAT program's own CPU path (its `isf`
+    command) timed on this machine's host cores, on rank 0 only.  When its
+    sources are not available here, the oracle's FP64 restatement of the same
+    loop stands in (kind "port")."""
+    import tempfile
     world, rank, local, pg = dist_setup()
     if rank != 0:
         return
     from oracle import build_oracle
-    build_oracle.build_lib()
     threads = os.cpu_count() or 1
-    traj, scheme, lat = isf_workload()
-    vectors = lattice_halfspace(lat["period"], lat["kmax"])
-    # size one step to a few seconds of host work
-    rate, sample, dt = cpu_rhok_sample(traj, vectors, threads, target_s=4.0 * max(1, 12 // max(args.steps, 1)))
-    vals = []
-    for _ in range(args.warmup):
-        cpu_rhok_sample(traj, vectors, threads, target_s=dt * 4)
-    for _ in range(args.steps):
-        r, sample, _ = cpu_rhok_sample(traj, vectors, threads, target_s=dt * 4)
-        vals.append(r)
-    value = statistics.median(vals)
+    binary, why = None, ""
+    try:
+        binary = build_oracle.build_reference()
+        if binary is None:
+            why = "reference sources not present (baseline/_ref/src or AMDAT_REFERENCE)"
+    except Exception as e:  # a failed build falls back to the restatement
+        why = f"reference build failed: {str(e)[-200:]}"
+    config = {"workload": "coherent ISF + S(k): rho_k(t), N=32000 (80:20), L=33.6, linear frames of a "
+                          "sigma=0.03 random walk; the reference's Wave_Density loop over atoms x vectors"}
+    if binary is not None:
+        with tempfile.TemporaryDirectory() as tmp:
+            one, units, desc = reference_isf_sample(binary, threads, tmp)
+            for _ in range(args.warmup):
+                one()
+            secs = [one() for _ in range(args.steps)]
+        dt = statistics.median(secs)
+        value = units / dt
+        kind, cores = "reference", 1
+        note = (f"the reference is run with -n {threads}; its Wave_Density and correlator loops have no "
+                "OpenMP, so one core does the work. Work is linear in atoms x frames x vectors, so the "
+                "rate carries to the full 400-frame workload (extrapolated).")
+    else:
+        build_oracle.build_lib()
+        traj, scheme, lat = isf_workload()
+        vectors = lattice_halfspace(lat["period"], lat["kmax"])
+        rate, desc, dt, _, _ = cpu_rhok_sample(traj, vectors, threads,
+                                               target_s=4.0 * max(1, 12 // max(args.steps, 1)))
+        vals = []
+        for _ in range(args.warmup):
+            cpu_rhok_sample(traj, vectors, threads, target_s=dt * 4)
+        for _ in range(args.steps):
+            vals.append(cpu_rhok_sample(traj, vectors, threads, target_s=dt * 4)[0])
+        value = statistics.median(vals)
+        kind, cores = "port", threads
+        note = f"{why}; the oracle's FP64 restatement of the reference loop (OpenMP over vectors) instead"
+    config["sample_per_step"] = desc
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "atom·k/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * dt, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": "coherent ISF + S(k): rho_k(t), N=32000, L=33.6, 400 linear "
-                                   "frames, all half-space lattice k with |k|<=20",
-                       "sample_per_step": sample},
-            "cpu_baseline": {"value": value, "unit": "atom·k/s", "cores": threads,
-                             "kind": "port", "sample": sample},
+            "vs_baseline": None, "dtype": "f32" if kind == "reference" else "f64", "data": "synthetic",
+            "config": config,
+            "cpu_baseline": {"value": value, "unit": "atom·k/s", "cores": cores, "kind": kind,
+                             "sample": desc},
             "e2e": {"value": value, "unit": "atom·k/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
-            "note": "CPU restatement of the reference's Wave_Density loop (FP64, OpenMP over "
-                    "vectors); the reference binary builds only on the x86 host"}
+            "note": note}
     print(json.dumps(line), flush=True)
 
 
@@ -447,6 +527,47 @@ def structure_bench(torch, stream, device, args, n_atoms=100000, box=48.9, frame
                     "sum (fma = 2), phase rotation (2 mul + 2 fma = 6); peak = 2 flops x 128 FP32 "
                     "lanes x SMs x 2.07 GHz"}
     return out
+
+
+def isf_device_checks(torch, eng, E, d_rho, off, d_corr, d_pc, d_sk, N, T, shells=(20, 60, 120, 199)):
+    """FP64 restatement on the device of the correlator and S(k) of a few whole
+    shells, from the engine's own rho table of the timed workload: S(k) =
+    <|rho|^2> / N over frames and the shell's vectors, F(k, gap) = mean over the
+    gap's time pairs (the scheduler's own pair table) of the shell mean of
+    Re rho(t0) Re rho(t1) + Im rho(t0) Im rho(t1), divided by N.  Returns the
+    largest deviations relative to S(k)."""
+    g, a, b = E.scheme_pairs(eng.scheme, 0, 1)
+    dev = d_rho.device
+    g_t = torch.from_numpy(g.astype(np.int64)).to(dev)
+    a_t = torch.from_numpy(a.astype(np.int64)).to(dev)
+    b_t = torch.from_numpy(b.astype(np.int64)).to(dev)
+    G = d_corr.shape[0]
+    corr = d_corr.double().cpu().numpy()
+    pc = d_pc.cpu().numpy()
+    sk = d_sk.double().cpu().numpy() / (N * T)
+    worst_f, worst_s, used, pairs_match = 0.0, 0.0, [], True
+    for m in shells:
+        if m + 1 >= len(off) or off[m + 1] == off[m]:
+            continue
+        used.append(int(m))
+        r = d_rho[:, int(off[m]):int(off[m + 1])].double()  # [T, V, 2]
+        s_ref = float((r ** 2).sum(-1).mean()) / N
+        worst_s = max(worst_s, abs(sk[m] - s_ref) / s_ref)
+        acc = torch.zeros(G, dtype=torch.float64, device=dev)
+        cnt = torch.zeros(G, dtype=torch.float64, device=dev)
+        for c0 in range(0, len(g), 512):
+            ta, tb, tg = a_t[c0:c0 + 512], b_t[c0:c0 + 512], g_t[c0:c0 + 512]
+            prod = (r[ta] * r[tb]).sum(-1).mean(1)
+            acc.index_add_(0, tg, prod)
+            cnt.index_add_(0, tg, torch.ones_like(prod))
+        pairs_match = pairs_match and bool((cnt.cpu().numpy().astype(np.int64) == pc).all())
+        f_ref = (acc / cnt.clamp(min=1) / N).cpu().numpy()
+        f_eng = corr[:, m] / (np.maximum(pc, 1) * N)
+        worst_f = max(worst_f, float(np.abs(f_eng - f_ref).max()) / s_ref)
+    return {"shells": used, "sk_worst_rel": worst_s, "isf_worst_rel_to_sk": worst_f,
+            "pair_counts_match": pairs_match,
+            "rule": "FP64 torch restatement on the device of S(k) and F(k,t) over whole shells, "
+                    "from the engine's rho table of the timed workload"}
 
 
 def main():
@@ -571,17 +692,31 @@ def main():
         torch.cuda.synchronize()
         barrier(pg)
         t0 = time.perf_counter()
-        for _ in range(max(1, min(args.steps, 2))):
+        for _ in range(args.steps):
             e2e_step()
         torch.cuda.synchronize()
-        e2e_ms = max_over_ranks(pg, 1e3 * (time.perf_counter() - t0) / max(1, min(args.steps, 2)))
+        e2e_ms = max_over_ranks(pg, 1e3 * (time.perf_counter() - t0) / max(1, args.steps))
+        del pinned
+        # one more step whose results are kept and checked (outside every timed region):
+        # the correlator and S(k) against an FP64 restatement on the device, and the
+        # rho table's middle frame against the FP64 oracle in the CPU leg below
+        hh, _, _ = eng.wave_density_lattice(0, lat["kmax"], lat["dk"], lat["period"], frames)
+        d_rho = torch.empty((T, nk, 2), dtype=torch.float32, device="cuda")
+        eng.wave_density_read(hh, T, nk, out_device=d_rho.data_ptr())
+        eng.isf(hh, hh, off, out_device=(d_corr.data_ptr(), d_pc.data_ptr()))
+        eng.structure_factor(hh, hh, off, out_device=d_sk.data_ptr())
+        torch.cuda.synchronize()
+        eng.wave_density_free(hh)
+        checks = isf_device_checks(torch, eng, E, d_rho, off, d_corr, d_pc, d_sk, N, T)
+        rho_mid = d_rho[T // 2].cpu().numpy()
+        del d_rho
         result["isf"] = dict(
             value=value, ms=ms, launches=launches, nk=nk, ns=ns, T=T, N=N, kname=kname, issued=issued,
             lat_ms=lat_ms, n_lat=n_lat, steps=args.steps, isf_ms=ms_isf / max(n_isf, 1), achieved=achieved,
             fp32_peak_max=fp32_peak_max, clocks=clk, plain_rate=plain_rate,
             e2e=job_rate(units, world, e2e_ms), e2e_ms=e2e_ms,
-            h2d=int(T * N * 3 * 4), d2h=int(G * ns * 8 + G * 8 + ns * 8))
-        del pinned
+            h2d=int(T * N * 3 * 4), d2h=int(G * ns * 8 + G * 8 + ns * 8),
+            checks=checks, rho_mid=rho_mid, kv=kv)
 
     if args.only in ("", "msd"):
         mtraj, mscheme = msd_workload()
@@ -603,18 +738,26 @@ def main():
             mstep()
         torch.cuda.synchronize()
         msteps = 50
+        # the trajectory (13 MB) fits in L2: every timed step is bracketed by its own
+        # events and L2 is flushed (a 256 MB write) between steps, outside the events
+        flush = torch.empty(64 << 20, dtype=torch.float32, device="cuda")
         eng.profile_reset(True)
-        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(msteps):
+        evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+               for _ in range(msteps)]
+        for e0, e1 in evs:
+            flush.fill_(1.0)
+            e0.record(stream)
             mstep()
-        e1.record(stream)
+            e1.record(stream)
         torch.cuda.synchronize()
-        mms = max_over_ranks(pg, e0.elapsed_time(e1) / msteps)
+        mms = max_over_ranks(pg, sum(e0.elapsed_time(e1) for e0, e1 in evs) / msteps)
         n_d, ms_d = eng.profile_kernel("disp_mixed_kernel")
         eng.profile_reset(False)
         npairs = int(d_cnt.sum().item()) // mtraj.n_atoms
         munits = float(npairs) * mtraj.n_atoms
+        m_out = dict(sum_d2=d_out[0].cpu().numpy(), sum_d4=d_out[1].cpu().numpy(),
+                     cnt=d_cnt.cpu().numpy(), fs=d_fs.cpu().numpy())
+        e0, e1 = evs[0]
         # the same pass as a prepared plan replayed from a CUDA graph (what repeated
         # analyses of one list use): no per-call table building or launch overhead
         mplan = eng.plan([0], shells=(shell, off), period=16.8, flags=E.PLAN_GRAPH | E.PLAN_AUTOTUNE)
@@ -632,9 +775,29 @@ def main():
         mstep(precision=1)
         eng.synchronize()
         mplain = munits / (time.perf_counter() - t0)
+        # end to end through the C ABI: the trajectory from pinned host memory, the
+        # per-gap sums back to the host, every step
+        MT, MN = mtraj.n_frames, mtraj.n_atoms
+        mpinned = torch.empty((MT, MN, 3), dtype=torch.float32, pin_memory=True)
+        mpinned.numpy()[...] = mtraj.unwrapped
+
+        def me2e():
+            eng.upload_ptr(mpinned.data_ptr(), MT, MN, mtraj.box)
+            eng.set_scheme(mscheme)
+            return eng.disp(0, shells=(shell, off), period=16.8)
+
+        for _ in range(3):
+            me2e()
+        t0 = time.perf_counter()
+        for _ in range(msteps):
+            me2e()
+        me2e_ms = max_over_ranks(pg, 1e3 * (time.perf_counter() - t0) / msteps)
+        del mpinned
         result["msd"] = dict(value=job_rate(munits, world, mms), ms=mms, kernel_ms=ms_d / max(n_d, 1),
                              plain=mplain, npairs=npairs, nvec=len(shell),
-                             plan_value=job_rate(munits, world, pms), plan_ms=pms)
+                             plan_value=job_rate(munits, world, pms), plan_ms=pms,
+                             e2e=job_rate(munits, world, me2e_ms), e2e_ms=me2e_ms,
+                             h2d=int(MT * MN * 12), d2h=int(G * (8 + 8 + 8 + 8)), out=m_out)
 
     if args.only == "perlist":
         # profiling aid: the batched workload's per-list MSD + NGP plan alone
@@ -769,54 +932,71 @@ def main():
         eng.upload(ptraj.unwrapped, ptraj.box)
         eng.set_scheme(pscheme)
         frames = np.arange(50, dtype=np.int32)
-        eng.profile_reset(True)
         eng.rdf(0, 0, frames[:2], 21.15, 500)  # warm-up
         torch.cuda.synchronize()
+        eng.profile_reset(True)
         t0 = time.perf_counter()
         counts = eng.rdf(0, 0, frames, 21.15, 500)
         rdf_s = time.perf_counter() - t0
         n_rdf, ms_rdf = eng.profile_kernel("pair_hist_kernel")
+        eng.profile_reset(False)
         gs_units = 64000.0 * int(E.scheme_counts(eng.scheme)[2])
         eng.disp(0, n_bins=200, bin_max=5.0)
         t0 = time.perf_counter()
         out = eng.disp(0, n_bins=200, bin_max=5.0)
         gs_s = time.perf_counter() - t0
-        # distinct van Hove: every time pair is N^2 pair distances; time the
-        # 301 time pairs of a 25-frame linear scheme as a bounded sample
-        sub = synth.TimeScheme.linear(25, 1.0)
-        eng.upload(ptraj.unwrapped[:25], ptraj.box)
-        eng.set_scheme(sub)
-        npairs_sub = int(E.scheme_counts(eng.scheme)[2])
+        # distinct van Hove over every one of the 1226 time pairs of the 50-frame scheme
+        npairs_gd = int(E.scheme_counts(eng.scheme)[2])
+        eng.profile_reset(True)
         t0 = time.perf_counter()
         eng.vhd(0, 0, 5.0, 200)
         gd_s = time.perf_counter() - t0
+        n_gd, ms_gd = eng.profile_kernel("pair_hist_kernel")
         eng.profile_reset(False)
         n = 64000.0
         result["pairs"] = dict(rdf_rate=50 * n * (n - 1) / rdf_s, rdf_ms=1e3 * rdf_s,
-                               rdf_kernel_ms=ms_rdf / max(n_rdf, 1) * 50 / 2,
+                               rdf_kernel_ms=ms_rdf, rdf_launches=n_rdf,
                                gs_rate=gs_units / gs_s, gs_ms=1e3 * gs_s,
-                               gd_rate=npairs_sub * n * (n - 1) / gd_s, gd_ms=1e3 * gd_s,
-                               gd_sample=npairs_sub, rdf_total=int(counts.sum()))
+                               gd_rate=npairs_gd * n * (n - 1) / gd_s, gd_ms=1e3 * gd_s,
+                               gd_kernel_ms=ms_gd, gd_pairs=npairs_gd, rdf_total=int(counts.sum()))
 
     if args.only in ("", "structure"):
         result["structure"] = structure_bench(torch, stream, local, args)
 
     # CPU baseline on rank 0 (bounded samples of both workloads)
+    # The same oracle runs are the parity check of the timed results: the sampled
+    # rho elements of the kept step's middle frame, and the MSD and F_s sums of the
+    # last timed MSD step (all outside the timed regions).
     cpu = None
-    if rank == 0 and not args.no_cpu and args.only in ("", "isf"):
+    if rank == 0 and not args.no_cpu and args.only in ("", "isf", "msd"):
         from oracle import build_oracle
         build_oracle.build_lib()
         threads = os.cpu_count() or 1
-        traj, _, lat = isf_workload(args.frames)
-        vectors = lattice_halfspace(lat["period"], lat["kmax"])
-        rate, sample, dt = cpu_rhok_sample(traj, vectors, threads)
-        cpu = {"value": rate, "unit": "atom·k/s", "cores": threads, "kind": "port",
-               "sample": sample + f" ({dt:.1f} s)"}
+        if "isf" in result:
+            r = result["isf"]
+            traj, _, lat = isf_workload(args.frames)
+            rate, sample, dt, idx, ref = cpu_rhok_sample(traj, r["kv"], threads)
+            cpu = {"value": rate, "unit": "atom·k/s", "cores": threads, "kind": "port",
+                   "sample": sample + f" ({dt:.1f} s)"}
+            d = (r["rho_mid"][idx].astype(np.float64) - ref[0]) / math.sqrt(traj.n_atoms)
+            r["checks"]["rho_vs_fp64_oracle"] = {
+                "frame": traj.n_frames // 2, "vectors": int(len(idx)),
+                "rms_over_sqrtN": float(np.sqrt((d ** 2).mean())),
+                "worst_over_sqrtN": float(np.abs(d).max()),
+                "bound": "rms <= 1e-6, worst <= 3e-6 (times sqrt(N))"}
         if "msd" in result:
+            m = result["msd"]
             mtraj, mscheme = msd_workload()
-            r2, s2, dt2 = cpu_disp_sample(mtraj, mscheme, lattice_shell(16.8, 7.0, 7.2), threads)
-            result["msd"]["cpu"] = {"value": r2, "unit": "atom·time-pairs/s", "cores": threads,
-                                    "kind": "port", "sample": s2 + f" ({dt2:.1f} s)"}
+            r2, s2, dt2, d2, fs = cpu_disp_sample(mtraj, mscheme, lattice_shell(16.8, 7.0, 7.2), threads)
+            m["cpu"] = {"value": r2, "unit": "atom·time-pairs/s", "cores": threads,
+                        "kind": "port", "sample": s2 + f" ({dt2:.1f} s)"}
+            o = m["out"]
+            c = np.maximum(o["cnt"], 1)
+            m["checks"] = {
+                "msd_worst_rel": float((np.abs(o["sum_d2"] - d2) / np.maximum(np.abs(d2), 1e-300))[o["cnt"] > 0].max()),
+                "fs_worst_abs": float(np.abs(o["fs"] / c - fs / (c * m["nvec"])).max()),
+                "bound": "MSD <= 1e-6 relative, F_s <= 1e-6 absolute, against the FP64 oracle over every "
+                         "time pair and atom"}
 
     if rank != 0:
         eng.close()
@@ -872,6 +1052,7 @@ def main():
                            "sample": "1 frame, all vectors",
                            "mixed_over_plain": r["value"] / world / r["plain_rate"]},
             "isf_correlator_ms": r["isf_ms"],
+            "parity": r["checks"],
         })
     if cpu:
         line["cpu_baseline"] = cpu
@@ -884,9 +1065,23 @@ def main():
                "kernel_ms": m["kernel_ms"],
                "plan_graph": {"value": m["plan_value"], "ms_per_step": m["plan_ms"],
                               "note": "the same pass as a prepared plan replayed from a CUDA graph"},
-               "fp64_plain": {"value": m["plain"], "mixed_over_plain": m["value"] / world / m["plain"]}}
+               "fp64_plain": {"value": m["plain"], "mixed_over_plain": m["value"] / world / m["plain"]},
+               "e2e": {"value": m["e2e"], "unit": "atom·time-pairs/s", "h2d_bytes_per_step": m["h2d"],
+                       "d2h_bytes_per_step": m["d2h"], "ms_per_step": m["e2e_ms"]},
+               "l2": "trajectory 13 MB < L2: a 256 MB write flushes L2 between timed steps"}
+        fp32_peak = 2 * FP32_LANES_PER_SM * sm_count * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
+        fs_tflops = 8.0 * m["npairs"] * 4000 * m["nvec"] / (m["kernel_ms"] / 1e3) / 1e12
+        sec["roofline"] = {
+            "bound": "fp32", "achieved": fs_tflops, "peak": fp32_peak, "unit": "TFLOP/s",
+            "frac": fs_tflops / fp32_peak, "traffic": None, "kernel": "disp_mixed_kernel",
+            "kernel_ms": m["kernel_ms"],
+            "achieved_rule": "algorithmic: 8 FP32 flops per atom x time pair x vector (one complex multiply "
+                             "and accumulate of a recursive phase), 2246 vectors, 316 pairs, 4000 atoms",
+            "peak_source": "FP32 FMA peak = 2 x 128 lanes x SMs x sm_max_mhz of MEASURED_PEAKS.json"}
         if "cpu" in m:
             sec["cpu_baseline"] = m["cpu"]
+        if "checks" in m:
+            sec["parity"] = m["checks"]
         if "value" not in line:
             line.update({"value": m["value"], "unit": "atom·time-pairs/s",
                          "ms_per_step": m["ms"], "config": {"workload": sec["workload"]}})
@@ -919,7 +1114,15 @@ def main():
                                                   "unit": "GB/s", "frac": gbs_ns / hbm,
                                                   "algorithmic_bytes": b["alg_bytes"],
                                                   "bytes_rule": "sum_l N_l x 361 frames x 12 B "
-                                                                "(each list's trajectory once)"}},
+                                                                "(each list's trajectory once)",
+                                                  "unique_atom_frac": b["unit_bytes"] / (b["ms_msd_ns"] / 1e3) / 1e9 / hbm,
+                                                  "unique_atom_rule": "unit atoms x 361 frames x 12 B: the floor "
+                                                                      "for nested lists (every atom once)",
+                                                  "dram_bytes_ncu": PERLIST_DRAM_BYTES,
+                                                  "dram_frac": PERLIST_DRAM_BYTES / (b["ms_msd_ns"] / 1e3) / 1e9 / hbm,
+                                                  "dram_rule": "physical DRAM bytes of one launch (one ncu "
+                                                               "capture) over this launch's event time; nested "
+                                                               "lists re-read frames from L2"}},
                         "gathered_layout_ms": b["ms_gathered"]},
             "msd_ngp_fs": {"value": b["units"] / (b["ms_fs"] / 1e3), "unit": "atom·time-pairs/s",
                            "ms_per_step": b["ms_fs"], "tile": b["info_fs"],
@@ -943,7 +1146,15 @@ def main():
                               "call_ms": v["call_ms"], "member_terms": v["terms"],
                               "roofline": {"bound": "hbm", "achieved": gb, "peak": hbm, "unit": "GB/s",
                                            "frac": gb / hbm}}
-        bins_line["msd_fs"]["roofline"]["bound"] = "fp32 (one cospif per vector)"
+        # F_s per bin: one SFU cosine per member term and vector, against the MUFU rate
+        v = b["bins"]["msd_fs"]
+        cos_rate = v["terms"] * b["nvec"] / (v["kernel_ms"] / 1e3)
+        mufu_peak = MUFU_PER_SM_CLK * sm_count * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6
+        bins_line["msd_fs"]["roofline"] = {
+            "bound": "sfu", "achieved": cos_rate / 1e9, "peak": mufu_peak / 1e9, "unit": "G cos/s",
+            "frac": cos_rate / mufu_peak,
+            "rule": f"one MUFU cosine per member term x vector ({b['nvec']} vectors); peak = 16 MUFU "
+                    "results per clock per SM x SMs x sm_max_mhz"}
         line["batched"]["bins"] = bins_line
         if "value" not in line:
             line.update({"value": b["units"] / (b["ms_fs"] / 1e3), "unit": "atom·time-pairs/s",
@@ -959,14 +1170,28 @@ def main():
             "note": "ingest = the system block alone (parse, upload, CUDA context); analyses_s = script - ingest"}
     if "pairs" in result:
         q = result["pairs"]
+        fp32_peak = 2 * FP32_LANES_PER_SM * sm_count * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
+        n = 64000.0
+        rdf_fl = 10.0 * 50 * n * (n - 1) / 2 / (q["rdf_kernel_ms"] / 1e3) / 1e12
+        gd_fl = 10.0 * q["gd_pairs"] * n * (n - 1) / (q["gd_kernel_ms"] / 1e3) / 1e12
+        pair_rule = ("algorithmic: 10 FP32 flops per visited pair (3 differences, 3 minimum-image "
+                     "corrections, 3 multiply-adds of |r|^2, 1 bin division); peak = FP32 FMA peak "
+                     "= 2 x 128 lanes x SMs x sm_max_mhz")
         line["pairs"] = {
             "workload": "N=64000, L=42.3, 50 linear frames (sigma 0.1): RDF 500 bins to L/2 over all "
                         "frames; G_s 200 bins to 5.0 over all 1226 time pairs; G_d 200 bins to 5.0 "
-                        f"on the first {q['gd_sample']} time pairs of a 25-frame scheme",
+                        f"over all {q['gd_pairs']} time pairs",
             "rdf": {"value": q["rdf_rate"], "unit": "ordered pairs/s", "ms_per_step": q["rdf_ms"],
-                    "counted_pairs_in_range": q["rdf_total"]},
+                    "kernel_ms": q["rdf_kernel_ms"], "counted_pairs_in_range": q["rdf_total"],
+                    "roofline": {"bound": "fp32", "achieved": rdf_fl, "peak": fp32_peak, "unit": "TFLOP/s",
+                                 "frac": rdf_fl / fp32_peak, "kernel": "pair_hist_kernel",
+                                 "rule": pair_rule + "; the symmetric pass visits each unordered pair once"}},
             "vhs": {"value": q["gs_rate"], "unit": "atom·time-pairs/s", "ms_per_step": q["gs_ms"]},
-            "vhd": {"value": q["gd_rate"], "unit": "ordered pairs/s", "ms_per_step": q["gd_ms"]}}
+            "vhd": {"value": q["gd_rate"], "unit": "ordered pairs/s", "ms_per_step": q["gd_ms"],
+                    "kernel_ms": q["gd_kernel_ms"],
+                    "roofline": {"bound": "fp32", "achieved": gd_fl, "peak": fp32_peak, "unit": "TFLOP/s",
+                                 "frac": gd_fl / fp32_peak, "kernel": "pair_hist_kernel",
+                                 "rule": pair_rule + "; every ordered pair of every time pair"}}}
     if "perlist" in result:
         line["perlist"] = result["perlist"]
     if "bins_only" in result:

@@ -1,11 +1,14 @@
 # Compiles the reference AMDAT program from its own sources, where they lie,
-# into oracle/_ref/ (object files, a generated version header, an FFTW stub
-# header, the extracted q-vector tables and the AMDAT binary).  Nothing is
-# written into the reference tree.  Usage (from the repository root):
-#   make -f oracle/ref.mk REF=/path/to/AMDAT -j8
-# The reference is used only as the parity checker and CPU baseline.
-REF     ?= /root/reference
-OUT     ?= oracle/_ref
+# into OUT (object files, a generated version header, an FFTW stub header, the
+# extracted q-vector tables and the AMDAT binary).  Nothing is written into the
+# reference tree.  Usage (from the repository root):
+#   make -f oracle/ref.mk REF=/path/to/AMDAT OUT=oracle/_ref/<machine> -j8
+# (oracle/build_oracle.py runs it).  The reference is used only as the parity
+# checker and the benchmark's CPU reference.
+ifndef REF
+$(error REF must name the AMDAT source tree)
+endif
+OUT     ?= oracle/_ref/$(shell uname -m)
 CXX     ?= g++
 CC      ?= gcc
 SEMVER  := $(strip $(shell cat $(REF)/VERSION 2>/dev/null || echo 0.0.0))

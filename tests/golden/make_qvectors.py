@@ -14,7 +14,9 @@ import zipfile
 
 import numpy as np
 
-ref = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+if len(sys.argv) != 2:
+    raise SystemExit("usage: make_qvectors.py <AMDAT source tree>")
+ref = sys.argv[1]
 z = zipfile.ZipFile(os.path.join(ref, "src", "qvectors", "qvectors.zip"))
 vecs, off = [], [0]
 for m in range(99):

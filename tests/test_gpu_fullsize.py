@@ -56,7 +56,8 @@ def test_headline_lattice_density_isf_and_sk(eng, headline):
     assert (nk, ns) == (2562052, 200)
     kv, off = eng.wave_density_vectors(h, nk, ns)
     rho = eng.wave_density_read(h, T, nk)
-    L = lat["period"]
+    # the engine forms phases with the FP32 box length (33.6f): so does the oracle
+    L = float(np.float32(lat["period"]))
     wrapped = traj.wrapped()
 
     # the lattice oracle against the direct FP64 sum on a few vectors
@@ -109,7 +110,7 @@ def test_msd_workload_full_size(eng):
     assert int(cnt.sum()) == 316 * traj.n_atoms
     np.testing.assert_allclose(out["sum_d2"], d2, rtol=1e-6, atol=1e-12)
     np.testing.assert_allclose(out["sum_d4"], d4, rtol=1e-6, atol=1e-14)
-    _, fs = orc.disp_fs_parallel(s, traj.unwrapped, shell, 16.8, THREADS)
+    _, fs = orc.disp_fs_parallel(s, traj.unwrapped, shell, float(np.float32(16.8)), THREADS)
     c = np.maximum(cnt, 1)
     err = np.abs(out["fs_sum"][:, 0] / c - fs / (c * len(shell))).max()
     print(f"F_s, 2246 vectors x 316 pairs x 4000 atoms: worst {err:.3e}")
@@ -137,7 +138,7 @@ def test_batched_largest_list_from_shared_plan(eng):
     np.testing.assert_allclose(out["sum_d4"][-1], d4, rtol=1e-6, atol=1e-14)
     # F_s of the first shell (m = 10) over every time pair of the largest list
     kv, off = shells
-    _, fs = orc.disp_fs_parallel(s, u[:, :big], kv[off[0]:off[1]], L, THREADS)
+    _, fs = orc.disp_fs_parallel(s, u[:, :big], kv[off[0]:off[1]], float(np.float32(L)), THREADS)
     c = np.maximum(cnt, 1)
     err = np.abs(out["fs_sum"][-1][:, 0] / c - fs / (c * (off[1] - off[0]))).max()
     print(f"largest list ({big} atoms, {int(cnt.sum()) // big} pairs): F_s shell 10 worst {err:.3e}")
