@@ -581,6 +581,8 @@ def main():
                                                    "perlist", "bins"],
                     help="run one workload only (profiling)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
+    ap.add_argument("--pair-frames", type=int, default=50,
+                    help="frames of the RDF / van Hove workload (profiling runs use fewer)")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -927,11 +929,12 @@ def main():
     if args.only in ("", "pairs"):
         # RDF + van Hove self/distinct: N=64000, L=42.3, 50 linear frames, sigma=0.1
         from amdat_gb300 import synth
-        pscheme = synth.TimeScheme.linear(50, 1.0)
+        PF = args.pair_frames
+        pscheme = synth.TimeScheme.linear(PF, 1.0)
         ptraj = synth.random_walk(64000, 42.3, pscheme, 0.1, seed=3, time_scaled=False)
         eng.upload(ptraj.unwrapped, ptraj.box)
         eng.set_scheme(pscheme)
-        frames = np.arange(50, dtype=np.int32)
+        frames = np.arange(PF, dtype=np.int32)
         eng.rdf(0, 0, frames[:2], 21.15, 500)  # warm-up
         torch.cuda.synchronize()
         eng.profile_reset(True)
@@ -954,7 +957,7 @@ def main():
         n_gd, ms_gd = eng.profile_kernel("pair_hist_kernel")
         eng.profile_reset(False)
         n = 64000.0
-        result["pairs"] = dict(rdf_rate=50 * n * (n - 1) / rdf_s, rdf_ms=1e3 * rdf_s,
+        result["pairs"] = dict(frames=PF, rdf_rate=PF * n * (n - 1) / rdf_s, rdf_ms=1e3 * rdf_s,
                                rdf_kernel_ms=ms_rdf, rdf_launches=n_rdf,
                                gs_rate=gs_units / gs_s, gs_ms=1e3 * gs_s,
                                gd_rate=npairs_gd * n * (n - 1) / gd_s, gd_ms=1e3 * gd_s,
@@ -1172,15 +1175,15 @@ def main():
         q = result["pairs"]
         fp32_peak = 2 * FP32_LANES_PER_SM * sm_count * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
         n = 64000.0
-        rdf_fl = 10.0 * 50 * n * (n - 1) / 2 / (q["rdf_kernel_ms"] / 1e3) / 1e12
+        rdf_fl = 10.0 * q["frames"] * n * (n - 1) / 2 / (q["rdf_kernel_ms"] / 1e3) / 1e12
         gd_fl = 10.0 * q["gd_pairs"] * n * (n - 1) / (q["gd_kernel_ms"] / 1e3) / 1e12
         pair_rule = ("algorithmic: 10 FP32 flops per visited pair (3 differences, 3 minimum-image "
                      "corrections, 3 multiply-adds of |r|^2, 1 bin division); peak = FP32 FMA peak "
                      "= 2 x 128 lanes x SMs x sm_max_mhz")
         line["pairs"] = {
-            "workload": "N=64000, L=42.3, 50 linear frames (sigma 0.1): RDF 500 bins to L/2 over all "
-                        "frames; G_s 200 bins to 5.0 over all 1226 time pairs; G_d 200 bins to 5.0 "
-                        f"over all {q['gd_pairs']} time pairs",
+            "workload": f"N=64000, L=42.3, {q['frames']} linear frames (sigma 0.1): RDF 500 bins to L/2 "
+                        f"over all frames; G_s 200 bins to 5.0 and G_d 200 bins to 5.0 over all "
+                        f"{q['gd_pairs']} time pairs",
             "rdf": {"value": q["rdf_rate"], "unit": "ordered pairs/s", "ms_per_step": q["rdf_ms"],
                     "kernel_ms": q["rdf_kernel_ms"], "counted_pairs_in_range": q["rdf_total"],
                     "roofline": {"bound": "fp32", "achieved": rdf_fl, "peak": fp32_peak, "unit": "TFLOP/s",

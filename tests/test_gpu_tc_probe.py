@@ -37,6 +37,23 @@ def test_umma_layout(probe):
     assert np.abs(got - ref).max() < 1e-4 * max(1.0, np.abs(ref).max()), np.abs(got - ref).max()
 
 
+def test_umma_a_from_tensor_memory(probe):
+    """The A operand read from tensor memory (the layout the lattice kernel's
+    builders write): D = A @ B^T for a 128x32 A and a 32x32 B."""
+    import torch
+    g = torch.Generator().manual_seed(1)
+    A = (torch.rand(128, 32, generator=g) * 2 - 1).half().cuda()
+    B = (torch.rand(32, 32, generator=g) * 2 - 1).half().cuda()
+    ref = (A.double().cpu() @ B.double().cpu().T).numpy()
+    D = torch.zeros(128, 32, dtype=torch.float32, device="cuda")
+    err = torch.zeros(1, dtype=torch.int32, device="cuda")
+    st = probe.tc_probe_tmem_a_run(C.c_void_p(A.data_ptr()), C.c_void_p(B.data_ptr()),
+                                   C.c_void_p(D.data_ptr()), C.c_void_p(err.data_ptr()))
+    assert st == 0 and int(err.item()) == 0
+    got = D.cpu().numpy()
+    assert np.abs(got - ref).max() < 1e-4 * max(1.0, np.abs(ref).max()), np.abs(got - ref).max()
+
+
 def test_bounded_wait_times_out_and_context_stays_usable(probe):
     """A wait on an mbarrier that nothing completes gives up after its bounded
     number of polls and reports it; the context then still runs kernels."""
