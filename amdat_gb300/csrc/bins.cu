@@ -69,6 +69,95 @@ __device__ __forceinline__ int bin_axis(float x, float lo, float hi, int n) {
   return (int)__dmul_rn(__ddiv_rn(num, den), (double)(float)n);
 }
 
+// --- distance bins (Trajectory_List_Bins distance constructors) -------------
+// The reference's FP32 chains, operation by operation (see amdat_bins_distance):
+// Coordinate::vector_unwrapped + length (src/coordinate.cpp:98-124,
+// src/coordinate.h:55) to the nearest member of another list, the minimum-image
+// distance to a point, or the distance to a plane.
+constexpr int BD_THREADS = 256;
+constexpr int BD_TILE = 1024;
+
+__device__ __forceinline__ float vu_axis(float d, float L) {
+  const float h = __fdiv_rn(L, 2.f);
+  if (d > h) return __fsub_rn(d, L);
+  if (d < -h) return __fadd_rn(d, L);
+  return d;
+}
+
+__device__ __forceinline__ float len3(float x, float y, float z) {
+  return __fsqrt_rn(__fadd_rn(__fadd_rn(__fmul_rn(x, x), __fmul_rn(y, y)), __fmul_rn(z, z)));
+}
+
+struct BDParams {
+  const float* w;
+  int64_t n_pad;
+  int32_t kind, axis, direction, n_bins;
+  int32_t n_binned, n_from;
+  int32_t binned_first, from_first;      // contiguous lists: first atom
+  const int32_t* binned_idx;             // gathered lists: atom indices (else null)
+  const int32_t* from_idx;
+  float3 box, point;
+  float position, thickness, box_max;
+  int32_t* bins;                         // [frames][n_pad], -1 already
+};
+
+__global__ void __launch_bounds__(BD_THREADS) bins_distance_kernel(BDParams p) {
+  __shared__ float sx[BD_TILE], sy[BD_TILE], sz[BD_TILE];
+  const int t = blockIdx.y;
+  const int i = blockIdx.x * BD_THREADS + threadIdx.x;
+  const float* W = p.w + (int64_t)t * 3 * p.n_pad;
+  const bool live = i < p.n_binned;
+  const int a = live ? (p.binned_idx ? p.binned_idx[i] : p.binned_first + i) : 0;
+  const float x = live ? W[a] : 0.f, y = live ? W[p.n_pad + a] : 0.f, z = live ? W[2 * p.n_pad + a] : 0.f;
+  float length = 0.f;
+  if (p.kind == 0) {
+    // nearest member of the other list, starting from the box's largest edge
+    length = p.box_max;
+    for (int j0 = 0; j0 < p.n_from; j0 += BD_TILE) {
+      const int nj = min(BD_TILE, p.n_from - j0);
+      __syncthreads();
+      for (int q = threadIdx.x; q < nj; q += BD_THREADS) {
+        const int aj = p.from_idx ? p.from_idx[j0 + q] : p.from_first + j0 + q;
+        sx[q] = W[aj];
+        sy[q] = W[p.n_pad + aj];
+        sz[q] = W[2 * p.n_pad + aj];
+      }
+      __syncthreads();
+      if (live)
+        for (int q = 0; q < nj; ++q) {
+          const float tl = len3(vu_axis(__fsub_rn(x, sx[q]), p.box.x), vu_axis(__fsub_rn(y, sy[q]), p.box.y),
+                                vu_axis(__fsub_rn(z, sz[q]), p.box.z));
+          length = tl < length ? tl : length;
+        }
+    }
+  } else if (p.kind == 1) {
+    // dist = r - point; dist -= box * (dist / (box * 0.5)).integer()
+    const float c[3] = {x, y, z}, pt[3] = {p.point.x, p.point.y, p.point.z};
+    const float L[3] = {p.box.x, p.box.y, p.box.z};
+    float d[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      d[k] = __fsub_rn(c[k], pt[k]);
+      const float q = (float)(int)__fdiv_rn(d[k], __fmul_rn(L[k], 0.5f));
+      d[k] = __fsub_rn(d[k], __fmul_rn(L[k], q));
+    }
+    length = len3(d[0], d[1], d[2]);
+  } else {
+    const float c = p.axis == 0 ? x : (p.axis == 1 ? y : z);
+    const float L = p.axis == 0 ? p.box.x : (p.axis == 1 ? p.box.y : p.box.z);
+    const float dist = __fsub_rn(c, p.position);
+    if (p.direction == 0)  // average: |L * int(dist / (L * .5)) - dist|, the quotient in double
+      length = fabsf(__fsub_rn(__fmul_rn(L, (float)(int)__ddiv_rn((double)dist, __dmul_rn((double)L, 0.5))), dist));
+    else if (p.direction == 1)  // above
+      length = dist < 0.f ? __fadd_rn(L, dist) : dist;
+    else  // below
+      length = dist < 0.f ? fabsf(dist) : __fsub_rn(L, dist);
+  }
+  if (!live) return;
+  const int b = (int)__fdiv_rn(length, p.thickness);
+  if (b >= 0 && b < p.n_bins) p.bins[(int64_t)t * p.n_pad + a] = b;
+}
+
 __global__ void bins_assign_kernel(const float* __restrict__ w, int64_t n_pad, int32_t n_atoms,
                                    int64_t n_terms, int3 nb, float3 lo, float3 hi,
                                    int32_t* __restrict__ bins) {
@@ -472,6 +561,64 @@ amdat_status amdat_bins_create(amdat_ctx* ctx, int32_t nx, int32_t ny, int32_t n
             ctx->w.ptr, ctx->n_pad, ctx->n_atoms, n, make_int3(nx, ny, nz), make_float3(lo[0], lo[1], lo[2]),
             make_float3(hi[0], hi[1], hi[2]), m->bin.ptr);
         check_launch("bins_assign_kernel");
+        count_launch(ctx);
+      }
+    } catch (...) {
+      delete m;
+      throw;
+    }
+    const int32_t h = ctx->next_bins++;
+    ctx->bin_maps[h] = m;
+    *handle = h;
+  });
+}
+
+amdat_status amdat_bins_distance(amdat_ctx* ctx, int32_t kind, int32_t binned, int32_t from,
+                                 const float* point, int32_t axis, int32_t direction, float position,
+                                 float thickness, int32_t n_bins, int32_t* handle) {
+  return guarded([&] {
+    check_ctx(ctx);
+    if (!ctx->have_traj) throw Error(AMDAT_ERR_STATE, "no trajectory uploaded");
+    AMDAT_REQUIRE(handle != nullptr, "null handle");
+    AMDAT_REQUIRE(kind >= 0 && kind <= 2, "kind must be 0 (trajectory), 1 (point) or 2 (plane)");
+    AMDAT_REQUIRE(n_bins >= 1 && n_bins <= (1 << 24), "n_bins must be in [1, 2^24]");
+    AMDAT_REQUIRE(thickness > 0.0f, "bin thickness must be positive");
+    AMDAT_REQUIRE(kind != 1 || point != nullptr, "null point");
+    AMDAT_REQUIRE(kind != 2 || (axis >= 0 && axis <= 2 && direction >= 0 && direction <= 2),
+                  "plane axis must be 0..2 and direction 0 (average), 1 (above) or 2 (below)");
+    const ListEntry& lb = list_entry(ctx, binned);
+    const ListEntry* lf = kind == 0 ? &list_entry(ctx, from) : nullptr;
+    auto* m = new BinMap();
+    try {
+      m->nx = (kind == 2 && axis == 0) ? n_bins : 1;
+      m->ny = (kind == 2 && axis == 1) ? n_bins : 1;
+      m->nz = (kind != 2 || axis == 2) ? n_bins : 1;
+      m->n_frames = ctx->n_frames, m->n_pad = ctx->n_pad;
+      m->bin.reserve((size_t)ctx->n_frames * ctx->n_pad);
+      AMDAT_CUDA(cudaMemsetAsync(m->bin.ptr, 0xff, (size_t)ctx->n_frames * ctx->n_pad * 4, ctx->stream));
+      if (lb.n > 0 && ctx->n_frames > 0) {
+        BDParams p{};
+        p.w = ctx->w.ptr;
+        p.n_pad = ctx->n_pad;
+        p.kind = kind, p.axis = axis, p.direction = direction, p.n_bins = n_bins;
+        p.n_binned = lb.n;
+        p.binned_first = lb.first;
+        p.binned_idx = lb.contiguous ? nullptr : lb.idx.ptr;
+        if (lf) {
+          p.n_from = lf->n;
+          p.from_first = lf->first;
+          p.from_idx = lf->contiguous ? nullptr : lf->idx.ptr;
+        }
+        p.box = make_float3(ctx->box[0], ctx->box[1], ctx->box[2]);
+        p.box_max = std::max(ctx->box[0], std::max(ctx->box[1], ctx->box[2]));
+        p.point = point ? make_float3(point[0], point[1], point[2]) : make_float3(0.f, 0.f, 0.f);
+        p.position = position;
+        p.thickness = thickness;
+        p.bins = m->bin.ptr;
+        AMDAT_REQUIRE(ctx->n_frames <= 65535, "at most 65535 frames");
+        dim3 grid((unsigned)ceil_div(lb.n, BD_THREADS), (unsigned)ctx->n_frames);
+        bins_distance_kernel<<<grid, BD_THREADS, 0, ctx->stream>>>(p);
+        check_launch("bins_distance_kernel");
         count_launch(ctx);
       }
     } catch (...) {

@@ -382,6 +382,129 @@ struct LatticePlan {
   std::vector<int32_t> entry_k;    // tile-major map to shell-sorted k, -1 = unused
 };
 
+// ---------------------------------------------------------------------------
+// binned structure factor: Bin_Static_Analysis<Structure_Factor>
+// (src/bin_static_analysis.h:69-111, src/control.cpp:2730-2737): bin b analyses
+// the time-dependent list (list && bin b), i.e. at each frame the list members
+// whose bin at that frame is b
+// ---------------------------------------------------------------------------
+constexpr int SKB_MAX_BINS = 4096;
+
+// each frame's list members sorted by bin, list order kept within a bin: one
+// warp per frame; seg[f][b] .. seg[f][b + 1] are bin b's slots of perm[f][]
+// (positions in the list)
+__global__ void __launch_bounds__(32)
+    bins_segment_kernel(const int32_t* __restrict__ bin_map, int64_t n_pad, const int32_t* __restrict__ frames,
+                        ListView lst, int32_t n_bins, int32_t* __restrict__ seg, int32_t* __restrict__ perm) {
+  extern __shared__ int32_t cursor[];  // [n_bins]
+  const int f = blockIdx.x, lane = threadIdx.x;
+  const int32_t* B = bin_map + (int64_t)frames[f] * n_pad;
+  for (int b = lane; b < n_bins; b += 32) cursor[b] = 0;
+  __syncwarp();
+  for (int i = lane; i < lst.n; i += 32) {
+    const int b = B[lst.idx ? lst.idx[i] : lst.first + i];
+    if (b >= 0 && b < n_bins) atomicAdd(&cursor[b], 1);
+  }
+  __syncwarp();
+  int32_t* S = seg + (int64_t)f * (n_bins + 1);
+  if (lane == 0) {
+    int s = 0;
+    for (int b = 0; b < n_bins; ++b) {
+      const int c = cursor[b];
+      cursor[b] = s;
+      S[b] = s;
+      s += c;
+    }
+    S[n_bins] = s;
+  }
+  __syncwarp();
+  for (int i0 = 0; i0 < lst.n; i0 += 32) {
+    const int i = i0 + lane;
+    int b = -1;
+    if (i < lst.n) {
+      b = B[lst.idx ? lst.idx[i] : lst.first + i];
+      if (b >= n_bins) b = -1;
+    }
+    // lanes of one bin take consecutive slots in lane (= list) order
+    const unsigned peers = __match_any_sync(0xffffffffu, b);
+    const int rank = __popc(peers & ((1u << lane) - 1u));
+    if (b >= 0) perm[(int64_t)f * lst.n + cursor[b] + rank] = i;
+    __syncwarp();
+    if (b >= 0 && rank == 0) cursor[b] += __popc(peers);
+    __syncwarp();
+  }
+}
+
+// P[b][k] = sum over frames, in frame order, of |rho_b(f, k)|^2 in FP64, where
+// rho_b(f, k) is the compensated FP32 sum of exp(i k.r) over bin b's members at
+// frame f (the list-mode phases and accumulation)
+__global__ void __launch_bounds__(RL_THREADS)
+    sk_bins_kernel(const int4* __restrict__ fx, int32_t n_list, int32_t n_frames,
+                   const int32_t* __restrict__ seg, const int32_t* __restrict__ perm, int32_t n_bins,
+                   const int4* __restrict__ kv, int32_t n_k, double* __restrict__ P) {
+  __shared__ int4 s_at[RL_ATOMS];
+  const int b = blockIdx.y;
+  const int k0 = blockIdx.x * RL_TILE;
+  int4 n[RL_KPT];
+  double p2[RL_KPT];
+#pragma unroll
+  for (int j = 0; j < RL_KPT; ++j) {
+    const int k = k0 + j * RL_THREADS + threadIdx.x;
+    n[j] = k < n_k ? kv[k] : make_int4(0, 0, 0, 0);
+    p2[j] = 0.0;
+  }
+  for (int f = 0; f < n_frames; ++f) {
+    const int s0 = seg[(int64_t)f * (n_bins + 1) + b], s1 = seg[(int64_t)f * (n_bins + 1) + b + 1];
+    const int4* F = fx + (int64_t)f * n_list;
+    const int32_t* Pm = perm + (int64_t)f * n_list;
+    KC acc[RL_KPT];
+    float pr[RL_KPT], pi[RL_KPT];
+#pragma unroll
+    for (int j = 0; j < RL_KPT; ++j) {
+      acc[j] = KC{0.f, 0.f, 0.f, 0.f};
+      pr[j] = pi[j] = 0.f;
+    }
+    int since_fold = 0;
+    for (int a0 = s0; a0 < s1; a0 += RL_ATOMS) {
+      const int na = min(RL_ATOMS, s1 - a0);
+      __syncthreads();
+      for (int i = threadIdx.x; i < na; i += RL_THREADS) s_at[i] = F[Pm[a0 + i]];
+      __syncthreads();
+      for (int a = 0; a < na; ++a) {
+        const int4 q = s_at[a];
+#pragma unroll
+        for (int j = 0; j < RL_KPT; ++j) {
+          const int32_t ph = (int32_t)((uint32_t)n[j].x * (uint32_t)q.x + (uint32_t)n[j].y * (uint32_t)q.y +
+                                       (uint32_t)n[j].z * (uint32_t)q.z);
+          float s, c;
+          phase_sincos(ph, &s, &c);
+          pr[j] += c;
+          pi[j] += s;
+        }
+        if (++since_fold == 128) {
+#pragma unroll
+          for (int j = 0; j < RL_KPT; ++j) {
+            kc_add(acc[j], pr[j], pi[j]);
+            pr[j] = pi[j] = 0.f;
+          }
+          since_fold = 0;
+        }
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < RL_KPT; ++j) {
+      kc_add(acc[j], pr[j], pi[j]);
+      const double re = (double)__fsub_rn(acc[j].sr, acc[j].cr), im = (double)__fsub_rn(acc[j].si, acc[j].ci);
+      p2[j] += re * re + im * im;
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < RL_KPT; ++j) {
+    const int k = k0 + j * RL_THREADS + threadIdx.x;
+    if (k < n_k) P[(int64_t)b * n_k + k] = p2[j];
+  }
+}
+
 }  // namespace amdat
 namespace amdat {
 void rhok_tc_run(amdat_ctx* ctx, const TcPlan& P, const int4* fx, int32_t n_list, int32_t n_frames,
@@ -617,6 +740,84 @@ amdat_status amdat_wave_density_free(amdat_ctx* ctx, int32_t handle) {
     rho_release(ctx, it->second->rho);
     delete it->second;
     ctx->densities.erase(it);
+  });
+}
+
+amdat_status amdat_structure_factor_bins(amdat_ctx* ctx, int32_t list, int32_t bins,
+                                         const int32_t* kvec_n, int32_t n_k, const int32_t* shell_offsets,
+                                         int32_t n_shells, float period, const int32_t* frames,
+                                         int32_t n_frames, double* s_sum, int64_t* n_atoms) {
+  return guarded([&] {
+    check_ctx(ctx);
+    if (!ctx->have_traj) throw Error(AMDAT_ERR_STATE, "no trajectory uploaded");
+    AMDAT_REQUIRE(s_sum != nullptr && n_atoms != nullptr, "null output");
+    AMDAT_REQUIRE(n_k >= 0 && (n_k == 0 || kvec_n != nullptr), "bad vector list");
+    AMDAT_REQUIRE(shell_offsets != nullptr && n_shells >= 1, "bad shell offsets");
+    AMDAT_REQUIRE(shell_offsets[0] == 0 && shell_offsets[n_shells] == n_k, "shell offsets must span 0..n_k");
+    for (int s = 0; s < n_shells; ++s)
+      AMDAT_REQUIRE(shell_offsets[s + 1] >= shell_offsets[s], "shell offsets must not decrease");
+    AMDAT_REQUIRE(period > 0.0f, "period must be positive");
+    check_frames(ctx, frames, n_frames);
+    for (int i = 0; i < 3 * n_k; ++i) AMDAT_REQUIRE(std::abs(kvec_n[i]) < (1 << 20), "lattice index too large");
+    const ListEntry& e = list_entry(ctx, list);
+    auto it = ctx->bin_maps.find(bins);
+    AMDAT_REQUIRE(it != ctx->bin_maps.end(), "unknown bin map handle");
+    const BinMap& m = *it->second;
+    AMDAT_REQUIRE(m.n_frames == ctx->n_frames && m.n_pad == ctx->n_pad, "bin map made for another trajectory");
+    const int32_t B = m.nx * m.ny * m.nz;
+    AMDAT_REQUIRE(B >= 1 && B <= SKB_MAX_BINS, "at most 4096 bins");
+    std::vector<int32_t> fr(frames, frames + n_frames);
+    std::vector<int4> kv4((size_t)std::max(n_k, 1));
+    for (int k = 0; k < n_k; ++k) kv4[k] = make_int4(kvec_n[3 * k], kvec_n[3 * k + 1], kvec_n[3 * k + 2], 0);
+    auto align = [](size_t x) { return (x + 255) & ~(size_t)255; };
+    const int64_t nl = std::max(e.n, 1);
+    size_t o = 0;
+    const size_t o_fr = o; o = align(o + (size_t)std::max(n_frames, 1) * 4);
+    const size_t o_kv = o; o = align(o + kv4.size() * sizeof(int4));
+    const size_t o_seg = o; o = align(o + (size_t)std::max(n_frames, 1) * (B + 1) * 4);
+    const size_t o_perm = o; o = align(o + (size_t)std::max(n_frames, 1) * nl * 4);
+    const size_t o_p = o; o = align(o + (size_t)B * std::max(n_k, 1) * 8);
+    unsigned char* base = ctx->scratch.reserve(o);
+    int4* fx = (int4*)ctx->scratch2.reserve((size_t)std::max(n_frames, 1) * nl * sizeof(int4));
+    if (n_frames > 0)
+      AMDAT_CUDA(cudaMemcpyAsync(base + o_fr, fr.data(), (size_t)n_frames * 4, cudaMemcpyHostToDevice, ctx->stream));
+    AMDAT_CUDA(cudaMemcpyAsync(base + o_kv, kv4.data(), kv4.size() * sizeof(int4), cudaMemcpyHostToDevice, ctx->stream));
+    std::vector<double> P((size_t)B * std::max(n_k, 1), 0.0);
+    std::vector<int32_t> seg((size_t)std::max(n_frames, 1) * (B + 1), 0);
+    if (n_frames > 0 && e.n > 0) {
+      fixed_turns_launch(ctx, (const int32_t*)(base + o_fr), n_frames, e, period, fx);
+      bins_segment_kernel<<<(unsigned)n_frames, 32, (size_t)B * 4, ctx->stream>>>(
+          m.bin.ptr, m.n_pad, (const int32_t*)(base + o_fr), view(e), B, (int32_t*)(base + o_seg),
+          (int32_t*)(base + o_perm));
+      check_launch("bins_segment_kernel");
+      count_launch(ctx);
+      if (n_k > 0) {
+        AMDAT_REQUIRE(B <= 65535, "too many bins for one launch");
+        dim3 grid((unsigned)ceil_div(n_k, RL_TILE), (unsigned)B);
+        KernelTimer kt(ctx, "sk_bins_kernel");
+        sk_bins_kernel<<<grid, RL_THREADS, 0, ctx->stream>>>(fx, e.n, n_frames, (const int32_t*)(base + o_seg),
+                                                            (const int32_t*)(base + o_perm), B,
+                                                            (const int4*)(base + o_kv), n_k, (double*)(base + o_p));
+        check_launch("sk_bins_kernel");
+        count_launch(ctx);
+        AMDAT_CUDA(cudaMemcpyAsync(P.data(), base + o_p, (size_t)B * n_k * 8, cudaMemcpyDeviceToHost, ctx->stream));
+      }
+      AMDAT_CUDA(cudaMemcpyAsync(seg.data(), base + o_seg, (size_t)n_frames * (B + 1) * 4, cudaMemcpyDeviceToHost,
+                                 ctx->stream));
+    }
+    AMDAT_CUDA(cudaStreamSynchronize(ctx->stream));
+    // shell means in a fixed order (FP64), member counts summed over frames
+    for (int b = 0; b < B; ++b) {
+      for (int s = 0; s < n_shells; ++s) {
+        const int h = shell_offsets[s + 1] - shell_offsets[s];
+        double acc = 0.0;
+        for (int k = shell_offsets[s]; k < shell_offsets[s + 1]; ++k) acc += P[(size_t)b * n_k + k];
+        s_sum[(size_t)b * n_shells + s] = h ? acc / h : 0.0;
+      }
+      int64_t na = 0;
+      for (int f = 0; f < n_frames; ++f) na += seg[(size_t)f * (B + 1) + b + 1] - seg[(size_t)f * (B + 1) + b];
+      n_atoms[b] = na;
+    }
   });
 }
 

@@ -57,6 +57,7 @@ EXPORTED = [
     "amdat_gsmooth_adjoint", "amdat_structure_factor_adjoint",
     "amdat_boxify", "amdat_bins_create", "amdat_bins_read", "amdat_bins_free",
     "amdat_disp_bins_run", "amdat_disp_bins_axes_run", "amdat_fast_particles", "amdat_timelist_create",
+    "amdat_bins_distance", "amdat_structure_factor_bins",
 ]
 
 PLAN_AUTOTUNE, PLAN_GRAPH, PLAN_NO_SHARING = 1, 2, 4
@@ -359,6 +360,28 @@ class Engine:
         h = C.c_int32()
         _check(lib().amdat_timelist_create(self._ctx, _p(off), _p(idx), C.byref(h)))
         return h.value
+
+    def bins_distance(self, kind, binned, from_list=0, point=(0.0, 0.0, 0.0), axis=0, direction=0,
+                      position=0.0, thickness=1.0, n_bins=1) -> int:
+        """Distance bin map (create_bin_list distance ...): kind 0 trajectory, 1 point, 2 plane."""
+        pt = np.ascontiguousarray(point, np.float32)
+        h = C.c_int32()
+        _check(lib().amdat_bins_distance(self._ctx, int(kind), int(binned), int(from_list), _p(pt), int(axis),
+                                         int(direction), C.c_float(position), C.c_float(thickness), int(n_bins),
+                                         C.byref(h)))
+        return h.value
+
+    def structure_factor_bins(self, list_h, bins_h, n_bins, kvec_n, shell_off, period, frames):
+        """Per-bin (sum over frames and shell of |rho|^2 / H, member-frame count)."""
+        kv = _i32(kvec_n).reshape(-1)
+        off = _i32(shell_off)
+        fr = _i32(frames)
+        S = len(off) - 1
+        s = np.zeros((n_bins, S))
+        n = np.zeros(n_bins, np.int64)
+        _check(lib().amdat_structure_factor_bins(self._ctx, int(list_h), int(bins_h), _p(kv), len(kv) // 3, _p(off),
+                                                 S, C.c_float(period), _p(fr), len(fr), _p(s), _p(n)))
+        return s, n
 
     def bins_free(self, handle):
         _check(lib().amdat_bins_free(self._ctx, int(handle)))

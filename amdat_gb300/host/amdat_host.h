@@ -145,6 +145,16 @@ class Trajectory_List_Bins {
   Trajectory_List_Bins(System* sys, int nx, int ny, int nz);
   Trajectory_List_Bins(System* sys, int nx, int ny, int nz, float xlo, float xhi, float ylo, float yhi,
                        float zlo, float zhi);
+  // distance bin lists (create_bin_list distance ..., src/control.cpp:3915-3990;
+  // src/trajectory_list_bins.cpp:461-948): the members of `binning` by their
+  // distance to the nearest member of `clustered`, to a point, or to a plane
+  // ("x"/"y"/"z" at `position`, direction "average", "above" or "below"), in
+  // bins of `thickness`; at most the number of bins the box holds
+  Trajectory_List_Bins(System* sys, float thickness, int n_bins, Trajectory_List* binning,
+                       Trajectory_List* clustered);
+  Trajectory_List_Bins(System* sys, float thickness, int n_bins, Trajectory_List* binning,
+                       const std::string& plane, float position, const std::string& direction);
+  Trajectory_List_Bins(System* sys, float thickness, int n_bins, Trajectory_List* binning, Coord point);
   // takes over a one-bin map the engine made (amdat_fast_particles)
   Trajectory_List_Bins(System* sys, int one_bin_handle);
   ~Trajectory_List_Bins();
@@ -386,11 +396,16 @@ class Structure_Factor : public Analysis {
   void analyze(Trajectory_List* list) override;
   void analyze(Trajectory_List* a, Trajectory_List* b) override;
   void write(const std::string& file) const override;
+  // Bin_Static_Analysis<Structure_Factor>: S(k) of the list members in each bin,
+  // membership per frame (a static analysis: persistence does not apply)
+  void analyze_bins(Trajectory_List* list, Trajectory_List_Bins* bins, bool persistent) override;
+  void select_bin(int b) override { sq_ = bin_sq_[b]; }
 
  private:
   const Wave_Vectors* wv_;
   int timescheme_;
   std::vector<float> sq_;
+  std::vector<std::vector<float>> bin_sq_;
 };
 
 // Radial_Distribution_Function (src/radial_distribution_function.cpp:32-350)

@@ -156,6 +156,70 @@ void Trajectory_List_Bins::assign(const float lo[3], const float hi[3]) {
   check(amdat_bins_create(sys_->ctx(), n_[0], n_[1], n_[2], lo, hi, &handle_), "bin list");
 }
 
+namespace {
+// the bins a distance binning can hold: int(length / thickness) + 1
+// (src/trajectory_list_bins.cpp:485-504, 604-700, 790-808)
+int distance_bin_limit(float length, float thickness) { return (int)(length / thickness) + 1; }
+// half the box diagonal, pow(pow(x, 2) + pow(y, 2) + pow(z, 2), .5) in FP64, stored to FP32
+float half_diagonal(const float* lo, const float* hi) {
+  double s = 0;
+  for (int d = 0; d < 3; ++d) {
+    const float h = (hi[d] - lo[d]) / 2;
+    s += std::pow(h, 2);
+  }
+  return (float)std::pow(s, .5);
+}
+}  // namespace
+
+Trajectory_List_Bins::Trajectory_List_Bins(System* sys, float thickness, int n_bins, Trajectory_List* binning,
+                                           Trajectory_List* clustered)
+    : sys_(sys), n_{1, 1, 1} {
+  if (binning->time_dependent() || clustered->time_dependent())
+    throw Error(AMDAT_ERR_ARGUMENT, "distance bin lists take static lists here");
+  n_[2] = std::min(n_bins, distance_bin_limit(half_diagonal(sys->bounds_lo(), sys->bounds_hi()), thickness));
+  check(amdat_boxify(sys_->ctx(), sys_->bounds_lo(), sys_->bounds_hi()), "boxify");
+  check(amdat_bins_distance(sys_->ctx(), 0, binning->handle(), clustered->handle(), nullptr, 0, 0, 0.f, thickness,
+                            n_[2], &handle_),
+        "distance bin list");
+}
+
+Trajectory_List_Bins::Trajectory_List_Bins(System* sys, float thickness, int n_bins, Trajectory_List* binning,
+                                           Coord point)
+    : sys_(sys), n_{1, 1, 1} {
+  if (binning->time_dependent()) throw Error(AMDAT_ERR_ARGUMENT, "distance bin lists take static lists here");
+  const float* lo = sys->bounds_lo();
+  const float* hi = sys->bounds_hi();
+  // Coordinate::operator> : beyond the box on any axis
+  if (point.x > hi[0] - lo[0] || point.y > hi[1] - lo[1] || point.z > hi[2] - lo[2])
+    throw Error(AMDAT_ERR_ARGUMENT, "point chosen does not lie withing the box dimmensions.");
+  n_[2] = std::min(n_bins, distance_bin_limit(half_diagonal(lo, hi), thickness));
+  const float p[3] = {point.x, point.y, point.z};
+  check(amdat_boxify(sys_->ctx(), lo, hi), "boxify");
+  check(amdat_bins_distance(sys_->ctx(), 1, binning->handle(), 0, p, 0, 0, 0.f, thickness, n_[2], &handle_),
+        "distance bin list");
+}
+
+Trajectory_List_Bins::Trajectory_List_Bins(System* sys, float thickness, int n_bins, Trajectory_List* binning,
+                                           const std::string& plane, float position, const std::string& direction)
+    : sys_(sys), n_{1, 1, 1} {
+  if (binning->time_dependent()) throw Error(AMDAT_ERR_ARGUMENT, "distance bin lists take static lists here");
+  const int axis = plane == "x" ? 0 : plane == "y" ? 1 : plane == "z" ? 2 : -1;
+  const int dir = direction == "average" ? 0 : direction == "above" ? 1 : direction == "below" ? 2 : -1;
+  if (axis < 0) throw Error(AMDAT_ERR_ARGUMENT, "plane " + plane + " not recognized, plane must be x, y, or z.");
+  if (dir < 0)
+    throw Error(AMDAT_ERR_ARGUMENT,
+                "could not recognize direction " + direction + ". valid choices are above, below or average.");
+  const float* lo = sys->bounds_lo();
+  const float* hi = sys->bounds_hi();
+  const float L = hi[axis] - lo[axis];
+  if (position > L) throw Error(AMDAT_ERR_ARGUMENT, "plane chosen does not lie within the box dimmensions.");
+  n_[axis] = std::min(n_bins, distance_bin_limit(dir == 0 ? L / 2 : L, thickness));
+  check(amdat_boxify(sys_->ctx(), lo, hi), "boxify");
+  check(amdat_bins_distance(sys_->ctx(), 2, binning->handle(), 0, nullptr, axis, dir, position, thickness,
+                            n_[axis], &handle_),
+        "distance bin list");
+}
+
 Trajectory_List_Bins::Trajectory_List_Bins(System* sys, int one_bin_handle)
     : sys_(sys), n_{1, 1, 1}, handle_(one_bin_handle) {}
 
@@ -714,6 +778,24 @@ void Structure_Factor::analyze(Trajectory_List* a, Trajectory_List* b) {
   const double n_total = (double)a->show_n_trajectories() * frames.size();
   sq_.assign(S, 0.f);
   for (int m = 0; m < S; ++m) sq_[m] = n_total != 0 ? (float)(s[m] / n_total) : 0.f;
+}
+
+void Structure_Factor::analyze_bins(Trajectory_List* list, Trajectory_List_Bins* bins, bool) {
+  if (list->time_dependent()) throw Error(AMDAT_ERR_ARGUMENT, "structure_factor bins take a static list here");
+  std::vector<int32_t> kv, off;
+  const int S = wv_->n_shells(), B = bins->n_bins();
+  wv_->shells(0, S - 1, kv, off);
+  const std::vector<int32_t> frames = onetime_frames(*system, timescheme_);
+  std::vector<double> s((size_t)B * S);
+  std::vector<int64_t> n(B);
+  check(amdat_structure_factor_bins(system->ctx(), list->handle(), bins->handle(), kv.data(), (int32_t)kv.size() / 3,
+                                    off.data(), S, wv_->period(), frames.data(), (int32_t)frames.size(), s.data(),
+                                    n.data()),
+        "binned structure factor");
+  // postprocess_list per bin: S /= the members counted over the frames
+  bin_sq_.assign(B, std::vector<float>(S, 0.f));
+  for (int b = 0; b < B; ++b)
+    for (int m = 0; m < S; ++m) bin_sq_[b][m] = n[b] != 0 ? (float)(s[(size_t)b * S + m] / (double)n[b]) : 0.f;
 }
 
 void Structure_Factor::write(const std::string& file) const {

@@ -108,15 +108,17 @@ class Control {
 
   // target line "list <name> [<name2>]" or "bin_list <bins> <list> [persistence]"
   // (Control::run_analysis, src/control.h:268-380)
-  void analyze_write(Analysis& an, const std::string& file) {
+  // dynamic: a time-correlation analysis (Control sets `dynamic`), whose bin_list
+  // target can take persistence (Bin_Dynamics_Analysis); static ones always run
+  // Bin_Static_Analysis
+  void analyze_write(Analysis& an, const std::string& file, bool dynamic = true) {
     const auto a = tokenize(read_line());
     if (!a.empty() && a[0] == "bin_list") {
       if (a.size() < 3) throw Error(AMDAT_ERR_ARGUMENT, "Insufficient number of arguments in bin_list target line.");
       auto it = bins_.find(a[1]);
       if (it == bins_.end()) throw Error(AMDAT_ERR_ARGUMENT, "Binned Trajectory list '" + a[1] + "' not found.");
       Trajectory_List* l = list(a[2]);
-      // persistence takes the Bin_Dynamics_Analysis path (the binned analyses here are all dynamic)
-      const bool persistent = a.size() >= 4 && std::atoi(a[3].c_str()) != 0;
+      const bool persistent = dynamic && a.size() >= 4 && std::atoi(a[3].c_str()) != 0;
       an.analyze_bins(l, it->second.get(), persistent);
       const auto names = bin_file_names(file, *it->second, persistent ? "." : "_");
       for (size_t b = 0; b < names.size(); ++b) {
@@ -165,7 +167,23 @@ class Control {
       need(10);
       b = std::make_unique<Trajectory_List_Bins>(&sys(), i(1), i(2), i(3), f(4), f(5), f(6), f(7), f(8), f(9));
     } else if (s[0] == "distance") {
-      throw Error(AMDAT_ERR_ARGUMENT, "distance bin lists are not part of this engine");
+      // distance trajectory <list> <from list> <thickness> <n_bins>
+      // distance point <list> <x> <y> <z> <thickness> <n_bins>
+      // distance plane <average|above|below> <list> <x|y|z> <position> <thickness> <n_bins>
+      const std::string sub = s.size() > 1 ? s[1] : "";
+      if (sub == "trajectory") {
+        need(6);
+        b = std::make_unique<Trajectory_List_Bins>(&sys(), f(4), i(5), list(s[2]), list(s[3]));
+      } else if (sub == "point") {
+        need(8);
+        b = std::make_unique<Trajectory_List_Bins>(&sys(), f(6), i(7), list(s[2]), Coord{f(3), f(4), f(5)});
+      } else if (sub == "plane") {
+        need(8);
+        b = std::make_unique<Trajectory_List_Bins>(&sys(), f(6), i(7), list(s[3]), s[4], f(5), s[2]);
+      } else {
+        throw Error(AMDAT_ERR_ARGUMENT,
+                    "distance binning type " + sub + " not recognized, use trajectory, point or plane.");
+      }
     } else {
       throw Error(AMDAT_ERR_ARGUMENT, "bin_list of type " + s[0] + " invalid");
     }
@@ -324,6 +342,12 @@ class Control {
       pathcheck(a[1]);
       Wave_Vectors wv(&sys(), a[3], (float)std::atof(a[4].c_str()));
       Structure_Factor s(&sys(), &wv, std::atoi(a[5].c_str()));
+      if (pos_ < lines_.size() && tokenize(lines_[pos_]).size() > 0 && tokenize(lines_[pos_])[0] == "bin_list") {
+        // Control::structure_factor (src/control.cpp:2730-2747): bins need the symmetric form
+        if (a[2] != "symmetric") throw Error(AMDAT_ERR_ARGUMENT, "Binning currently only functions with symmetric S(k).");
+        analyze_write(s, a[1], false);
+        return;
+      }
       auto t1 = targets();
       if (a[2] == "symmetric") s.analyze(t1[0]);
       else if (a[2] == "asymmetric") s.analyze(t1[0], targets()[0]);

@@ -221,6 +221,26 @@ amdat_status amdat_bins_create(amdat_ctx* ctx, int32_t nx, int32_t ny, int32_t n
                                const float hi[3], int32_t* handle);
 amdat_status amdat_bins_read(amdat_ctx* ctx, int32_t handle, int32_t out_flags, int32_t* bins,
                              int64_t* counts);
+/* Distance bins (create_bin_list distance trajectory|point|plane,
+ * src/control.cpp:3915-3990; Trajectory_List_Bins, src/trajectory_list_bins.cpp:
+ * 461-948 and assign_bins_distance_*, :1097-1760), from the wrapped coordinates
+ * (boxify first, as create_bin_list does).  Every member of list `binned` gets,
+ * in every frame, bin int(length / thickness) when it is below n_bins, else
+ * none; atoms outside the list get none.  length, with the reference's FP32
+ * chains:
+ *   kind 0: the smallest Coordinate::vector_unwrapped length (box of the
+ *           context) to a member of list `from` in the same frame, starting
+ *           from the box's largest edge;
+ *   kind 1: |dist| with dist = r - point, dist -= box * (dist / (box * 0.5)).integer();
+ *   kind 2: along `axis` (0 x, 1 y, 2 z), dist = r - position; direction 0
+ *           (average): |L * int(dist / (L * 0.5)) - dist| (the quotient in FP64),
+ *           1 (above): dist < 0 ? L + dist : dist, 2 (below): dist < 0 ? |dist| : L - dist.
+ * The map's bins lie along z (kinds 0, 1) or along the plane's axis (kind 2); the
+ * caller applies the reference's limit on n_bins.  Use the handle like
+ * amdat_bins_create's. */
+amdat_status amdat_bins_distance(amdat_ctx* ctx, int32_t kind, int32_t binned, int32_t from,
+                                 const float point[3], int32_t axis, int32_t direction, float position,
+                                 float thickness, int32_t n_bins, int32_t* handle);
 amdat_status amdat_bins_free(amdat_ctx* ctx, int32_t handle);
 
 /* Fast_Particles (src/fast_particles.cpp; Control::find_fast and
@@ -340,6 +360,17 @@ amdat_status amdat_isf_run(amdat_ctx* ctx, int32_t density1, int32_t density2, i
                            double* corr_sum, int64_t* pair_count);
 /* Static structure factor: s_sum[s] = sum over the density's frames and the
  * shell's vectors of Re(rho1 conj(rho2)) / H_s. */
+/* Structure factor of every bin: the bin_list target of structure_factor
+ * (src/control.cpp:2730-2737, Bin_Static_Analysis<Structure_Factor>,
+ * src/bin_static_analysis.h:69-111).  Bin b of the map analyses, at each of
+ * the given frames, the list members whose bin at that frame is b:
+ *   s_sum[b][s] = sum over frames and the shell's vectors of |rho_b(k)|^2 / H_s
+ *   n_atoms[b]  = number of (member, frame) terms
+ * (S(k) of the bin = s_sum / n_atoms).  k = 2 pi n / period; at most 4096 bins. */
+amdat_status amdat_structure_factor_bins(amdat_ctx* ctx, int32_t list, int32_t bins,
+                                         const int32_t* kvec_n, int32_t n_k, const int32_t* shell_offsets,
+                                         int32_t n_shells, float period, const int32_t* frames,
+                                         int32_t n_frames, double* s_sum, int64_t* n_atoms);
 amdat_status amdat_structure_factor_run(amdat_ctx* ctx, int32_t density1, int32_t density2,
                                         const int32_t* shell_offsets, int32_t n_shells,
                                         int32_t out_flags, double* s_sum);

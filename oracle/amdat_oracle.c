@@ -728,6 +728,135 @@ void orc_structure_factor(const orc_scheme* s, int32_t ts, const float* r, int32
   free(fr);
 }
 
+/* Structure factor of every bin: Bin_Static_Analysis<Structure_Factor>
+ * (src/bin_static_analysis.h:69-111, src/control.cpp:2730-2737).  Bin b analyses
+ * the time-dependent list (list && bin b): at each frame of the time scheme the
+ * list members whose bin at that frame is b (ascending atom order), exactly as
+ * orc_structure_factor does for a static list; n_atoms counts the members of
+ * each frame.  bins[t][a] (-1 = no bin); sq[bin][shell]. */
+void orc_structure_factor_bins(const orc_scheme* s, int32_t ts, const float* r, int32_t n_atoms,
+                               const int32_t* list, int32_t n_list, const int32_t* bins, int32_t n_bins,
+                               const int32_t* kvec_n, const int32_t* off, int32_t n_shells, float spacing,
+                               double box_len, int32_t mode, double* sq) {
+  int T = orc_n_timesteps(s);
+  int* fr = (int*)malloc(sizeof(int) * (T + 1));
+  int nf = onetime_frames(s, ts, fr);
+  int nk = off[n_shells];
+  int32_t* mem = (int32_t*)malloc(sizeof(int32_t) * (n_list > 0 ? n_list : 1));
+  float* k = (float*)malloc(sizeof(float) * 3 * (nk > 0 ? nk : 1));
+  for (int i = 0; i < 3 * nk; ++i) k[i] = (float)kvec_n[i] * spacing;
+  float* re = (float*)malloc(sizeof(float) * (nk > 0 ? nk : 1));
+  float* im = (float*)malloc(sizeof(float) * (nk > 0 ? nk : 1));
+  double* rho = (double*)malloc(sizeof(double) * 2 * (nk > 0 ? nk : 1));
+  for (int b = 0; b < n_bins; ++b) {
+    float Sf[128] = {0};
+    double Sd[128] = {0};
+    int na = 0;
+    for (int f = 0; f < nf; ++f) {
+      int t = fr[f], nm = 0;
+      for (int j = 0; j < n_list; ++j)
+        if (bins[(size_t)t * n_atoms + list[j]] == b) mem[nm++] = list[j];
+      if (mode == ORC_REF32) {
+        for (int v = 0; v < nk; ++v) { re[v] = 0; im[v] = 0; }
+        for (int j = 0; j < nm; ++j) {
+          int a = mem[j];
+          float x = POS(r, t, a, 0), y = POS(r, t, a, 1), z = POS(r, t, a, 2);
+          for (int v = 0; v < nk; ++v) {
+            float kr = k[3 * v] * x + k[3 * v + 1] * y + k[3 * v + 2] * z;
+            re[v] += cosf(kr);
+            im[v] += sinf(kr);
+          }
+        }
+        for (int m = 0; m < n_shells && m < 128; ++m) {
+          int cnt = off[m + 1] - off[m];
+          for (int v = off[m]; v < off[m + 1]; ++v) Sf[m] += (re[v] * re[v] + im[v] * im[v]) / (float)cnt;
+        }
+      } else {
+        orc_rhok(r, n_atoms, mem, nm, &t, 1, kvec_n, nk, spacing, box_len, ORC_F64, rho);
+        for (int m = 0; m < n_shells && m < 128; ++m) {
+          int cnt = off[m + 1] - off[m];
+          double acc = 0;
+          for (int v = off[m]; v < off[m + 1]; ++v) acc += rho[2 * v] * rho[2 * v] + rho[2 * v + 1] * rho[2 * v + 1];
+          Sd[m] += cnt ? acc / cnt : 0;
+        }
+      }
+      na += nm;
+    }
+    for (int m = 0; m < n_shells && m < 128; ++m) {
+      if (mode == ORC_REF32) {
+        if ((float)na != 0) Sf[m] /= (float)na;
+        else Sf[m] = 0;
+        sq[(size_t)b * n_shells + m] = Sf[m];
+      } else {
+        sq[(size_t)b * n_shells + m] = na != 0 ? Sd[m] / na : 0;
+      }
+    }
+  }
+  free(fr); free(mem); free(k); free(re); free(im); free(rho);
+}
+
+/* Distance bins (Trajectory_List_Bins, src/trajectory_list_bins.cpp): the bin of
+ * every list member in every frame from its wrapped (boxified) coordinates, -1
+ * for atoms outside the list or beyond the last bin.  The FP32 chains are the
+ * reference's, operation by operation.
+ *   kind 0, assign_bins_distance_clusters (:1097-1170): the smallest
+ *     Coordinate::vector_unwrapped length to a member of `from` at the same frame,
+ *     starting from the box's largest edge; bin = int(length / thickness).
+ *   kind 1, assign_bins_distance_point (:1321-1420): dist = r - point, then
+ *     dist -= box * (dist / (box * 0.5)).integer(); bin = int(|dist| / thickness).
+ *   kind 2, assign_bins_distance_plane (:1489-1700): along axis, dist = r - position;
+ *     average (direction 0): |L * int(dist / (L * 0.5)) - dist| with the quotient in
+ *     double; above (1): dist < 0 ? L + dist : dist; below (2): dist < 0 ? |dist| : L - dist.
+ * Bins are along z (kinds 0, 1) or along the plane's axis (kind 2), n_bins of
+ * them; the flat index is the bin's index on that axis. */
+static float vu_len(float dx, float dy, float dz, const float* box) {
+  float p[3] = {dx, dy, dz};
+  for (int d = 0; d < 3; ++d) {
+    if (p[d] > box[d] / 2) p[d] = p[d] - box[d];
+    else if (p[d] < -box[d] / 2) p[d] = p[d] + box[d];
+  }
+  return sqrtf(p[0] * p[0] + p[1] * p[1] + p[2] * p[2]);
+}
+
+void orc_bins_distance(const float* w, int32_t n_frames, int32_t n_atoms, const float* box, int32_t kind,
+                       const int32_t* binned, int32_t n_binned, const int32_t* from, int32_t n_from,
+                       const float* point, int32_t axis, int32_t direction, float position, float thickness,
+                       int32_t n_bins, int32_t* bins) {
+  for (size_t i = 0; i < (size_t)n_frames * n_atoms; ++i) bins[i] = -1;
+  const float bmax = box[0] > box[1] ? (box[0] > box[2] ? box[0] : box[2]) : (box[1] > box[2] ? box[1] : box[2]);
+  for (int t = 0; t < n_frames; ++t)
+    for (int i = 0; i < n_binned; ++i) {
+      const int a = binned[i];
+      const float* c = &w[((size_t)t * n_atoms + a) * 3];
+      float length = 0;
+      if (kind == 0) {
+        length = bmax;
+        for (int j = 0; j < n_from; ++j) {
+          const float* q = &w[((size_t)t * n_atoms + from[j]) * 3];
+          float tl = vu_len(c[0] - q[0], c[1] - q[1], c[2] - q[2], box);
+          length = tl < length ? tl : length;
+        }
+      } else if (kind == 1) {
+        float d[3];
+        for (int k = 0; k < 3; ++k) {
+          d[k] = c[k] - point[k];
+          const float half = box[k] * 0.5f;
+          const float q = (float)(int)(d[k] / half);
+          d[k] -= box[k] * q;
+        }
+        length = sqrtf(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+      } else {
+        const float L = box[axis];
+        const float dist = c[axis] - position;
+        if (direction == 0) length = fabsf(L * (float)(int)((double)dist / ((double)L * 0.5)) - dist);
+        else if (direction == 1) length = dist < 0 ? L + dist : dist;
+        else length = dist < 0 ? fabsf(dist) : L - dist;
+      }
+      const int b = (int)(length / thickness);
+      if (b >= 0 && b < n_bins) bins[(size_t)t * n_atoms + a] = b;
+    }
+}
+
 /* ------------------------------------------------------------------------- */
 /* pair histograms                                                           */
 /* ------------------------------------------------------------------------- */

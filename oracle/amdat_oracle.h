@@ -111,6 +111,14 @@ void orc_structure_factor(const orc_scheme* s, int32_t timescheme, const float* 
                           float spacing, double box_len, int32_t mode, double* sq);
 /* Radial_Distribution_Function symmetric (radial_distribution_function.cpp:32-285):
  * counts[t][b] (ordered pairs i!=j), mean g(r) as written by the reference. */
+void orc_structure_factor_bins(const orc_scheme* s, int32_t timescheme, const float* wrapped,
+                               int32_t n_atoms, const int32_t* list, int32_t n_list, const int32_t* bins,
+                               int32_t n_bins, const int32_t* kvec_n, const int32_t* shell_off,
+                               int32_t n_shells, float spacing, double box_len, int32_t mode, double* sq);
+void orc_bins_distance(const float* wrapped, int32_t n_frames, int32_t n_atoms, const float* box, int32_t kind,
+                       const int32_t* binned, int32_t n_binned, const int32_t* from, int32_t n_from,
+                       const float* point, int32_t axis, int32_t direction, float position, float thickness,
+                       int32_t n_bins, int32_t* bins);
 void orc_rdf(const orc_scheme* s, int32_t timescheme, const float* wrapped, int32_t n_atoms,
              const float* box, const int32_t* list, int32_t n_list, int32_t n_bins,
              float max_distance, int64_t* counts, double* mean_rdf);

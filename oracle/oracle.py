@@ -333,6 +333,38 @@ def rhok_parallel(wrapped, frames, kvec_n, box_len, n_threads):
     return out
 
 
+def structure_factor_bins(s, timescheme, wrapped, lst, bins, n_bins, kvec_n, shell_off, spacing, box_len,
+                          mode=F64):
+    """Per-bin S(k) [bins][shells] of the time-dependent lists (list && bin)."""
+    r = _f32(wrapped)
+    lst = _i32(lst)
+    b = _i32(bins)
+    kv = _i32(kvec_n).reshape(-1)
+    off = _i32(shell_off)
+    ns = len(off) - 1
+    out = np.zeros((n_bins, ns))
+    lib().orc_structure_factor_bins(C.byref(s), int(timescheme), _p(r), r.shape[1], _p(lst), len(lst), _p(b),
+                                    int(n_bins), _p(kv), _p(off), ns, C.c_float(spacing), C.c_double(box_len),
+                                    mode, _p(out))
+    return out
+
+
+def bins_distance(wrapped, box, kind, binned, from_list=None, point=(0, 0, 0), axis=0, direction=0,
+                  position=0.0, thickness=1.0, n_bins=1):
+    """Distance bin map [frames][atoms] (-1 = none): kind 0 to the nearest member
+    of from_list, 1 to a point, 2 to a plane (direction 0 average, 1 above, 2 below)."""
+    r = _f32(wrapped)
+    bx = _f32(box)
+    bl = _i32(binned)
+    fl = _i32(from_list if from_list is not None else [])
+    pt = _f32(point)
+    out = np.zeros((r.shape[0], r.shape[1]), np.int32)
+    lib().orc_bins_distance(_p(r), r.shape[0], r.shape[1], _p(bx), int(kind), _p(bl), len(bl), _p(fl), len(fl),
+                            _p(pt), int(axis), int(direction), C.c_float(position), C.c_float(thickness),
+                            int(n_bins), _p(out))
+    return out
+
+
 def rhok_lattice(wrapped, frames, kvec_n, box_len, n_threads):
     """FP64 rho(k) of integer-lattice vectors from per-axis phasor tables (every
     atom of the trajectory); agrees with rhok_parallel to FP64 rounding."""

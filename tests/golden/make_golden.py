@@ -211,6 +211,46 @@ bin_list cells b
 isfs ./isfs_cells.dat 7 7 xyz 0 1
 bin_list cells all
 """),
+    # distance bin lists (trajectory, point, plane with each direction) as targets of
+    # msd, isfs and structure_factor, and rectangular bins as structure_factor targets
+    "bins_distance": dict(
+        n=240, box=6.0, sigma=0.25, seed=131, fractions=(0.9, 0.1),
+        scheme=synth.TimeScheme.exponential(3, 6, 1.4, 0, 0, 0.01),
+        commands="""create_list all
+all
+create_list b
+type_system 2
+create_bin_list near_b
+distance trajectory all b 0.5 4
+msd ./msd_near.dat
+bin_list near_b all
+isfs ./isfs_near.dat 8 9 xyz 0
+bin_list near_b all 1
+structure_factor ./sk_near.dat symmetric xyz 0 -1
+bin_list near_b all
+create_bin_list shells
+distance point all 3.0 2.5 1.0 0.75 3
+msd ./msd_shells.dat
+bin_list shells all
+structure_factor ./sk_shells.dat symmetric xyz 0 -1
+bin_list shells all
+create_bin_list zlayers
+distance plane average all z 2.0 0.8 3
+msd ./msd_zavg.dat
+bin_list zlayers all
+create_bin_list xabove
+distance plane above all x 1.5 1.0 4
+msd ./msd_xabove.dat
+bin_list xabove all 1
+create_bin_list ybelow
+distance plane below all y 4.0 1.25 3
+isfs ./isfs_ybelow.dat 7 7 xyz 0
+bin_list ybelow all
+create_bin_list grid
+all 1 2 1
+structure_factor ./sk_grid.dat symmetric xyz 0 -1
+bin_list grid all
+"""),
     # msd_2d and mean_displacement per bin (static and persistent) and of a
     # fast-particle list
     "bins_axes": dict(

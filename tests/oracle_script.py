@@ -210,6 +210,9 @@ class OracleRun:
 
     def make_bins(self, spec):
         lo, hi = self.box_bounds()
+        if spec[0] == "distance":
+            self.wrapped = orc.boxify(self.wrapped, lo, hi)  # System::boxify, kept for later commands
+            return self.distance_bins(spec, lo, hi)
         n = [int(spec[1]), int(spec[2]), int(spec[3])]
         if spec[0] == "all":
             rlo, rhi = lo.copy(), hi.copy()
@@ -224,6 +227,45 @@ class OracleRun:
             raise ValueError(spec)
         self.wrapped = orc.boxify(self.wrapped, lo, hi)  # System::boxify, kept for later commands
         return dict(n=n, bins=orc.assign_bins(self.wrapped, n, rlo, rhi))
+
+    def distance_bins(self, spec, lo, hi):
+        """create_bin_list distance trajectory|point|plane (src/control.cpp:3915-3990)
+        with the bin-count limits of the Trajectory_List_Bins constructors
+        (src/trajectory_list_bins.cpp:461-560, 560-765, 766-948)."""
+        box = (hi - lo).astype(np.float32)  # boundaries: hi - lo per axis
+        half = (box / f32(2)).astype(np.float32)
+
+        def diag_limit(th):
+            # pow(pow(x,2) + pow(y,2) + pow(z,2), .5) in double, stored to float
+            d = f32(float(np.sqrt(sum(float(h) ** 2 for h in half))))
+            return int(f32(d / th)) + 1
+
+        sub = spec[1]
+        if sub == "trajectory":  # distance trajectory <list> <from list> <thickness> <n_bins>
+            th, nb = f32(float(spec[4])), int(spec[5])
+            nz = min(nb, diag_limit(th))
+            bins = orc.bins_distance(self.wrapped, box, 0, self.lists[spec[2]], self.lists[spec[3]],
+                                     thickness=th, n_bins=nz)
+            return dict(n=[1, 1, nz], bins=bins)
+        if sub == "point":  # distance point <list> <x> <y> <z> <thickness> <n_bins>
+            th, nb = f32(float(spec[6])), int(spec[7])
+            nz = min(nb, diag_limit(th))
+            pt = np.array([float(v) for v in spec[3:6]], np.float32)
+            bins = orc.bins_distance(self.wrapped, box, 1, self.lists[spec[2]], point=pt, thickness=th,
+                                     n_bins=nz)
+            return dict(n=[1, 1, nz], bins=bins)
+        if sub == "plane":  # distance plane <direction> <list> <axis> <position> <thickness> <n_bins>
+            direction = {"average": 0, "above": 1, "below": 2}[spec[2]]
+            axis = {"x": 0, "y": 1, "z": 2}[spec[4]]
+            pos, th, nb = f32(float(spec[5])), f32(float(spec[6])), int(spec[7])
+            extent = half[axis] if direction == 0 else box[axis]
+            nb = min(nb, int(f32(extent / th)) + 1)
+            bins = orc.bins_distance(self.wrapped, box, 2, self.lists[spec[3]], axis=axis, direction=direction,
+                                     position=pos, thickness=th, n_bins=nb)
+            n = [1, 1, 1]
+            n[axis] = nb
+            return dict(n=n, bins=bins)
+        raise ValueError(spec)
 
     @staticmethod
     def bin_names(stem, n, sep):
@@ -269,6 +311,13 @@ class OracleRun:
         elif cmd == "mean_displacement":
             md = orc.mean_disp_bins(s, self.unwrapped, lst, spec["bins"], B, int(persist), self.mode)
             texts = [self.md_text(md[b], s) for b in range(B)]
+        elif cmd == "structure_factor":
+            # a static analysis: Bin_Static_Analysis whatever the target line's persistence
+            persist = False
+            kv, off, sp, L, ts = self.sk_shells(a)
+            S = orc.structure_factor_bins(s, ts, self.wrapped, lst, spec["bins"], B, kv, off, float(sp), L,
+                                          self.mode)
+            texts = [self.sk_text(S[b], kv, off, sp) for b in range(B)]
         else:
             raise ValueError(cmd)
         for b, name in self.bin_names(self.name(a[1]), n, "." if persist else "_"):
@@ -364,14 +413,21 @@ class OracleRun:
             txt += fmt(t[g]) + "\t" + "".join(v + "\t" for v in vals[:-1]) + vals[-1] + "\n"
         self.files[self.name(a[1])] = txt
 
-    def cmd_structure_factor(self, a, lst):
+    def sk_shells(self, a):
         maxlen = float(a[4])
         ts = int(a[5])
         L = maxlen if maxlen > 0 else self.min_box()
         sp = wv.spacing(L)
         kv, off = self.shells(0, 98)
+        return kv, off, sp, L, ts
+
+    def cmd_structure_factor(self, a, lst):
+        kv, off, sp, L, ts = self.sk_shells(a)
         s = self.scheme()
         S = orc.structure_factor(s, ts, self.wrapped, lst, kv, off, float(sp), L, self.mode)
+        self.files[self.name(a[1])] = self.sk_text(S, kv, off, sp)
+
+    def sk_text(self, S, kv, off, sp):
         approx = wv.approx_wavenumbers(sp)
         txt = (f"Structure factor data created by AMDAT v.{VERSION}\n"
                "Nominal_q\tMean_q\tStddev_q\tMean_qx\tMean_qy\tMean_qz\tS(q)\n")
@@ -382,7 +438,7 @@ class OracleRun:
                               fmt(wv.stdev_wavenumber(vecs)), fmt(mv[0]), fmt(mv[1]), fmt(mv[2]),
                               fmt(f32(S[m]))]) + "\n"
         txt += "\n"
-        self.files[self.name(a[1])] = txt
+        return txt
 
     def cmd_rdf(self, a, lst):
         nb, ts, maxlen = int(a[3]), int(a[4]), float(a[5])

@@ -283,3 +283,83 @@ def test_timelist_matches_oracle(eng):
         m = out["count"][0] > 0
         np.testing.assert_allclose(out["sum_d2"][0][m] / out["count"][0][m], msd[0][m], rtol=1e-6, atol=1e-12)
     eng.bins_free(h)
+
+
+DISTANCE_CASES = [
+    dict(kind=0, thickness=0.5, n_bins=4, from_type=1),                       # nearest member of type 2
+    dict(kind=0, thickness=0.3, n_bins=9, from_type=1, gathered=True),
+    dict(kind=1, thickness=0.75, n_bins=3, point=(3.0, 2.5, 1.0)),
+    dict(kind=1, thickness=0.4, n_bins=12, point=(0.0, 5.9, 3.3), gathered=True),
+    dict(kind=2, thickness=0.8, n_bins=3, axis=2, direction=0, position=2.0),   # average
+    dict(kind=2, thickness=1.0, n_bins=4, axis=0, direction=1, position=1.5),   # above
+    dict(kind=2, thickness=1.25, n_bins=3, axis=1, direction=2, position=4.0),  # below
+    dict(kind=2, thickness=0.35, n_bins=8, axis=0, direction=0, position=5.5, gathered=True),
+]
+
+
+@pytest.mark.parametrize("c", DISTANCE_CASES, ids=lambda c: "k{kind}_t{thickness}".format(**c))
+def test_distance_bin_map_matches_oracle(eng, c):
+    """create_bin_list distance trajectory|point|plane: every member's bin in every
+    frame, bit-exact against the oracle's restatement of the reference's FP32
+    chains (the golden case bins_distance pins the oracle to the reference)."""
+    traj, _, _ = load("bins_distance")
+    w = _wrapped_with_strays(traj, seed=7)
+    eng.upload(traj.unwrapped, traj.box, traj.box_lo, wrapped=w)
+    lo, hi = _bounds(traj)
+    eng.boxify(lo, hi)
+    wb = orc.boxify(w, lo, hi)
+    N = traj.n_atoms
+    binned = np.arange(N, dtype=np.int32)
+    if c.get("gathered"):
+        binned = np.sort(np.random.default_rng(3).choice(N, N // 2, replace=False)).astype(np.int32)
+    hb = eng.list(binned) if c.get("gathered") else 0
+    frm = np.nonzero(traj.types == c.get("from_type", 0))[0].astype(np.int32) if c["kind"] == 0 else None
+    hf = eng.list(frm) if frm is not None else 0
+    box = (hi - lo).astype(f32)
+    kw = dict(point=c.get("point", (0, 0, 0)), axis=c.get("axis", 0), direction=c.get("direction", 0),
+              position=c.get("position", 0.0), thickness=c["thickness"], n_bins=c["n_bins"])
+    h = eng.bins_distance(c["kind"], hb, hf, **kw)
+    nbx = [1, 1, 1]
+    nbx[c.get("axis", 2) if c["kind"] == 2 else 2] = c["n_bins"]
+    B = nbx[0] * nbx[1] * nbx[2]
+    got, counts = eng.bins_read(h, traj.n_frames, N, B)
+    ref = orc.bins_distance(wb, box, c["kind"], binned, frm, **kw)
+    np.testing.assert_array_equal(got, ref)
+    assert (got >= 0).sum() > 0
+    for b in range(B):
+        np.testing.assert_array_equal(counts[:, b], (ref == b).sum(1))
+    eng.bins_free(h)
+
+
+@pytest.mark.parametrize("kind", [0, 1, 2])
+def test_structure_factor_bins_match_oracle(eng, qvectors, kind):
+    """S(k) per bin (structure_factor with a bin_list target): the list members in
+    the bin at each frame, every reference q-vector shell, <= 1e-5 relative to
+    the FP64 oracle (the reference's own per-bin files: tests/golden/bins_distance)."""
+    traj, _, _ = load("bins_distance")
+    eng.upload(traj.unwrapped, traj.box, traj.box_lo)
+    eng.set_scheme(traj.scheme)
+    lo, hi = _bounds(traj)
+    eng.boxify(lo, hi)
+    wb = orc.boxify(traj.wrapped(), lo, hi)
+    N = traj.n_atoms
+    lst = np.arange(N, dtype=np.int32)
+    box = (hi - lo).astype(f32)
+    frm = np.nonzero(traj.types == 1)[0].astype(np.int32)
+    args = {0: dict(kind=0, thickness=0.5, n_bins=4), 1: dict(kind=1, thickness=0.75, n_bins=3, point=(3.0, 2.5, 1.0)),
+            2: dict(kind=2, thickness=1.0, n_bins=3, axis=1, direction=0, position=2.0)}[kind]
+    B = args["n_bins"]
+    kw = {k: v for k, v in args.items() if k != "kind"}
+    h = eng.bins_distance(kind, 0, eng.list(frm) if kind == 0 else 0, **kw)
+    bins = orc.bins_distance(wb, box, kind, lst, frm if kind == 0 else None, **kw)
+    L = float(f32(traj.box.min()))
+    n, off = qvectors
+    kv, off = n[off[0]:off[40]], off[:41] - off[0]
+    frames = np.arange(traj.n_frames, dtype=np.int32)
+    s_sum, cnt = eng.structure_factor_bins(0, h, B, kv, off, L, frames)
+    s = orc.scheme(traj.scheme)
+    ref = orc.structure_factor_bins(s, -1, wb, lst, bins, B, kv, off, float(wv.spacing(L)), L, orc.F64)
+    np.testing.assert_array_equal(cnt, [(bins == b).sum() for b in range(B)])
+    got = s_sum / np.maximum(cnt, 1)[:, None]
+    np.testing.assert_allclose(got, ref, rtol=1e-5, atol=1e-7)
+    eng.bins_free(h)
