@@ -15,6 +15,8 @@
 // list commands), takes the list named on the command line, and writes its MSD
 // through the GPU-backed analysis:
 //   gpu_msd_binding <script> <list name> <output file>
+#include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <string>
@@ -46,9 +48,13 @@ static void check(amdat_status st) {
   }
 }
 
-// the first exponent of an exponential scheme: the value whose time line equals
-// the System's (System::show_time)
+// the first exponent of an exponential scheme: the value whose time line is
+// nearest the System's (System::show_time); time lines of neighbouring first
+// exponents differ by a factor of the base, so a match within 1e-4 relative
+// identifies it whatever the rounding of the two computations
 static int show_first_exponent(System* sys) {
+  int best = -1;
+  double best_err = 1e-4;
   for (int fe = 0; fe < 64; ++fe) {
     amdat_scheme s;
     if (amdat_scheme_init(&s, AMDAT_EXPONENTIAL, sys->show_n_exponentials(), sys->show_n_exponential_steps(),
@@ -56,12 +62,21 @@ static int show_first_exponent(System* sys) {
       continue;
     std::vector<float> tl(sys->show_n_timesteps()), gaps(sys->show_n_timegaps());
     if (amdat_scheme_times(&s, tl.data(), gaps.data()) != AMDAT_OK) continue;
-    bool same = true;
-    for (int t = 0; t < sys->show_n_timesteps() && same; ++t) same = tl[t] == sys->show_time(t);
-    if (same) return fe;
+    double err = 0;
+    for (int t = 0; t < sys->show_n_timesteps(); ++t) {
+      const double a = tl[t], b = sys->show_time(t);
+      err = std::max(err, std::fabs(a - b) / std::max(std::fabs(b), 1e-30));
+    }
+    if (err < best_err) {
+      best_err = err;
+      best = fe;
+    }
   }
-  fprintf(stderr, "no first exponent reproduces the system's time line\n");
-  exit(1);
+  if (best < 0) {
+    fprintf(stderr, "no first exponent reproduces the system's time line\n");
+    exit(1);
+  }
+  return best;
 }
 
 // one engine context per System: the unwrapped trajectory [frame][atom][3] and

@@ -63,5 +63,8 @@ def test_binding_writes_reference_msd(binding, tmp_path, case, list_name, golden
     for a, b in zip(got[1:], ref[1:]):
         ta, va = a.split("\t")
         tb, vb = b.split("\t")
-        assert ta == tb
+        # times: the reference objects built on this machine form them (aarch64 gcc
+        # contracts the time line's multiply-add, x86-64 does not), the file came
+        # from an x86-64 build
+        assert abs(float(ta) - float(tb)) <= 1e-5 * max(abs(float(tb)), 1e-12), (a, b)
         assert abs(float(va) - float(vb)) <= 2e-3 * max(abs(float(vb)), 1e-12), (a, b)
