@@ -15,8 +15,8 @@
 // the correctly rounded chain only when the estimate lies within its error
 // bound of a bin edge.
 //
-// A block owns 256 members i of list 1 (positions in registers) and streams
-// list 2 through shared memory in tiles of 1024.  Counts go to per-warp
+// A block owns 512 members i of list 1 (two per thread, positions in
+// registers) and streams list 2 through shared memory in tiles of 1024.  Counts go to per-warp
 // shared-memory histograms, then once per block to the global int64
 // histogram with integer atomics (exact, order-independent).  For the RDF
 // with list1 == list2 the unordered pairs j > i are visited once and counted
@@ -31,6 +31,7 @@
 namespace amdat {
 
 constexpr int PH_THREADS = 256;
+constexpr int PH_I_PER_BLOCK = 2 * PH_THREADS;  // two list-1 members per thread
 constexpr int PH_JT = 1024;
 
 struct PHList {
@@ -69,29 +70,69 @@ struct PHParams {
   unsigned long long* counts;  // [rows][n_bins]
 };
 
-// SYM: the symmetric pass (list1 == list2, one frame): j > i, each pair counted twice
+// one pair: the reference's FP32 minimum-image length and its bin, counted into
+// the warp's shared histogram
+template <bool SYM>
+__device__ __forceinline__ void pair_term(const PHParams& p, float4 c, float xi, float yi, float zi,
+                                          unsigned int* hist, unsigned int inc) {
+  const float mx = min_image(__fsub_rn(c.x, xi), p.box.x);
+  const float my = min_image(__fsub_rn(c.y, yi), p.box.y);
+  const float mz = min_image(__fsub_rn(c.z, zi), p.box.z);
+  const float s2 = __fadd_rn(__fadd_rn(__fmul_rn(mx, mx), __fmul_rn(my, my)), __fmul_rn(mz, mz));
+  if (s2 < p.s2_cut) {
+    // bin = int(sqrt_rn(s2) / bin_size), the reference's chain.  First from
+    // rsqrtf (<= 2 ulp) and the reciprocal bin size: within 1e-6 relative of
+    // the exact quotient, so its integer part is the exact one unless the
+    // quotient lies within that margin of an integer; those pairs (and s2 = 0)
+    // take the correctly rounded chain.  (The symmetric RDF pass, where most
+    // pairs are in range; the sparse distinct van Hove pass keeps the short
+    // exact branch.)
+    int b;
+    if (SYM) {
+      const float x = __fmul_rn(__fmul_rn(s2, rsqrtf(s2)), p.inv_bin);
+      b = (int)x;
+      const float frac = __fsub_rn(x, (float)b);
+      const float margin = fmaf(x, 1e-6f, 1e-6f);
+      if (!(s2 > 0.f) || frac <= margin || frac >= 1.f - margin)
+        b = (int)__fdiv_rn(__fsqrt_rn(s2), p.bin_size);
+    } else {
+      b = (int)__fdiv_rn(__fsqrt_rn(s2), p.bin_size);
+    }
+    if (b >= 0 && b < p.n_bins) atomicAdd(hist + b, inc);
+  }
+}
+
+// SYM: the symmetric pass (list1 == list2, one frame): j > i, each pair counted
+// twice.  A thread holds two members of list 1 (i and i + PH_THREADS) in
+// registers, so each staged list-2 position (one 16-byte shared load: x, y, z
+// and the atom index) serves two pairs.
 template <bool SYM>
 __global__ void __launch_bounds__(PH_THREADS)
     pair_hist_kernel(PHParams p) {
   extern __shared__ unsigned int sh_hist[];  // [8 warps][n_bins]
-  __shared__ float sx[PH_JT], sy[PH_JT], sz[PH_JT];
-  __shared__ int sid[PH_JT];
+  __shared__ float4 sj[PH_JT];               // x, y, z, atom index bits
   const int q = blockIdx.y;
   const float* A = p.w + (int64_t)p.frame_a[q] * 3 * p.n_pad;
   const float* B = p.w + (int64_t)p.frame_b[q] * 3 * p.n_pad;
   const int warp = threadIdx.x >> 5;
   unsigned int* hist = sh_hist + warp * p.n_bins;
   for (int b = threadIdx.x; b < 8 * p.n_bins; b += blockDim.x) sh_hist[b] = 0u;
-  const int i0 = blockIdx.x * PH_THREADS;
-  const int i = i0 + threadIdx.x;
-  const bool live = i < p.l1.n;
-  int ai = -1;
-  float xi = 0.f, yi = 0.f, zi = 0.f;
-  if (live) {
-    ai = member(p.l1, i);
-    xi = A[ai];
-    yi = A[p.n_pad + ai];
-    zi = A[2 * p.n_pad + ai];
+  const int i0 = blockIdx.x * PH_I_PER_BLOCK;
+  const int ia = i0 + threadIdx.x, ib = ia + PH_THREADS;
+  const bool la = ia < p.l1.n, lb = ib < p.l1.n;
+  int aa = -1, ab = -1;
+  float xa = 0.f, ya = 0.f, za = 0.f, xb = 0.f, yb = 0.f, zb = 0.f;
+  if (la) {
+    aa = member(p.l1, ia);
+    xa = A[aa];
+    ya = A[p.n_pad + aa];
+    za = A[2 * p.n_pad + aa];
+  }
+  if (lb) {
+    ab = member(p.l1, ib);
+    xb = A[ab];
+    yb = A[p.n_pad + ab];
+    zb = A[2 * p.n_pad + ab];
   }
   const unsigned int inc = SYM ? 2u : 1u;
   const int j_begin = SYM ? i0 : 0;
@@ -101,43 +142,17 @@ __global__ void __launch_bounds__(PH_THREADS)
     __syncthreads();
     for (int t = threadIdx.x; t < nj; t += blockDim.x) {
       const int aj = member(p.l2, j0 + t);
-      sid[t] = aj;
-      sx[t] = B[aj];
-      sy[t] = B[p.n_pad + aj];
-      sz[t] = B[2 * p.n_pad + aj];
+      sj[t] = make_float4(B[aj], B[p.n_pad + aj], B[2 * p.n_pad + aj], __int_as_float(aj));
     }
     __syncthreads();
-    if (!live) continue;
-    int t_begin = 0;
-    if (SYM) t_begin = max(0, i + 1 - j0);  // j > i
+    if (!la) continue;  // lb implies la
+    // j > i for the symmetric pass (i != j is implied), i != j checked otherwise
+    const int t_begin = SYM ? max(0, ia + 1 - j0) : 0;
+    const int t_b = SYM ? ib + 1 - j0 : 0;  // the second member's first t
     for (int t = t_begin; t < nj; ++t) {
-      // i != j: implied by j > i for the symmetric pass, checked otherwise
-      if (!SYM && sid[t] == ai) continue;
-      const float mx = min_image(__fsub_rn(sx[t], xi), p.box.x);
-      const float my = min_image(__fsub_rn(sy[t], yi), p.box.y);
-      const float mz = min_image(__fsub_rn(sz[t], zi), p.box.z);
-      const float s2 = __fadd_rn(__fadd_rn(__fmul_rn(mx, mx), __fmul_rn(my, my)), __fmul_rn(mz, mz));
-      if (s2 < p.s2_cut) {
-        // bin = int(sqrt_rn(s2) / bin_size), the reference's chain.  First from
-        // rsqrtf (<= 2 ulp) and the reciprocal bin size: within 1e-6 relative of
-        // the exact quotient, so its integer part is the exact one unless the
-        // quotient lies within that margin of an integer; those pairs (and
-        // s2 = 0) take the correctly rounded chain.
-        // (the symmetric RDF pass, where most pairs are in range; the sparse
-        // distinct van Hove pass keeps the short exact branch)
-        int b;
-        if (SYM) {
-          const float x = __fmul_rn(__fmul_rn(s2, rsqrtf(s2)), p.inv_bin);
-          b = (int)x;
-          const float frac = __fsub_rn(x, (float)b);
-          const float margin = fmaf(x, 1e-6f, 1e-6f);
-          if (!(s2 > 0.f) || frac <= margin || frac >= 1.f - margin)
-            b = (int)__fdiv_rn(__fsqrt_rn(s2), p.bin_size);
-        } else {
-          b = (int)__fdiv_rn(__fsqrt_rn(s2), p.bin_size);
-        }
-        if (b >= 0 && b < p.n_bins) atomicAdd(hist + b, inc);
-      }
+      const float4 c = sj[t];
+      if (SYM || __float_as_int(c.w) != aa) pair_term<SYM>(p, c, xa, ya, za, hist, inc);
+      if (lb && (SYM ? t >= t_b : __float_as_int(c.w) != ab)) pair_term<SYM>(p, c, xb, yb, zb, hist, inc);
     }
   }
   __syncthreads();
@@ -196,7 +211,7 @@ static void run_pair_hist(amdat_ctx* ctx, const ListEntry& l1, const ListEntry& 
     if (shm > 48 * 1024)
       AMDAT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
     AMDAT_REQUIRE(n_q <= 65535, "at most 65535 frames or time pairs per call");
-    dim3 grid((unsigned)ceil_div(l1.n, PH_THREADS), (unsigned)n_q);
+    dim3 grid((unsigned)ceil_div(l1.n, PH_I_PER_BLOCK), (unsigned)n_q);
     KernelTimer kt(ctx, "pair_hist_kernel");
     kern<<<grid, PH_THREADS, shm, ctx->stream>>>(p);
     check_launch("pair_hist_kernel");
