@@ -302,23 +302,24 @@ __global__ void __launch_bounds__(MODE == 0 ? DISP_THREADS : FS_THREADS)
         for (int ax = 0; ax < 3; ++ax)
           for (int n = 0; n <= p.nmax; ++n)
             tab[ax * stride + n * nthr + tid] = cos_fixed((int32_t)((uint32_t)n * (uint32_t)f[ax]));
-        const float* cx = tab + tid;
-        const float* cy = tab + stride + tid;
-        const float* cz = tab + 2 * stride + tid;
+        // octant representatives: (x, y, z) table offsets for FS_THREADS threads
+        // (the launch's block size in this mode), .w = multiplicity as FP32 bits;
+        // terms summed in blocks of 32, each block added to the compensated sum
+        const float* T = tab + tid;
         for (int s = 0; s < n_fs; ++s) {
           KSum acc = {0.f, 0.f};
-          float blk = 0.f;
-          int cnt = 0;
-          for (int v = p.kv_off[s]; v < p.kv_off[s + 1]; ++v) {
-            const int4 r = __ldg(p.kv + v);  // octant representative, .w = multiplicity
-            blk = fmaf((float)r.w * cx[r.x * nthr] * cy[r.y * nthr], cz[r.z * nthr], blk);
-            if (++cnt == 32) {
-              kadd(acc, blk);
-              blk = 0.f;
-              cnt = 0;
+          const int v_begin = p.kv_off[s], v_end = p.kv_off[s + 1];
+          for (int v0 = v_begin; v0 < v_end; v0 += 32) {
+            const int v1 = min(v0 + 32, v_end);
+            float blk = 0.f;
+#pragma unroll 4
+            for (int v = v0; v < v1; ++v) {
+              const int4 r = __ldg(p.kv + v);
+              blk = fmaf(__int_as_float(r.w) * T[r.x] * T[r.y], T[r.z], blk);
             }
+            kadd(acc, blk);
           }
-          kadd(acc, blk);
+          if ((v_end - v_begin) % 32 == 0) kadd(acc, 0.f);  // the closing (empty) block
           kadd(fs[s], __fmul_rn(__fsub_rn(acc.s, acc.c), p.inv_count[s]));
         }
       }
@@ -529,6 +530,16 @@ static bool octant_shells(const int32_t* off, const int32_t* kvec, int n_shells,
     out.off.push_back((int32_t)out.kv.size());
     const int cnt = off[s + 1] - off[s];
     out.inv_count.push_back(cnt ? 1.0f / (float)cnt : 0.0f);
+  }
+  // each representative as the F_s kernel reads it: its three offsets into the
+  // per-thread cosine tables ([axis][n][thread] of FS_THREADS threads) and its
+  // multiplicity as FP32 bits
+  const int stride = (out.nmax + 1) * FS_THREADS;
+  for (auto& r : out.kv) {
+    const float w = (float)r.w;
+    int32_t wbits;
+    std::memcpy(&wbits, &w, 4);
+    r = make_int4(r.x * FS_THREADS, stride + r.y * FS_THREADS, 2 * stride + r.z * FS_THREADS, wbits);
   }
   out.mode = 2;
   return true;

@@ -1087,8 +1087,10 @@ def main():
             sec["parity"] = m["checks"]
         if "value" not in line:
             line.update({"value": m["value"], "unit": "atom·time-pairs/s",
-                         "ms_per_step": m["ms"], "config": {"workload": sec["workload"]}})
-            line["msd_detail"] = {k: sec[k] for k in ("kernel_ms", "plan_graph", "fp64_plain")}
+                         "ms_per_step": m["ms"], "config": {"workload": sec["workload"]},
+                         "e2e": sec["e2e"], "roofline": sec["roofline"]})
+            line["msd_detail"] = {k: v for k, v in sec.items()
+                                  if k not in ("workload", "value", "unit", "ms_per_step", "e2e", "roofline")}
         else:
             line["secondary"] = sec
     if "batched" in result:
