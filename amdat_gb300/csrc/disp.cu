@@ -101,7 +101,28 @@ struct DispParams {
   const float* inv_count;    // [n_fs] 1 / vectors in shell
   int32_t nmax;              // octant mode table size - 1
   float period;              // L of k = 2 pi n / L
+  int32_t n_rep_smem;        // octant mode: representatives of the pass staged in shared memory (0: read from kv)
 };
+
+// octant mode: the compensated sum over one shell's representatives (blocks of
+// 32 terms, each block added to the sum), reading the representatives from
+// shared memory or through the read-only cache
+template <bool SMEM>
+__device__ __forceinline__ KSum octant_shell_sum(const int4* R, const float* T, int v_begin, int v_end) {
+  KSum acc = {0.f, 0.f};
+  for (int v0 = v_begin; v0 < v_end; v0 += 32) {
+    const int v1 = min(v0 + 32, v_end);
+    float blk = 0.f;
+#pragma unroll 4
+    for (int v = v0; v < v1; ++v) {
+      const int4 r = SMEM ? R[v] : __ldg(R + v);
+      blk = fmaf(__int_as_float(r.w) * T[r.x] * T[r.y], T[r.z], blk);
+    }
+    kadd(acc, blk);
+  }
+  if ((v_end - v_begin) % 32 == 0) kadd(acc, 0.f);  // the closing (empty) block
+  return acc;
+}
 
 template <int MODE, bool GS>
 __global__ void __launch_bounds__(MODE == 0 ? DISP_THREADS : FS_THREADS)
@@ -114,6 +135,10 @@ __global__ void __launch_bounds__(MODE == 0 ? DISP_THREADS : FS_THREADS)
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
   const int n_fs = MODE ? p.n_fs : 0;
+  // octant mode: the pass's representatives, after the tables, when they fit
+  int4* reps = reinterpret_cast<int4*>(tab + (MODE == 2 ? 3 * (p.nmax + 1) * nthr : 0));
+  if (MODE == 2 && p.n_rep_smem)
+    for (int i = tid; i < p.n_rep_smem; i += nthr) reps[i] = __ldg(p.kv + p.kv_off[0] + i);
 
   // the next item's counter slot is fetched while the current item is
   // processed (two slots: slot i & 1 is read after the barrier that ends item
@@ -307,19 +332,9 @@ __global__ void __launch_bounds__(MODE == 0 ? DISP_THREADS : FS_THREADS)
         // terms summed in blocks of 32, each block added to the compensated sum
         const float* T = tab + tid;
         for (int s = 0; s < n_fs; ++s) {
-          KSum acc = {0.f, 0.f};
-          const int v_begin = p.kv_off[s], v_end = p.kv_off[s + 1];
-          for (int v0 = v_begin; v0 < v_end; v0 += 32) {
-            const int v1 = min(v0 + 32, v_end);
-            float blk = 0.f;
-#pragma unroll 4
-            for (int v = v0; v < v1; ++v) {
-              const int4 r = __ldg(p.kv + v);
-              blk = fmaf(__int_as_float(r.w) * T[r.x] * T[r.y], T[r.z], blk);
-            }
-            kadd(acc, blk);
-          }
-          if ((v_end - v_begin) % 32 == 0) kadd(acc, 0.f);  // the closing (empty) block
+          const KSum acc = p.n_rep_smem
+                               ? octant_shell_sum<true>(reps - p.kv_off[0], T, p.kv_off[s], p.kv_off[s + 1])
+                               : octant_shell_sum<false>(p.kv, T, p.kv_off[s], p.kv_off[s + 1]);
           kadd(fs[s], __fmul_rn(__fsub_rn(acc.s, acc.c), p.inv_count[s]));
         }
       }
@@ -837,7 +852,15 @@ static void plan_launch(amdat_ctx* ctx, amdat_disp_plan& pl, const PairTable& P)
     const int mode = nfs ? pl.sh.mode : 0;
     const int threads = mode ? FS_THREADS : DISP_THREADS;
     size_t shm = gs ? (size_t)((pl.NB + 3) & ~3) * 4 : 0;
-    if (mode == 2) shm += (size_t)3 * (pl.sh.nmax + 1) * threads * 4;
+    if (mode == 2) {
+      shm += (size_t)3 * (pl.sh.nmax + 1) * threads * 4;
+      // the pass's representatives in shared memory when they take at most 32 KB
+      const int n_rep = pl.sh.off[s0 + nfs] - pl.sh.off[s0];
+      if (n_rep <= 2048) {
+        p.n_rep_smem = n_rep;
+        shm += (size_t)n_rep * sizeof(int4);
+      }
+    }
     auto launch = [&](auto kernel) {
       if (shm > 48 * 1024)
         AMDAT_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
