@@ -101,8 +101,31 @@ struct DispParams {
   const float* inv_count;    // [n_fs] 1 / vectors in shell
   int32_t nmax;              // octant mode table size - 1
   float period;              // L of k = 2 pi n / L
-  int32_t n_rep_smem;        // octant mode: representatives of the pass staged in shared memory (0: read from kv)
+  int32_t n_rep_smem;        // F_s vectors (list) or representatives (octant) of the pass in shared memory (0: read from kv)
 };
+
+// list mode: the compensated sum over one shell's vectors of the cosine of the
+// exact fixed-point phase (blocks of 32 terms), the vectors read from shared
+// memory or through the read-only cache
+template <bool SMEM>
+__device__ __forceinline__ KSum list_shell_sum(const int4* R, int32_t fx, int32_t fy, int32_t fz, int v_begin,
+                                               int v_end) {
+  KSum acc = {0.f, 0.f};
+  for (int v0 = v_begin; v0 < v_end; v0 += 32) {
+    const int v1 = min(v0 + 32, v_end);
+    float blk = 0.f;
+#pragma unroll 4
+    for (int v = v0; v < v1; ++v) {
+      const int4 n = SMEM ? R[v] : __ldg(R + v);
+      const int32_t ph = (int32_t)((uint32_t)n.x * (uint32_t)fx + (uint32_t)n.y * (uint32_t)fy +
+                                   (uint32_t)n.z * (uint32_t)fz);
+      blk += cos_fixed_sfu(ph);
+    }
+    kadd(acc, blk);
+  }
+  if ((v_end - v_begin) % 32 == 0) kadd(acc, 0.f);  // the closing (empty) block
+  return acc;
+}
 
 // octant mode: the compensated sum over one shell's representatives (blocks of
 // 32 terms, each block added to the sum), reading the representatives from
@@ -135,9 +158,10 @@ __global__ void __launch_bounds__(MODE == 0 ? DISP_THREADS : FS_THREADS)
   const int tid = threadIdx.x, nthr = blockDim.x;
   const int lane = tid & 31, warp = tid >> 5, nwarp = nthr >> 5;
   const int n_fs = MODE ? p.n_fs : 0;
-  // octant mode: the pass's representatives, after the tables, when they fit
+  // F_s: the pass's vectors (list mode) or representatives (octant mode, after
+  // the tables) in shared memory, when they fit
   int4* reps = reinterpret_cast<int4*>(tab + (MODE == 2 ? 3 * (p.nmax + 1) * nthr : 0));
-  if (MODE == 2 && p.n_rep_smem)
+  if (MODE != 0 && p.n_rep_smem)
     for (int i = tid; i < p.n_rep_smem; i += nthr) reps[i] = __ldg(p.kv + p.kv_off[0] + i);
 
   // the next item's counter slot is fetched while the current item is
@@ -299,21 +323,9 @@ __global__ void __launch_bounds__(MODE == 0 ? DISP_THREADS : FS_THREADS)
         const int32_t fy = turns_fixed(dy, p.period);
         const int32_t fz = turns_fixed(dz, p.period);
         for (int s = 0; s < n_fs; ++s) {
-          KSum acc = {0.f, 0.f};
-          float blk = 0.f;
-          int cnt = 0;
-          for (int v = p.kv_off[s]; v < p.kv_off[s + 1]; ++v) {
-            const int4 n = __ldg(p.kv + v);
-            const int32_t ph = (int32_t)((uint32_t)n.x * (uint32_t)fx + (uint32_t)n.y * (uint32_t)fy +
-                                         (uint32_t)n.z * (uint32_t)fz);
-            blk += cos_fixed_sfu(ph);
-            if (++cnt == 32) {
-              kadd(acc, blk);
-              blk = 0.f;
-              cnt = 0;
-            }
-          }
-          kadd(acc, blk);
+          const KSum acc = p.n_rep_smem
+                               ? list_shell_sum<true>(reps - p.kv_off[0], fx, fy, fz, p.kv_off[s], p.kv_off[s + 1])
+                               : list_shell_sum<false>(p.kv, fx, fy, fz, p.kv_off[s], p.kv_off[s + 1]);
           kadd(fs[s], __fmul_rn(__fsub_rn(acc.s, acc.c), p.inv_count[s]));
         }
       }
@@ -852,9 +864,9 @@ static void plan_launch(amdat_ctx* ctx, amdat_disp_plan& pl, const PairTable& P)
     const int mode = nfs ? pl.sh.mode : 0;
     const int threads = mode ? FS_THREADS : DISP_THREADS;
     size_t shm = gs ? (size_t)((pl.NB + 3) & ~3) * 4 : 0;
-    if (mode == 2) {
-      shm += (size_t)3 * (pl.sh.nmax + 1) * threads * 4;
-      // the pass's representatives in shared memory when they take at most 32 KB
+    if (mode == 2) shm += (size_t)3 * (pl.sh.nmax + 1) * threads * 4;
+    if (mode != 0) {
+      // the pass's vectors / representatives in shared memory when they take at most 32 KB
       const int n_rep = pl.sh.off[s0 + nfs] - pl.sh.off[s0];
       if (n_rep <= 2048) {
         p.n_rep_smem = n_rep;
