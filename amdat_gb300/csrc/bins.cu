@@ -213,6 +213,8 @@ struct BnParams {
   double* acc;     // [bin][gap][stride]
   unsigned long long* cnt;  // [bin][gap]
   int32_t staged;  // per-block shared accumulators
+  int32_t n_kv_smem;    // F_s vectors staged in shared memory (0: read from kv)
+  int32_t kv_smem_off;  // their byte offset in dynamic shared memory (16-byte aligned)
 };
 
 // FS: F_s shells in the columns after |dr|^2 (and |dr|^4); AXES: the columns are
@@ -226,6 +228,9 @@ __global__ void __launch_bounds__(BN_THREADS) disp_bins_kernel(BnParams p) {
   const int stride = p.stride;
   double* sacc = bn_smem;
   unsigned int* scnt = reinterpret_cast<unsigned int*>(bn_smem + (size_t)p.n_bins * stride);
+  int4* skv = reinterpret_cast<int4*>(reinterpret_cast<unsigned char*>(bn_smem) + p.kv_smem_off);
+  if (FS)  // ordered before the first read by the loop's first barrier
+    for (int i = tid; i < p.n_kv_smem; i += BN_THREADS) skv[i] = __ldg(p.kv + i);
 
   for (;;) {
     if (tid == 0) s_item = atomicAdd(p.counter, 1);
@@ -271,21 +276,8 @@ __global__ void __launch_bounds__(BN_THREADS) disp_bins_kernel(BnParams p) {
 #pragma unroll
             for (int s = 0; s < BN_MAX_FS; ++s) {
               if (s >= p.n_fs) break;
-              KSum acc = {0.f, 0.f};
-              float blk = 0.f;
-              int cnt = 0;
-              for (int q = p.kv_off[s]; q < p.kv_off[s + 1]; ++q) {
-                const int4 n = __ldg(p.kv + q);
-                const int32_t ph = (int32_t)((uint32_t)n.x * (uint32_t)fx + (uint32_t)n.y * (uint32_t)fy +
-                                             (uint32_t)n.z * (uint32_t)fz);
-                blk += cos_fixed_sfu(ph);
-                if (++cnt == 32) {
-                  kadd(acc, blk);
-                  blk = 0.f;
-                  cnt = 0;
-                }
-              }
-              kadd(acc, blk);
+              const KSum acc = p.n_kv_smem ? list_shell_sum<true>(skv, fx, fy, fz, p.kv_off[s], p.kv_off[s + 1])
+                                           : list_shell_sum<false>(p.kv, fx, fy, fz, p.kv_off[s], p.kv_off[s + 1]);
               v[2 + s] = __fmul_rn(__fsub_rn(acc.s, acc.c), p.inv_count[s]);
             }
           }
@@ -846,6 +838,12 @@ static amdat_status disp_bins_impl(amdat_ctx* ctx, int32_t list, int32_t bins, i
       const size_t stage = (size_t)B * stride * 8 + (size_t)B * 4;
       p.staged = stage <= BN_STAGE_LIMIT ? 1 : 0;
       size_t shm = p.staged ? stage : 0;
+      if (n_shells && kv.size() <= 2048) {  // the vectors in shared memory when they take at most 32 KB
+        shm = (shm + 15) & ~(size_t)15;
+        p.kv_smem_off = (int32_t)shm;
+        p.n_kv_smem = (int32_t)kv.size();
+        shm += kv.size() * sizeof(int4);
+      }
       auto kern = axes ? disp_bins_kernel<false, true> : (n_shells ? disp_bins_kernel<true> : disp_bins_kernel<false>);
       if (sum_kernel) {
         kern = axes ? disp_bins_sum_kernel<true> : disp_bins_sum_kernel<false>;

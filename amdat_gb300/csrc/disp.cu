@@ -104,29 +104,6 @@ struct DispParams {
   int32_t n_rep_smem;        // F_s vectors (list) or representatives (octant) of the pass in shared memory (0: read from kv)
 };
 
-// list mode: the compensated sum over one shell's vectors of the cosine of the
-// exact fixed-point phase (blocks of 32 terms), the vectors read from shared
-// memory or through the read-only cache
-template <bool SMEM>
-__device__ __forceinline__ KSum list_shell_sum(const int4* R, int32_t fx, int32_t fy, int32_t fz, int v_begin,
-                                               int v_end) {
-  KSum acc = {0.f, 0.f};
-  for (int v0 = v_begin; v0 < v_end; v0 += 32) {
-    const int v1 = min(v0 + 32, v_end);
-    float blk = 0.f;
-#pragma unroll 4
-    for (int v = v0; v < v1; ++v) {
-      const int4 n = SMEM ? R[v] : __ldg(R + v);
-      const int32_t ph = (int32_t)((uint32_t)n.x * (uint32_t)fx + (uint32_t)n.y * (uint32_t)fy +
-                                   (uint32_t)n.z * (uint32_t)fz);
-      blk += cos_fixed_sfu(ph);
-    }
-    kadd(acc, blk);
-  }
-  if ((v_end - v_begin) % 32 == 0) kadd(acc, 0.f);  // the closing (empty) block
-  return acc;
-}
-
 // octant mode: the compensated sum over one shell's representatives (blocks of
 // 32 terms, each block added to the sum), reading the representatives from
 // shared memory or through the read-only cache

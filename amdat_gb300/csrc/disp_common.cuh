@@ -58,4 +58,29 @@ __device__ __forceinline__ float cos_fixed_sfu(int32_t phase) {
   return __cosf(__fmul_rn((float)r, 1.4629180792671596e-09f));  // 2 pi / 2^32
 }
 
+// F_s of one displacement over a list of lattice vectors: the compensated sum
+// of the cosines of the exact fixed-point phases, in blocks of 32 terms (each
+// block summed plainly, then added to the compensated sum, and a closing empty
+// block when the count is a multiple of 32), the vectors read from shared memory
+// (SMEM) or through the read-only cache
+template <bool SMEM>
+__device__ __forceinline__ KSum list_shell_sum(const int4* R, int32_t fx, int32_t fy, int32_t fz, int v_begin,
+                                               int v_end) {
+  KSum acc = {0.f, 0.f};
+  for (int v0 = v_begin; v0 < v_end; v0 += 32) {
+    const int v1 = min(v0 + 32, v_end);
+    float blk = 0.f;
+#pragma unroll 4
+    for (int v = v0; v < v1; ++v) {
+      const int4 n = SMEM ? R[v] : __ldg(R + v);
+      const int32_t ph = (int32_t)((uint32_t)n.x * (uint32_t)fx + (uint32_t)n.y * (uint32_t)fy +
+                                   (uint32_t)n.z * (uint32_t)fz);
+      blk += cos_fixed_sfu(ph);
+    }
+    kadd(acc, blk);
+  }
+  if ((v_end - v_begin) % 32 == 0) kadd(acc, 0.f);  // the closing (empty) block
+  return acc;
+}
+
 }  // namespace amdat
