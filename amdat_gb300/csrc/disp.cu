@@ -1052,7 +1052,9 @@ static amdat_disp_plan* plan_create(amdat_ctx* ctx, const amdat_disp_request* re
     if (P.n_pairs > 0 && unit_atoms > 0)
       chunk = std::max<int64_t>(pl->S ? 128 : 1024,
                                 std::min<int64_t>(DISP_CHUNK, ceil_div(unit_atoms * P.n_pairs, want_items)));
-    int bps = pl->S ? 4 : 8;
+    // list-mode F_s holds few registers and only its vectors in shared memory:
+    // more resident blocks hide the latency of its cosine chain
+    int bps = pl->S ? (pl->sh.mode == 1 ? 8 : 4) : 8;
     char keybuf[256];
     std::snprintf(keybuf, sizeof(keybuf), "sm%d_mode%d_S%d_NB%d_L%d_U%d_atoms%lld_unit%lld_pairs%lld",
                   ctx->n_sm, pl->S ? pl->sh.mode : 0, pl->S, pl->NB, n_lists, pl->n_units,
@@ -1068,7 +1070,8 @@ static amdat_disp_plan* plan_create(amdat_ctx* ctx, const amdat_disp_request* re
       // MSD-only streams memory (large chunks, more resident blocks)
       const std::vector<int> chunks = pl->S ? std::vector<int>{256, 512, 1024, 2048}
                                             : std::vector<int>{1024, 2048, 4096, 8192};
-      const std::vector<int> bpss = pl->S ? std::vector<int>{2, 4} : std::vector<int>{4, 8};
+      const std::vector<int> bpss = pl->S ? (pl->sh.mode == 1 ? std::vector<int>{4, 8, 16} : std::vector<int>{2, 4, 8})
+                                          : std::vector<int>{4, 8};
       cudaEvent_t a, b;
       AMDAT_CUDA(cudaEventCreate(&a));
       AMDAT_CUDA(cudaEventCreate(&b));

@@ -57,6 +57,10 @@ __device__ __forceinline__ float cos_fixed_sfu(int32_t phase) {
   const int32_t r = (int32_t)((uint32_t)phase << 1);
   return __cosf(__fmul_rn((float)r, 1.4629180792671596e-09f));  // 2 pi / 2^32
 }
+// the same cosine of a phase already doubled (units of 2^-32 turn, [-1/2, 1/2))
+__device__ __forceinline__ float cos_turn32_sfu(int32_t r) {
+  return __cosf(__fmul_rn((float)r, 1.4629180792671596e-09f));  // 2 pi / 2^32
+}
 
 // F_s of one displacement over a list of lattice vectors: the compensated sum
 // of the cosines of the exact fixed-point phases, in blocks of 32 terms (each
@@ -66,6 +70,8 @@ __device__ __forceinline__ float cos_fixed_sfu(int32_t phase) {
 template <bool SMEM>
 __device__ __forceinline__ KSum list_shell_sum(const int4* R, int32_t fx, int32_t fy, int32_t fz, int v_begin,
                                                int v_end) {
+  // n . (2 f) mod 2^32 is the doubled phase cos_fixed_sfu forms from n . f
+  const uint32_t gx = (uint32_t)fx << 1, gy = (uint32_t)fy << 1, gz = (uint32_t)fz << 1;
   KSum acc = {0.f, 0.f};
   for (int v0 = v_begin; v0 < v_end; v0 += 32) {
     const int v1 = min(v0 + 32, v_end);
@@ -73,9 +79,7 @@ __device__ __forceinline__ KSum list_shell_sum(const int4* R, int32_t fx, int32_
 #pragma unroll 4
     for (int v = v0; v < v1; ++v) {
       const int4 n = SMEM ? R[v] : __ldg(R + v);
-      const int32_t ph = (int32_t)((uint32_t)n.x * (uint32_t)fx + (uint32_t)n.y * (uint32_t)fy +
-                                   (uint32_t)n.z * (uint32_t)fz);
-      blk += cos_fixed_sfu(ph);
+      blk += cos_turn32_sfu((int32_t)((uint32_t)n.x * gx + (uint32_t)n.y * gy + (uint32_t)n.z * gz));
     }
     kadd(acc, blk);
   }

@@ -383,7 +383,7 @@ def test_plans_graph_and_autotune(eng, tmp_path, monkeypatch):
     tuned.run()
     c = tuned.read()
     info = tuned.info()
-    assert info["chunk"] in (256, 512, 1024, 2048) and info["blocks_per_sm"] in (2, 4)
+    assert info["chunk"] in (256, 512, 1024, 2048) and info["blocks_per_sm"] in (2, 4, 8, 16)
     assert cache.exists() and '"chunk"' in cache.read_text()
     for out in (a, b, c):
         for i, r in enumerate(ref):
