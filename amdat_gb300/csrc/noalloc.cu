@@ -14,11 +14,12 @@
 //
 // The host finds the array's device address with cudaGetSymbolAddress once per
 // device (the first call on each device, with that device current), then
-// passes it to the kernels.  That first call may load the module, so it should
-// come before any stream capture.  All calls share the one array and it keeps
-// the last call's contents: each call clears the work counter itself, and two
-// calls whose GPU work overlaps (different streams, or host threads on the same
-// device) race on the array, so callers must order them.
+// passes it to the kernels.  Each call copies its tables from host vectors it
+// frees on return, so a stream under capture is refused (AMDAT_ERR_STATE).
+// All calls share the one array and it keeps the last call's contents: each
+// call clears the work counter itself, and two calls whose GPU work overlaps
+// (different streams, or host threads on the same device) race on the array,
+// so callers must order them.
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -165,6 +166,16 @@ extern "C" amdat_status amdat_disp_moments_noalloc(const amdat_scheme* scheme, i
                                       (int32_t)((int64_t)n_atoms * (c + 1) / nch), 0});
     }
     gap_first[G] = (int32_t)items.size();
+    // the table copies below read host vectors freed on return: a captured
+    // graph would keep their addresses, so capture is refused
+    cudaStream_t st = (cudaStream_t)cuda_stream;
+    cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+    const cudaError_t ce = cudaStreamIsCapturing(st, &capture);
+    if (ce == cudaErrorStreamCaptureImplicit || (ce == cudaSuccess && capture != cudaStreamCaptureStatusNone)) {
+      (void)cudaGetLastError();
+      throw Error(AMDAT_ERR_STATE, "amdat_disp_moments_noalloc cannot run on a stream under capture");
+    }
+    AMDAT_CUDA(ce);
     // scratch layout: [counter | t0 | t1 | gap_first | items | partials]
     unsigned char* base = noalloc_scratch_address();
     size_t o = 0;
@@ -175,7 +186,6 @@ extern "C" amdat_status amdat_disp_moments_noalloc(const amdat_scheme* scheme, i
     const size_t o_items = o; o = align(o + items.size() * sizeof(NoallocItem));
     const size_t o_part = o; o = align(o + items.size() * 2 * sizeof(double));
     AMDAT_REQUIRE(o <= NOALLOC_SCRATCH_BYTES, "work exceeds the 16 MiB no-allocation scratch");
-    cudaStream_t st = (cudaStream_t)cuda_stream;
     AMDAT_CUDA(cudaMemsetAsync(base + o_counter, 0, sizeof(int32_t), st));
     if (n_pairs) {
       AMDAT_CUDA(cudaMemcpyAsync(base + o_t0, P.t0.data(), n_pairs * 4, cudaMemcpyHostToDevice, st));

@@ -1,31 +1,43 @@
 // Tensor-core (tcgen05) Fourier densities over the whole half-space lattice.
 //
 // rho[(nx,ny), nz] = sum_j W_j(nx,ny) Z_j(nz), W = X(nx) Y(ny), is a complex
-// GEMM with the atoms as the reduction axis.  As a real GEMM per tile:
-//   A (128 x 2J): rows 0..63   = [Wr, -Wi] of 64 (nx,ny) rows (8 nx x 8 ny),
-//                 rows 64..127 = [Wi,  Wr]           (k = 2j, 2j+1 per atom j)
+// GEMM with the atoms as the reduction axis.  As a real GEMM per tile of 64
+// complex (nx,ny) rows (8 nx x 8 ny) and n consecutive nz:
+//   A (128 x 2J): lane 2r   = [Wr, -Wi] of complex row r (k = 2j, 2j+1 per atom j)
+//                 lane 2r+1 = [Wi,  Wr]
 //   B (  n x 2J): [Zr, Zi] for n consecutive nz (n <= 128, a multiple of 16,
 //                 sized per tile to the nz extent of its 64 rows)
-//   D = A B^T  (128 x n): rows 0..63 = Re rho, rows 64..127 = Im rho.
-// Operands are FP16 split into hi + lo parts (x = hi + lo to ~2^-22), and each
-// chunk of 32 atoms runs three tcgen05.mma passes, hi*lo + lo*hi + hi*hi (small
-// terms first), accumulating in FP32 tensor memory.  The tensor core's FP32
-// accumulation drops low bits as the accumulator grows, so an accumulation
-// never spans more than TC_GROUP chunks (64 atoms): the accumulator is then
-// drained into Kahan-compensated sums that also live in tensor memory.  The
-// phases are the exact fixed-point phases of the FP32 kernels (fraction of the
-// box in units of 2^-31 turns).
+//   D = A B^T  (128 x n): lane 2r = Re rho, lane 2r + 1 = Im rho.
+// The lane pair of a complex row sits in one tensor-memory lane quadrant, so
+// one warp writes both rows.  Lane 2r holds conj(X) conj(Y) and lane 2r + 1
+// holds (i conj(X)) conj(Y): both are one complex product of a per-lane X
+// variant and conj(Y), so the builders need no sign or swap fix-ups.
+// Operands are FP16 split into hi + lo parts (hi = x rounded to a multiple of
+// 2^-11, exact in FP16; lo = x - hi to ~2^-24), and each chunk of 32 atoms
+// runs three tcgen05.mma passes, hi*lo + lo*hi + hi*hi (small terms first),
+// accumulating in FP32 tensor memory.  The tensor core's FP32 accumulation
+// drops low bits as the accumulator grows, so an accumulation never spans more
+// than TC_GROUP chunks (64 atoms): the drain warps then add the accumulator
+// into compensated sums held in their registers (TwoSum) and write the
+// rounding residual back into the accumulator, where the next accumulation on
+// it starts.  The phases are the exact fixed-point phases of the FP32 kernels
+// (fraction of the box in units of 2^-31 turns).
 //
 // Per frame batch, zgen_kernel precomputes the B operands (Z hi/lo in the
-// K-major 128-byte-swizzled layout, one blob per (frame, nz window, chunk)).  The
-// main kernel is warp-specialised, one CTA per SM, 512 TMEM columns:
-//   warps 0-3   drain: TMEM accumulator -> Kahan (s, c) columns, then the epilogue
-//   warp 4      producer: bulk copies (cp.async.bulk) of Z hi/lo and the X/Y
-//               phase tables of each chunk into a 3-stage ring
-//   warps 5-6   MMA issuers, one per accumulator (alternate 64-atom groups):
-//               12 tcgen05.mma per chunk
-//   warps 7-22  builders: the A operand of the chunk (W = X Y products, FP16
-//               split, swizzled K-major stores) into the same ring stage
+// K-major 128-byte-swizzled layout, one blob per (frame, nz window, chunk)) and
+// xygen_kernel the X and Y phase tables.  The main kernel is warp-specialised,
+// one CTA per SM, 512 tensor-memory columns (two 128-column accumulators, four
+// 64-column A stages):
+//   warps 0-15   drain: accumulator -> register sums (lane quadrant warp % 4,
+//                16-column blocks 4 i + warp / 4), then the epilogue
+//   warp 16      producer: bulk copies (cp.async.bulk) of Z hi/lo and the X/Y
+//                tables of each chunk into a 4-stage shared-memory ring (stages
+//                sized to the nz window)
+//   warps 17-18  MMA issuers, one per accumulator (alternate 64-atom groups):
+//                12 tcgen05.mma per chunk, A read from tensor memory
+//   warps 19-26  builders: the A operand of the chunk (W products, FP16 split)
+//                stored into tensor memory (lane quadrant warp % 4, atoms
+//                16 x ((warp - 19) / 4) onwards)
 // Hand-offs are mbarriers (bulk-copy transactions, tcgen05.commit, thread
 // arrivals); every wait is bounded, and a timeout makes every role stop, wait
 // for its own copies and MMAs, free tensor memory and report through an error
@@ -49,42 +61,43 @@ constexpr int TC_ROWS = 64;                   // complex rows (8 nx x 8 ny)
 constexpr int TC_NMAX = 128;                  // widest nz window (MMA N)
 constexpr int TC_M = 2 * TC_ROWS;             // MMA M = 128
 constexpr int TC_GROUP = 2;                   // chunks per tensor-memory accumulation
-constexpr int TC_S = 3;                       // ring stages (Z, X, Y and the A operand of one chunk)
-constexpr int TC_PRODUCER_WARP = 4;
-constexpr int TC_MMA_WARP = 5;                // warps 5 and 6: one per accumulator
+constexpr int TC_S = 4;                       // ring stages: Z, X, Y in shared memory, A in tensor memory
+constexpr uint32_t TC_HDR = 1024;             // barrier header ahead of the ring
+constexpr uint32_t TC_SMEM_MAX = 227 * 1024;  // dynamic shared memory per block
+constexpr int TC_DRAIN_WARPS = 16;            // warps 0-15
+constexpr int TC_DRAIN_PAR = TC_DRAIN_WARPS / 4;  // drain warps per lane quadrant
+constexpr int TC_PRODUCER_WARP = 16;
+constexpr int TC_MMA_WARP = 17;               // warps 17 and 18: one per accumulator
 constexpr int TC_MMA_WARPS = 2;
-constexpr int TC_BUILD_WARP0 = TC_MMA_WARP + TC_MMA_WARPS;
-constexpr int TC_BUILDERS = 512;              // 16 builder warps
-constexpr int TC_BUILD_GROUP = TC_BUILDERS / 2;  // two groups of 8 warps, alternate chunks
-constexpr int TC_DRAINERS = 128;              // warps 0-3, one per TMEM lane quadrant
-constexpr int TC_THREADS = 32 * TC_BUILD_WARP0 + TC_BUILDERS;  // 736
-constexpr uint32_t TC_A_BYTES = TC_M * TC_K * 2;      // 16 KB (one of hi / lo)
-constexpr uint32_t TC_ZHALF = TC_NMAX * TC_K * 2;     // 16 KB (one of hi / lo, widest window)
-constexpr uint32_t TC_XYB = TC_J * 8 * sizeof(float2);  // 2 KB: 8 phases of 32 atoms (X or Y)
-constexpr uint32_t TC_STAGE = 2 * TC_ZHALF + 2 * TC_XYB;  // Z hi, Z lo, X, Y
-constexpr uint32_t TC_WAIT = 1u << 19;                // try_wait calls of <= 1 us (~0.5 s bound)
-// tensor-memory columns: two accumulators, then the Kahan sums and compensations
-constexpr uint32_t TC_COL_ACC = 0, TC_COL_S = 2 * TC_NMAX, TC_COL_C = 3 * TC_NMAX;
-constexpr uint32_t TC_TMEM_COLS = 4 * TC_NMAX;        // 512
+constexpr int TC_BUILD_WARP0 = TC_MMA_WARP + TC_MMA_WARPS;  // warps 19-26
+constexpr int TC_BUILD_WARPS = 8;
+constexpr int TC_THREADS = 32 * (TC_BUILD_WARP0 + TC_BUILD_WARPS);  // 864
+constexpr uint32_t TC_XB = TC_J * 2 * 8 * sizeof(float2);     // 4 KB: 32 atoms x 2 lane variants x 8 nx
+constexpr uint32_t TC_YB = TC_J * 8 * sizeof(float2);         // 2 KB: 32 atoms x 8 ny
+constexpr uint32_t TC_XYB = TC_XB + TC_YB;                    // one (block, chunk) table pair
+constexpr uint32_t TC_WAIT = 1u << 19;                        // try_wait calls of <= 1 us (~0.5 s bound)
+// tensor-memory columns: two accumulators, then four A stages of [hi | lo] (32 columns each)
+constexpr uint32_t TC_COL_ACC = 0, TC_COL_A = 2 * TC_NMAX, TC_A_COLS = 2 * (TC_K / 2);
+constexpr uint32_t TC_TMEM_COLS = 512;
+static_assert(TC_COL_A + TC_S * TC_A_COLS <= TC_TMEM_COLS, "accumulators and A stages must fit tensor memory");
 
-
-struct TcSmem {
-  unsigned char z[TC_S][TC_STAGE];      // [stage] Z hi, Z lo, X, Y; the epilogue stages D here
-  unsigned char a[TC_S][2][TC_A_BYTES];  // [stage][hi|lo]
-  uint64_t full_z[TC_S], full_a[TC_S];  // bulk copies landed / A built
-  uint64_t empty[TC_S];                 // the stage's MMAs finished (one commit per chunk)
+struct TcHdr {
+  uint64_t full_z[TC_S];  // the stage's copies landed
+  uint64_t full_a[TC_S];  // the stage's A operand built
+  uint64_t empty[TC_S];   // the stage's MMAs finished (shared-memory and tensor-memory halves)
   uint64_t full_acc[2], empty_acc[2];
   uint64_t mma_done;
   uint32_t tmem;
-  volatile int bad;        // any role gave up
-  int build_stop[2][2];    // [group][chunk parity]: written by the group's first thread before its barrier
-  int z_issued, z_landed;  // bulk copies issued / seen complete
+  volatile int bad;  // any role gave up
+  int z_issued;      // bulk copies issued
 };
-static_assert(sizeof(float) * TC_M * (TC_NMAX + 1) <= sizeof(((TcSmem*)0)->z), "D staging must fit the Z ring");
-// operands use the 128-byte-swizzled K-major layout: 128-byte rows, 1024-byte aligned tiles
+static_assert(sizeof(TcHdr) <= TC_HDR, "the barrier header must fit its slot");
+// the Z operands use the 128-byte-swizzled K-major layout: 128-byte rows, 1024-byte aligned tiles
 static_assert(TC_K * 2 == 128, "one chunk's K must fill a 128-byte swizzle row");
-static_assert(TC_STAGE % 1024 == 0 && TC_ZHALF % 1024 == 0 && TC_A_BYTES % 1024 == 0,
-              "every operand tile must start on a 1024-byte boundary");
+
+// shared-memory ring stage bytes for nz windows of nzw: Z hi, Z lo (nzw rows of
+// 128 bytes each, 1024-byte aligned for a multiple of 8 rows), X, Y
+__host__ __device__ constexpr uint32_t tc_zstage(int nzw) { return 2u * (uint32_t)nzw * TC_K * 2 + TC_XYB; }
 
 __device__ __forceinline__ void tc_split(float x, __half& hi, __half& lo) {
   hi = __float2half_rn(x);
@@ -93,6 +106,42 @@ __device__ __forceinline__ void tc_split(float x, __half& hi, __half& lo) {
 
 __device__ __forceinline__ void tc_phase(int32_t ph, float* s, float* c) {
   sincospif(__fmul_rn((float)ph, 9.313225746154785e-10f), s, c);  // ph * 2^-30 * pi
+}
+
+// ---- packed FP32 pairs (one instruction for both halves) ---------------------
+__device__ __forceinline__ uint64_t f2_pack(float lo, float hi) {
+  uint64_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void f2_unpack(uint64_t v, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ uint64_t f2_add(uint64_t a, uint64_t b) {
+  uint64_t d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ uint64_t f2_sub(uint64_t a, uint64_t b) {
+  uint64_t d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+
+// hi/lo FP16 pair of (a, b) with |a|, |b| <= 1: hi = round to a multiple of
+// 2^-11 (6144 = 1.5 * 2^12 has a 2^-11 ulp, so (x + 6144) - 6144 rounds x to
+// that grid; every such value in [-1, 1] is exact in FP16), lo = x - hi exactly
+// in FP32 (|lo| <= 2^-12), rounded once to FP16.  Packed as (a: low half, b: high half).
+__device__ __forceinline__ void tc_split2(float a, float b, uint32_t& hi, uint32_t& lo) {
+  const uint64_t w = f2_pack(a, b), c = f2_pack(6144.0f, 6144.0f);
+  const uint64_t h = f2_sub(f2_add(w, c), c);
+  const uint64_t l = f2_sub(w, h);
+  float ha, hb, la, lb;
+  f2_unpack(h, ha, hb);
+  f2_unpack(l, la, lb);
+  const __half2 H = __floats2half2_rn(ha, hb), L = __floats2half2_rn(la, lb);
+  hi = *reinterpret_cast<const uint32_t*>(&H);
+  lo = *reinterpret_cast<const uint32_t*>(&L);
 }
 
 // Z operands of one frame batch: blob (f, zblk, chunk) = [hi][lo], each an
@@ -125,37 +174,37 @@ __global__ void __launch_bounds__(256)
   }
 }
 
-// X/Y table of a 32-atom block: 8 rows (lattice index offset m) of 16 chunks
-// of 16 bytes, chunk = two atoms' (cos, sin).  Atom pair p = j / 2 of row m
-// sits in chunk 16 m + ((m + p) & 15): a builder warp's 128-bit loads (8
-// rows x 4 atom quads, or one row broadcast) are then free of bank conflicts.
-// Returns the float2 index of (atom j, row m).
-__device__ __forceinline__ int xy_slot(int j, int m) { return 2 * (16 * m + ((m + (j >> 1)) & 15)) + (j & 1); }
-
-// X and Y phase tables of one frame batch: for axis a (0 = x, 1 = y), block b
-// of 8 lattice indices (n = -nmax + 8 b + m) and chunk c of 32 atoms, a 2 KB
-// block at ((f * 2 + a) * n_blk + b) * n_chunks + c holding exp(i 2 pi n q_a)
+// X and Y phase tables of one frame batch.  For block b of 8 lattice indices
+// (n = -nmax + 8 b + m) and chunk c of 32 atoms, TC_XYB bytes at
+// (f * n_blk + b) * n_chunks + c; atom pair p = j / 2, element j % 2 of a float4:
+//   X (4 KB): float4 p * 16 + m * 2 + v, the lane variant v of
+//             X_j(n) = exp(i 2 pi n qx_j): v = 0 conj(X) = (cos, -sin),
+//             v = 1 i conj(X) = (sin, cos)
+//   Y (2 KB): float4 p * 8 + m, Y_j(n) = (cos, sin)
+// The eight lanes of a builder quarter warp (four nx, both variants, one ny)
+// read eight distinct bank groups of X and one broadcast float4 of Y.
 __global__ void __launch_bounds__(256)
     xygen_kernel(const int4* __restrict__ fx, int32_t n_list, int32_t n_chunks, int32_t n_blk,
                  int32_t nmax, float2* __restrict__ xybuf) {
-  const int blk = blockIdx.x;  // ((f * 2 + axis) * n_blk + b) * n_chunks + c
+  const int blk = blockIdx.x;  // (f * n_blk + b) * n_chunks + c
   const int c = blk % n_chunks;
   const int b = (blk / n_chunks) % n_blk;
-  const int axis = (blk / (n_chunks * n_blk)) & 1;
-  const int f = blk / (n_chunks * n_blk * 2);
-  float2* out = xybuf + (size_t)blk * (TC_J * 8);
+  const int f = blk / (n_chunks * n_blk);
+  float2* X = xybuf + (size_t)blk * (TC_XYB / sizeof(float2));
+  float2* Y = X + TC_XB / sizeof(float2);
   const int4* F = fx + (int64_t)f * n_list;
-  for (int e = threadIdx.x; e < TC_J * 8; e += blockDim.x) {
-    const int j = e >> 3, m = e & 7;
-    const int a = c * TC_J + j;
-    float sn = 0.f, cs = 0.f;
-    if (a < n_list) {
-      const int32_t q = axis ? F[a].y : F[a].x;
-      const int32_t n = -nmax + 8 * b + m;
-      tc_phase((int32_t)((uint32_t)n * (uint32_t)q), &sn, &cs);
-    }
-    out[xy_slot(j, m)] = make_float2(cs, sn);
+  const int e = threadIdx.x;  // 256 = 32 atoms x 8 indices
+  const int j = e >> 3, m = e & 7, p = j >> 1;
+  const int a = c * TC_J + j;
+  float xs = 0.f, xc = 0.f, ys = 0.f, yc = 0.f;
+  if (a < n_list) {
+    const int32_t n = -nmax + 8 * b + m;
+    tc_phase((int32_t)((uint32_t)n * (uint32_t)F[a].x), &xs, &xc);
+    tc_phase((int32_t)((uint32_t)n * (uint32_t)F[a].y), &ys, &yc);
   }
+  X[(p * 16 + m * 2 + 0) * 2 + (j & 1)] = make_float2(xc, -xs);
+  X[(p * 16 + m * 2 + 1) * 2 + (j & 1)] = make_float2(xs, xc);
+  Y[(p * 8 + m) * 2 + (j & 1)] = make_float2(yc, ys);
 }
 
 // warp-uniform bounded wait: lane 0 reads the block's error flag and polls,
@@ -168,37 +217,41 @@ __device__ __forceinline__ bool warp_wait(uint64_t* mbar, uint32_t parity, volat
 
 __global__ void __launch_bounds__(TC_THREADS, 1)
     rhok_tc_kernel(int32_t n_list, int32_t n_chunks, int32_t n_zblk, int32_t nzw, int32_t n_blk,
-                   int32_t nmax, const TcTile* __restrict__ tiles, const int32_t* __restrict__ entry_k,
-                   const unsigned char* __restrict__ zbuf, const float2* __restrict__ xybuf,
-                   int32_t frame0, int32_t n_k, float2* __restrict__ rho, int* __restrict__ err) {
+                   int32_t nmax, const TcTile* __restrict__ tiles,
+                   const int32_t* __restrict__ entry_k, const unsigned char* __restrict__ zbuf,
+                   const float2* __restrict__ xybuf, int32_t frame0, int32_t n_k, float2* __restrict__ rho,
+                   int* __restrict__ err) {
   extern __shared__ unsigned char smem_raw[];
-  TcSmem& S = *reinterpret_cast<TcSmem*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~(uintptr_t)1023);
+  unsigned char* base = reinterpret_cast<unsigned char*>((reinterpret_cast<uintptr_t>(smem_raw) + 1023) &
+                                                         ~(uintptr_t)1023);
+  TcHdr& S = *reinterpret_cast<TcHdr*>(base);
+  unsigned char* ring = base + TC_HDR;  // TC_S stages of zstage bytes
   const TcTile T = tiles[blockIdx.x];
   const int fl = blockIdx.y;  // frame within the batch
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int n = T.n;
-  const uint32_t zhalf = (uint32_t)nzw * TC_K * 2;
+  const uint32_t zhalf = (uint32_t)nzw * TC_K * 2, zstage = tc_zstage(nzw);
   const unsigned char* Z = zbuf + ((size_t)fl * n_zblk + T.zblk) * (size_t)n_chunks * 2 * zhalf;
-  const float2* XT = xybuf + (((size_t)fl * 2 + 0) * n_blk + (T.nx0 + nmax) / 8) * (size_t)n_chunks * (TC_J * 8);
-  const float2* YT = xybuf + (((size_t)fl * 2 + 1) * n_blk + (T.ny0 + nmax) / 8) * (size_t)n_chunks * (TC_J * 8);
+  constexpr size_t XY_F2 = TC_XYB / sizeof(float2);
+  const float2* XT = xybuf + ((size_t)fl * n_blk + (T.nx0 + nmax) / 8) * (size_t)n_chunks * XY_F2;
+  const float2* YT = xybuf + ((size_t)fl * n_blk + (T.ny0 + nmax) / 8) * (size_t)n_chunks * XY_F2 +
+                     TC_XB / sizeof(float2);
   const int n_groups = (n_chunks + TC_GROUP - 1) / TC_GROUP;
 
   if (tid == 0) {
     for (int s = 0; s < TC_S; ++s) {
       umma::mbar_init(&S.full_z[s], 1);
-      umma::mbar_init(&S.full_a[s], TC_BUILD_GROUP);  // one group builds each chunk
+      umma::mbar_init(&S.full_a[s], TC_BUILD_WARPS);
       umma::mbar_init(&S.empty[s], 1);
     }
     for (int b = 0; b < 2; ++b) {
       umma::mbar_init(&S.full_acc[b], 1);
-      umma::mbar_init(&S.empty_acc[b], TC_DRAINERS);
+      umma::mbar_init(&S.empty_acc[b], TC_DRAIN_WARPS);
     }
     umma::mbar_init(&S.mma_done, TC_MMA_WARPS);
     umma::fence_mbarrier_init();
     S.bad = 0;
-    S.build_stop[0][0] = S.build_stop[0][1] = S.build_stop[1][0] = S.build_stop[1][1] = 0;
     S.z_issued = 0;
-    S.z_landed = 0;
   }
   if (warp == 0) {
     umma::tmem_alloc(&S.tmem, TC_TMEM_COLS);
@@ -208,6 +261,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   __syncthreads();
   umma::fence_after_sync();
   const uint32_t tmem = S.tmem;
+  const uint32_t lanes = (uint32_t)(32 * (warp & 3)) << 16;  // this warp's tensor-memory lane quadrant
 
   if (warp == TC_PRODUCER_WARP) {
     // ---- producer: Z(c), X(c), Y(c) into ring stage c % TC_S once the MMAs of c - TC_S are done
@@ -219,67 +273,86 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           S.bad = 1;
           break;
         }
+        unsigned char* dst = ring + (size_t)s * zstage;
         const unsigned char* src = Z + (size_t)c * 2 * zhalf;
-        umma::mbar_expect_tx(&S.full_z[s], 2u * n * TC_K * 2 + 2 * TC_XYB);
-        umma::bulk_g2s(S.z[s], src, (uint32_t)n * TC_K * 2, &S.full_z[s]);
-        umma::bulk_g2s(S.z[s] + TC_ZHALF, src + zhalf, (uint32_t)n * TC_K * 2, &S.full_z[s]);
-        umma::bulk_g2s(S.z[s] + 2 * TC_ZHALF, XT + (size_t)c * (TC_J * 8), TC_XYB, &S.full_z[s]);
-        umma::bulk_g2s(S.z[s] + 2 * TC_ZHALF + TC_XYB, YT + (size_t)c * (TC_J * 8), TC_XYB, &S.full_z[s]);
+        umma::mbar_expect_tx(&S.full_z[s], 2u * n * TC_K * 2 + TC_XYB);
+        umma::bulk_g2s(dst, src, (uint32_t)n * TC_K * 2, &S.full_z[s]);
+        umma::bulk_g2s(dst + zhalf, src + zhalf, (uint32_t)n * TC_K * 2, &S.full_z[s]);
+        umma::bulk_g2s(dst + 2 * zhalf, XT + (size_t)c * XY_F2, TC_XB, &S.full_z[s]);
+        umma::bulk_g2s(dst + 2 * zhalf + TC_XB, YT + (size_t)c * XY_F2, TC_YB, &S.full_z[s]);
       }
       S.z_issued = c;
     }
   } else if (warp >= TC_MMA_WARP && warp < TC_MMA_WARP + TC_MMA_WARPS) {
     // ---- MMA issuers: warp TC_MMA_WARP + b issues the groups of accumulator b
     // (even / odd groups), so two threads keep the tensor pipe fed; the two
-    // accumulators are independent, and each chunk's stage is read by one issuer
+    // accumulators are independent, and each chunk is read by one issuer
     const int mine = warp - TC_MMA_WARP;
     if (lane == 0) {
       const uint32_t idesc = umma::idesc_f16_f32(TC_M, n);
-      // descriptors are built once: a descriptor's address field is the byte
-      // address >> 4 (14 bits, all of shared memory), so moving to another
-      // stage, the lo half (both 1024-byte aligned) or the next k-step (32 B
-      // inside the swizzled 128-byte rows) adds a constant
-      const uint64_t a_desc0 = umma::smem_desc_sw128(umma::smem_addr(S.a[0][0]));
-      const uint64_t b_desc0 = umma::smem_desc_sw128(umma::smem_addr(S.z[0]));
-      constexpr uint32_t A_STAGE16 = (2 * TC_A_BYTES) >> 4, A_LO16 = TC_A_BYTES >> 4;
-      constexpr uint32_t B_STAGE16 = TC_STAGE >> 4, B_LO16 = TC_ZHALF >> 4;
+      // the B descriptor's address field is the byte address >> 4 (14 bits, all
+      // of shared memory), so the ring stage, the lo half (both 1024-byte
+      // aligned) and the k-step (32 B inside the swizzled 128-byte rows) add to it
+      const uint64_t b_desc0 = umma::smem_desc_sw128(umma::smem_addr(ring));
+      const uint32_t b_stage16 = zstage >> 4, b_lo16 = zhalf >> 4;
+      constexpr uint32_t A_LO = TC_K / 2;
+      static_assert(TC_S == 2 * TC_GROUP, "a ring cycle holds one group of each accumulator");
+      // the chunk loop is unrolled over the ring, so the stage (sd) and the
+      // accumulator (sd / TC_GROUP) of every MMA are offsets from loop-invariant
+      // bases: one thread issues a tcgen05.mma in ~50 cycles at best, and
+      // per-MMA arithmetic or waits add to that
       bool ok = true;
-      for (int c = 0; c < n_chunks; ++c) {
-        const int sz = c % TC_S, sa = sz, g = c / TC_GROUP, buf = g & 1;
-        if (buf != mine) continue;
-        if (S.bad || !umma::mbar_wait(&S.full_z[sz], (c / TC_S) & 1, TC_WAIT)) {
-          ok = false;
-          break;
-        }
-        atomicMax(&S.z_landed, c + 1);
-        if (!umma::mbar_wait(&S.full_a[sa], (c / TC_S) & 1, TC_WAIT) ||
-            (c % TC_GROUP == 0 && !umma::mbar_wait(&S.empty_acc[buf], ((g >> 1) & 1) ^ 1, TC_WAIT))) {
-          ok = false;
-          break;
-        }
-        umma::fence_after_sync();
-        const uint32_t d = tmem + TC_COL_ACC + (uint32_t)(buf * TC_NMAX);
-        const uint64_t ad = a_desc0 + (uint64_t)(sa * A_STAGE16), bd = b_desc0 + (uint64_t)(sz * B_STAGE16);
-        // small cross terms first, then hi*hi, so the accumulator is still small
-        // while the 2^-11-sized terms are added
-        const uint64_t pa[3] = {ad, ad + A_LO16, ad}, pb[3] = {bd + B_LO16, bd, bd};
+      for (int c0 = 0; c0 < n_chunks && ok; c0 += TC_S) {
 #pragma unroll
-        for (int pass = 0; pass < 3; ++pass)
+        for (int sd = 0; sd < TC_S; ++sd) {
+          const int buf = sd / TC_GROUP, c = c0 + sd;
+          if (buf != mine) continue;
+          if (c >= n_chunks) break;
+          const int g = c / TC_GROUP;
+          if (S.bad || !umma::mbar_wait(&S.full_z[sd], (c0 / TC_S) & 1, TC_WAIT) ||
+              !umma::mbar_wait(&S.full_a[sd], (c0 / TC_S) & 1, TC_WAIT) ||
+              (sd % TC_GROUP == 0 && !umma::mbar_wait(&S.empty_acc[buf], ((g >> 1) & 1) ^ 1, TC_WAIT))) {
+            ok = false;
+            break;
+          }
+          umma::fence_after_sync();
+          const uint32_t d = tmem + TC_COL_ACC + (uint32_t)(buf * TC_NMAX);
+          const uint32_t a = tmem + TC_COL_A + (uint32_t)(sd * TC_A_COLS);
+          const uint64_t bd = b_desc0 + (uint64_t)sd * b_stage16;
+          // small cross terms first, then hi*hi, so the accumulator is still small
+          // while the 2^-11-sized terms are added; an accumulator's first group
+          // starts from zero, later ones from the residual the drain left
+          const uint32_t first = (c0 == 0 && sd % TC_GROUP == 0) ? 0u : 1u;
+          const uint32_t pa[3] = {a, a + A_LO, a};
+          const uint64_t pb[3] = {bd + b_lo16, bd, bd};
 #pragma unroll
-          for (int ks = 0; ks < TC_K / 16; ++ks)
-            umma::mma_f16(d, pa[pass] + (uint64_t)(ks * 2), pb[pass] + (uint64_t)(ks * 2), idesc,
-                          (c % TC_GROUP == 0 && pass == 0 && ks == 0) ? 0u : 1u);
-        umma::mma_commit(&S.empty[sz]);
-        if (c % TC_GROUP == TC_GROUP - 1 || c == n_chunks - 1) umma::mma_commit(&S.full_acc[buf]);
+          for (int pass = 0; pass < 3; ++pass)
+#pragma unroll
+            for (int ks = 0; ks < TC_K / 16; ++ks)
+              umma::mma_f16_tmem_a(d, pa[pass] + (uint32_t)(ks * 8), pb[pass] + (uint64_t)(ks * 2), idesc,
+                                   (pass == 0 && ks == 0) ? first : 1u);
+          umma::mma_commit(&S.empty[sd]);
+          if (sd % TC_GROUP == TC_GROUP - 1 || c == n_chunks - 1) umma::mma_commit(&S.full_acc[buf]);
+        }
       }
       if (!ok) S.bad = 1;
       // every MMA this thread issued has finished once mma_done completes
       umma::mma_commit(&S.mma_done);
       if (!umma::mbar_wait(&S.mma_done, 0, TC_WAIT)) S.bad = 1;
     }
-  } else if (warp < 4) {
-    // ---- drain: accumulator of group g -> Kahan sums (s, c) in tensor memory
-    const uint32_t lanes = (uint32_t)(32 * warp) << 16;
+  } else if (warp < TC_DRAIN_WARPS) {
+    // ---- drain: accumulator of group g -> compensated register sums.  Warp w
+    // owns lane quadrant w % 4 and the 16-column blocks TC_DRAIN_PAR i + w / 4
+    // (i < 2): s += acc by TwoSum on packed FP32 pairs, the rounding residual
+    // goes back into the accumulator.  Four warps per quadrant keep a drain
+    // short: the next group on this accumulator waits for it
+    const int par = warp >> 2;
+    constexpr int NB = TC_NMAX / 16 / TC_DRAIN_PAR;  // column blocks per warp
+    uint64_t sp[NB][8];  // column pairs of the sums
+#pragma unroll
+    for (int i = 0; i < NB; ++i)
+#pragma unroll
+      for (int k = 0; k < 8; ++k) sp[i][k] = 0ull;
     bool ok = true;
     for (int g = 0; g < n_groups; ++g) {
       const int buf = g & 1;
@@ -288,140 +361,110 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         break;
       }
       umma::fence_after_sync();
-      for (int cb = 0; cb < n; cb += 16) {
-        uint32_t v[16], s[16], cc[16];
-        umma::tmem_ld_32x32b_x16(tmem + lanes + TC_COL_ACC + (uint32_t)(buf * TC_NMAX + cb), v);
-        if (g > 0) {
-          umma::tmem_ld_32x32b_x16(tmem + lanes + TC_COL_S + (uint32_t)cb, s);
-          umma::tmem_ld_32x32b_x16(tmem + lanes + TC_COL_C + (uint32_t)cb, cc);
-        }
-        umma::tmem_ld_wait();
-        if (g == 0) {
 #pragma unroll
-          for (int i = 0; i < 16; ++i) {
-            s[i] = v[i];
-            cc[i] = 0u;
-          }
-        } else {
+      for (int i = 0; i < NB; ++i) {
+        const int cb = 16 * (TC_DRAIN_PAR * i + par);
+        if (cb < n) {
+          uint32_t v[16];  // accumulator in, residual out
+          const uint32_t col = tmem + lanes + TC_COL_ACC + (uint32_t)(buf * TC_NMAX + cb);
+          umma::tmem_ld_32x32b_x16(col, v);
+          umma::tmem_ld_wait();
 #pragma unroll
-          for (int i = 0; i < 16; ++i) {
-            const float sv = __uint_as_float(s[i]), cv = __uint_as_float(cc[i]);
-            const float y = __fsub_rn(__uint_as_float(v[i]), cv);
-            const float t = __fadd_rn(sv, y);
-            cc[i] = __float_as_uint(__fsub_rn(__fsub_rn(t, sv), y));
-            s[i] = __float_as_uint(t);
+          for (int k = 0; k < 8; ++k) {
+            // t = s + a, bb = t - s, e = (s - (t - bb)) + (a - bb)
+            const uint64_t s2 = sp[i][k];
+            const uint64_t a2 = f2_pack(__uint_as_float(v[2 * k]), __uint_as_float(v[2 * k + 1]));
+            const uint64_t t2 = f2_add(s2, a2);
+            const uint64_t bb = f2_sub(t2, s2);
+            const uint64_t e2 = f2_add(f2_sub(s2, f2_sub(t2, bb)), f2_sub(a2, bb));
+            sp[i][k] = t2;
+            float e0, e1;
+            f2_unpack(e2, e0, e1);
+            v[2 * k] = __float_as_uint(e0);
+            v[2 * k + 1] = __float_as_uint(e1);
           }
+          umma::tmem_st_32x32b_x16(col, v);
         }
-        umma::tmem_st_32x32b_x16(tmem + lanes + TC_COL_S + (uint32_t)cb, s);
-        umma::tmem_st_32x32b_x16(tmem + lanes + TC_COL_C + (uint32_t)cb, cc);
       }
       umma::tmem_st_wait();
       umma::fence_before_sync();
-      umma::mbar_arrive(&S.empty_acc[buf]);
+      __syncwarp();
+      if (lane == 0) umma::mbar_arrive(&S.empty_acc[buf]);
     }
     if (ok && n_groups > 0) {
-      // epilogue: s - c into the D staging area (the Z ring is idle: every copy
-      // was consumed by an MMA that completed before the last group's commit)
-      constexpr int DP = TC_NMAX + 1;
-      float* D = reinterpret_cast<float*>(S.z[0]);
-      const int row = 32 * warp + lane;
-      for (int cb = 0; cb < n; cb += 16) {
-        uint32_t s[16], cc[16];
-        umma::tmem_ld_32x32b_x16(tmem + lanes + TC_COL_S + (uint32_t)cb, s);
-        umma::tmem_ld_32x32b_x16(tmem + lanes + TC_COL_C + (uint32_t)cb, cc);
-        umma::tmem_ld_wait();
+      // epilogue: the sums into the D staging area, rows of n + 1 floats (the
+      // ring is idle: every copy was consumed by an MMA that completed before
+      // the last group's commit)
+      const int DP = n + 1;
+      float* D = reinterpret_cast<float*>(ring);
+      const int row = 32 * (warp & 3) + lane;
 #pragma unroll
-        for (int i = 0; i < 16; ++i)
-          D[row * DP + cb + i] = __fsub_rn(__uint_as_float(s[i]), __uint_as_float(cc[i]));
+      for (int i = 0; i < NB; ++i) {
+        const int cb = 16 * (TC_DRAIN_PAR * i + par);
+        if (cb < n)
+#pragma unroll
+          for (int k = 0; k < 8; ++k) f2_unpack(sp[i][k], D[row * DP + cb + 2 * k], D[row * DP + cb + 2 * k + 1]);
       }
     }
     if (!ok) S.bad = 1;
   } else {
-    // ---- builders: A(c) = W products of the streamed X/Y tables into stage c % TC_S.
-    // Two groups of 8 warps build alternate chunks (group g: chunks c with c % 2 == g),
-    // so the wait / build / fence chain of one chunk overlaps the next one's.
-    const int btid = tid - 32 * TC_BUILD_WARP0;
-    const int grp = btid / TC_BUILD_GROUP, gtid = btid % TC_BUILD_GROUP, gw = gtid >> 5;
-    for (int c = grp; c < n_chunks; c += 2) {
-      const int sa = c % TC_S, sz = sa, par = (c >> 1) & 1;
-      // the group's first thread decides for the group (X/Y of chunk c landed;
-      // the stage's copies landing implies its previous MMAs finished, since the
-      // producer waited for them, so the A half of the stage is free too); the
-      // flag alternates with the group's chunk parity so a slow reader of one
-      // chunk never sees the next one's decision
-      if (gtid == 0) {
-        const bool go = !S.bad && umma::mbar_wait(&S.full_z[sz], (c / TC_S) & 1, TC_WAIT);
-        S.build_stop[grp][par] = go ? 0 : 1;
-      }
-      __syncwarp();
-      if (grp == 0)
-        umma::named_barrier(1, TC_BUILD_GROUP);
-      else
-        umma::named_barrier(2, TC_BUILD_GROUP);
-      if (*(volatile int*)&S.build_stop[grp][par]) {
-        if (gtid == 0) S.bad = 1;
+    // ---- builders: A(c) = the chunk's W products into tensor-memory stage c % TC_S.
+    // Thread = A lane L = 32 (warp % 4) + lane: complex row r = L / 2 (nx offset
+    // r % 8, ny offset r / 8), variant v = L % 2 (0: [Wr, -Wi], 1: [Wi, Wr]);
+    // the row's atoms 16 u .. 16 u + 15, u = (warp - TC_BUILD_WARP0) / 4
+    const int L = 32 * (warp & 3) + lane;
+    const int r = L >> 1, v = L & 1, m = r & 7, yo = r >> 3;
+    const int u = (warp - TC_BUILD_WARP0) >> 2;
+    for (int c = 0; c < n_chunks; ++c) {
+      const int as = c % TC_S;
+      // X/Y of chunk c landed; the stage's copies landing implies the MMAs of
+      // chunk c - TC_S finished (the producer waited for them), so the A stage
+      // in tensor memory is free too
+      if (!warp_wait(&S.full_z[as], (c / TC_S) & 1, &S.bad)) {
+        S.bad = 1;
         break;
       }
-      // A operand: thread = complex row r (nx = lane % 8, ny = warp of the group)
-      // and the atom octet o (atom quads 2o, 2o+1): four 128-bit loads each of X
-      // and Y, eight 128-bit stores (hi and lo of the real row [Wr, -Wi] and of
-      // the imaginary row [Wi, Wr] for both quads), all free of bank conflicts
-      const float4* X4 = reinterpret_cast<const float4*>(S.z[sz] + 2 * TC_ZHALF);
-      const float4* Y4 = X4 + TC_J * 8 / 2;
-      const int m = lane & 7, rg = gw, o = lane >> 3;
-      const int r = rg * 8 + m;
+      const unsigned char* st = ring + (size_t)as * zstage + 2 * zhalf;
+      const float4* X4 = reinterpret_cast<const float4*>(st);
+      const float4* Y4 = reinterpret_cast<const float4*>(st + TC_XB);
+      uint32_t hi[16], lo[16];
 #pragma unroll
-      for (int h = 0; h < 2; ++h) {
-        const int q = 2 * o + h;
-        const float4 xa = X4[16 * m + ((m + 2 * q) & 15)], xb = X4[16 * m + ((m + 2 * q + 1) & 15)];
-        const float4 ya = Y4[16 * rg + ((rg + 2 * q) & 15)], yb = Y4[16 * rg + ((rg + 2 * q + 1) & 15)];
-        const float xr[4] = {xa.x, xa.z, xb.x, xb.z}, xi[4] = {xa.y, xa.w, xb.y, xb.w};
-        const float yr[4] = {ya.x, ya.z, yb.x, yb.z}, yi[4] = {ya.y, ya.w, yb.y, yb.w};
-        uint32_t hre[4], lre[4], him[4], lim[4];
-#pragma unroll
-        for (int a = 0; a < 4; ++a) {
-          const float wr = fmaf(xr[a], yr[a], -xi[a] * yi[a]);
-          const float nwi = fmaf(-xr[a], yi[a], -xi[a] * yr[a]);  // -Im W
-          // hi = fp16(w), lo = fp16(w - hi) of the real row (Wr, -Wi); the
-          // imaginary row (Wi, Wr) is the same pair swapped with the first
-          // element negated (round to nearest is symmetric)
-          const __half2 hi = __floats2half2_rn(wr, nwi);
-          const float2 hb = __half22float2(hi);
-          const __half2 lo = __floats2half2_rn(__fsub_rn(wr, hb.x), __fsub_rn(nwi, hb.y));
-          hre[a] = *reinterpret_cast<const uint32_t*>(&hi);
-          lre[a] = *reinterpret_cast<const uint32_t*>(&lo);
-          him[a] = __byte_perm(hre[a], 0, 0x1032) ^ 0x00008000u;
-          lim[a] = __byte_perm(lre[a], 0, 0x1032) ^ 0x00008000u;
-        }
-        const uint32_t o_re = (uint32_t)(r * 128 + ((q ^ (r & 7)) << 4));  // K = 8q..8q+7, 128-byte swizzle
-        const uint32_t o_im = o_re + (uint32_t)TC_ROWS * 128;                  // row r + 64, same swizzle
-        *reinterpret_cast<uint4*>(S.a[sa][0] + o_re) = make_uint4(hre[0], hre[1], hre[2], hre[3]);
-        *reinterpret_cast<uint4*>(S.a[sa][1] + o_re) = make_uint4(lre[0], lre[1], lre[2], lre[3]);
-        *reinterpret_cast<uint4*>(S.a[sa][0] + o_im) = make_uint4(him[0], him[1], him[2], him[3]);
-        *reinterpret_cast<uint4*>(S.a[sa][1] + o_im) = make_uint4(lim[0], lim[1], lim[2], lim[3]);
+      for (int pp = 0; pp < 8; ++pp) {
+        const int p = 8 * u + pp;
+        const float4 x = X4[p * 16 + m * 2 + v];  // (ar, ai) of atoms 2p, 2p + 1
+        const float4 y = Y4[p * 8 + yo];          // (yr, yi) of atoms 2p, 2p + 1
+        // (ar + i ai) conj(yr + i yi)
+        tc_split2(fmaf(x.x, y.x, x.y * y.y), fmaf(x.y, y.x, -(x.x * y.y)), hi[2 * pp], lo[2 * pp]);
+        tc_split2(fmaf(x.z, y.z, x.w * y.w), fmaf(x.w, y.z, -(x.z * y.w)), hi[2 * pp + 1], lo[2 * pp + 1]);
       }
-      umma::fence_proxy_async_smem();
-      umma::mbar_arrive(&S.full_a[sa]);
+      const uint32_t col = tmem + lanes + TC_COL_A + (uint32_t)(as * TC_A_COLS + 16 * u);
+      umma::tmem_st_32x32b_x16(col, hi);
+      umma::tmem_st_32x32b_x16(col + TC_K / 2, lo);
+      umma::tmem_st_wait();
+      umma::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) umma::mbar_arrive(&S.full_a[as]);
     }
   }
 
   __syncthreads();
   if (S.bad) {
     // copies still in flight land before the block exits
+    // (the last copy issued into each stage; earlier ones were waited for)
     if (tid == 32 * TC_PRODUCER_WARP)
-      for (int c = S.z_landed; c < S.z_issued; ++c)
+      for (int c = std::max(0, S.z_issued - TC_S); c < S.z_issued; ++c)
         umma::mbar_wait(&S.full_z[c % TC_S], (c / TC_S) & 1, TC_WAIT);
     if (tid == 0) atomicExch(err, 1);
   } else if (n_groups > 0) {
-    constexpr int DP = TC_NMAX + 1;
-    const float* D = reinterpret_cast<const float*>(S.z[0]);
+    const int DP = n + 1;
+    const float* D = reinterpret_cast<const float*>(ring);
     const int32_t* E = entry_k + T.entry0;
     float2* out = rho + (int64_t)(frame0 + fl) * n_k;
     for (int e = tid; e < TC_ROWS * n; e += TC_THREADS) {
       const int k = E[e];
       if (k >= 0) {
         const int r = e / n, col = e % n;
-        out[k] = make_float2(D[r * DP + col], D[(TC_ROWS + r) * DP + col]);
+        out[k] = make_float2(D[(2 * r) * DP + col], D[(2 * r + 1) * DP + col]);
       }
     }
   }
@@ -512,7 +555,7 @@ void rhok_tc_run(amdat_ctx* ctx, const TcPlan& P, const int4* fx, int32_t n_list
   const int32_t n_blk = 2 * P.nmax / 8 + 1;  // 8-index blocks from -nmax covering the tiles
   const size_t zblob = (size_t)2 * P.nzw * TC_K * 2;
   const size_t z_frame = (size_t)P.n_zblk * n_chunks * zblob;
-  const size_t xy_frame = (size_t)2 * n_blk * n_chunks * TC_XYB;
+  const size_t xy_frame = (size_t)n_blk * n_chunks * TC_XYB;
   const size_t per_frame = z_frame + xy_frame;
   // frame batches bound the operand buffers to ~1 GB
   const int32_t batch = (int32_t)std::max<size_t>(1, std::min<size_t>(n_frames, (size_t)(1u << 30) / per_frame));
@@ -520,7 +563,12 @@ void rhok_tc_run(amdat_ctx* ctx, const TcPlan& P, const int4* fx, int32_t n_list
   float2* xybuf = reinterpret_cast<float2*>(zbuf + z_frame * batch);
   int* d_err = (int*)(zbuf + per_frame * batch);
   AMDAT_CUDA(cudaMemsetAsync(d_err, 0, sizeof(int), ctx->stream));
-  const size_t shm = sizeof(TcSmem) + 1024;
+  // the ring beside the barrier header (1024 bytes of alignment slack); the
+  // epilogue stages D (128 rows of n + 1 floats) in the idle ring
+  const uint32_t zstage = tc_zstage(P.nzw);
+  const size_t shm = 1024 + TC_HDR + (size_t)TC_S * zstage;
+  AMDAT_REQUIRE(shm <= TC_SMEM_MAX, "nz window too wide for the tensor-core ring");
+  AMDAT_REQUIRE((size_t)TC_S * zstage >= sizeof(float) * TC_M * (P.nzw + 1), "ring too small for the D staging");
   AMDAT_CUDA(cudaFuncSetAttribute(rhok_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)shm));
   for (int32_t f0 = 0; f0 < n_frames; f0 += batch) {
     const int32_t nb = std::min(batch, n_frames - f0);
@@ -528,7 +576,7 @@ void rhok_tc_run(amdat_ctx* ctx, const TcPlan& P, const int4* fx, int32_t n_list
         fx + (int64_t)f0 * n_list, n_list, n_chunks, P.n_zblk, P.nzw, zbuf);
     check_launch("zgen_kernel");
     count_launch(ctx);
-    xygen_kernel<<<(unsigned)(nb * 2 * n_blk * n_chunks), 256, 0, ctx->stream>>>(
+    xygen_kernel<<<(unsigned)(nb * n_blk * n_chunks), 256, 0, ctx->stream>>>(
         fx + (int64_t)f0 * n_list, n_list, n_chunks, n_blk, P.nmax, xybuf);
     check_launch("xygen_kernel");
     count_launch(ctx);

@@ -434,9 +434,12 @@ amdat_status amdat_structure_factor_adjoint(amdat_ctx* ctx, int32_t density,
  * in a 16 MiB __device__ array that every GPU loading this library holds until
  * exit.  The work must fit in it: one work item per time pair and atom chunk,
  * about 419k items at most, so a scheme of more than about 419k time pairs
- * (a linear scheme of more than about 915 frames) returns AMDAT_ERR_ARGUMENT.  The first call on a device looks
- * up the array's address (and may load the module), so make it before any
- * stream capture.  Calls share the array: calls whose GPU work overlaps race.
+ * (a linear scheme of more than about 915 frames) returns AMDAT_ERR_ARGUMENT.
+ * Each call copies its tables from host memory it frees on return, so a stream
+ * under capture (or the legacy stream while any capture is active) is refused
+ * with AMDAT_ERR_STATE; the first call on a device also looks up the array's
+ * address and may load the module.  Calls share the array: calls whose GPU
+ * work overlaps race.
  * ------------------------------------------------------------------------- */
 amdat_status amdat_disp_moments_noalloc(const amdat_scheme* scheme, int32_t fullblock,
                                         const float* d_xyz, int32_t n_frames, int32_t n_atoms,

@@ -5,6 +5,7 @@ Its sums must match amdat_disp_run's (list of all atoms) to 1e-6 relative,
 call after call.  This file is collected last so a failure here does not stop
 the other GPU tests."""
 import ctypes as C
+import warnings
 
 import numpy as np
 import pytest
@@ -93,3 +94,36 @@ def test_noalloc_many_pairs_one_chunk(engine_mod):
     assert st == 0, E.lib().amdat_last_error()
     np.testing.assert_allclose(d2.cpu().numpy(), ref["sum_d2"], rtol=1e-6, atol=1e-12)
     np.testing.assert_allclose(d4.cpu().numpy(), ref["sum_d4"], rtol=1e-6, atol=1e-14)
+
+
+def test_noalloc_refuses_stream_capture(engine_mod):
+    """A call on a stream under capture is refused before any GPU work (its
+    table copies read host memory freed on return); the same call made after
+    the capture runs normally."""
+    import torch
+    E = engine_mod
+    scheme = synth.TimeScheme.exponential(3, 5, 1.3, 0, 0, 0.01)
+    traj = synth.random_walk(64, 6.0, scheme, 0.2, seed=7)
+    x = torch.from_numpy(np.ascontiguousarray(traj.unwrapped)).cuda()
+    s = E.make_scheme(scheme)
+    G = E.scheme_counts(s)[1]
+    d2 = torch.zeros(G, dtype=torch.float64, device="cuda")
+    d4 = torch.zeros_like(d2)
+    stream = torch.cuda.Stream()
+    graph = torch.cuda.CUDAGraph()
+
+    def call(strm):
+        return E.lib().amdat_disp_moments_noalloc(C.byref(s), 0, C.c_void_p(x.data_ptr()),
+                                                  traj.n_frames, traj.n_atoms,
+                                                  C.c_void_p(strm.cuda_stream),
+                                                  C.c_void_p(d2.data_ptr()), C.c_void_p(d4.data_ptr()))
+    torch.cuda.synchronize()
+    with warnings.catch_warnings():  # the captured graph is empty
+        warnings.simplefilter("ignore")
+        with torch.cuda.graph(graph, stream=stream):
+            st = call(stream)
+    assert st == 2 and b"capture" in E.lib().amdat_last_error()
+    st = call(stream)
+    stream.synchronize()
+    assert st == 0, E.lib().amdat_last_error()
+    assert float(d2.sum().item()) > 0.0
