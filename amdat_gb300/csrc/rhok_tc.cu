@@ -76,7 +76,8 @@ constexpr uint32_t TC_XB = TC_J * 2 * 8 * sizeof(float2);     // 4 KB: 32 atoms 
 constexpr uint32_t TC_YB = TC_J * 8 * sizeof(float2);         // 2 KB: 32 atoms x 8 ny
 constexpr uint32_t TC_XYB = TC_XB + TC_YB;                    // one (block, chunk) table pair
 constexpr uint32_t TC_WAIT = 1u << 19;                        // try_wait calls of <= 1 us (~0.5 s bound)
-// tensor-memory columns: two accumulators, then four A stages of [hi | lo] (32 columns each)
+// tensor-memory columns: two accumulators, then four A stages of 64 columns:
+// per 16-atom half u, [hi (16 columns) | lo (16 columns)] at 32 u
 constexpr uint32_t TC_COL_ACC = 0, TC_COL_A = 2 * TC_NMAX, TC_A_COLS = 2 * (TC_K / 2);
 constexpr uint32_t TC_TMEM_COLS = 512;
 static_assert(TC_COL_A + TC_S * TC_A_COLS <= TC_TMEM_COLS, "accumulators and A stages must fit tensor memory");
@@ -292,10 +293,12 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       const uint32_t idesc = umma::idesc_f16_f32(TC_M, n);
       // the B descriptor's address field is the byte address >> 4 (14 bits, all
       // of shared memory), so the ring stage, the lo half (both 1024-byte
-      // aligned) and the k-step (32 B inside the swizzled 128-byte rows) add to it
+      // aligned) and the k-step (32 B inside the swizzled 128-byte rows) add to
+      // it; k-step ks (atoms 8 ks .. 8 ks + 7) of the A stage is column
+      // 32 (ks / 2) + 8 (ks % 2), its lo part 16 columns on
       const uint64_t b_desc0 = umma::smem_desc_sw128(umma::smem_addr(ring));
       const uint32_t b_stage16 = zstage >> 4, b_lo16 = zhalf >> 4;
-      constexpr uint32_t A_LO = TC_K / 2;
+      constexpr uint32_t A_LO = 16;
       static_assert(TC_S == 2 * TC_GROUP, "a ring cycle holds one group of each accumulator");
       // the chunk loop is unrolled over the ring, so the stage (sd) and the
       // accumulator (sd / TC_GROUP) of every MMA are offsets from loop-invariant
@@ -329,7 +332,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           for (int pass = 0; pass < 3; ++pass)
 #pragma unroll
             for (int ks = 0; ks < TC_K / 16; ++ks)
-              umma::mma_f16_tmem_a(d, pa[pass] + (uint32_t)(ks * 8), pb[pass] + (uint64_t)(ks * 2), idesc,
+              umma::mma_f16_tmem_a(d, pa[pass] + (uint32_t)(32 * (ks / 2) + 8 * (ks % 2)), pb[pass] + (uint64_t)(ks * 2), idesc,
                                    (pass == 0 && ks == 0) ? first : 1u);
           umma::mma_commit(&S.empty[sd]);
           if (sd % TC_GROUP == TC_GROUP - 1 || c == n_chunks - 1) umma::mma_commit(&S.full_acc[buf]);
@@ -427,19 +430,17 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
       const unsigned char* st = ring + (size_t)as * zstage + 2 * zhalf;
       const float4* X4 = reinterpret_cast<const float4*>(st);
       const float4* Y4 = reinterpret_cast<const float4*>(st + TC_XB);
-      uint32_t hi[16], lo[16];
+      uint32_t hl[32];  // hi of the 16 atoms, then lo
 #pragma unroll
       for (int pp = 0; pp < 8; ++pp) {
         const int p = 8 * u + pp;
         const float4 x = X4[p * 16 + m * 2 + v];  // (ar, ai) of atoms 2p, 2p + 1
         const float4 y = Y4[p * 8 + yo];          // (yr, yi) of atoms 2p, 2p + 1
         // (ar + i ai) conj(yr + i yi)
-        tc_split2(fmaf(x.x, y.x, x.y * y.y), fmaf(x.y, y.x, -(x.x * y.y)), hi[2 * pp], lo[2 * pp]);
-        tc_split2(fmaf(x.z, y.z, x.w * y.w), fmaf(x.w, y.z, -(x.z * y.w)), hi[2 * pp + 1], lo[2 * pp + 1]);
+        tc_split2(fmaf(x.x, y.x, x.y * y.y), fmaf(x.y, y.x, -(x.x * y.y)), hl[2 * pp], hl[16 + 2 * pp]);
+        tc_split2(fmaf(x.z, y.z, x.w * y.w), fmaf(x.w, y.z, -(x.z * y.w)), hl[2 * pp + 1], hl[17 + 2 * pp]);
       }
-      const uint32_t col = tmem + lanes + TC_COL_A + (uint32_t)(as * TC_A_COLS + 16 * u);
-      umma::tmem_st_32x32b_x16(col, hi);
-      umma::tmem_st_32x32b_x16(col + TC_K / 2, lo);
+      umma::tmem_st_32x32b_x32(tmem + lanes + TC_COL_A + (uint32_t)(as * TC_A_COLS + 32 * u), hl);
       umma::tmem_st_wait();
       umma::fence_before_sync();
       __syncwarp();
