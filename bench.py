@@ -40,10 +40,10 @@ PEAKS_FILE = os.path.join(HERE, "MEASURED_PEAKS.json")
 FP32_LANES_PER_SM = 128
 # DRAM bytes (read + write) per frame of one rhok_tc_kernel launch on the headline
 # lattice (N=32000, |k|<=20, L=33.6), from one ncu capture of a 2-frame launch of
-# this kernel (815.5 MB read + 42.8 MB written).  Every stream of the launch is per
+# this kernel (941.9 MB read + 42.7 MB written).  Every stream of the launch is per
 # frame (X/Y phase tables, Z operands, rho rows), so a launch over f frames moves f
 # times this.
-TC_DRAM_BYTES_PER_FRAME = (815.539e6 + 42.798e6) / 2
+TC_DRAM_BYTES_PER_FRAME = (941.943e6 + 42.651e6) / 2
 # DRAM bytes (read + write) of one launch of the per-list MSD + NGP plan over the 64
 # nested lists, from one ncu capture of disp_mixed_kernel on that workload
 PERLIST_DRAM_BYTES = 2.33e9
