@@ -40,6 +40,7 @@
 
 #include "disp_common.cuh"
 #include "engine.h"
+#include "umma.cuh"
 
 namespace amdat {
 
@@ -387,6 +388,220 @@ __global__ void disp_finalize_kernel(const double* __restrict__ part, int32_t n_
   (void)k_begin;
 }
 
+// ---------------------------------------------------------------------------
+// bulk-copy-staged MSD + NGP moments (members contiguous, no F_s, no G_s;
+// selected with AMDAT_DISP_KERNEL=bulk when a plan is made).
+// One producer thread walks the items (work counter shared with the other
+// blocks) and streams each (pair, up to BK_SEG atoms) segment's six planes (x,
+// y, z at t0 and t1) into a BK_STAGES-deep shared-memory ring with
+// cp.async.bulk, running ahead across items; the consumer warps reduce each
+// segment from shared memory (16-byte loads of four atoms per plane) and write
+// an item's partials after its last segment.  The few atoms before the first
+// and after the last whole quad of a pair's range take direct loads.
+// ---------------------------------------------------------------------------
+constexpr int BK_CONSUMERS = 8;   // consumer warps
+constexpr int BK_THREADS = 32 * (BK_CONSUMERS + 1);
+constexpr uint32_t BK_WAIT = 1u << 20;  // try_wait calls of <= 1 us
+
+struct BkMeta {
+  int32_t item;      // < 0: no more work
+  int32_t s_lo, s_hi;  // whole-quad atom range in the stage
+  int32_t h_lo, h_hi;  // atoms loaded directly (the pair's ragged ends)
+  int32_t t_lo, t_hi;
+  int32_t t0, t1;
+  int32_t last;      // the item's last segment
+};
+// BK_SEG atoms per segment (a multiple of 4), BK_STAGES ring stages
+template <int BK_SEG, int BK_STAGES>
+struct BkSmem {
+  float buf[BK_STAGES][6][BK_SEG];
+  BkMeta meta[BK_STAGES];
+  uint64_t full[BK_STAGES], empty[BK_STAGES];
+  // the item reductions alternate between two buffers: consumer warps fill
+  // red[b] and arrive on red_full[b]; warp 0 sums it and arrives on red_empty[b]
+  KSum red[2][BK_CONSUMERS][2];
+  uint64_t red_full[2], red_empty[2];
+  volatile int bad;
+};
+
+template <int BK_SEG, int BK_STAGES>
+__global__ void __launch_bounds__(BK_THREADS) disp_bulk_kernel(DispParams p, int* __restrict__ err) {
+  extern __shared__ unsigned char bk_raw[];
+  using Smem = BkSmem<BK_SEG, BK_STAGES>;
+  Smem& S = *reinterpret_cast<Smem*>((reinterpret_cast<uintptr_t>(bk_raw) + 127) & ~(uintptr_t)127);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (tid == 0) {
+    for (int s = 0; s < BK_STAGES; ++s) {
+      umma::mbar_init(&S.full[s], 1);
+      umma::mbar_init(&S.empty[s], BK_CONSUMERS);
+    }
+    for (int b = 0; b < 2; ++b) {
+      umma::mbar_init(&S.red_full[b], BK_CONSUMERS);
+      umma::mbar_init(&S.red_empty[b], 1);
+    }
+    umma::fence_mbarrier_init();
+    S.bad = 0;
+  }
+  __syncthreads();
+  const int64_t plane = p.n_pad;
+  if (warp == BK_CONSUMERS) {
+    // ---- producer
+    if (lane == 0) {
+      int seg = 0;
+      auto next_stage = [&](int& st) -> bool {
+        st = seg % BK_STAGES;
+        return !S.bad && umma::mbar_wait(&S.empty[st], ((seg / BK_STAGES) & 1) ^ 1, BK_WAIT);
+      };
+      bool ok = true;
+      for (;;) {
+        const int slot = atomicAdd(p.counter, 1);
+        if (slot >= p.n_items) break;
+        const DispDesc d = p.desc[slot];
+        const int lo = d.first + d.a0, hi = d.first + d.a1;
+        // whole quads [lo4, hi4); ranges under eight atoms go by direct loads
+        int lo4 = (lo + 3) & ~3, hi4 = hi & ~3;
+        if (hi - lo < 8) lo4 = hi4 = lo;
+        for (int pi = 0; pi < d.n_pairs && ok; ++pi) {
+          const int2 tt = d.n_pairs > 1 ? __ldg(p.frames + d.pf + pi) : make_int2(d.t0, d.t1);
+          int s_lo = lo4;
+          do {
+            const int s_hi = min(s_lo + BK_SEG, hi4);
+            int st;
+            if (!next_stage(st)) {
+              ok = false;
+              break;
+            }
+            const bool first = s_lo == lo4, end = s_hi == hi4;
+            BkMeta& m = S.meta[st];
+            m.item = d.item;
+            m.s_lo = s_lo;
+            m.s_hi = s_hi;
+            m.h_lo = first ? lo : 0;
+            m.h_hi = first ? (hi - lo < 8 ? hi : lo4) : 0;
+            m.t_lo = end && hi - lo >= 8 ? hi4 : 0;
+            m.t_hi = end && hi - lo >= 8 ? hi : 0;
+            m.t0 = tt.x;
+            m.t1 = tt.y;
+            m.last = end && pi == d.n_pairs - 1;
+            const uint32_t bytes = (uint32_t)(s_hi - s_lo) * 4u;
+            if (bytes) {
+              umma::mbar_expect_tx(&S.full[st], 6u * bytes);
+#pragma unroll
+              for (int k = 0; k < 6; ++k) {
+                const int t = k < 3 ? tt.x : tt.y;
+                umma::bulk_g2s(S.buf[st][k], p.u + ((int64_t)t * 3 + (k % 3)) * plane + s_lo, bytes, &S.full[st]);
+              }
+            } else {
+              umma::mbar_arrive(&S.full[st]);
+            }
+            ++seg;
+            s_lo = s_hi;
+          } while (s_lo < hi4);
+        }
+        if (!ok) break;
+      }
+      // the stop marker; after a failure the consumers leave through the error flag
+      bool stopped = false;
+      int st;
+      if (ok && next_stage(st)) {
+        S.meta[st].item = -1;
+        umma::mbar_arrive(&S.full[st]);
+        stopped = true;
+      }
+      if (!stopped) S.bad = 1;
+      // copies still in flight land before the block exits (segments whose
+      // stage no later issue reused)
+      for (int s = max(0, seg - BK_STAGES + (stopped ? 1 : 0)); s < seg; ++s)
+        umma::mbar_wait(&S.full[s % BK_STAGES], (s / BK_STAGES) & 1, BK_WAIT);
+    }
+  } else {
+    // ---- consumers
+    KSum m2 = {0.f, 0.f}, m4 = {0.f, 0.f};
+    const int ct = tid;  // 0 .. 32 * BK_CONSUMERS - 1
+    auto term = [&](float dx, float dy, float dz) {
+      const float e = sq3(dx, dy, dz);
+      kadd(m2, e);
+      kadd(m4, e * e);
+    };
+    int n_done = 0;  // items this block's consumers finished
+    for (int seg = 0;; ++seg) {
+      const int st = seg % BK_STAGES;
+      bool ok = true;
+      if (lane == 0) ok = umma::mbar_wait(&S.full[st], (seg / BK_STAGES) & 1, BK_WAIT) && !S.bad;
+      if (!__shfl_sync(0xffffffffu, ok ? 1 : 0, 0)) {
+        S.bad = 1;
+        break;
+      }
+      const BkMeta m = S.meta[st];
+      if (m.item < 0) break;
+      const int nq = (m.s_hi - m.s_lo) >> 2;
+      const float4* P[6];
+#pragma unroll
+      for (int k = 0; k < 6; ++k) P[k] = reinterpret_cast<const float4*>(S.buf[st][k]);
+      for (int q = ct; q < nq; q += 32 * BK_CONSUMERS) {
+        const float4 x0 = P[0][q], y0 = P[1][q], z0 = P[2][q], x1 = P[3][q], y1 = P[4][q], z1 = P[5][q];
+        term(__fsub_rn(x1.x, x0.x), __fsub_rn(y1.x, y0.x), __fsub_rn(z1.x, z0.x));
+        term(__fsub_rn(x1.y, x0.y), __fsub_rn(y1.y, y0.y), __fsub_rn(z1.y, z0.y));
+        term(__fsub_rn(x1.z, x0.z), __fsub_rn(y1.z, y0.z), __fsub_rn(z1.z, z0.z));
+        term(__fsub_rn(x1.w, x0.w), __fsub_rn(y1.w, y0.w), __fsub_rn(z1.w, z0.w));
+      }
+      const int nh = m.h_hi - m.h_lo, nt = m.t_hi - m.t_lo;
+      if (ct < nh + nt) {
+        const int atom = ct < nh ? m.h_lo + ct : m.t_lo + (ct - nh);
+        const float* X0 = p.u + (int64_t)m.t0 * 3 * plane;
+        const float* X1 = p.u + (int64_t)m.t1 * 3 * plane;
+        term(__fsub_rn(__ldg(X1 + atom), __ldg(X0 + atom)),
+             __fsub_rn(__ldg(X1 + plane + atom), __ldg(X0 + plane + atom)),
+             __fsub_rn(__ldg(X1 + 2 * plane + atom), __ldg(X0 + 2 * plane + atom)));
+      }
+      __syncwarp();
+      if (lane == 0) umma::mbar_arrive(&S.empty[st]);
+      if (m.last) {
+        // the item's partials: warp shuffles, then FP64 over the consumer warps
+        // in warp order (buffer b = item parity; use u of it waits for warp 0
+        // to have read use u - 1)
+        const int b = n_done & 1, u = n_done >> 1;
+        KSum v[2] = {m2, m4};
+#pragma unroll
+        for (int k = 0; k < 2; ++k)
+#pragma unroll
+          for (int off = 16; off > 0; off >>= 1) v[k] = kmerge(v[k], kshfl(v[k], off));
+        if (lane == 0) ok = umma::mbar_wait(&S.red_empty[b], (u & 1) ^ 1, BK_WAIT);
+        if (!__shfl_sync(0xffffffffu, ok ? 1 : 0, 0)) {
+          S.bad = 1;
+          break;
+        }
+        if (lane == 0) {
+          S.red[b][warp][0] = v[0];
+          S.red[b][warp][1] = v[1];
+          umma::mbar_arrive(&S.red_full[b]);
+        }
+        if (warp == 0) {
+          if (lane == 0) ok = umma::mbar_wait(&S.red_full[b], u & 1, BK_WAIT);
+          if (!__shfl_sync(0xffffffffu, ok ? 1 : 0, 0)) {
+            S.bad = 1;
+            break;
+          }
+          __syncwarp();  // lane 1 reads after lane 0's acquire
+          if (lane < 2) {
+            double acc = 0.0;
+            for (int w = 0; w < BK_CONSUMERS; ++w)
+              acc += (double)S.red[b][w][lane].s - (double)S.red[b][w][lane].c;
+            p.part[(int64_t)m.item * p.n_out + lane] = acc;
+          }
+          __syncwarp();
+          if (lane == 0) umma::mbar_arrive(&S.red_empty[b]);
+        }
+        ++n_done;
+        m2 = KSum{0.f, 0.f};
+        m4 = KSum{0.f, 0.f};
+      }
+    }
+  }
+  __syncthreads();
+  if (tid == 0 && S.bad) atomicExch(err, 1);
+}
+
 // Sums each list's membership classes into the list's outputs (one block per
 // (list, gap); classes in ascending order, FP64; G_s counts as integers).
 __global__ void disp_combine_kernel(int32_t G, int32_t S, int32_t NB, const int32_t* __restrict__ lu_off,
@@ -688,6 +903,7 @@ struct amdat_disp_plan {
   amdat::DevBuf<int32_t> class_idx;       // atoms of gathered classes
   int chunk = 0, blocks_per_sm = 0, n_items = 0;
   double tuned_ms = 0.0;
+  bool bulk = false;  // MSD + NGP through the bulk-copy-staged kernel
   // device: [descriptors | pair frames | item_first | counters | kv | off | inv | lu_off | lu_units |
   //          part | unit d2 | d4 | fs | gs | list d2 | d4 | fs | gs]
   amdat::DevBuf<unsigned char> dev;
@@ -761,7 +977,7 @@ static void plan_tables(amdat_ctx* ctx, amdat_disp_plan& pl, const PairTable& P,
   pl.o_desc = o; o = align(o + std::max<size_t>(desc.size(), 1) * sizeof(DispDesc));
   pl.o_frames = o; o = align(o + std::max<size_t>(frames.size(), 1) * sizeof(int2));
   pl.o_first = o; o = align(o + item_first.size() * 4);
-  pl.o_counter = o; o = align(o + 4 * (size_t)pl.n_passes);
+  pl.o_counter = o; o = align(o + 4 * ((size_t)pl.n_passes + 1));  // work counters, then an error word
   pl.o_kv = o; o = align(o + std::max<size_t>(pl.sh.kv.size(), 1) * sizeof(int4));
   pl.o_off = o; o = align(o + std::max<size_t>(pl.sh.off.size(), 1) * 4);
   pl.o_inv = o; o = align(o + std::max<size_t>(pl.sh.inv_count.size(), 1) * 4);
@@ -812,7 +1028,7 @@ static void plan_launch(amdat_ctx* ctx, amdat_disp_plan& pl, const PairTable& P)
     AMDAT_CUDA(cudaMemsetAsync(base + pl.o_ud2, 0, pl.bytes - pl.o_ud2, ctx->stream));
     return;
   }
-  AMDAT_CUDA(cudaMemsetAsync(base + pl.o_counter, 0, 4 * (size_t)pl.n_passes, ctx->stream));
+  AMDAT_CUDA(cudaMemsetAsync(base + pl.o_counter, 0, 4 * ((size_t)pl.n_passes + 1), ctx->stream));
   for (int pass = 0; pass < pl.n_passes; ++pass) {
     const int s0 = pass * MAX_FS;
     const int nfs = pl.S ? std::min(MAX_FS, pl.S - s0) : 0;
@@ -870,7 +1086,23 @@ static void plan_launch(amdat_ctx* ctx, amdat_disp_plan& pl, const PairTable& P)
       check_launch("disp_mixed_kernel");
       count_launch(ctx);
     };
-    if (mode == 0) { if (gs) launch(disp_mixed_kernel<0, true>); else launch(disp_mixed_kernel<0, false>); }
+    if (mode == 0 && !gs && pl.bulk) {
+      auto bulk = [&](auto kernel, size_t smem_bytes, int per_sm) {
+        const size_t bshm = smem_bytes + 128;
+        AMDAT_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bshm));
+        const int grid = (int)std::min<int64_t>((int64_t)per_sm * ctx->n_sm, pl.n_items);
+        KernelTimer kt(ctx, "disp_bulk_kernel");
+        kernel<<<grid, BK_THREADS, bshm, ctx->stream>>>(p, (int*)(base + pl.o_counter) + pl.n_passes);
+        check_launch("disp_bulk_kernel");
+        count_launch(ctx);
+      };
+      // 512-atom segments, 4 stages, 4 blocks per SM: the fastest of the ring
+      // shapes measured (2048 x 4 x 1, 1024 x 8 x 1, 1024 x 4 x 2, 512 x 8 x 2
+      // were slower; each block's single producer thread paces its ring)
+      bulk(disp_bulk_kernel<512, 4>, sizeof(BkSmem<512, 4>), 4);
+    } else if (mode == 0) {
+      if (gs) launch(disp_mixed_kernel<0, true>); else launch(disp_mixed_kernel<0, false>);
+    }
     else if (mode == 1) { if (gs) launch(disp_mixed_kernel<1, true>); else launch(disp_mixed_kernel<1, false>); }
     else { if (gs) launch(disp_mixed_kernel<2, true>); else launch(disp_mixed_kernel<2, false>); }
     disp_finalize_kernel<<<(unsigned)n_ug, 256, 0, ctx->stream>>>(
@@ -1045,6 +1277,14 @@ static amdat_disp_plan* plan_create(amdat_ctx* ctx, const amdat_disp_request* re
     for (int l = 0; l < n_lists; ++l)
       for (int g = 0; g < pl->G; ++g)
         pl->pairs[(size_t)l * pl->G + g] = (int64_t)pl->lsize[l] * (P.gap_first[g + 1] - P.gap_first[g]);
+    // MSD + NGP with contiguous members may run the bulk-copy-staged kernel
+    // (AMDAT_DISP_KERNEL=bulk at plan creation)
+    {
+      const char* kern = std::getenv("AMDAT_DISP_KERNEL");
+      bool contiguous = true;
+      for (const ListDev& u : pl->udev) contiguous = contiguous && u.idx == nullptr;
+      pl->bulk = kern && std::strcmp(kern, "bulk") == 0 && pl->S == 0 && pl->NB == 0 && contiguous;
+    }
     // default tile: full chunks stream memory; F_s or few pairs want smaller
     // chunks to keep every SM busy
     const int64_t want_items = (int64_t)ctx->n_sm * 16;
@@ -1056,8 +1296,8 @@ static amdat_disp_plan* plan_create(amdat_ctx* ctx, const amdat_disp_request* re
     // more resident blocks hide the latency of its cosine chain
     int bps = pl->S ? (pl->sh.mode == 1 ? 8 : 4) : 8;
     char keybuf[256];
-    std::snprintf(keybuf, sizeof(keybuf), "sm%d_mode%d_S%d_NB%d_L%d_U%d_atoms%lld_unit%lld_pairs%lld",
-                  ctx->n_sm, pl->S ? pl->sh.mode : 0, pl->S, pl->NB, n_lists, pl->n_units,
+    std::snprintf(keybuf, sizeof(keybuf), "sm%d_mode%d%s_S%d_NB%d_L%d_U%d_atoms%lld_unit%lld_pairs%lld",
+                  ctx->n_sm, pl->S ? pl->sh.mode : 0, pl->bulk ? "b" : "", pl->S, pl->NB, n_lists, pl->n_units,
                   (long long)total_atoms, (long long)unit_atoms, (long long)P.n_pairs);
     const std::string key(keybuf);
     auto hit = tune_cache().find(key);
@@ -1160,7 +1400,12 @@ static void plan_read(amdat_ctx* ctx, amdat_disp_plan* pl, int32_t out_flags, do
     else
       std::memcpy(atom_pairs, pl->pairs.data(), n_lg * 8);
   }
-  if (out_flags == AMDAT_OUT_HOST || atom_pairs) AMDAT_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (out_flags == AMDAT_OUT_HOST || atom_pairs || pl->bulk) AMDAT_CUDA(cudaStreamSynchronize(ctx->stream));
+  if (pl->bulk) {
+    int err = 0;
+    AMDAT_CUDA(cudaMemcpy(&err, base + pl->o_counter + 4 * (size_t)pl->n_passes, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) throw Error(AMDAT_ERR_TIMEOUT, "bulk-staged displacement kernel: a bounded wait timed out");
+  }
 }
 
 static void disp_run_impl(amdat_ctx* ctx, const amdat_disp_request* req, const int32_t* lists,

@@ -879,6 +879,18 @@ def main():
         p_fs_ns = eng.plan(nested, shells=shells, period=L, flags=ns_flags)
         ms_fs_ns = max_over_ranks(pg, time_plan(p_fs_ns, 1))
         p_fs_ns.close()
+        # the same MSD + NGP plans through the bulk-copy-staged kernel (frames
+        # streamed into a shared-memory ring by cp.async.bulk)
+        os.environ["AMDAT_DISP_KERNEL"] = "bulk"
+        try:
+            p_bk = eng.plan(nested, flags=E.PLAN_AUTOTUNE | E.PLAN_GRAPH)
+            p_bk_ns = eng.plan(nested, flags=ns_flags)
+        finally:
+            del os.environ["AMDAT_DISP_KERNEL"]
+        ms_bulk = max_over_ranks(pg, time_plan(p_bk, 10))
+        ms_bulk_ns = max_over_ranks(pg, time_plan(p_bk_ns, 10))
+        p_bk.close()
+        p_bk_ns.close()
         # gathered layout (original atom order, index lists) for comparison
         eng.upload(btraj.unwrapped, btraj.box)
         eng.set_scheme(bscheme)
@@ -920,7 +932,8 @@ def main():
             ms_msd=ms_msd, ms_fs=ms_fs, ms_gathered=ms_g, units=units, tune_s=tune_s,
             info_msd=info_msd, info_fs=info_fs, launches=blaunch, plain_rate=plain_rate,
             alg_bytes=alg_bytes, unit_bytes=unit_bytes, share=share, ms_msd_ns=ms_msd_ns,
-            ms_fs_ns=ms_fs_ns, nvec=int(shells[1][-1]), sum_n=int(sizes.sum()), npairs=npairs,
+            ms_fs_ns=ms_fs_ns, ms_bulk=ms_bulk, ms_bulk_ns=ms_bulk_ns,
+            nvec=int(shells[1][-1]), sum_n=int(sizes.sum()), npairs=npairs,
             bins=bin_ms, n_atoms=int(btraj.n_atoms), frames=int(frames_used))
 
     if args.only in ("", "cli") and rank == 0:
@@ -1128,7 +1141,14 @@ def main():
                                                   "dram_rule": "physical DRAM bytes of one launch (one ncu "
                                                                "capture) over this launch's event time; nested "
                                                                "lists re-read frames from L2"}},
-                        "gathered_layout_ms": b["ms_gathered"]},
+                        "gathered_layout_ms": b["ms_gathered"],
+                        "bulk_staged": {"ms_per_step": b["ms_bulk"], "per_list_ms_per_step": b["ms_bulk_ns"],
+                                        "frac": b["unit_bytes"] / (b["ms_bulk"] / 1e3) / 1e9 / hbm,
+                                        "per_list_frac": b["alg_bytes"] / (b["ms_bulk_ns"] / 1e3) / 1e9 / hbm,
+                                        "rule": "the same MSD + NGP plans through disp_bulk_kernel (each "
+                                                "(pair, 512-atom) segment's six planes streamed into a "
+                                                "4-stage shared-memory ring by cp.async.bulk, "
+                                                "AMDAT_DISP_KERNEL=bulk); frac in the same bytes as above"}},
             "msd_ngp_fs": {"value": b["units"] / (b["ms_fs"] / 1e3), "unit": "atom·time-pairs/s",
                            "ms_per_step": b["ms_fs"], "tile": b["info_fs"],
                            "per_list": {"value": b["units"] / (b["ms_fs_ns"] / 1e3),

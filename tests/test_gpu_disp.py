@@ -255,6 +255,44 @@ def test_plan_sharing_matches_per_list(eng, engine_mod, layout):
     alone.close()
 
 
+@pytest.mark.parametrize("sharing", [True, False])
+def test_bulk_staged_kernel_matches_direct_and_oracle(eng, engine_mod, monkeypatch, sharing):
+    """The bulk-copy-staged MSD + NGP kernel (AMDAT_DISP_KERNEL=bulk at plan
+    creation) gives the direct kernel's sums up to summation order and the
+    oracle's to 1e-6, on
+    contiguous lists with ragged ends, ranges under eight atoms (direct loads)
+    and small lists whose items span several pairs."""
+    E = engine_mod
+    traj, _, _ = load("lin_binary")
+    eng.upload(traj.unwrapped, traj.box)
+    eng.set_scheme(traj.scheme)
+    n = traj.n_atoms
+    ranges = [(0, n), (3, n - 2), (5, 6), (0, 8), (9, 17), (17, 250), (1, 130)]
+    handles = [eng.list(np.arange(a, b, dtype=np.int32)) for a, b in ranges]
+    flags = 0 if sharing else E.PLAN_NO_SHARING
+    monkeypatch.delenv("AMDAT_DISP_KERNEL", raising=False)
+    direct = eng.plan(handles, flags=flags)
+    monkeypatch.setenv("AMDAT_DISP_KERNEL", "bulk")
+    bulk = eng.plan(handles, flags=flags)
+    monkeypatch.delenv("AMDAT_DISP_KERNEL")
+    direct.run()
+    bulk.run()
+    a, b = direct.read(), bulk.read()
+    direct.close()
+    bulk.close()
+    np.testing.assert_array_equal(a["atom_pairs"], b["atom_pairs"])
+    # both kernels keep compensated FP32 sums per thread in their own order
+    # (each within a few 1e-9 of the exact sum): 1e-7 between them, 1e-6 to the oracle
+    np.testing.assert_allclose(b["sum_d2"], a["sum_d2"], rtol=1e-7, atol=1e-12)
+    np.testing.assert_allclose(b["sum_d4"], a["sum_d4"], rtol=1e-7, atol=1e-14)
+    s = orc.scheme(traj.scheme)
+    for i, (lo, hi) in enumerate(ranges[:3]):
+        d2, d4, cnt = orc.disp_moments(s, traj.unwrapped[:, lo:hi])
+        np.testing.assert_array_equal(b["atom_pairs"][i], cnt)
+        np.testing.assert_allclose(b["sum_d2"][i], d2, rtol=1e-6, atol=1e-12)
+        np.testing.assert_allclose(b["sum_d4"][i], d4, rtol=1e-6, atol=1e-14)
+
+
 @pytest.mark.parametrize("fb", [0, 1])
 def test_multi_pair_items_match_oracle(eng, engine_mod, fb):
     """Moments-only plans give lists below half a chunk several pairs of one
