@@ -965,16 +965,30 @@ def main():
         npairs_gd = int(E.scheme_counts(eng.scheme)[2])
         eng.profile_reset(True)
         t0 = time.perf_counter()
-        eng.vhd(0, 0, 5.0, 200)
+        gd_counts = eng.vhd(0, 0, 5.0, 200)
         gd_s = time.perf_counter() - t0
-        n_gd, ms_gd = eng.profile_kernel("pair_hist_kernel")
+        n_gd, ms_gd = eng.profile_kernel("pair_hist_cells_kernel")
         eng.profile_reset(False)
+        # the same G_d through the all-pairs pass (every ordered pair visited)
+        os.environ["AMDAT_PAIR_CELLS"] = "off"
+        try:
+            eng.profile_reset(True)
+            t0 = time.perf_counter()
+            gd_all = eng.vhd(0, 0, 5.0, 200)
+            gd_all_s = time.perf_counter() - t0
+            _, ms_gd_all = eng.profile_kernel("pair_hist_kernel")
+            eng.profile_reset(False)
+        finally:
+            del os.environ["AMDAT_PAIR_CELLS"]
+        gd_same = bool(np.array_equal(gd_counts, gd_all))
         n = 64000.0
         result["pairs"] = dict(frames=PF, rdf_rate=PF * n * (n - 1) / rdf_s, rdf_ms=1e3 * rdf_s,
                                rdf_kernel_ms=ms_rdf, rdf_launches=n_rdf,
                                gs_rate=gs_units / gs_s, gs_ms=1e3 * gs_s,
                                gd_rate=npairs_gd * n * (n - 1) / gd_s, gd_ms=1e3 * gd_s,
-                               gd_kernel_ms=ms_gd, gd_pairs=npairs_gd, rdf_total=int(counts.sum()))
+                               gd_kernel_ms=ms_gd, gd_pairs=npairs_gd, rdf_total=int(counts.sum()),
+                               gd_all_ms=1e3 * gd_all_s, gd_all_kernel_ms=ms_gd_all, gd_same=gd_same,
+                               gd_cells=int(math.floor(42.3 / (5.0 * (1 + 1e-4)))) ** 3)
 
     if args.only in ("", "structure"):
         result["structure"] = structure_bench(torch, stream, local, args)
@@ -1198,7 +1212,10 @@ def main():
         fp32_peak = 2 * FP32_LANES_PER_SM * sm_count * float(peaks.get("sm_max_mhz", 2070.0)) * 1e6 / 1e12
         n = 64000.0
         rdf_fl = 10.0 * q["frames"] * n * (n - 1) / 2 / (q["rdf_kernel_ms"] / 1e3) / 1e12
-        gd_fl = 10.0 * q["gd_pairs"] * n * (n - 1) / (q["gd_kernel_ms"] / 1e3) / 1e12
+        # the cell pass visits each atom's 27 neighbour cells: ~27 / cells of the pairs
+        gd_visited = q["gd_pairs"] * n * n * 27.0 / q["gd_cells"]
+        gd_fl = 10.0 * gd_visited / (q["gd_kernel_ms"] / 1e3) / 1e12
+        gd_all_fl = 10.0 * q["gd_pairs"] * n * (n - 1) / (q["gd_all_kernel_ms"] / 1e3) / 1e12
         pair_rule = ("algorithmic: 10 FP32 flops per visited pair (3 differences, 3 minimum-image "
                      "corrections, 3 multiply-adds of |r|^2, 1 bin division); peak = FP32 FMA peak "
                      "= 2 x 128 lanes x SMs x sm_max_mhz")
@@ -1214,9 +1231,17 @@ def main():
             "vhs": {"value": q["gs_rate"], "unit": "atom·time-pairs/s", "ms_per_step": q["gs_ms"]},
             "vhd": {"value": q["gd_rate"], "unit": "ordered pairs/s", "ms_per_step": q["gd_ms"],
                     "kernel_ms": q["gd_kernel_ms"],
+                    "unit_rule": "every ordered pair of every time pair (the reference's loop), per second",
                     "roofline": {"bound": "fp32", "achieved": gd_fl, "peak": fp32_peak, "unit": "TFLOP/s",
-                                 "frac": gd_fl / fp32_peak, "kernel": "pair_hist_kernel",
-                                 "rule": pair_rule + "; every ordered pair of every time pair"}}}
+                                 "frac": gd_fl / fp32_peak, "kernel": "pair_hist_cells_kernel",
+                                 "rule": pair_rule + f"; visited pairs = time pairs x N^2 x 27 / "
+                                                     f"{q['gd_cells']} cells (each atom's 27 neighbour "
+                                                     f"cells of width >= 5.0)"},
+                    "all_pairs": {"ms_per_step": q["gd_all_ms"], "kernel_ms": q["gd_all_kernel_ms"],
+                                  "counts_equal": q["gd_same"],
+                                  "roofline_frac": gd_all_fl / fp32_peak,
+                                  "rule": "the same call with AMDAT_PAIR_CELLS=off: every ordered pair "
+                                          "visited by pair_hist_kernel"}}}
     if "perlist" in result:
         line["perlist"] = result["perlist"]
     if "bins_only" in result:

@@ -102,3 +102,55 @@ def test_rdf_lattice_distances_on_bin_edges(eng, nb, maxd):
     counts = eng.rdf(0, 0, np.array([0, 1], np.int32), maxd, nb)
     ref, _ = orc.rdf(s, -1, traj.unwrapped, traj.box, lst, nb, maxd)
     np.testing.assert_array_equal(counts, ref)
+
+
+def test_vhd_cells_match_all_pairs_and_oracle(eng, monkeypatch):
+    """Short-range distinct van Hove on a box of six cells per axis: the cell-list
+    pass (27 neighbour cells of each atom) gives the all-pairs pass's counts and
+    the oracle's, bit for bit."""
+    scheme = synth.TimeScheme.linear(5, 1.0)
+    traj = synth.random_walk(3000, 20.0, scheme, 0.6, seed=21, time_scaled=False)
+    eng.upload(traj.unwrapped, traj.box)
+    eng.set_scheme(scheme)
+    monkeypatch.delenv("AMDAT_PAIR_CELLS", raising=False)
+    cells = eng.vhd(0, 0, 3.0, 60)
+    monkeypatch.setenv("AMDAT_PAIR_CELLS", "off")
+    direct = eng.vhd(0, 0, 3.0, 60)
+    monkeypatch.delenv("AMDAT_PAIR_CELLS")
+    np.testing.assert_array_equal(cells, direct)
+    assert cells.sum() > 0
+    s = orc.scheme(scheme)
+    lst = np.arange(traj.n_atoms, dtype=np.int32)
+    ref, _ = orc.vhd(s, traj.wrapped(), traj.box, lst, 3.0, 60)
+    np.testing.assert_array_equal(cells, ref)
+
+
+@pytest.mark.parametrize("maxd,nb", [(3.0, 60), (2.0, 40)])
+def test_pair_cells_lattice_on_cell_and_bin_edges(eng, monkeypatch, maxd, nb):
+    """A cubic lattice (1331 atoms, spacing 1) whose sites sit on cell edges and
+    whose distances fall on bin edges: the cell-list ordered pass (two handles
+    of the same atoms) gives the all-pairs ordered pass's and the symmetric
+    pass's counts, and the oracle's."""
+    g = np.arange(11, dtype=np.float64)
+    pos = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    rng = np.random.default_rng(3)
+    jitter = np.zeros_like(pos)
+    jitter[::5] = rng.normal(0, 1e-6, (len(pos[::5]), 3))
+    frame = (pos + jitter).astype(np.float32)
+    traj = synth.Trajectory(unwrapped=np.stack([frame, frame]), box=np.full(3, np.float32(11.0), np.float32),
+                            box_lo=np.zeros(3, np.float32), types=np.zeros(len(pos), np.int32),
+                            scheme=synth.TimeScheme.linear(2, 1.0))
+    eng.upload(traj.unwrapped, traj.box, traj.box_lo, wrapped=traj.unwrapped)
+    fr = np.array([0, 1], np.int32)
+    allh = eng.list(np.arange(len(pos), dtype=np.int32))  # same members, another handle
+    monkeypatch.delenv("AMDAT_PAIR_CELLS", raising=False)
+    cells = eng.rdf(0, allh, fr, maxd, nb)
+    monkeypatch.setenv("AMDAT_PAIR_CELLS", "off")
+    direct = eng.rdf(0, allh, fr, maxd, nb)
+    monkeypatch.delenv("AMDAT_PAIR_CELLS")
+    sym = eng.rdf(0, 0, fr, maxd, nb)
+    np.testing.assert_array_equal(cells, direct)
+    np.testing.assert_array_equal(cells, sym)
+    s = orc.scheme(traj.scheme)
+    ref, _ = orc.rdf(s, -1, traj.unwrapped, traj.box, np.arange(len(pos), dtype=np.int32), nb, maxd)
+    np.testing.assert_array_equal(cells, ref)
