@@ -280,6 +280,44 @@ __global__ void __launch_bounds__(MODE == 0 ? DISP_THREADS : FS_THREADS)
         }
       }
     }
+    if (MODE == 1 && !GS) {
+      // list-mode F_s: a thread's atoms a and a + nthr together (the same atoms
+      // and the same order of every sum as one atom per step below)
+      for (; a_start + nthr < it.a1; a_start += 2 * nthr) {
+        const int atom_a = L.idx ? __ldg(L.idx + a_start) : L.first + a_start;
+        const int atom_b = L.idx ? __ldg(L.idx + a_start + nthr) : L.first + a_start + nthr;
+        float d[2][3];
+#pragma unroll
+        for (int ax = 0; ax < 3; ++ax) {
+          d[0][ax] = __fsub_rn(__ldg(X1 + ax * p.n_pad + atom_a), __ldg(X0 + ax * p.n_pad + atom_a));
+          d[1][ax] = __fsub_rn(__ldg(X1 + ax * p.n_pad + atom_b), __ldg(X0 + ax * p.n_pad + atom_b));
+        }
+        if (p.want_moments) {
+#pragma unroll
+          for (int k = 0; k < 2; ++k) {
+            const float d2 = fmaf(d[k][2], d[k][2], fmaf(d[k][1], d[k][1], d[k][0] * d[k][0]));
+            kadd(m2, d2);
+            kadd(m4, d2 * d2);
+          }
+        }
+        int32_t f[2][3];
+#pragma unroll
+        for (int k = 0; k < 2; ++k)
+#pragma unroll
+          for (int ax = 0; ax < 3; ++ax) f[k][ax] = turns_fixed(d[k][ax], p.period);
+        for (int s = 0; s < n_fs; ++s) {
+          KSum acc_a, acc_b;
+          if (p.n_rep_smem)
+            list_shell_sum2<true>(reps - p.kv_off[0], f[0][0], f[0][1], f[0][2], f[1][0], f[1][1], f[1][2],
+                                  p.kv_off[s], p.kv_off[s + 1], acc_a, acc_b);
+          else
+            list_shell_sum2<false>(p.kv, f[0][0], f[0][1], f[0][2], f[1][0], f[1][1], f[1][2], p.kv_off[s],
+                                   p.kv_off[s + 1], acc_a, acc_b);
+          kadd(fs[s], __fmul_rn(__fsub_rn(acc_a.s, acc_a.c), p.inv_count[s]));
+          kadd(fs[s], __fmul_rn(__fsub_rn(acc_b.s, acc_b.c), p.inv_count[s]));
+        }
+      }
+    }
     for (int a = a_start; a < it.a1; a += nthr) {
       const int atom = L.idx ? __ldg(L.idx + a) : L.first + a;
       const float dx = __fsub_rn(__ldg(X1 + atom), __ldg(X0 + atom));

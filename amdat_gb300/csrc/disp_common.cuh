@@ -87,4 +87,59 @@ __device__ __forceinline__ KSum list_shell_sum(const int4* R, int32_t fx, int32_
   return acc;
 }
 
+// packed FP32 pairs (one instruction for both halves, each rounded to nearest)
+__device__ __forceinline__ uint64_t pk2(float lo, float hi) {
+  uint64_t r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void upk2(uint64_t v, float& lo, float& hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
+}
+__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
+  uint64_t d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ uint64_t mul2(uint64_t a, uint64_t b) {
+  uint64_t d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+
+// list_shell_sum for two displacements at once (each vector read once for
+// both; the scale multiply and the block sums as packed pairs).  Each result
+// is the one list_shell_sum gives for that displacement, bit for bit.
+template <bool SMEM>
+__device__ __forceinline__ void list_shell_sum2(const int4* R, int32_t fxa, int32_t fya, int32_t fza, int32_t fxb,
+                                                int32_t fyb, int32_t fzb, int v_begin, int v_end, KSum& acc_a,
+                                                KSum& acc_b) {
+  const uint32_t ax = (uint32_t)fxa << 1, ay = (uint32_t)fya << 1, az = (uint32_t)fza << 1;
+  const uint32_t bx = (uint32_t)fxb << 1, by = (uint32_t)fyb << 1, bz = (uint32_t)fzb << 1;
+  const uint64_t scale = pk2(1.4629180792671596e-09f, 1.4629180792671596e-09f);  // 2 pi / 2^32
+  acc_a = KSum{0.f, 0.f};
+  acc_b = KSum{0.f, 0.f};
+  for (int v0 = v_begin; v0 < v_end; v0 += 32) {
+    const int v1 = min(v0 + 32, v_end);
+    uint64_t blk = 0ull;  // (0.f, 0.f)
+#pragma unroll 4
+    for (int v = v0; v < v1; ++v) {
+      const int4 n = SMEM ? R[v] : __ldg(R + v);
+      const int32_t pa = (int32_t)((uint32_t)n.x * ax + (uint32_t)n.y * ay + (uint32_t)n.z * az);
+      const int32_t pb = (int32_t)((uint32_t)n.x * bx + (uint32_t)n.y * by + (uint32_t)n.z * bz);
+      float xa, xb;
+      upk2(mul2(pk2((float)pa, (float)pb), scale), xa, xb);
+      blk = add2(blk, pk2(__cosf(xa), __cosf(xb)));
+    }
+    float ba, bb;
+    upk2(blk, ba, bb);
+    kadd(acc_a, ba);
+    kadd(acc_b, bb);
+  }
+  if ((v_end - v_begin) % 32 == 0) {  // the closing (empty) block
+    kadd(acc_a, 0.f);
+    kadd(acc_b, 0.f);
+  }
+}
+
 }  // namespace amdat
