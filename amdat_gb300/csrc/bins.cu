@@ -248,65 +248,89 @@ __global__ void __launch_bounds__(BN_THREADS) disp_bins_kernel(BnParams p) {
       for (int i = tid; i < p.n_bins; i += BN_THREADS) scnt[i] = 0u;
       __syncthreads();
     }
-    for (int base = it.a0; base < it.a1; base += BN_THREADS) {
-      const int a = base + tid;
-      int b = -1;
-      float v[2 + BN_MAX_FS];
+    // with F_s a thread takes atoms base + tid and base + BN_THREADS + tid per
+    // step: both atoms' shell sums share each vector load, and the two are
+    // aggregated one after the other (the order of one atom per step)
+    constexpr int H = FS ? 2 : 1;
+    for (int base = it.a0; base < it.a1; base += H * BN_THREADS) {
+      int bins_h[H];
+      float v[H][2 + BN_MAX_FS];
+      float dr[H][3];
 #pragma unroll
-      for (int k = 0; k < 2 + BN_MAX_FS; ++k) v[k] = 0.f;
-      if (a < it.a1) {
-        const int atom = p.list_idx ? __ldg(p.list_idx + a) : p.list_first + a;
-        b = __ldg(B0 + atom);
-        if (b >= 0 && p.persistent && __ldg(B1 + atom) != b) b = -1;
-        if (b >= 0) {
-          const float dx = __fsub_rn(__ldg(X1 + atom), __ldg(X0 + atom));
-          const float dy = __fsub_rn(__ldg(X1 + p.n_pad + atom), __ldg(X0 + p.n_pad + atom));
-          const float dz = __fsub_rn(__ldg(X1 + 2 * p.n_pad + atom), __ldg(X0 + 2 * p.n_pad + atom));
-          if (AXES) {
-            v[0] = dx, v[1] = dy, v[2] = dz;
-            v[3] = __fmul_rn(dx, dx), v[4] = __fmul_rn(dy, dy), v[5] = __fmul_rn(dz, dz);
-          } else {
-            v[0] = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
-            v[1] = v[0] * v[0];
-          }
-          if (FS) {
-            const int32_t fx = turns_fixed(dx, p.period);
-            const int32_t fy = turns_fixed(dy, p.period);
-            const int32_t fz = turns_fixed(dz, p.period);
+      for (int h = 0; h < H; ++h) {
+        bins_h[h] = -1;
 #pragma unroll
-            for (int s = 0; s < BN_MAX_FS; ++s) {
-              if (s >= p.n_fs) break;
-              const KSum acc = p.n_kv_smem ? list_shell_sum<true>(skv, fx, fy, fz, p.kv_off[s], p.kv_off[s + 1])
-                                           : list_shell_sum<false>(p.kv, fx, fy, fz, p.kv_off[s], p.kv_off[s + 1]);
-              v[2 + s] = __fmul_rn(__fsub_rn(acc.s, acc.c), p.inv_count[s]);
+        for (int k = 0; k < 2 + BN_MAX_FS; ++k) v[h][k] = 0.f;
+        dr[h][0] = dr[h][1] = dr[h][2] = 0.f;
+        const int a = base + h * BN_THREADS + tid;
+        if (a < it.a1) {
+          const int atom = p.list_idx ? __ldg(p.list_idx + a) : p.list_first + a;
+          int b = __ldg(B0 + atom);
+          if (b >= 0 && p.persistent && __ldg(B1 + atom) != b) b = -1;
+          if (b >= 0) {
+            const float dx = __fsub_rn(__ldg(X1 + atom), __ldg(X0 + atom));
+            const float dy = __fsub_rn(__ldg(X1 + p.n_pad + atom), __ldg(X0 + p.n_pad + atom));
+            const float dz = __fsub_rn(__ldg(X1 + 2 * p.n_pad + atom), __ldg(X0 + 2 * p.n_pad + atom));
+            if (AXES) {
+              v[h][0] = dx, v[h][1] = dy, v[h][2] = dz;
+              v[h][3] = __fmul_rn(dx, dx), v[h][4] = __fmul_rn(dy, dy), v[h][5] = __fmul_rn(dz, dz);
+            } else {
+              v[h][0] = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+              v[h][1] = v[h][0] * v[h][0];
             }
+            dr[h][0] = dx, dr[h][1] = dy, dr[h][2] = dz;
           }
+          bins_h[h] = b;
         }
       }
-      // lanes of one bin: the lowest adds their terms (lane order, FP64)
-      // staged columns: |dr|^2, then |dr|^4 only when asked for, then the shells
+      if (FS && (bins_h[0] >= 0 || bins_h[H - 1] >= 0)) {
+        int32_t f[H][3];
 #pragma unroll
-      for (int k = 0; k < 2 + BN_MAX_FS; ++k)
-        if (k < stride)
-          s_val[warp][lane][k] = (AXES || k == 0 || p.want_d4) ? v[k] : v[k + 1 < 2 + BN_MAX_FS ? k + 1 : k];
-      __syncwarp();
-      const unsigned peers = __match_any_sync(0xffffffffu, b);
-      if (b >= 0 && lane == __ffs(peers) - 1) {
-        const unsigned n_peers = (unsigned)__popc(peers);
-        for (int k = 0; k < stride; ++k) {
-          double sum = 0.0;
-          for (unsigned m = peers; m; m &= m - 1) sum += (double)s_val[warp][__ffs(m) - 1][k];
-          if (p.staged)
-            atomicAdd(sacc + b * stride + k, sum);
+        for (int h = 0; h < H; ++h)
+#pragma unroll
+          for (int ax = 0; ax < 3; ++ax) f[h][ax] = turns_fixed(dr[h][ax], p.period);
+#pragma unroll
+        for (int s = 0; s < BN_MAX_FS; ++s) {
+          if (s >= p.n_fs) break;
+          KSum acc_a, acc_b;
+          if (p.n_kv_smem)
+            list_shell_sum2<true>(skv, f[0][0], f[0][1], f[0][2], f[H - 1][0], f[H - 1][1], f[H - 1][2],
+                                  p.kv_off[s], p.kv_off[s + 1], acc_a, acc_b);
           else
-            atomicAdd(p.acc + ((int64_t)b * p.n_gaps + it.gap) * stride + k, sum);
+            list_shell_sum2<false>(p.kv, f[0][0], f[0][1], f[0][2], f[H - 1][0], f[H - 1][1], f[H - 1][2],
+                                   p.kv_off[s], p.kv_off[s + 1], acc_a, acc_b);
+          v[0][2 + s] = __fmul_rn(__fsub_rn(acc_a.s, acc_a.c), p.inv_count[s]);
+          v[H - 1][2 + s] = __fmul_rn(__fsub_rn(acc_b.s, acc_b.c), p.inv_count[s]);
         }
-        if (p.staged)
-          atomicAdd(scnt + b, n_peers);
-        else
-          atomicAdd(p.cnt + (int64_t)b * p.n_gaps + it.gap, (unsigned long long)n_peers);
       }
-      __syncwarp();
+#pragma unroll
+      for (int h = 0; h < H; ++h) {
+        const int b = bins_h[h];
+        // lanes of one bin: the lowest adds their terms (lane order, FP64)
+        // staged columns: |dr|^2, then |dr|^4 only when asked for, then the shells
+#pragma unroll
+        for (int k = 0; k < 2 + BN_MAX_FS; ++k)
+          if (k < stride)
+            s_val[warp][lane][k] = (AXES || k == 0 || p.want_d4) ? v[h][k] : v[h][k + 1 < 2 + BN_MAX_FS ? k + 1 : k];
+        __syncwarp();
+        const unsigned peers = __match_any_sync(0xffffffffu, b);
+        if (b >= 0 && lane == __ffs(peers) - 1) {
+          const unsigned n_peers = (unsigned)__popc(peers);
+          for (int k = 0; k < stride; ++k) {
+            double sum = 0.0;
+            for (unsigned m = peers; m; m &= m - 1) sum += (double)s_val[warp][__ffs(m) - 1][k];
+            if (p.staged)
+              atomicAdd(sacc + b * stride + k, sum);
+            else
+              atomicAdd(p.acc + ((int64_t)b * p.n_gaps + it.gap) * stride + k, sum);
+          }
+          if (p.staged)
+            atomicAdd(scnt + b, n_peers);
+          else
+            atomicAdd(p.cnt + (int64_t)b * p.n_gaps + it.gap, (unsigned long long)n_peers);
+        }
+        __syncwarp();
+      }
     }
     if (p.staged) {
       __syncthreads();
