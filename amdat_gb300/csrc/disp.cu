@@ -397,33 +397,28 @@ __global__ void __launch_bounds__(MODE == 0 ? DISP_THREADS : FS_THREADS)
   }
 }
 
-// Sums the partials of each (list, gap) in a fixed order (FP64).
+// Sums the partials of each (unit, gap) in a fixed order (FP64): one warp per
+// output (lanes stride over the items, then a fixed shuffle tree).
 __global__ void disp_finalize_kernel(const double* __restrict__ part, int32_t n_out,
-                                     const int32_t* __restrict__ item_first,  // [n_lists*G + 1]
-                                     int32_t k_begin, double* __restrict__ out_d2,
+                                     const int32_t* __restrict__ item_first,  // [n_lg + 1]
+                                     int32_t n_lg, double* __restrict__ out_d2,
                                      double* __restrict__ out_d4, double* __restrict__ out_fs,
                                      int32_t fs_stride, int32_t fs_offset, int32_t n_fs,
                                      int32_t want_moments) {
-  const int lg = blockIdx.x;
+  const int n_red = 2 + n_fs, lane = threadIdx.x & 31;
+  const int64_t gw = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (gw >= (int64_t)n_lg * n_red) return;
+  const int lg = (int)(gw / n_red), k = (int)(gw % n_red);
+  if (k < 2 && !want_moments) return;
   const int i0 = item_first[lg], i1 = item_first[lg + 1];
-  __shared__ double red[8][32];
-  const int n_red = 2 + n_fs;
-  for (int k = 0; k < n_red; ++k) {
-    double acc = 0.0;
-    for (int i = i0 + threadIdx.x; i < i1; i += blockDim.x) acc += part[(int64_t)i * n_out + k];
-    for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5][k & 31] = acc;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      double t = 0.0;
-      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w][k & 31];
-      if (k == 0 && want_moments && out_d2) out_d2[lg] = t;
-      if (k == 1 && want_moments && out_d4) out_d4[lg] = t;
-      if (k >= 2 && out_fs) out_fs[(int64_t)lg * fs_stride + fs_offset + (k - 2)] = t;
-    }
-    __syncthreads();
+  double acc = 0.0;
+  for (int i = i0 + lane; i < i1; i += 32) acc += part[(int64_t)i * n_out + k];
+  for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+  if (lane == 0) {
+    if (k == 0 && out_d2) out_d2[lg] = acc;
+    if (k == 1 && out_d4) out_d4[lg] = acc;
+    if (k >= 2 && out_fs) out_fs[(int64_t)lg * fs_stride + fs_offset + (k - 2)] = acc;
   }
-  (void)k_begin;
 }
 
 // ---------------------------------------------------------------------------
@@ -640,27 +635,38 @@ __global__ void __launch_bounds__(BK_THREADS) disp_bulk_kernel(DispParams p, int
   if (tid == 0 && S.bad) atomicExch(err, 1);
 }
 
-// Sums each list's membership classes into the list's outputs (one block per
-// (list, gap); classes in ascending order, FP64; G_s counts as integers).
-__global__ void disp_combine_kernel(int32_t G, int32_t S, int32_t NB, const int32_t* __restrict__ lu_off,
+// Sums each list's membership classes into the list's outputs (FP64, classes
+// in ascending order per lane, then a fixed shuffle tree): one warp per
+// (list, gap, column).
+__global__ void disp_combine_kernel(int32_t G, int32_t S, int32_t n_lg, const int32_t* __restrict__ lu_off,
                                     const int32_t* __restrict__ lu_units, const double* __restrict__ ud2,
                                     const double* __restrict__ ud4, const double* __restrict__ ufs,
-                                    const unsigned long long* __restrict__ ugs, double* __restrict__ d2,
-                                    double* __restrict__ d4, double* __restrict__ fs,
-                                    unsigned long long* __restrict__ gs) {
-  const int lg = blockIdx.x, l = lg / G, g = lg % G;
+                                    double* __restrict__ d2, double* __restrict__ d4, double* __restrict__ fs) {
+  const int n_red = 2 + S, S1 = S > 0 ? S : 1, lane = threadIdx.x & 31;
+  const int64_t gw = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (gw >= (int64_t)n_lg * n_red) return;
+  const int lg = (int)(gw / n_red), k = (int)(gw % n_red), l = lg / G, g = lg % G;
   const int u0 = lu_off[l], u1 = lu_off[l + 1];
-  const int S1 = S > 0 ? S : 1;
-  for (int k = threadIdx.x; k < 2 + S; k += blockDim.x) {
-    double acc = 0.0;
-    for (int i = u0; i < u1; ++i) {
-      const int64_t ug = (int64_t)lu_units[i] * G + g;
-      acc += k == 0 ? ud2[ug] : (k == 1 ? ud4[ug] : ufs[ug * S1 + (k - 2)]);
-    }
+  double acc = 0.0;
+  for (int i = u0 + lane; i < u1; i += 32) {
+    const int64_t ug = (int64_t)lu_units[i] * G + g;
+    acc += k == 0 ? ud2[ug] : (k == 1 ? ud4[ug] : ufs[ug * S1 + (k - 2)]);
+  }
+  for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+  if (lane == 0) {
     if (k == 0) d2[lg] = acc;
     else if (k == 1) d4[lg] = acc;
     else fs[(int64_t)lg * S1 + (k - 2)] = acc;
   }
+}
+
+// G_s counts of each list: the sums of its classes' counts (integers)
+__global__ void disp_combine_gs_kernel(int32_t G, int32_t NB, const int32_t* __restrict__ lu_off,
+                                       const int32_t* __restrict__ lu_units,
+                                       const unsigned long long* __restrict__ ugs,
+                                       unsigned long long* __restrict__ gs) {
+  const int lg = blockIdx.x, l = lg / G, g = lg % G;
+  const int u0 = lu_off[l], u1 = lu_off[l + 1];
   for (int b = threadIdx.x; b < NB; b += blockDim.x) {
     unsigned long long c = 0ull;
     for (int i = u0; i < u1; ++i) c += ugs[((int64_t)lu_units[i] * G + g) * NB + b];
@@ -1143,21 +1149,27 @@ static void plan_launch(amdat_ctx* ctx, amdat_disp_plan& pl, const PairTable& P)
     }
     else if (mode == 1) { if (gs) launch(disp_mixed_kernel<1, true>); else launch(disp_mixed_kernel<1, false>); }
     else { if (gs) launch(disp_mixed_kernel<2, true>); else launch(disp_mixed_kernel<2, false>); }
-    disp_finalize_kernel<<<(unsigned)n_ug, 256, 0, ctx->stream>>>(
-        p.part, pl.n_out, (const int32_t*)(base + pl.o_first), 0,
+    disp_finalize_kernel<<<(unsigned)ceil_div((int64_t)n_ug * (2 + nfs), 8), 256, 0, ctx->stream>>>(
+        p.part, pl.n_out, (const int32_t*)(base + pl.o_first), (int32_t)n_ug,
         pass == 0 ? (double*)(base + pl.o_ud2) : nullptr, pass == 0 ? (double*)(base + pl.o_ud4) : nullptr,
         pl.S ? (double*)(base + pl.o_ufs) : nullptr, std::max(pl.S, 1), s0, nfs, pass == 0 ? 1 : 0);
     check_launch("disp_finalize_kernel");
     count_launch(ctx);
   }
   if (pl.classes) {
-    disp_combine_kernel<<<(unsigned)n_lg, 128, 0, ctx->stream>>>(
-        pl.G, pl.S, pl.NB, (const int32_t*)(base + pl.o_luo), (const int32_t*)(base + pl.o_luu),
+    disp_combine_kernel<<<(unsigned)ceil_div((int64_t)n_lg * (2 + pl.S), 8), 256, 0, ctx->stream>>>(
+        pl.G, pl.S, (int32_t)n_lg, (const int32_t*)(base + pl.o_luo), (const int32_t*)(base + pl.o_luu),
         (const double*)(base + pl.o_ud2), (const double*)(base + pl.o_ud4), (const double*)(base + pl.o_ufs),
-        (const unsigned long long*)(base + pl.o_ugs), (double*)(base + pl.o_d2), (double*)(base + pl.o_d4),
-        (double*)(base + pl.o_fs), (unsigned long long*)(base + pl.o_gs));
+        (double*)(base + pl.o_d2), (double*)(base + pl.o_d4), (double*)(base + pl.o_fs));
     check_launch("disp_combine_kernel");
     count_launch(ctx);
+    if (pl.NB) {
+      disp_combine_gs_kernel<<<(unsigned)n_lg, 128, 0, ctx->stream>>>(
+          pl.G, pl.NB, (const int32_t*)(base + pl.o_luo), (const int32_t*)(base + pl.o_luu),
+          (const unsigned long long*)(base + pl.o_ugs), (unsigned long long*)(base + pl.o_gs));
+      check_launch("disp_combine_gs_kernel");
+      count_launch(ctx);
+    }
   }
 }
 

@@ -578,7 +578,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--frames", type=int, default=400, help="frames of the headline workload")
     ap.add_argument("--only", default="", choices=["", "isf", "msd", "batched", "pairs", "structure", "cli",
-                                                   "perlist", "bins"],
+                                                   "perlist", "shared", "bins"],
                     help="run one workload only (profiling)")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline")
     ap.add_argument("--pair-frames", type=int, default=50,
@@ -801,13 +801,15 @@ def main():
                              e2e=job_rate(munits, world, me2e_ms), e2e_ms=me2e_ms,
                              h2d=int(MT * MN * 12), d2h=int(G * (8 + 8 + 8 + 8)), out=m_out)
 
-    if args.only == "perlist":
-        # profiling aid: the batched workload's per-list MSD + NGP plan alone
+    if args.only in ("perlist", "shared"):
+        # profiling aid: the batched workload's per-list (or membership-class
+        # shared) MSD + NGP plan alone
         btraj, bscheme, sizes, perm = batched_workload()
         eng.upload(btraj.unwrapped[:, perm], btraj.box)
         eng.set_scheme(bscheme)
         nested = [eng.list(np.arange(n, dtype=np.int32)) for n in sizes]
-        plan = eng.plan(nested, flags=E.PLAN_AUTOTUNE | E.PLAN_NO_SHARING)
+        pflags = E.PLAN_AUTOTUNE | (E.PLAN_NO_SHARING if args.only == "perlist" else 0)
+        plan = eng.plan(nested, flags=pflags)
         for _ in range(args.warmup):
             plan.run()
         torch.cuda.synchronize()
@@ -815,7 +817,8 @@ def main():
         for _ in range(args.steps):
             plan.run()
         torch.cuda.synchronize()
-        result["perlist"] = dict(ms=1e3 * (time.perf_counter() - t0) / max(args.steps, 1), info=plan.info())
+        result["perlist"] = dict(ms=1e3 * (time.perf_counter() - t0) / max(args.steps, 1), info=plan.info(),
+                                 plan=args.only)
         plan.close()
 
     if args.only == "bins":
