@@ -6,6 +6,8 @@
 
 #include <cstdint>
 
+#include "f32x2.cuh"
+
 namespace amdat {
 
 // --- compensated FP32 helpers ------------------------------------------------
@@ -85,26 +87,6 @@ __device__ __forceinline__ KSum list_shell_sum(const int4* R, int32_t fx, int32_
   }
   if ((v_end - v_begin) % 32 == 0) kadd(acc, 0.f);  // the closing (empty) block
   return acc;
-}
-
-// packed FP32 pairs (one instruction for both halves, each rounded to nearest)
-__device__ __forceinline__ uint64_t pk2(float lo, float hi) {
-  uint64_t r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-  return r;
-}
-__device__ __forceinline__ void upk2(uint64_t v, float& lo, float& hi) {
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-}
-__device__ __forceinline__ uint64_t add2(uint64_t a, uint64_t b) {
-  uint64_t d;
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ uint64_t mul2(uint64_t a, uint64_t b) {
-  uint64_t d;
-  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
 }
 
 // list_shell_sum for two displacements at once (each vector read once for

@@ -50,6 +50,7 @@
 #include <vector>
 
 #include "engine.h"
+#include "f32x2.cuh"
 #include "tc_tiles.h"
 #include "umma.cuh"
 
@@ -109,37 +110,17 @@ __device__ __forceinline__ void tc_phase(int32_t ph, float* s, float* c) {
   sincospif(__fmul_rn((float)ph, 9.313225746154785e-10f), s, c);  // ph * 2^-30 * pi
 }
 
-// ---- packed FP32 pairs (one instruction for both halves) ---------------------
-__device__ __forceinline__ uint64_t f2_pack(float lo, float hi) {
-  uint64_t r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-  return r;
-}
-__device__ __forceinline__ void f2_unpack(uint64_t v, float& lo, float& hi) {
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(v));
-}
-__device__ __forceinline__ uint64_t f2_add(uint64_t a, uint64_t b) {
-  uint64_t d;
-  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-__device__ __forceinline__ uint64_t f2_sub(uint64_t a, uint64_t b) {
-  uint64_t d;
-  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
-  return d;
-}
-
 // hi/lo FP16 pair of (a, b) with |a|, |b| <= 1: hi = round to a multiple of
 // 2^-11 (6144 = 1.5 * 2^12 has a 2^-11 ulp, so (x + 6144) - 6144 rounds x to
 // that grid; every such value in [-1, 1] is exact in FP16), lo = x - hi exactly
 // in FP32 (|lo| <= 2^-12), rounded once to FP16.  Packed as (a: low half, b: high half).
 __device__ __forceinline__ void tc_split2(float a, float b, uint32_t& hi, uint32_t& lo) {
-  const uint64_t w = f2_pack(a, b), c = f2_pack(6144.0f, 6144.0f);
-  const uint64_t h = f2_sub(f2_add(w, c), c);
-  const uint64_t l = f2_sub(w, h);
+  const uint64_t w = pk2(a, b), c = pk2(6144.0f, 6144.0f);
+  const uint64_t h = sub2(add2(w, c), c);
+  const uint64_t l = sub2(w, h);
   float ha, hb, la, lb;
-  f2_unpack(h, ha, hb);
-  f2_unpack(l, la, lb);
+  upk2(h, ha, hb);
+  upk2(l, la, lb);
   const __half2 H = __floats2half2_rn(ha, hb), L = __floats2half2_rn(la, lb);
   hi = *reinterpret_cast<const uint32_t*>(&H);
   lo = *reinterpret_cast<const uint32_t*>(&L);
@@ -376,13 +357,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           for (int k = 0; k < 8; ++k) {
             // t = s + a, bb = t - s, e = (s - (t - bb)) + (a - bb)
             const uint64_t s2 = sp[i][k];
-            const uint64_t a2 = f2_pack(__uint_as_float(v[2 * k]), __uint_as_float(v[2 * k + 1]));
-            const uint64_t t2 = f2_add(s2, a2);
-            const uint64_t bb = f2_sub(t2, s2);
-            const uint64_t e2 = f2_add(f2_sub(s2, f2_sub(t2, bb)), f2_sub(a2, bb));
+            const uint64_t a2 = pk2(__uint_as_float(v[2 * k]), __uint_as_float(v[2 * k + 1]));
+            const uint64_t t2 = add2(s2, a2);
+            const uint64_t bb = sub2(t2, s2);
+            const uint64_t e2 = add2(sub2(s2, sub2(t2, bb)), sub2(a2, bb));
             sp[i][k] = t2;
             float e0, e1;
-            f2_unpack(e2, e0, e1);
+            upk2(e2, e0, e1);
             v[2 * k] = __float_as_uint(e0);
             v[2 * k + 1] = __float_as_uint(e1);
           }
@@ -406,7 +387,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
         const int cb = 16 * (TC_DRAIN_PAR * i + par);
         if (cb < n)
 #pragma unroll
-          for (int k = 0; k < 8; ++k) f2_unpack(sp[i][k], D[row * DP + cb + 2 * k], D[row * DP + cb + 2 * k + 1]);
+          for (int k = 0; k < 8; ++k) upk2(sp[i][k], D[row * DP + cb + 2 * k], D[row * DP + cb + 2 * k + 1]);
       }
     }
     if (!ok) S.bad = 1;
