@@ -18,7 +18,7 @@
 // accumulating in FP32 tensor memory.  The tensor core's FP32 accumulation
 // drops low bits as the accumulator grows, so an accumulation never spans more
 // than TC_GROUP chunks (64 atoms): the drain warps then add the accumulator
-// into compensated sums held in their registers (TwoSum) and write the
+// into compensated sums held in their registers (Fast2Sum) and write the
 // rounding residual back into the accumulator, where the next accumulation on
 // it starts.  The phases are the exact fixed-point phases of the FP32 kernels
 // (fraction of the box in units of 2^-31 turns).
@@ -327,7 +327,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
   } else if (warp < TC_DRAIN_WARPS) {
     // ---- drain: accumulator of group g -> compensated register sums.  Warp w
     // owns lane quadrant w % 4 and the 16-column blocks TC_DRAIN_PAR i + w / 4
-    // (i < 2): s += acc by TwoSum on packed FP32 pairs, the rounding residual
+    // (i < 2): s += acc by Fast2Sum on packed FP32 pairs, the rounding residual
     // goes back into the accumulator.  Four warps per quadrant keep a drain
     // short: the next group on this accumulator waits for it
     const int par = warp >> 2;
@@ -355,12 +355,13 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
           umma::tmem_ld_wait();
 #pragma unroll
           for (int k = 0; k < 8; ++k) {
-            // t = s + a, bb = t - s, e = (s - (t - bb)) + (a - bb)
+            // Fast2Sum: t = s + a, e = a - (t - s), exact while |s| >= |a|; when
+            // a 64-atom partial outweighs the running sum the residual may lose
+            // about an ulp of the partial (~1e-6), far inside the error bounds
             const uint64_t s2 = sp[i][k];
             const uint64_t a2 = pk2(__uint_as_float(v[2 * k]), __uint_as_float(v[2 * k + 1]));
             const uint64_t t2 = add2(s2, a2);
-            const uint64_t bb = sub2(t2, s2);
-            const uint64_t e2 = add2(sub2(s2, sub2(t2, bb)), sub2(a2, bb));
+            const uint64_t e2 = sub2(a2, sub2(t2, s2));
             sp[i][k] = t2;
             float e0, e1;
             upk2(e2, e0, e1);
