@@ -28,16 +28,16 @@
 // xygen_kernel the X and Y phase tables.  The main kernel is warp-specialised,
 // one CTA per SM, 512 tensor-memory columns (two 128-column accumulators, four
 // 64-column A stages):
-//   warps 0-15   drain: accumulator -> register sums (lane quadrant warp % 4,
-//                16-column blocks 4 i + warp / 4), then the epilogue
-//   warp 16      producer: bulk copies (cp.async.bulk) of Z hi/lo and the X/Y
+//   warps 0-7    drain: accumulator -> register sums (lane quadrant warp % 4,
+//                16-column blocks 2 i + warp / 4), then the epilogue
+//   warp 8       producer: bulk copies (cp.async.bulk) of Z hi/lo and the X/Y
 //                tables of each chunk into a 4-stage shared-memory ring (stages
 //                sized to the nz window)
-//   warps 17-18  MMA issuers, one per accumulator (alternate 64-atom groups):
+//   warps 9-10   MMA issuers, one per accumulator (alternate 64-atom groups):
 //                12 tcgen05.mma per chunk, A read from tensor memory
-//   warps 19-26  builders: the A operand of the chunk (W products, FP16 split)
+//   warps 11-18  builders: the A operand of the chunk (W products, FP16 split)
 //                stored into tensor memory (lane quadrant warp % 4, atoms
-//                16 x ((warp - 19) / 4) onwards)
+//                16 x ((warp - 11) / 4) onwards)
 // Hand-offs are mbarriers (bulk-copy transactions, tcgen05.commit, thread
 // arrivals); every wait is bounded, and a timeout makes every role stop, wait
 // for its own copies and MMAs, free tensor memory and report through an error
@@ -65,14 +65,14 @@ constexpr int TC_GROUP = 2;                   // chunks per tensor-memory accumu
 constexpr int TC_S = 4;                       // ring stages: Z, X, Y in shared memory, A in tensor memory
 constexpr uint32_t TC_HDR = 1024;             // barrier header ahead of the ring
 constexpr uint32_t TC_SMEM_MAX = 227 * 1024;  // dynamic shared memory per block
-constexpr int TC_DRAIN_WARPS = 16;            // warps 0-15
+constexpr int TC_DRAIN_WARPS = 8;             // warps 0-7
 constexpr int TC_DRAIN_PAR = TC_DRAIN_WARPS / 4;  // drain warps per lane quadrant
-constexpr int TC_PRODUCER_WARP = 16;
-constexpr int TC_MMA_WARP = 17;               // warps 17 and 18: one per accumulator
+constexpr int TC_PRODUCER_WARP = 8;
+constexpr int TC_MMA_WARP = 9;                // warps 9 and 10: one per accumulator
 constexpr int TC_MMA_WARPS = 2;
-constexpr int TC_BUILD_WARP0 = TC_MMA_WARP + TC_MMA_WARPS;  // warps 19-26
+constexpr int TC_BUILD_WARP0 = TC_MMA_WARP + TC_MMA_WARPS;  // warps 11-18
 constexpr int TC_BUILD_WARPS = 8;
-constexpr int TC_THREADS = 32 * (TC_BUILD_WARP0 + TC_BUILD_WARPS);  // 864
+constexpr int TC_THREADS = 32 * (TC_BUILD_WARP0 + TC_BUILD_WARPS);  // 608
 constexpr uint32_t TC_XB = TC_J * 2 * 8 * sizeof(float2);     // 4 KB: 32 atoms x 2 lane variants x 8 nx
 constexpr uint32_t TC_YB = TC_J * 8 * sizeof(float2);         // 2 KB: 32 atoms x 8 ny
 constexpr uint32_t TC_XYB = TC_XB + TC_YB;                    // one (block, chunk) table pair
